@@ -1,0 +1,429 @@
+// C ABI of libgbhf (declarations and reference citations in include/gbhf.h).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "gbhf_internal.h"
+
+using namespace gbhf;
+
+namespace {
+
+gbhf_status check_ctx(gbhf_ctx* c) {
+  if (!c) return GBHF_ERR_BAD_INPUT;
+  cudaError_t e = cudaSetDevice(c->device);
+  if (e != cudaSuccess) return cuda_fail(c, e, "cudaSetDevice");
+  return GBHF_OK;
+}
+
+#define CTX_CHECK(c)                            \
+  do {                                          \
+    if (!(c)) return GBHF_ERR_BAD_INPUT;        \
+    gbhf_status s0__ = check_ctx(c);            \
+    if (s0__ != GBHF_OK) return s0__;           \
+    (c)->err.clear();                           \
+  } while (0)
+
+template <typename T>
+gbhf_status upload(gbhf_ctx* c, DBuf<T>& d, const T* h, size_t n) {
+  GBHF_CUDA(c, d.alloc(n));
+  GBHF_CUDA(c, cudaMemcpyAsync(d.p, h, n * sizeof(T), cudaMemcpyHostToDevice, c->stream));
+  return GBHF_OK;
+}
+
+gbhf_status download(gbhf_ctx* c, void* h, const void* d, size_t bytes) {
+  GBHF_CUDA(c, cudaMemcpyAsync(h, d, bytes, cudaMemcpyDeviceToHost, c->stream));
+  GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
+  return GBHF_OK;
+}
+
+bool need_basis(gbhf_ctx* c) {
+  if (!c->basis_dev) {
+    c->err = "no basis set (call gbhf_set_basis first)";
+    return false;
+  }
+  return true;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gbhf_version(void) { return 1; }
+
+gbhf_status gbhf_create(gbhf_ctx** out, int device) {
+  if (!out) return GBHF_ERR_BAD_INPUT;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) return GBHF_ERR_NO_DEVICE;
+  if (device < 0 || device >= ndev) return GBHF_ERR_NO_DEVICE;
+  if (cudaSetDevice(device) != cudaSuccess) return GBHF_ERR_NO_DEVICE;
+  gbhf_ctx* c = new gbhf_ctx;
+  c->device = device;
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) {
+    delete c;
+    return GBHF_ERR_NO_DEVICE;
+  }
+  c->nsm = prop.multiProcessorCount;
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete c;
+    return GBHF_ERR_CUDA;
+  }
+  for (auto& e : c->ev) cudaEventCreate(&e);
+  *out = c;
+  return GBHF_OK;
+}
+
+gbhf_status gbhf_destroy(gbhf_ctx* c) {
+  if (!c) return GBHF_OK;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  for (auto& e : c->ev)
+    if (e) cudaEventDestroy(e);
+  cudaStream_t s = c->stream;
+  delete c;   // frees device buffers
+  if (s) cudaStreamDestroy(s);
+  return GBHF_OK;
+}
+
+const char* gbhf_last_error(gbhf_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+gbhf_status gbhf_set_basis(gbhf_ctx* c, int n_atoms, const double* xyz, const double* Z, int n_cgf,
+                           const int* cgf_atom, const int* cgf_lxyz, const int* cgf_nprim, const double* coef,
+                           const double* expo) {
+  CTX_CHECK(c);
+  c->tasks.thr_all = -1;
+  c->tasks.thr64 = -1;
+  return build_basis(c, n_atoms, xyz, Z, n_cgf, cgf_atom, cgf_lxyz, cgf_nprim, coef, expo);
+}
+
+gbhf_status gbhf_set_boys_grid(gbhf_ctx* c, const double* grid) {
+  CTX_CHECK(c);
+  if (!grid) return fail(c, GBHF_ERR_BAD_INPUT, "null grid");
+  for (int i = 0; i < 15 * 1001; ++i)
+    if (!std::isfinite(grid[i])) return fail(c, GBHF_ERR_BAD_INPUT, "Boys grid holds a non-finite value");
+  GBHF_TRY(upload(c, c->boys_ref, grid, 15 * 1001));
+  GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
+  c->have_grid = true;
+  return GBHF_OK;
+}
+
+gbhf_status gbhf_generate_boys_grid(gbhf_ctx* c, double* grid_out) {
+  CTX_CHECK(c);
+  GBHF_CUDA(c, c->boys_ref.alloc(15 * 1001));
+  GBHF_TRY(boys_ref_grid_dev(c, c->boys_ref.p));
+  c->have_grid = true;
+  if (grid_out) return download(c, grid_out, c->boys_ref.p, 15 * 1001 * sizeof(double));
+  return GBHF_OK;
+}
+
+gbhf_status gbhf_boys(gbhf_ctx* c, int mode, int m_max, int n, const double* x, double* out) {
+  CTX_CHECK(c);
+  if (n < 0 || (n > 0 && (!x || !out))) return fail(c, GBHF_ERR_BAD_INPUT, "gbhf_boys: bad arguments");
+  const bool ref = mode == GBHF_MODE_REFERENCE;
+  if (ref && !c->have_grid) return fail(c, GBHF_ERR_BAD_INPUT, "reference mode needs gbhf_set_boys_grid");
+  for (int i = 0; i < n; ++i)
+    if (!(x[i] >= 0) || !std::isfinite(x[i])) return fail(c, GBHF_ERR_BAD_INPUT, "gbhf_boys: x must be finite, >= 0");
+  GBHF_TRY(ensure_boys_tables(c));
+  if (n == 0) return GBHF_OK;
+  DBuf<double> dx, dout;
+  GBHF_TRY(upload(c, dx, x, n));
+  GBHF_CUDA(c, dout.alloc((size_t)n * (m_max + 1)));
+  GBHF_TRY(boys_dev(c, ref, m_max, n, dx.p, dout.p));
+  return download(c, out, dout.p, (size_t)n * (m_max + 1) * sizeof(double));
+}
+
+gbhf_status gbhf_overlap(gbhf_ctx* c, int mode, double* s_flat) {
+  CTX_CHECK(c);
+  if (!need_basis(c)) return GBHF_ERR_BAD_INPUT;
+  if (!s_flat) return fail(c, GBHF_ERR_BAD_INPUT, "null output");
+  GBHF_TRY(ensure_boys_tables(c));
+  const size_t ntri = (size_t)c->basis.nbf * (c->basis.nbf + 1) / 2;
+  GBHF_WS(c, d, 15, ntri);
+  GBHF_TRY(onee_matrices(c, mode == GBHF_MODE_REFERENCE, d, nullptr));
+  return download(c, s_flat, d, ntri * sizeof(double));
+}
+
+gbhf_status gbhf_hcore(gbhf_ctx* c, int mode, double* h_flat) {
+  CTX_CHECK(c);
+  if (!need_basis(c)) return GBHF_ERR_BAD_INPUT;
+  if (!h_flat) return fail(c, GBHF_ERR_BAD_INPUT, "null output");
+  GBHF_TRY(ensure_boys_tables(c));
+  const size_t ntri = (size_t)c->basis.nbf * (c->basis.nbf + 1) / 2;
+  GBHF_WS(c, d, 16, ntri);
+  GBHF_TRY(onee_matrices(c, mode == GBHF_MODE_REFERENCE, nullptr, d));
+  return download(c, h_flat, d, ntri * sizeof(double));
+}
+
+int64_t gbhf_eri_canonical_length(int n) {
+  if (n <= 0) return 0;
+  const int64_t p = (int64_t)n * (n + 1) / 2;
+  return p * (p + 1) / 2;
+}
+
+gbhf_status gbhf_eri_canonical(gbhf_ctx* c, int mode, double* eri, int64_t length) {
+  CTX_CHECK(c);
+  if (!need_basis(c)) return GBHF_ERR_BAD_INPUT;
+  const int64_t need = gbhf_eri_canonical_length(c->basis.nbf);
+  if (!eri || length < need) return fail(c, GBHF_ERR_BAD_INPUT, "ERI output buffer too small");
+  GBHF_TRY(ensure_boys_tables(c));
+  DBuf<double> d;
+  GBHF_CUDA(c, d.alloc((size_t)need));
+  GBHF_TRY(eri_canonical_dev(c, mode == GBHF_MODE_REFERENCE, d.p));
+  return download(c, eri, d.p, (size_t)need * sizeof(double));
+}
+
+gbhf_status gbhf_fock(gbhf_ctx* c, int mode, int precision, double schwarz_cutoff, double mixed_cutoff,
+                      const double* h_flat, const double* d_flat, double* f_flat) {
+  CTX_CHECK(c);
+  if (!need_basis(c)) return GBHF_ERR_BAD_INPUT;
+  if (!h_flat || !d_flat || !f_flat) return fail(c, GBHF_ERR_BAD_INPUT, "null pointer");
+  if (!(schwarz_cutoff >= 0) || !(mixed_cutoff >= 0)) return fail(c, GBHF_ERR_BAD_INPUT, "cutoffs must be >= 0");
+  GBHF_TRY(ensure_boys_tables(c));
+  const int n = c->basis.nbf;
+  const size_t nn = (size_t)n * n, ntri = (size_t)n * (n + 1) / 2;
+  GBHF_WS(c, fH, 15, ntri);
+  GBHF_WS(c, fD, 16, ntri);
+  GBHF_WS(c, fF, 17, ntri);
+  GBHF_CUDA(c, cudaMemcpyAsync(fH, h_flat, ntri * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  GBHF_CUDA(c, cudaMemcpyAsync(fD, d_flat, ntri * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  if (mode == GBHF_MODE_REFERENCE) {
+    if (!c->have_grid) return fail(c, GBHF_ERR_BAD_INPUT, "reference mode needs gbhf_set_boys_grid");
+    const long long P = (long long)ntri;
+    DBuf<double> eri;
+    GBHF_CUDA(c, eri.alloc((size_t)(P * (P + 1) / 2)));
+    GBHF_TRY(eri_canonical_dev(c, true, eri.p));
+    GBHF_TRY(fock_canonical_dev(c, fH, fD, eri.p, fF));
+    return download(c, f_flat, fF, ntri * sizeof(double));
+  }
+  GBHF_WS(c, Dsq, 18, nn);
+  GBHF_WS(c, Hsq, 19, nn);
+  GBHF_WS(c, Gpp, 20, nn);
+  GBHF_WS(c, Fsq, 21, nn);
+  GBHF_TRY(flat_to_square(c, n, fD, Dsq));
+  GBHF_TRY(flat_to_square(c, n, fH, Hsq));
+  GBHF_CUDA(c, cudaMemsetAsync(Gpp, 0, nn * sizeof(double), c->stream));
+  GBHF_TRY(jk_build(c, Dsq, Gpp, precision, schwarz_cutoff, mixed_cutoff, 1.0));
+  GBHF_TRY(add_sym(c, n, Hsq, Gpp, Fsq));
+  GBHF_TRY(square_to_flat(c, n, Fsq, fF));
+  return download(c, f_flat, fF, ntri * sizeof(double));
+}
+
+gbhf_status gbhf_symm_ortho(gbhf_ctx* c, int n, const double* s_square, double* x_square) {
+  CTX_CHECK(c);
+  if (n <= 0 || !s_square || !x_square) return fail(c, GBHF_ERR_BAD_INPUT, "bad arguments");
+  const size_t nn = (size_t)n * n;
+  GBHF_WS(c, S, 15, nn);
+  GBHF_WS(c, X, 16, nn);
+  GBHF_CUDA(c, cudaMemcpyAsync(S, s_square, nn * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  GBHF_TRY(symm_ortho_dev(c, n, S, X));
+  return download(c, x_square, X, nn * sizeof(double));
+}
+
+gbhf_status gbhf_eigen_solve(gbhf_ctx* c, int n, const double* a_square, double* evals, double* evecs) {
+  CTX_CHECK(c);
+  if (n <= 0 || !a_square || !evals || !evecs) return fail(c, GBHF_ERR_BAD_INPUT, "bad arguments");
+  const size_t nn = (size_t)n * n;
+  GBHF_WS(c, A, 15, nn);
+  GBHF_WS(c, V, 16, nn);
+  GBHF_WS(c, w, 17, (size_t)n);
+  GBHF_CUDA(c, cudaMemcpyAsync(A, a_square, nn * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  GBHF_TRY(eigh(c, n, A, w, V, nullptr));
+  GBHF_TRY(download(c, evals, w, n * sizeof(double)));
+  return download(c, evecs, V, nn * sizeof(double));
+}
+
+gbhf_status gbhf_diagonal_hf(gbhf_ctx* c, int n, const double* f_flat, const double* x_square, int n_occupied,
+                             double* coeff, double* density_flat, double* orb_energies) {
+  CTX_CHECK(c);
+  if (n <= 0 || !f_flat || !x_square || n_occupied < 0 || n_occupied > n)
+    return fail(c, GBHF_ERR_BAD_INPUT, "bad arguments");
+  const size_t nn = (size_t)n * n, ntri = (size_t)n * (n + 1) / 2;
+  GBHF_WS(c, fF, 15, ntri);
+  GBHF_WS(c, Fsq, 16, nn);
+  GBHF_WS(c, X, 17, nn);
+  GBHF_WS(c, C, 18, nn);
+  GBHF_WS(c, Dsq, 19, nn);
+  GBHF_WS(c, eps, 20, (size_t)n);
+  GBHF_WS(c, fD, 21, ntri);
+  GBHF_CUDA(c, cudaMemcpyAsync(fF, f_flat, ntri * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  GBHF_CUDA(c, cudaMemcpyAsync(X, x_square, nn * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  GBHF_TRY(flat_to_square(c, n, fF, Fsq));
+  GBHF_TRY(diagonal_hf_dev(c, n, Fsq, X, n_occupied, C, Dsq, eps, nullptr));
+  GBHF_TRY(square_to_flat(c, n, Dsq, fD));
+  if (coeff) GBHF_TRY(download(c, coeff, C, nn * sizeof(double)));
+  if (density_flat) GBHF_TRY(download(c, density_flat, fD, ntri * sizeof(double)));
+  if (orb_energies) GBHF_TRY(download(c, orb_energies, eps, n * sizeof(double)));
+  GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
+  return GBHF_OK;
+}
+
+gbhf_status gbhf_diis_error(gbhf_ctx* c, int n, const double* f_flat, const double* s_flat, const double* d_flat,
+                            const double* x_square, double* e_square) {
+  CTX_CHECK(c);
+  if (n <= 0 || !f_flat || !s_flat || !d_flat || !x_square || !e_square)
+    return fail(c, GBHF_ERR_BAD_INPUT, "bad arguments");
+  const size_t nn = (size_t)n * n, ntri = (size_t)n * (n + 1) / 2;
+  GBHF_WS(c, t, 15, ntri);
+  GBHF_WS(c, F, 16, nn);
+  GBHF_WS(c, S, 17, nn);
+  GBHF_WS(c, D, 18, nn);
+  GBHF_WS(c, X, 19, nn);
+  GBHF_WS(c, E, 20, nn);
+  GBHF_CUDA(c, cudaMemcpyAsync(t, f_flat, ntri * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  GBHF_TRY(flat_to_square(c, n, t, F));
+  GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
+  GBHF_CUDA(c, cudaMemcpyAsync(t, s_flat, ntri * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  GBHF_TRY(flat_to_square(c, n, t, S));
+  GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
+  GBHF_CUDA(c, cudaMemcpyAsync(t, d_flat, ntri * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  GBHF_TRY(flat_to_square(c, n, t, D));
+  GBHF_CUDA(c, cudaMemcpyAsync(X, x_square, nn * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  GBHF_TRY(diis_error_dev(c, n, F, S, D, X, E));
+  return download(c, e_square, E, nn * sizeof(double));
+}
+
+gbhf_status gbhf_gauss_elem(gbhf_ctx* c, int m, const double* a, const double* b, double* x) {
+  CTX_CHECK(c);
+  if (!a || !b || !x) return fail(c, GBHF_ERR_BAD_INPUT, "null pointer");
+  bool ok = false;
+  GBHF_TRY(gauss_elem_dev_call(c, m, a, b, x, &ok));
+  if (!ok) return fail(c, GBHF_ERR_SINGULAR, "Gauss elimination: rank deficient or non-finite system");
+  return GBHF_OK;
+}
+
+gbhf_status gbhf_diis_extrapolate(gbhf_ctx* c, int n, int n_hist, const double* errors_square,
+                                  const double* focks_flat, double* f_out_flat, int* n_used) {
+  CTX_CHECK(c);
+  if (n <= 0 || n_hist < 0 || n_hist > 7 || !errors_square || !focks_flat || !f_out_flat)
+    return fail(c, GBHF_ERR_BAD_INPUT, "bad arguments");
+  const size_t nn = (size_t)n * n, ntri = (size_t)n * (n + 1) / 2;
+  const int k0 = n_hist + 1;
+  DBuf<double> E, Fv, out, dots;
+  GBHF_TRY(upload(c, E, errors_square, nn * k0));
+  GBHF_TRY(upload(c, Fv, focks_flat, ntri * k0));
+  GBHF_CUDA(c, out.alloc(ntri));
+  GBHF_CUDA(c, dots.alloc(64));
+  // B_ij = tr(e_i^T e_j)
+  std::vector<double> B((size_t)k0 * k0);
+  for (int i = 0; i < k0; ++i) {
+    std::vector<const double*> mats;
+    for (int j = 0; j < k0; ++j) mats.push_back(E.p + nn * j);
+    GBHF_TRY(dot_matrices(c, (int)nn, k0, mats.data(), E.p + nn * i, dots.p));
+    GBHF_TRY(download(c, &B[(size_t)i * k0], dots.p, k0 * sizeof(double)));
+  }
+  int k = k0;
+  while (true) {
+    const int m = k + 1;
+    std::vector<double> Bm((size_t)m * m, 0.0), rhs(m, 0.0), x(m, 0.0);
+    for (int i = 0; i < k; ++i)
+      for (int j = 0; j < k; ++j) Bm[(size_t)i * m + j] = B[(size_t)i * k0 + j];
+    for (int i = 0; i < k; ++i) {
+      Bm[(size_t)i * m + k] = -1;
+      Bm[(size_t)k * m + i] = -1;
+    }
+    rhs[k] = -1;
+    bool ok = false;
+    GBHF_TRY(gauss_elem_dev_call(c, m, Bm.data(), rhs.data(), x.data(), &ok));
+    if (ok) {
+      std::vector<const double*> mats;
+      for (int j = 0; j < k; ++j) mats.push_back(Fv.p + ntri * j);
+      GBHF_CUDA(c, cudaMemcpyAsync(dots.p, x.data(), k * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+      GBHF_TRY(lincomb(c, (int)ntri, k, mats.data(), dots.p, out.p));
+      if (n_used) *n_used = k - 1;
+      return download(c, f_out_flat, out.p, ntri * sizeof(double));
+    }
+    if (k == 1) return fail(c, GBHF_ERR_SINGULAR, "DIIS system singular with no stored vectors left");
+    --k;
+  }
+}
+
+void gbhf_scf_opts_reference(gbhf_scf_opts* o) {
+  if (!o) return;
+  std::memset(o, 0, sizeof(*o));
+  o->mode = GBHF_MODE_REFERENCE;
+  o->precision = GBHF_PREC_FP64;
+  o->guess = GBHF_GUESS_HARRIS;
+  o->diis_size = 5;
+  o->max_iter = 30;
+  o->incremental = 0;
+  o->full_rebuild_every = 0;
+  o->final_fp64 = 0;
+  o->ref_stop_rule = 1;
+  o->conv_error = 1e-7;
+  o->conv_energy = 1e-10;
+  o->conv_density = 1e-8;
+  o->diis_start = 0.1;
+  o->schwarz_cutoff = 0.0;
+  o->mixed_cutoff = 0.0;
+  o->charge = 0.0;
+}
+
+void gbhf_scf_opts_baseline(gbhf_scf_opts* o) {
+  if (!o) return;
+  std::memset(o, 0, sizeof(*o));
+  o->mode = GBHF_MODE_EXACT;
+  o->precision = GBHF_PREC_FP64;
+  o->guess = GBHF_GUESS_CORE;
+  o->diis_size = 6;
+  o->max_iter = 100;
+  o->incremental = 0;
+  o->full_rebuild_every = 8;
+  o->final_fp64 = 1;
+  o->ref_stop_rule = 0;
+  o->conv_error = 1e-7;
+  o->conv_energy = 1e-10;
+  o->conv_density = 1e-8;
+  o->diis_start = 1e30;
+  o->schwarz_cutoff = 1e-12;
+  o->mixed_cutoff = 1e-4;
+  o->charge = 0.0;
+}
+
+gbhf_status gbhf_scf(gbhf_ctx* c, const gbhf_scf_opts* opts, gbhf_result* result) {
+  CTX_CHECK(c);
+  if (!opts) return fail(c, GBHF_ERR_BAD_INPUT, "null options");
+  return scf_run(c, opts, result);
+}
+
+gbhf_status gbhf_gradient(gbhf_ctx* c, int precision, double schwarz_cutoff, const double* d_flat,
+                          const double* w_flat, double* grad) {
+  CTX_CHECK(c);
+  (void)precision;
+  (void)schwarz_cutoff;
+  (void)d_flat;
+  (void)w_flat;
+  (void)grad;
+  return fail(c, GBHF_ERR_UNSUPPORTED, "gradient kernels not built yet");
+}
+
+gbhf_status gbhf_scf_batch(gbhf_ctx* c, int n_mol, const int* atom_off, const int* cgf_off, const double* xyz_bohr,
+                           const double* charges, const int* cgf_atom, const int* cgf_lxyz, const int* cgf_nprim,
+                           const double* prim_coef, const double* prim_exp, const gbhf_scf_opts* opts,
+                           double* energies, int* iterations, int* converged, double* grads) {
+  CTX_CHECK(c);
+  (void)n_mol; (void)atom_off; (void)cgf_off; (void)xyz_bohr; (void)charges; (void)cgf_atom; (void)cgf_lxyz;
+  (void)cgf_nprim; (void)prim_coef; (void)prim_exp; (void)opts; (void)energies; (void)iterations;
+  (void)converged; (void)grads;
+  return fail(c, GBHF_ERR_UNSUPPORTED, "batched SCF not built yet");
+}
+
+gbhf_status gbhf_profile_reset(gbhf_ctx* c, int enable_events) {
+  CTX_CHECK(c);
+  c->prof = Profile();
+  c->prof.events = enable_events != 0;
+  return GBHF_OK;
+}
+
+gbhf_status gbhf_profile_read(gbhf_ctx* c, double* stats, int n_stats) {
+  CTX_CHECK(c);
+  if (!stats) return fail(c, GBHF_ERR_BAD_INPUT, "null pointer");
+  const double v[8] = {c->prof.jk_ms64, c->prof.jk_ms32, c->prof.prim64, c->prof.prim32,
+                       c->prof.shellq,  c->prof.fnq,     (double)c->prof.launches, c->prof.dense_ms};
+  for (int i = 0; i < n_stats && i < 8; ++i) stats[i] = v[i];
+  return GBHF_OK;
+}
+
+}  // extern "C"

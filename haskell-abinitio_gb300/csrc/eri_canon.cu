@@ -1,0 +1,393 @@
+// One-electron matrices, canonical ERI array, Fock from stored ERIs, Boys
+// values and shell-pair Schwarz bounds (FP64, generic angular momentum).
+#include <cmath>
+#include <vector>
+
+#include "gbhf_internal.h"
+#include "gbhf_md.cuh"
+
+namespace gbhf {
+
+__device__ __forceinline__ long tri_l(long n) { return n * (n + 1) / 2; }
+__device__ __forceinline__ long flat2_dev(long dim, long x, long y) {
+  if (x > y) {
+    long t = x;
+    x = y;
+    y = t;
+  }
+  return x * dim - tri_l(x - 1) + (y - x);
+}
+
+// ------------------------------------------------------------ Boys ----
+__global__ void k_boys(bool ref, const double* __restrict__ grid, const double* __restrict__ tab, int mmax, int n,
+                       const double* __restrict__ x, double* __restrict__ out) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double F[MD_LMAX + 12];
+  boys_generic(ref, grid, tab, mmax, x[i], F);
+  for (int m = 0; m <= mmax; ++m) out[i * (mmax + 1) + m] = F[m];
+}
+
+gbhf_status boys_dev(gbhf_ctx* c, bool ref, int mmax, int n, const double* d_x, double* d_out) {
+  if (mmax < 0 || mmax > MD_LMAX + 8 || (!ref && mmax + BOYS64_NTERM > BOYS_NCOL) || (ref && mmax > 9))
+    return fail(c, GBHF_ERR_BAD_INPUT, "gbhf_boys: m_max out of range");
+  if (n <= 0) return GBHF_OK;
+  k_boys<<<(n + 127) / 128, 128, 0, c->stream>>>(ref, c->boys_ref.p, c->boys64.p, mmax, n, d_x, d_out);
+  count_launch(c);
+  GBHF_CUDA(c, cudaGetLastError());
+  return GBHF_OK;
+}
+
+// ------------------------------------------------- one-electron terms ----
+// obaraSaika table s(m,n), m <= 2, n <= 4 (Integrals/IntegralsEvaluation.hs:209-221)
+__device__ inline void os_table(double gamma, double s00, double pax, double pbx, int M, int N, double s[3][5]) {
+  const double c = 1.0 / (2.0 * gamma);
+  for (int m = 0; m <= M; ++m)
+    for (int n = 0; n <= N; ++n) {
+      double v;
+      if (m == 0 && n == 0) {
+        v = s00;
+      } else if (m == 0) {
+        v = pbx * s[0][n - 1] + (n >= 2 ? c * (n - 1) * s[0][n - 2] : 0.0);
+      } else if (n == 0) {
+        v = pax * s[m - 1][0] + (m >= 2 ? c * (m - 1) * s[m - 2][0] : 0.0);
+      } else {
+        v = pax * s[m - 1][n] + c * ((m >= 2 ? (m - 1) * s[m - 2][n] : 0.0) + n * s[m - 1][n - 1]);
+      }
+      s[m][n] = v;
+    }
+}
+
+__global__ void k_onee(bool ref, int nbf, int natoms, const double* __restrict__ xyz, const double* __restrict__ Z,
+                       const int* __restrict__ fn, const double* __restrict__ coef, const double* __restrict__ expo,
+                       const double* __restrict__ grid, const double* __restrict__ tab, double* __restrict__ S,
+                       double* __restrict__ H) {
+  const int i = blockIdx.y;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= nbf || j < i) return;
+  const DevFn f = load_fn(fn, i), g = load_fn(fn, j);
+  const double *A = xyz + 3 * f.atom, *B = xyz + 3 * g.atom;
+  const long out = flat2_dev(nbf, i, j);
+  // overlap (sijContracted, IntegralsEvaluation.hs:181-206)
+  bool same = false;
+  if (ref) {
+    same = f.l[0] == g.l[0] && f.l[1] == g.l[1] && f.l[2] == g.l[2] && f.np == g.np && A[0] == B[0] &&
+           A[1] == B[1] && A[2] == B[2];
+    for (int k = 0; same && k < f.np; ++k)
+      same = coef[f.off + k] == coef[g.off + k] && expo[f.off + k] == expo[g.off + k];
+  }
+  double s_sum = 0, t_sum = 0, v_sum = 0;
+  const int L = f.l[0] + f.l[1] + f.l[2] + g.l[0] + g.l[1] + g.l[2];
+  double F[MD_LMAX + 1];
+  double R[MD_D * MD_D * MD_D];
+  for (int p1 = 0; p1 < f.np; ++p1)
+    for (int p2 = 0; p2 < g.np; ++p2) {
+      const double c1 = coef[f.off + p1], e1 = expo[f.off + p1];
+      const double c2 = coef[g.off + p2], e2 = expo[g.off + p2];
+      const double p = e1 + e2, mu = e1 * e2 / p;
+      const double cte = sqrt(GBHF_PI / p);
+      double P[3], sx[3], tx[3];
+      EAx E[3];
+      for (int x = 0; x < 3; ++x) {
+        P[x] = (e1 * A[x] + e2 * B[x]) / p;
+        const double ab = A[x] - B[x];
+        const double ex = exp(-mu * ab * ab);
+        double s[3][5];
+        const int l1 = f.l[x], l2 = g.l[x];
+        os_table(p, ex * cte, P[x] - A[x], P[x] - B[x], l1, l2 + 2, s);
+        sx[x] = s[l1][l2];
+        // kinetic 1-D term (tab, IntegralsEvaluation.hs:263-280)
+        tx[x] = -2.0 * e2 * e2 * s[l1][l2 + 2] + e2 * (2 * l2 + 1) * s[l1][l2] -
+                (l2 >= 2 ? 0.5 * l2 * (l2 - 1) * s[l1][l2 - 2] : 0.0);
+        e_axis(E[x], l1, l2, p, P[x] - A[x], P[x] - B[x], ex);
+      }
+      s_sum += (c1 * c2) * (sx[0] * sx[1] * sx[2]);
+      t_sum += c1 * c2 * (tx[0] * sx[1] * sx[2] + sx[0] * tx[1] * sx[2] + sx[0] * sx[1] * tx[2]);
+      // nuclear attraction (vijHermite/mcMurchie, IntegralsEvaluation.hs:395-414)
+      for (int cn = 0; cn < natoms; ++cn) {
+        const double* Cc = xyz + 3 * cn;
+        const double PC[3] = {P[0] - Cc[0], P[1] - Cc[1], P[2] - Cc[2]};
+        boys_generic(ref, grid, tab, L, p * (PC[0] * PC[0] + PC[1] * PC[1] + PC[2] * PC[2]), F);
+        hermite_r<MD_LMAX>(L, p, PC[0], PC[1], PC[2], F, R);
+        double sum = 0;
+        for (int t = 0; t <= f.l[0] + g.l[0]; ++t)
+          for (int u = 0; u <= f.l[1] + g.l[1]; ++u)
+            for (int v = 0; v <= f.l[2] + g.l[2]; ++v)
+              sum += E[0].get(f.l[0], g.l[0], t) * E[1].get(f.l[1], g.l[1], u) * E[2].get(f.l[2], g.l[2], v) *
+                     R[(t * MD_D + u) * MD_D + v];
+        v_sum += (-Z[cn]) * (c1 * c2 * 2.0 * (GBHF_PI / p) * sum);
+      }
+    }
+  if (S) S[out] = same ? 1.0 : s_sum;
+  if (H) H[out] = t_sum + v_sum;
+}
+
+gbhf_status onee_matrices(gbhf_ctx* c, bool ref, double* d_S, double* d_H) {
+  const Basis& b = c->basis;
+  if (b.maxL > 2) return fail(c, GBHF_ERR_UNSUPPORTED, "one-electron integrals support s, p, d functions");
+  if (ref && !c->have_grid) return fail(c, GBHF_ERR_BAD_INPUT, "reference mode needs gbhf_set_boys_grid");
+  dim3 grid((b.nbf + 63) / 64, b.nbf);
+  k_onee<<<grid, 64, 0, c->stream>>>(ref, b.nbf, b.natoms, c->d_xyz.p, c->d_Z.p, c->d_fn.p, c->d_coef.p,
+                                      c->d_exp.p, c->boys_ref.p, c->boys64.p, d_S, d_H);
+  count_launch(c);
+  GBHF_CUDA(c, cudaGetLastError());
+  return GBHF_OK;
+}
+
+// ------------------------------------------------- canonical ERIs ----
+// Key (i<=j | k<=l) with (i,j) <= (k,l) lexicographically <=> flat pair
+// indices P = flat(i,j) <= Q = flat(k,l).  The position in the reference's
+// enumeration order (calcIntegrals, HartreeFock.hs:166-181) is
+// off[i*n+j] + (k == i ? l - j : (n - j) + sum_{k'=i+1}^{k-1}(n-k') + l - k).
+__device__ __forceinline__ long canon_pos(const long* __restrict__ off, long n, long i, long j, long k, long l) {
+  long idx = off[i * n + j];
+  if (k == i) return idx + (l - j);
+  idx += n - j;
+  const long m = k - i - 1;
+  idx += m * n - (m * i + tri_l(m));
+  return idx + (l - k);
+}
+
+__device__ __forceinline__ void sort_key(long& i, long& j, long& k, long& l) {
+  long t;
+  if (i > j) { t = i; i = j; j = t; }
+  if (k > l) { t = k; k = l; l = t; }
+  if (i > k || (i == k && j > l)) {
+    t = i; i = k; k = t;
+    t = j; j = l; l = t;
+  }
+}
+
+__global__ void k_eri_canonical(bool ref, int nbf, const int* __restrict__ pair_i, const int* __restrict__ pair_j,
+                                long npair, const long* __restrict__ off, const double* __restrict__ xyz,
+                                const int* __restrict__ fn, const double* __restrict__ coef,
+                                const double* __restrict__ expo, const double* __restrict__ grid,
+                                const double* __restrict__ tab, double* __restrict__ eri) {
+  const long P = blockIdx.y;
+  const long Q = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (Q >= npair || Q < P) return;
+  const long i = pair_i[P], j = pair_j[P], k = pair_i[Q], l = pair_j[Q];
+  eri[canon_pos(off, nbf, i, j, k, l)] =
+      eri_fn_generic(ref, xyz, fn, coef, expo, grid, tab, (int)i, (int)j, (int)k, (int)l);
+}
+
+static void canonical_offsets(long n, std::vector<long>& off) {
+  off.assign(n * n, 0);
+  long acc = 0;
+  for (long i = 0; i < n; ++i)
+    for (long j = i; j < n; ++j) {
+      off[i * n + j] = acc;
+      acc += (n - j) + (n - i - 1) * (n - i) / 2;
+    }
+}
+
+struct CanonAux {
+  DBuf<int> pi, pj;
+  DBuf<long> off;
+};
+
+static gbhf_status canon_aux(gbhf_ctx* c, CanonAux& aux) {
+  const long n = c->basis.nbf, np = n * (n + 1) / 2;
+  std::vector<int> hi(np), hj(np);
+  long q = 0;
+  for (long i = 0; i < n; ++i)
+    for (long j = i; j < n; ++j, ++q) {
+      hi[q] = (int)i;
+      hj[q] = (int)j;
+    }
+  std::vector<long> off;
+  canonical_offsets(n, off);
+  GBHF_CUDA(c, aux.pi.alloc(np));
+  GBHF_CUDA(c, aux.pj.alloc(np));
+  GBHF_CUDA(c, aux.off.alloc(n * n));
+  GBHF_CUDA(c, cudaMemcpyAsync(aux.pi.p, hi.data(), np * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  GBHF_CUDA(c, cudaMemcpyAsync(aux.pj.p, hj.data(), np * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  GBHF_CUDA(c, cudaMemcpyAsync(aux.off.p, off.data(), n * n * sizeof(long), cudaMemcpyHostToDevice, c->stream));
+  GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
+  return GBHF_OK;
+}
+
+gbhf_status eri_canonical_dev(gbhf_ctx* c, bool ref, double* d_eri) {
+  const Basis& b = c->basis;
+  if (b.maxL > 1) return fail(c, GBHF_ERR_UNSUPPORTED, "canonical ERIs support s and p functions");
+  if (ref && !c->have_grid) return fail(c, GBHF_ERR_BAD_INPUT, "reference mode needs gbhf_set_boys_grid");
+  CanonAux aux;
+  GBHF_TRY(canon_aux(c, aux));
+  const long np = (long)b.nbf * (b.nbf + 1) / 2;
+  if (np > 65535) return fail(c, GBHF_ERR_UNSUPPORTED, "canonical ERI array too large");
+  dim3 grid((unsigned)((np + 127) / 128), (unsigned)np);
+  k_eri_canonical<<<grid, 128, 0, c->stream>>>(ref, b.nbf, aux.pi.p, aux.pj.p, np, aux.off.p, c->d_xyz.p,
+                                                c->d_fn.p, c->d_coef.p, c->d_exp.p, c->boys_ref.p, c->boys64.p,
+                                                d_eri);
+  count_launch(c);
+  GBHF_CUDA(c, cudaGetLastError());
+  GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
+  return GBHF_OK;
+}
+
+// calcGmatrix/sliceIntegrals (HartreeFock.hs:225-260):
+// F_ab = H_ab + sum_l sum_k D_lk [(ab|kl) - 1/2 (al|kb)], flat in and out.
+__global__ void k_fock_canonical(int n, const long* __restrict__ off, const double* __restrict__ H,
+                                 const double* __restrict__ D, const double* __restrict__ eri,
+                                 double* __restrict__ F) {
+  const int a = blockIdx.y;
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= n || b < a) return;
+  double g = 0;
+  for (long l = 0; l < n; ++l) {
+    double row = 0;
+    for (long k = 0; k < n; ++k) {
+      long i1 = a, j1 = b, k1 = k, l1 = l;
+      sort_key(i1, j1, k1, l1);
+      long i2 = a, j2 = l, k2 = k, l2 = b;
+      sort_key(i2, j2, k2, l2);
+      const double coul = eri[canon_pos(off, n, i1, j1, k1, l1)];
+      const double exch = eri[canon_pos(off, n, i2, j2, k2, l2)];
+      row += D[flat2_dev(n, l, k)] * (coul - 0.5 * exch);
+    }
+    g += row;
+  }
+  const long o = flat2_dev(n, a, b);
+  F[o] = H[o] + g;
+}
+
+gbhf_status fock_canonical_dev(gbhf_ctx* c, const double* d_H, const double* d_D, const double* d_eri, double* d_F) {
+  CanonAux aux;
+  GBHF_TRY(canon_aux(c, aux));
+  const int n = c->basis.nbf;
+  dim3 grid((n + 63) / 64, n);
+  k_fock_canonical<<<grid, 64, 0, c->stream>>>(n, aux.off.p, d_H, d_D, d_eri, d_F);
+  count_launch(c);
+  GBHF_CUDA(c, cudaGetLastError());
+  GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
+  return GBHF_OK;
+}
+
+// ------------------------------------------------- Schwarz bounds ----
+// Q_AB = sqrt(max_{a in A, b in B} (ab|ab)), exact numerics.
+__global__ void k_schwarz(int npairs, const int* __restrict__ pa, const int* __restrict__ pb,
+                          const int* __restrict__ shell_f0, const int* __restrict__ shell_nc,
+                          const double* __restrict__ xyz, const int* __restrict__ fn,
+                          const double* __restrict__ coef, const double* __restrict__ expo,
+                          const double* __restrict__ tab, double* __restrict__ Q) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= npairs) return;
+  const int A = pa[t], B = pb[t];
+  double mx = 0;
+  for (int a = 0; a < shell_nc[A]; ++a)
+    for (int b = 0; b < shell_nc[B]; ++b) {
+      const int fa = shell_f0[A] + a, fb = shell_f0[B] + b;
+      const double v = eri_fn_generic(false, xyz, fn, coef, expo, nullptr, tab, fa, fb, fa, fb);
+      mx = fmax(mx, fabs(v));
+    }
+  Q[t] = sqrt(mx);
+}
+
+gbhf_status schwarz_pairs_dev(gbhf_ctx* c, const int* d_A, const int* d_B, int npairs, double* d_Q) {
+  const Basis& b = c->basis;
+  const int ns = (int)b.shells.size();
+  std::vector<int> f0(ns), nc(ns);
+  for (int s = 0; s < ns; ++s) {
+    f0[s] = b.shells[s].f0;
+    nc[s] = b.shells[s].ncomp;
+  }
+  DBuf<int> df0, dnc;
+  GBHF_CUDA(c, df0.alloc(ns));
+  GBHF_CUDA(c, dnc.alloc(ns));
+  GBHF_CUDA(c, cudaMemcpyAsync(df0.p, f0.data(), ns * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  GBHF_CUDA(c, cudaMemcpyAsync(dnc.p, nc.data(), ns * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  if (npairs > 0) {
+    k_schwarz<<<(npairs + 63) / 64, 64, 0, c->stream>>>(npairs, d_A, d_B, df0.p, dnc.p, c->d_xyz.p, c->d_fn.p,
+                                                       c->d_coef.p, c->d_exp.p, c->boys64.p, d_Q);
+    count_launch(c);
+    GBHF_CUDA(c, cudaGetLastError());
+  }
+  GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
+  return GBHF_OK;
+}
+
+}  // namespace gbhf
+
+namespace gbhf {
+
+// generateGridBoys 0.1 (NumericalTools/TableBoys.hs:58-63) on the device:
+// grid[m*1001+i] = boysF m (0.1 i).  boysF (Boys.hs:54-66): m = 0 from erf
+// (asymptotic beyond 50); m >= 1 by Kummer's integral with the 256-point
+// Gauss-Legendre rule that kummer selects for err = 0.1 (Boys.hs:106-118).
+__global__ void k_boys_ref_grid(const double* __restrict__ xq, const double* __restrict__ wq, int nq,
+                                double* __restrict__ grid) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= 15 * 1001) return;
+  const int m = idx / 1001, i = idx % 1001;
+  const double x = 0.1 * i;
+  double v;
+  if (m == 0) {
+    if (x > 50) v = asympt_boys_ref(0.0, x);
+    else if (x > 0.0) v = 0.5 * sqrt(GBHF_PI / x) * erf(sqrt(x));
+    else v = 1.0;
+  } else {
+    const double n = m, a = n + 0.5, b = n + 1.5, z = -x;
+    const double gamma_factor = tgamma(b) / (tgamma(a) * tgamma(b - a));
+    const double e = exp(1.0);
+    double acc = 0;
+    for (int k = 0; k < nq; ++k) {
+      const double t1 = 0.5 * ((1.0 - 0.0) * xq[k] + 1.0 + 0.0);
+      const double t2 = 0.5 * ((1.0 - 0.0) * (-xq[k]) + 1.0 + 0.0);
+      const double f1 = (pow(e, z * t1) * pow(1 - t1, b - a - 1)) * pow(t1, a - 1);
+      const double f2 = (pow(e, z * t2) * pow(1 - t2, b - a - 1)) * pow(t2, a - 1);
+      acc += wq[k] * (f1 + f2);
+    }
+    v = gamma_factor * (0.5 * (1.0 - 0.0) * acc) / (2 * n + 1);
+  }
+  grid[idx] = v;
+}
+
+// Positive Gauss-Legendre nodes/weights of the n-point rule, ascending
+// (Newton iteration on P_n in long double).
+static void gauss_legendre_pos(int n, std::vector<double>& xs, std::vector<double>& ws) {
+  const int half = n / 2;
+  xs.assign(half, 0.0);
+  ws.assign(half, 0.0);
+  for (int i = 0; i < half; ++i) {
+    long double z = cosl(3.14159265358979323846264338327950288L * (i + 0.75L) / (n + 0.5L));
+    long double pp = 1;
+    for (int it = 0; it < 100; ++it) {
+      long double p1 = 1, p2 = 0;
+      for (int j = 1; j <= n; ++j) {
+        const long double p3 = p2;
+        p2 = p1;
+        p1 = ((2 * j - 1) * z * p2 - (j - 1) * p3) / j;
+      }
+      pp = n * (z * p1 - p2) / (z * z - 1);
+      const long double z1 = z;
+      z = z1 - p1 / pp;
+      if (fabsl(z - z1) < 1e-30L) break;
+    }
+    long double p1 = 1, p2 = 0;
+    for (int j = 1; j <= n; ++j) {
+      const long double p3 = p2;
+      p2 = p1;
+      p1 = ((2 * j - 1) * z * p2 - (j - 1) * p3) / j;
+    }
+    pp = n * (z * p1 - p2) / (z * z - 1);
+    xs[half - 1 - i] = (double)z;
+    ws[half - 1 - i] = (double)(2.0L / ((1 - z * z) * pp * pp));
+  }
+}
+
+gbhf_status boys_ref_grid_dev(gbhf_ctx* c, double* d_grid) {
+  std::vector<double> xs, wsv;
+  gauss_legendre_pos(256, xs, wsv);
+  DBuf<double> dx, dw;
+  GBHF_CUDA(c, dx.alloc(xs.size()));
+  GBHF_CUDA(c, dw.alloc(wsv.size()));
+  GBHF_CUDA(c, cudaMemcpyAsync(dx.p, xs.data(), xs.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  GBHF_CUDA(c, cudaMemcpyAsync(dw.p, wsv.data(), wsv.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  k_boys_ref_grid<<<(15 * 1001 + 127) / 128, 128, 0, c->stream>>>(dx.p, dw.p, (int)xs.size(), d_grid);
+  count_launch(c);
+  GBHF_CUDA(c, cudaGetLastError());
+  GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
+  return GBHF_OK;
+}
+
+}  // namespace gbhf

@@ -1,0 +1,800 @@
+// GENERATED by gen_eri.py -- do not edit by hand.
+#pragma once
+
+// ---- class (ss|ss): 1x1 integrals, L = 0
+template <typename T, typename Acc>
+__device__ __forceinline__ void eri_ketprim_ssss(const T* __restrict__ sb, int nbra,
+    const T q, const T invq, const T Qx, const T Qy, const T Qz,
+    const T QCx, const T QCy, const T QCz, const T QDx, const T QDy, const T QDz,
+    const T Kcd, const T* __restrict__ boys, Acc& acc) {
+  const T ONE = T(1);
+  (void)QCx; (void)QCy; (void)QCz; (void)QDx; (void)QDy; (void)QDz;
+  const T hq = T(0.5) * invq;
+  const T ekp00_000 = ONE;
+  #pragma unroll 1
+  for (int kb = 0; kb < nbra; ++kb) {
+    const T p = sb[BRA_P * BRA_STRIDE + kb], invp = sb[BRA_INVP * BRA_STRIDE + kb];
+    const T Px = sb[BRA_PX * BRA_STRIDE + kb], Py = sb[BRA_PY * BRA_STRIDE + kb], Pz = sb[BRA_PZ * BRA_STRIDE + kb];
+    const T Kab = sb[BRA_K * BRA_STRIDE + kb];
+    const T X = Px - Qx, Y = Py - Qy, Z = Pz - Qz;
+    const T ppq = p + q;
+    const T rs = rsqrt_t(ppq);
+    const T alpha = p * q * (rs * rs);
+    const T Tb = alpha * (X * X + Y * Y + Z * Z);
+    const T pref = T(TWO_PI_2P5) * Kab * Kcd * invp * invq * rs;
+    T F[1];
+    boys_eval<T, 0>(Tb, boys, F);
+    const T m2a = T(-2) * alpha;
+    T scale = pref;
+    const T R0_000 = scale * F[0];
+    const T hp = T(0.5) * invp;
+    {
+      const T W_000 = ekp00_000 * R0_000;
+      acc[0] += W_000;
+    }
+  }
+}
+
+// ---- class (ps|ss): 3x1 integrals, L = 1
+template <typename T, typename Acc>
+__device__ __forceinline__ void eri_ketprim_psss(const T* __restrict__ sb, int nbra,
+    const T q, const T invq, const T Qx, const T Qy, const T Qz,
+    const T QCx, const T QCy, const T QCz, const T QDx, const T QDy, const T QDz,
+    const T Kcd, const T* __restrict__ boys, Acc& acc) {
+  const T ONE = T(1);
+  (void)QCx; (void)QCy; (void)QCz; (void)QDx; (void)QDy; (void)QDz;
+  const T hq = T(0.5) * invq;
+  const T ekp00_000 = ONE;
+  #pragma unroll 1
+  for (int kb = 0; kb < nbra; ++kb) {
+    const T p = sb[BRA_P * BRA_STRIDE + kb], invp = sb[BRA_INVP * BRA_STRIDE + kb];
+    const T Px = sb[BRA_PX * BRA_STRIDE + kb], Py = sb[BRA_PY * BRA_STRIDE + kb], Pz = sb[BRA_PZ * BRA_STRIDE + kb];
+    const T PAx = sb[BRA_PAX * BRA_STRIDE + kb], PAy = sb[BRA_PAY * BRA_STRIDE + kb], PAz = sb[BRA_PAZ * BRA_STRIDE + kb];
+    const T Kab = sb[BRA_K * BRA_STRIDE + kb];
+    const T X = Px - Qx, Y = Py - Qy, Z = Pz - Qz;
+    const T ppq = p + q;
+    const T rs = rsqrt_t(ppq);
+    const T alpha = p * q * (rs * rs);
+    const T Tb = alpha * (X * X + Y * Y + Z * Z);
+    const T pref = T(TWO_PI_2P5) * Kab * Kcd * invp * invq * rs;
+    T F[2];
+    boys_eval<T, 1>(Tb, boys, F);
+    const T m2a = T(-2) * alpha;
+    T scale = pref;
+    const T R0_000 = scale * F[0];
+    scale *= m2a;
+    const T R1_000 = scale * F[1];
+    const T R0_001 = Z * R1_000;
+    const T R0_010 = Y * R1_000;
+    const T R0_100 = X * R1_000;
+    const T hp = T(0.5) * invp;
+    const T ebx100 = PAx;
+    const T ebx101 = hp * (ONE);
+    const T eby100 = PAy;
+    const T eby101 = hp * (ONE);
+    const T ebz100 = PAz;
+    const T ebz101 = hp * (ONE);
+    {
+      const T W_000 = ekp00_000 * R0_000;
+      const T W_001 = ekp00_000 * R0_001;
+      const T W_010 = ekp00_000 * R0_010;
+      const T W_100 = ekp00_000 * R0_100;
+      acc[0] += fma_t(ebx101, W_100, ebx100 * W_000);
+      acc[1] += fma_t(eby101, W_010, eby100 * W_000);
+      acc[2] += fma_t(ebz101, W_001, ebz100 * W_000);
+    }
+  }
+}
+
+// ---- class (ps|ps): 3x3 integrals, L = 2
+template <typename T, typename Acc>
+__device__ __forceinline__ void eri_ketprim_psps(const T* __restrict__ sb, int nbra,
+    const T q, const T invq, const T Qx, const T Qy, const T Qz,
+    const T QCx, const T QCy, const T QCz, const T QDx, const T QDy, const T QDz,
+    const T Kcd, const T* __restrict__ boys, Acc& acc) {
+  const T ONE = T(1);
+  (void)QCx; (void)QCy; (void)QCz; (void)QDx; (void)QDy; (void)QDz;
+  const T hq = T(0.5) * invq;
+  const T ekx100 = QCx;
+  const T ekx101 = hq * (ONE);
+  const T eky100 = QCy;
+  const T eky101 = hq * (ONE);
+  const T ekz100 = QCz;
+  const T ekz101 = hq * (ONE);
+  const T ekp00_000 = ekx100;
+  const T ekp00_100 = -(ekx101);
+  const T ekp10_000 = eky100;
+  const T ekp10_010 = -(eky101);
+  const T ekp20_000 = ekz100;
+  const T ekp20_001 = -(ekz101);
+  #pragma unroll 1
+  for (int kb = 0; kb < nbra; ++kb) {
+    const T p = sb[BRA_P * BRA_STRIDE + kb], invp = sb[BRA_INVP * BRA_STRIDE + kb];
+    const T Px = sb[BRA_PX * BRA_STRIDE + kb], Py = sb[BRA_PY * BRA_STRIDE + kb], Pz = sb[BRA_PZ * BRA_STRIDE + kb];
+    const T PAx = sb[BRA_PAX * BRA_STRIDE + kb], PAy = sb[BRA_PAY * BRA_STRIDE + kb], PAz = sb[BRA_PAZ * BRA_STRIDE + kb];
+    const T Kab = sb[BRA_K * BRA_STRIDE + kb];
+    const T X = Px - Qx, Y = Py - Qy, Z = Pz - Qz;
+    const T ppq = p + q;
+    const T rs = rsqrt_t(ppq);
+    const T alpha = p * q * (rs * rs);
+    const T Tb = alpha * (X * X + Y * Y + Z * Z);
+    const T pref = T(TWO_PI_2P5) * Kab * Kcd * invp * invq * rs;
+    T F[3];
+    boys_eval<T, 2>(Tb, boys, F);
+    const T m2a = T(-2) * alpha;
+    T scale = pref;
+    const T R0_000 = scale * F[0];
+    scale *= m2a;
+    const T R1_000 = scale * F[1];
+    scale *= m2a;
+    const T R2_000 = scale * F[2];
+    const T R0_001 = Z * R1_000;
+    const T R0_010 = Y * R1_000;
+    const T R0_100 = X * R1_000;
+    const T R1_001 = Z * R2_000;
+    const T R0_002 = R1_000 + Z * R1_001;
+    const T R0_011 = Y * R1_001;
+    const T R1_010 = Y * R2_000;
+    const T R0_020 = R1_000 + Y * R1_010;
+    const T R0_101 = X * R1_001;
+    const T R0_110 = X * R1_010;
+    const T R1_100 = X * R2_000;
+    const T R0_200 = R1_000 + X * R1_100;
+    const T hp = T(0.5) * invp;
+    const T ebx100 = PAx;
+    const T ebx101 = hp * (ONE);
+    const T eby100 = PAy;
+    const T eby101 = hp * (ONE);
+    const T ebz100 = PAz;
+    const T ebz101 = hp * (ONE);
+    {
+      const T W_000 = fma_t(ekp00_100, R0_100, ekp00_000 * R0_000);
+      const T W_001 = fma_t(ekp00_100, R0_101, ekp00_000 * R0_001);
+      const T W_010 = fma_t(ekp00_100, R0_110, ekp00_000 * R0_010);
+      const T W_100 = fma_t(ekp00_100, R0_200, ekp00_000 * R0_100);
+      acc[0] += fma_t(ebx101, W_100, ebx100 * W_000);
+      acc[3] += fma_t(eby101, W_010, eby100 * W_000);
+      acc[6] += fma_t(ebz101, W_001, ebz100 * W_000);
+    }
+    {
+      const T W_000 = fma_t(ekp10_010, R0_010, ekp10_000 * R0_000);
+      const T W_001 = fma_t(ekp10_010, R0_011, ekp10_000 * R0_001);
+      const T W_010 = fma_t(ekp10_010, R0_020, ekp10_000 * R0_010);
+      const T W_100 = fma_t(ekp10_010, R0_110, ekp10_000 * R0_100);
+      acc[1] += fma_t(ebx101, W_100, ebx100 * W_000);
+      acc[4] += fma_t(eby101, W_010, eby100 * W_000);
+      acc[7] += fma_t(ebz101, W_001, ebz100 * W_000);
+    }
+    {
+      const T W_000 = fma_t(ekp20_001, R0_001, ekp20_000 * R0_000);
+      const T W_001 = fma_t(ekp20_001, R0_002, ekp20_000 * R0_001);
+      const T W_010 = fma_t(ekp20_001, R0_011, ekp20_000 * R0_010);
+      const T W_100 = fma_t(ekp20_001, R0_101, ekp20_000 * R0_100);
+      acc[2] += fma_t(ebx101, W_100, ebx100 * W_000);
+      acc[5] += fma_t(eby101, W_010, eby100 * W_000);
+      acc[8] += fma_t(ebz101, W_001, ebz100 * W_000);
+    }
+  }
+}
+
+// ---- class (pp|ss): 9x1 integrals, L = 2
+template <typename T, typename Acc>
+__device__ __forceinline__ void eri_ketprim_ppss(const T* __restrict__ sb, int nbra,
+    const T q, const T invq, const T Qx, const T Qy, const T Qz,
+    const T QCx, const T QCy, const T QCz, const T QDx, const T QDy, const T QDz,
+    const T Kcd, const T* __restrict__ boys, Acc& acc) {
+  const T ONE = T(1);
+  (void)QCx; (void)QCy; (void)QCz; (void)QDx; (void)QDy; (void)QDz;
+  const T hq = T(0.5) * invq;
+  const T ekp00_000 = ONE;
+  #pragma unroll 1
+  for (int kb = 0; kb < nbra; ++kb) {
+    const T p = sb[BRA_P * BRA_STRIDE + kb], invp = sb[BRA_INVP * BRA_STRIDE + kb];
+    const T Px = sb[BRA_PX * BRA_STRIDE + kb], Py = sb[BRA_PY * BRA_STRIDE + kb], Pz = sb[BRA_PZ * BRA_STRIDE + kb];
+    const T PAx = sb[BRA_PAX * BRA_STRIDE + kb], PAy = sb[BRA_PAY * BRA_STRIDE + kb], PAz = sb[BRA_PAZ * BRA_STRIDE + kb];
+    const T PBx = sb[BRA_PBX * BRA_STRIDE + kb], PBy = sb[BRA_PBY * BRA_STRIDE + kb], PBz = sb[BRA_PBZ * BRA_STRIDE + kb];
+    const T Kab = sb[BRA_K * BRA_STRIDE + kb];
+    const T X = Px - Qx, Y = Py - Qy, Z = Pz - Qz;
+    const T ppq = p + q;
+    const T rs = rsqrt_t(ppq);
+    const T alpha = p * q * (rs * rs);
+    const T Tb = alpha * (X * X + Y * Y + Z * Z);
+    const T pref = T(TWO_PI_2P5) * Kab * Kcd * invp * invq * rs;
+    T F[3];
+    boys_eval<T, 2>(Tb, boys, F);
+    const T m2a = T(-2) * alpha;
+    T scale = pref;
+    const T R0_000 = scale * F[0];
+    scale *= m2a;
+    const T R1_000 = scale * F[1];
+    scale *= m2a;
+    const T R2_000 = scale * F[2];
+    const T R0_001 = Z * R1_000;
+    const T R0_010 = Y * R1_000;
+    const T R0_100 = X * R1_000;
+    const T R1_001 = Z * R2_000;
+    const T R0_002 = R1_000 + Z * R1_001;
+    const T R0_011 = Y * R1_001;
+    const T R1_010 = Y * R2_000;
+    const T R0_020 = R1_000 + Y * R1_010;
+    const T R0_101 = X * R1_001;
+    const T R0_110 = X * R1_010;
+    const T R1_100 = X * R2_000;
+    const T R0_200 = R1_000 + X * R1_100;
+    const T hp = T(0.5) * invp;
+    const T ebx010 = PBx;
+    const T ebx011 = hp * (ONE);
+    const T ebx100 = PAx;
+    const T ebx101 = hp * (ONE);
+    const T ebx110 = PAx * ebx010 + ebx011;
+    const T ebx111 = hp * (ebx010 + ebx100);
+    const T ebx112 = (hp * T(0.5)) * (ebx011 + ebx101);
+    const T eby010 = PBy;
+    const T eby011 = hp * (ONE);
+    const T eby100 = PAy;
+    const T eby101 = hp * (ONE);
+    const T eby110 = PAy * eby010 + eby011;
+    const T eby111 = hp * (eby010 + eby100);
+    const T eby112 = (hp * T(0.5)) * (eby011 + eby101);
+    const T ebz010 = PBz;
+    const T ebz011 = hp * (ONE);
+    const T ebz100 = PAz;
+    const T ebz101 = hp * (ONE);
+    const T ebz110 = PAz * ebz010 + ebz011;
+    const T ebz111 = hp * (ebz010 + ebz100);
+    const T ebz112 = (hp * T(0.5)) * (ebz011 + ebz101);
+    {
+      const T W_000 = ekp00_000 * R0_000;
+      const T W_001 = ekp00_000 * R0_001;
+      const T W_010 = ekp00_000 * R0_010;
+      const T W_100 = ekp00_000 * R0_100;
+      const T W_002 = ekp00_000 * R0_002;
+      const T W_011 = ekp00_000 * R0_011;
+      const T W_020 = ekp00_000 * R0_020;
+      const T W_101 = ekp00_000 * R0_101;
+      const T W_110 = ekp00_000 * R0_110;
+      const T W_200 = ekp00_000 * R0_200;
+      acc[0] += fma_t(ebx112, W_200, fma_t(ebx111, W_100, ebx110 * W_000));
+      acc[1] += fma_t(ebx101 * eby011, W_110, fma_t(ebx101 * eby010, W_100, fma_t(ebx100 * eby011, W_010, ebx100 * eby010 * W_000)));
+      acc[2] += fma_t(ebx101 * ebz011, W_101, fma_t(ebx101 * ebz010, W_100, fma_t(ebx100 * ebz011, W_001, ebx100 * ebz010 * W_000)));
+      acc[3] += fma_t(ebx011 * eby101, W_110, fma_t(ebx011 * eby100, W_100, fma_t(ebx010 * eby101, W_010, ebx010 * eby100 * W_000)));
+      acc[4] += fma_t(eby112, W_020, fma_t(eby111, W_010, eby110 * W_000));
+      acc[5] += fma_t(eby101 * ebz011, W_011, fma_t(eby101 * ebz010, W_010, fma_t(eby100 * ebz011, W_001, eby100 * ebz010 * W_000)));
+      acc[6] += fma_t(ebx011 * ebz101, W_101, fma_t(ebx011 * ebz100, W_100, fma_t(ebx010 * ebz101, W_001, ebx010 * ebz100 * W_000)));
+      acc[7] += fma_t(eby011 * ebz101, W_011, fma_t(eby011 * ebz100, W_010, fma_t(eby010 * ebz101, W_001, eby010 * ebz100 * W_000)));
+      acc[8] += fma_t(ebz112, W_002, fma_t(ebz111, W_001, ebz110 * W_000));
+    }
+  }
+}
+
+// ---- class (pp|ps): 9x3 integrals, L = 3
+template <typename T, typename Acc>
+__device__ __forceinline__ void eri_ketprim_ppps(const T* __restrict__ sb, int nbra,
+    const T q, const T invq, const T Qx, const T Qy, const T Qz,
+    const T QCx, const T QCy, const T QCz, const T QDx, const T QDy, const T QDz,
+    const T Kcd, const T* __restrict__ boys, Acc& acc) {
+  const T ONE = T(1);
+  (void)QCx; (void)QCy; (void)QCz; (void)QDx; (void)QDy; (void)QDz;
+  const T hq = T(0.5) * invq;
+  const T ekx100 = QCx;
+  const T ekx101 = hq * (ONE);
+  const T eky100 = QCy;
+  const T eky101 = hq * (ONE);
+  const T ekz100 = QCz;
+  const T ekz101 = hq * (ONE);
+  const T ekp00_000 = ekx100;
+  const T ekp00_100 = -(ekx101);
+  const T ekp10_000 = eky100;
+  const T ekp10_010 = -(eky101);
+  const T ekp20_000 = ekz100;
+  const T ekp20_001 = -(ekz101);
+  #pragma unroll 1
+  for (int kb = 0; kb < nbra; ++kb) {
+    const T p = sb[BRA_P * BRA_STRIDE + kb], invp = sb[BRA_INVP * BRA_STRIDE + kb];
+    const T Px = sb[BRA_PX * BRA_STRIDE + kb], Py = sb[BRA_PY * BRA_STRIDE + kb], Pz = sb[BRA_PZ * BRA_STRIDE + kb];
+    const T PAx = sb[BRA_PAX * BRA_STRIDE + kb], PAy = sb[BRA_PAY * BRA_STRIDE + kb], PAz = sb[BRA_PAZ * BRA_STRIDE + kb];
+    const T PBx = sb[BRA_PBX * BRA_STRIDE + kb], PBy = sb[BRA_PBY * BRA_STRIDE + kb], PBz = sb[BRA_PBZ * BRA_STRIDE + kb];
+    const T Kab = sb[BRA_K * BRA_STRIDE + kb];
+    const T X = Px - Qx, Y = Py - Qy, Z = Pz - Qz;
+    const T ppq = p + q;
+    const T rs = rsqrt_t(ppq);
+    const T alpha = p * q * (rs * rs);
+    const T Tb = alpha * (X * X + Y * Y + Z * Z);
+    const T pref = T(TWO_PI_2P5) * Kab * Kcd * invp * invq * rs;
+    T F[4];
+    boys_eval<T, 3>(Tb, boys, F);
+    const T m2a = T(-2) * alpha;
+    T scale = pref;
+    const T R0_000 = scale * F[0];
+    scale *= m2a;
+    const T R1_000 = scale * F[1];
+    scale *= m2a;
+    const T R2_000 = scale * F[2];
+    scale *= m2a;
+    const T R3_000 = scale * F[3];
+    const T R0_001 = Z * R1_000;
+    const T R0_010 = Y * R1_000;
+    const T R0_100 = X * R1_000;
+    const T R1_001 = Z * R2_000;
+    const T R0_002 = R1_000 + Z * R1_001;
+    const T R0_011 = Y * R1_001;
+    const T R1_010 = Y * R2_000;
+    const T R0_020 = R1_000 + Y * R1_010;
+    const T R0_101 = X * R1_001;
+    const T R0_110 = X * R1_010;
+    const T R1_100 = X * R2_000;
+    const T R0_200 = R1_000 + X * R1_100;
+    const T R2_001 = Z * R3_000;
+    const T R1_002 = R2_000 + Z * R2_001;
+    const T R0_003 = T(2) * R1_001 + Z * R1_002;
+    const T R0_012 = Y * R1_002;
+    const T R1_011 = Y * R2_001;
+    const T R0_021 = R1_001 + Y * R1_011;
+    const T R2_010 = Y * R3_000;
+    const T R1_020 = R2_000 + Y * R2_010;
+    const T R0_030 = T(2) * R1_010 + Y * R1_020;
+    const T R0_102 = X * R1_002;
+    const T R0_111 = X * R1_011;
+    const T R0_120 = X * R1_020;
+    const T R1_101 = X * R2_001;
+    const T R0_201 = R1_001 + X * R1_101;
+    const T R1_110 = X * R2_010;
+    const T R0_210 = R1_010 + X * R1_110;
+    const T R2_100 = X * R3_000;
+    const T R1_200 = R2_000 + X * R2_100;
+    const T R0_300 = T(2) * R1_100 + X * R1_200;
+    const T hp = T(0.5) * invp;
+    const T ebx010 = PBx;
+    const T ebx011 = hp * (ONE);
+    const T ebx100 = PAx;
+    const T ebx101 = hp * (ONE);
+    const T ebx110 = PAx * ebx010 + ebx011;
+    const T ebx111 = hp * (ebx010 + ebx100);
+    const T ebx112 = (hp * T(0.5)) * (ebx011 + ebx101);
+    const T eby010 = PBy;
+    const T eby011 = hp * (ONE);
+    const T eby100 = PAy;
+    const T eby101 = hp * (ONE);
+    const T eby110 = PAy * eby010 + eby011;
+    const T eby111 = hp * (eby010 + eby100);
+    const T eby112 = (hp * T(0.5)) * (eby011 + eby101);
+    const T ebz010 = PBz;
+    const T ebz011 = hp * (ONE);
+    const T ebz100 = PAz;
+    const T ebz101 = hp * (ONE);
+    const T ebz110 = PAz * ebz010 + ebz011;
+    const T ebz111 = hp * (ebz010 + ebz100);
+    const T ebz112 = (hp * T(0.5)) * (ebz011 + ebz101);
+    {
+      const T W_000 = fma_t(ekp00_100, R0_100, ekp00_000 * R0_000);
+      const T W_001 = fma_t(ekp00_100, R0_101, ekp00_000 * R0_001);
+      const T W_010 = fma_t(ekp00_100, R0_110, ekp00_000 * R0_010);
+      const T W_100 = fma_t(ekp00_100, R0_200, ekp00_000 * R0_100);
+      const T W_002 = fma_t(ekp00_100, R0_102, ekp00_000 * R0_002);
+      const T W_011 = fma_t(ekp00_100, R0_111, ekp00_000 * R0_011);
+      const T W_020 = fma_t(ekp00_100, R0_120, ekp00_000 * R0_020);
+      const T W_101 = fma_t(ekp00_100, R0_201, ekp00_000 * R0_101);
+      const T W_110 = fma_t(ekp00_100, R0_210, ekp00_000 * R0_110);
+      const T W_200 = fma_t(ekp00_100, R0_300, ekp00_000 * R0_200);
+      acc[0] += fma_t(ebx112, W_200, fma_t(ebx111, W_100, ebx110 * W_000));
+      acc[3] += fma_t(ebx101 * eby011, W_110, fma_t(ebx101 * eby010, W_100, fma_t(ebx100 * eby011, W_010, ebx100 * eby010 * W_000)));
+      acc[6] += fma_t(ebx101 * ebz011, W_101, fma_t(ebx101 * ebz010, W_100, fma_t(ebx100 * ebz011, W_001, ebx100 * ebz010 * W_000)));
+      acc[9] += fma_t(ebx011 * eby101, W_110, fma_t(ebx011 * eby100, W_100, fma_t(ebx010 * eby101, W_010, ebx010 * eby100 * W_000)));
+      acc[12] += fma_t(eby112, W_020, fma_t(eby111, W_010, eby110 * W_000));
+      acc[15] += fma_t(eby101 * ebz011, W_011, fma_t(eby101 * ebz010, W_010, fma_t(eby100 * ebz011, W_001, eby100 * ebz010 * W_000)));
+      acc[18] += fma_t(ebx011 * ebz101, W_101, fma_t(ebx011 * ebz100, W_100, fma_t(ebx010 * ebz101, W_001, ebx010 * ebz100 * W_000)));
+      acc[21] += fma_t(eby011 * ebz101, W_011, fma_t(eby011 * ebz100, W_010, fma_t(eby010 * ebz101, W_001, eby010 * ebz100 * W_000)));
+      acc[24] += fma_t(ebz112, W_002, fma_t(ebz111, W_001, ebz110 * W_000));
+    }
+    {
+      const T W_000 = fma_t(ekp10_010, R0_010, ekp10_000 * R0_000);
+      const T W_001 = fma_t(ekp10_010, R0_011, ekp10_000 * R0_001);
+      const T W_010 = fma_t(ekp10_010, R0_020, ekp10_000 * R0_010);
+      const T W_100 = fma_t(ekp10_010, R0_110, ekp10_000 * R0_100);
+      const T W_002 = fma_t(ekp10_010, R0_012, ekp10_000 * R0_002);
+      const T W_011 = fma_t(ekp10_010, R0_021, ekp10_000 * R0_011);
+      const T W_020 = fma_t(ekp10_010, R0_030, ekp10_000 * R0_020);
+      const T W_101 = fma_t(ekp10_010, R0_111, ekp10_000 * R0_101);
+      const T W_110 = fma_t(ekp10_010, R0_120, ekp10_000 * R0_110);
+      const T W_200 = fma_t(ekp10_010, R0_210, ekp10_000 * R0_200);
+      acc[1] += fma_t(ebx112, W_200, fma_t(ebx111, W_100, ebx110 * W_000));
+      acc[4] += fma_t(ebx101 * eby011, W_110, fma_t(ebx101 * eby010, W_100, fma_t(ebx100 * eby011, W_010, ebx100 * eby010 * W_000)));
+      acc[7] += fma_t(ebx101 * ebz011, W_101, fma_t(ebx101 * ebz010, W_100, fma_t(ebx100 * ebz011, W_001, ebx100 * ebz010 * W_000)));
+      acc[10] += fma_t(ebx011 * eby101, W_110, fma_t(ebx011 * eby100, W_100, fma_t(ebx010 * eby101, W_010, ebx010 * eby100 * W_000)));
+      acc[13] += fma_t(eby112, W_020, fma_t(eby111, W_010, eby110 * W_000));
+      acc[16] += fma_t(eby101 * ebz011, W_011, fma_t(eby101 * ebz010, W_010, fma_t(eby100 * ebz011, W_001, eby100 * ebz010 * W_000)));
+      acc[19] += fma_t(ebx011 * ebz101, W_101, fma_t(ebx011 * ebz100, W_100, fma_t(ebx010 * ebz101, W_001, ebx010 * ebz100 * W_000)));
+      acc[22] += fma_t(eby011 * ebz101, W_011, fma_t(eby011 * ebz100, W_010, fma_t(eby010 * ebz101, W_001, eby010 * ebz100 * W_000)));
+      acc[25] += fma_t(ebz112, W_002, fma_t(ebz111, W_001, ebz110 * W_000));
+    }
+    {
+      const T W_000 = fma_t(ekp20_001, R0_001, ekp20_000 * R0_000);
+      const T W_001 = fma_t(ekp20_001, R0_002, ekp20_000 * R0_001);
+      const T W_010 = fma_t(ekp20_001, R0_011, ekp20_000 * R0_010);
+      const T W_100 = fma_t(ekp20_001, R0_101, ekp20_000 * R0_100);
+      const T W_002 = fma_t(ekp20_001, R0_003, ekp20_000 * R0_002);
+      const T W_011 = fma_t(ekp20_001, R0_012, ekp20_000 * R0_011);
+      const T W_020 = fma_t(ekp20_001, R0_021, ekp20_000 * R0_020);
+      const T W_101 = fma_t(ekp20_001, R0_102, ekp20_000 * R0_101);
+      const T W_110 = fma_t(ekp20_001, R0_111, ekp20_000 * R0_110);
+      const T W_200 = fma_t(ekp20_001, R0_201, ekp20_000 * R0_200);
+      acc[2] += fma_t(ebx112, W_200, fma_t(ebx111, W_100, ebx110 * W_000));
+      acc[5] += fma_t(ebx101 * eby011, W_110, fma_t(ebx101 * eby010, W_100, fma_t(ebx100 * eby011, W_010, ebx100 * eby010 * W_000)));
+      acc[8] += fma_t(ebx101 * ebz011, W_101, fma_t(ebx101 * ebz010, W_100, fma_t(ebx100 * ebz011, W_001, ebx100 * ebz010 * W_000)));
+      acc[11] += fma_t(ebx011 * eby101, W_110, fma_t(ebx011 * eby100, W_100, fma_t(ebx010 * eby101, W_010, ebx010 * eby100 * W_000)));
+      acc[14] += fma_t(eby112, W_020, fma_t(eby111, W_010, eby110 * W_000));
+      acc[17] += fma_t(eby101 * ebz011, W_011, fma_t(eby101 * ebz010, W_010, fma_t(eby100 * ebz011, W_001, eby100 * ebz010 * W_000)));
+      acc[20] += fma_t(ebx011 * ebz101, W_101, fma_t(ebx011 * ebz100, W_100, fma_t(ebx010 * ebz101, W_001, ebx010 * ebz100 * W_000)));
+      acc[23] += fma_t(eby011 * ebz101, W_011, fma_t(eby011 * ebz100, W_010, fma_t(eby010 * ebz101, W_001, eby010 * ebz100 * W_000)));
+      acc[26] += fma_t(ebz112, W_002, fma_t(ebz111, W_001, ebz110 * W_000));
+    }
+  }
+}
+
+// ---- class (pp|pp): 9x9 integrals, L = 4
+template <typename T, typename Acc>
+__device__ __forceinline__ void eri_ketprim_pppp(const T* __restrict__ sb, int nbra,
+    const T q, const T invq, const T Qx, const T Qy, const T Qz,
+    const T QCx, const T QCy, const T QCz, const T QDx, const T QDy, const T QDz,
+    const T Kcd, const T* __restrict__ boys, Acc& acc) {
+  const T ONE = T(1);
+  (void)QCx; (void)QCy; (void)QCz; (void)QDx; (void)QDy; (void)QDz;
+  const T hq = T(0.5) * invq;
+  const T ekx010 = QDx;
+  const T ekx011 = hq * (ONE);
+  const T ekx100 = QCx;
+  const T ekx101 = hq * (ONE);
+  const T ekx110 = QCx * ekx010 + ekx011;
+  const T ekx111 = hq * (ekx010 + ekx100);
+  const T ekx112 = (hq * T(0.5)) * (ekx011 + ekx101);
+  const T eky010 = QDy;
+  const T eky011 = hq * (ONE);
+  const T eky100 = QCy;
+  const T eky101 = hq * (ONE);
+  const T eky110 = QCy * eky010 + eky011;
+  const T eky111 = hq * (eky010 + eky100);
+  const T eky112 = (hq * T(0.5)) * (eky011 + eky101);
+  const T ekz010 = QDz;
+  const T ekz011 = hq * (ONE);
+  const T ekz100 = QCz;
+  const T ekz101 = hq * (ONE);
+  const T ekz110 = QCz * ekz010 + ekz011;
+  const T ekz111 = hq * (ekz010 + ekz100);
+  const T ekz112 = (hq * T(0.5)) * (ekz011 + ekz101);
+  const T ekp00_000 = ekx110;
+  const T ekp00_100 = -(ekx111);
+  const T ekp00_200 = ekx112;
+  const T ekp01_000 = ekx100 * eky010;
+  const T ekp01_010 = -(ekx100 * eky011);
+  const T ekp01_100 = -(ekx101 * eky010);
+  const T ekp01_110 = ekx101 * eky011;
+  const T ekp02_000 = ekx100 * ekz010;
+  const T ekp02_001 = -(ekx100 * ekz011);
+  const T ekp02_100 = -(ekx101 * ekz010);
+  const T ekp02_101 = ekx101 * ekz011;
+  const T ekp10_000 = ekx010 * eky100;
+  const T ekp10_010 = -(ekx010 * eky101);
+  const T ekp10_100 = -(ekx011 * eky100);
+  const T ekp10_110 = ekx011 * eky101;
+  const T ekp11_000 = eky110;
+  const T ekp11_010 = -(eky111);
+  const T ekp11_020 = eky112;
+  const T ekp12_000 = eky100 * ekz010;
+  const T ekp12_001 = -(eky100 * ekz011);
+  const T ekp12_010 = -(eky101 * ekz010);
+  const T ekp12_011 = eky101 * ekz011;
+  const T ekp20_000 = ekx010 * ekz100;
+  const T ekp20_001 = -(ekx010 * ekz101);
+  const T ekp20_100 = -(ekx011 * ekz100);
+  const T ekp20_101 = ekx011 * ekz101;
+  const T ekp21_000 = eky010 * ekz100;
+  const T ekp21_001 = -(eky010 * ekz101);
+  const T ekp21_010 = -(eky011 * ekz100);
+  const T ekp21_011 = eky011 * ekz101;
+  const T ekp22_000 = ekz110;
+  const T ekp22_001 = -(ekz111);
+  const T ekp22_002 = ekz112;
+  #pragma unroll 1
+  for (int kb = 0; kb < nbra; ++kb) {
+    const T p = sb[BRA_P * BRA_STRIDE + kb], invp = sb[BRA_INVP * BRA_STRIDE + kb];
+    const T Px = sb[BRA_PX * BRA_STRIDE + kb], Py = sb[BRA_PY * BRA_STRIDE + kb], Pz = sb[BRA_PZ * BRA_STRIDE + kb];
+    const T PAx = sb[BRA_PAX * BRA_STRIDE + kb], PAy = sb[BRA_PAY * BRA_STRIDE + kb], PAz = sb[BRA_PAZ * BRA_STRIDE + kb];
+    const T PBx = sb[BRA_PBX * BRA_STRIDE + kb], PBy = sb[BRA_PBY * BRA_STRIDE + kb], PBz = sb[BRA_PBZ * BRA_STRIDE + kb];
+    const T Kab = sb[BRA_K * BRA_STRIDE + kb];
+    const T X = Px - Qx, Y = Py - Qy, Z = Pz - Qz;
+    const T ppq = p + q;
+    const T rs = rsqrt_t(ppq);
+    const T alpha = p * q * (rs * rs);
+    const T Tb = alpha * (X * X + Y * Y + Z * Z);
+    const T pref = T(TWO_PI_2P5) * Kab * Kcd * invp * invq * rs;
+    T F[5];
+    boys_eval<T, 4>(Tb, boys, F);
+    const T m2a = T(-2) * alpha;
+    T scale = pref;
+    const T R0_000 = scale * F[0];
+    scale *= m2a;
+    const T R1_000 = scale * F[1];
+    scale *= m2a;
+    const T R2_000 = scale * F[2];
+    scale *= m2a;
+    const T R3_000 = scale * F[3];
+    scale *= m2a;
+    const T R4_000 = scale * F[4];
+    const T R0_001 = Z * R1_000;
+    const T R0_010 = Y * R1_000;
+    const T R0_100 = X * R1_000;
+    const T R1_001 = Z * R2_000;
+    const T R0_002 = R1_000 + Z * R1_001;
+    const T R0_011 = Y * R1_001;
+    const T R1_010 = Y * R2_000;
+    const T R0_020 = R1_000 + Y * R1_010;
+    const T R0_101 = X * R1_001;
+    const T R0_110 = X * R1_010;
+    const T R1_100 = X * R2_000;
+    const T R0_200 = R1_000 + X * R1_100;
+    const T R2_001 = Z * R3_000;
+    const T R1_002 = R2_000 + Z * R2_001;
+    const T R0_003 = T(2) * R1_001 + Z * R1_002;
+    const T R0_012 = Y * R1_002;
+    const T R1_011 = Y * R2_001;
+    const T R0_021 = R1_001 + Y * R1_011;
+    const T R2_010 = Y * R3_000;
+    const T R1_020 = R2_000 + Y * R2_010;
+    const T R0_030 = T(2) * R1_010 + Y * R1_020;
+    const T R0_102 = X * R1_002;
+    const T R0_111 = X * R1_011;
+    const T R0_120 = X * R1_020;
+    const T R1_101 = X * R2_001;
+    const T R0_201 = R1_001 + X * R1_101;
+    const T R1_110 = X * R2_010;
+    const T R0_210 = R1_010 + X * R1_110;
+    const T R2_100 = X * R3_000;
+    const T R1_200 = R2_000 + X * R2_100;
+    const T R0_300 = T(2) * R1_100 + X * R1_200;
+    const T R3_001 = Z * R4_000;
+    const T R2_002 = R3_000 + Z * R3_001;
+    const T R1_003 = T(2) * R2_001 + Z * R2_002;
+    const T R0_004 = T(3) * R1_002 + Z * R1_003;
+    const T R0_013 = Y * R1_003;
+    const T R1_012 = Y * R2_002;
+    const T R0_022 = R1_002 + Y * R1_012;
+    const T R2_011 = Y * R3_001;
+    const T R1_021 = R2_001 + Y * R2_011;
+    const T R0_031 = T(2) * R1_011 + Y * R1_021;
+    const T R3_010 = Y * R4_000;
+    const T R2_020 = R3_000 + Y * R3_010;
+    const T R1_030 = T(2) * R2_010 + Y * R2_020;
+    const T R0_040 = T(3) * R1_020 + Y * R1_030;
+    const T R0_103 = X * R1_003;
+    const T R0_112 = X * R1_012;
+    const T R0_121 = X * R1_021;
+    const T R0_130 = X * R1_030;
+    const T R1_102 = X * R2_002;
+    const T R0_202 = R1_002 + X * R1_102;
+    const T R1_111 = X * R2_011;
+    const T R0_211 = R1_011 + X * R1_111;
+    const T R1_120 = X * R2_020;
+    const T R0_220 = R1_020 + X * R1_120;
+    const T R2_101 = X * R3_001;
+    const T R1_201 = R2_001 + X * R2_101;
+    const T R0_301 = T(2) * R1_101 + X * R1_201;
+    const T R2_110 = X * R3_010;
+    const T R1_210 = R2_010 + X * R2_110;
+    const T R0_310 = T(2) * R1_110 + X * R1_210;
+    const T R3_100 = X * R4_000;
+    const T R2_200 = R3_000 + X * R3_100;
+    const T R1_300 = T(2) * R2_100 + X * R2_200;
+    const T R0_400 = T(3) * R1_200 + X * R1_300;
+    const T hp = T(0.5) * invp;
+    const T ebx010 = PBx;
+    const T ebx011 = hp * (ONE);
+    const T ebx100 = PAx;
+    const T ebx101 = hp * (ONE);
+    const T ebx110 = PAx * ebx010 + ebx011;
+    const T ebx111 = hp * (ebx010 + ebx100);
+    const T ebx112 = (hp * T(0.5)) * (ebx011 + ebx101);
+    const T eby010 = PBy;
+    const T eby011 = hp * (ONE);
+    const T eby100 = PAy;
+    const T eby101 = hp * (ONE);
+    const T eby110 = PAy * eby010 + eby011;
+    const T eby111 = hp * (eby010 + eby100);
+    const T eby112 = (hp * T(0.5)) * (eby011 + eby101);
+    const T ebz010 = PBz;
+    const T ebz011 = hp * (ONE);
+    const T ebz100 = PAz;
+    const T ebz101 = hp * (ONE);
+    const T ebz110 = PAz * ebz010 + ebz011;
+    const T ebz111 = hp * (ebz010 + ebz100);
+    const T ebz112 = (hp * T(0.5)) * (ebz011 + ebz101);
+    {
+      const T W_000 = fma_t(ekp00_200, R0_200, fma_t(ekp00_100, R0_100, ekp00_000 * R0_000));
+      const T W_001 = fma_t(ekp00_200, R0_201, fma_t(ekp00_100, R0_101, ekp00_000 * R0_001));
+      const T W_010 = fma_t(ekp00_200, R0_210, fma_t(ekp00_100, R0_110, ekp00_000 * R0_010));
+      const T W_100 = fma_t(ekp00_200, R0_300, fma_t(ekp00_100, R0_200, ekp00_000 * R0_100));
+      const T W_002 = fma_t(ekp00_200, R0_202, fma_t(ekp00_100, R0_102, ekp00_000 * R0_002));
+      const T W_011 = fma_t(ekp00_200, R0_211, fma_t(ekp00_100, R0_111, ekp00_000 * R0_011));
+      const T W_020 = fma_t(ekp00_200, R0_220, fma_t(ekp00_100, R0_120, ekp00_000 * R0_020));
+      const T W_101 = fma_t(ekp00_200, R0_301, fma_t(ekp00_100, R0_201, ekp00_000 * R0_101));
+      const T W_110 = fma_t(ekp00_200, R0_310, fma_t(ekp00_100, R0_210, ekp00_000 * R0_110));
+      const T W_200 = fma_t(ekp00_200, R0_400, fma_t(ekp00_100, R0_300, ekp00_000 * R0_200));
+      acc[0] += fma_t(ebx112, W_200, fma_t(ebx111, W_100, ebx110 * W_000));
+      acc[9] += fma_t(ebx101 * eby011, W_110, fma_t(ebx101 * eby010, W_100, fma_t(ebx100 * eby011, W_010, ebx100 * eby010 * W_000)));
+      acc[18] += fma_t(ebx101 * ebz011, W_101, fma_t(ebx101 * ebz010, W_100, fma_t(ebx100 * ebz011, W_001, ebx100 * ebz010 * W_000)));
+      acc[27] += fma_t(ebx011 * eby101, W_110, fma_t(ebx011 * eby100, W_100, fma_t(ebx010 * eby101, W_010, ebx010 * eby100 * W_000)));
+      acc[36] += fma_t(eby112, W_020, fma_t(eby111, W_010, eby110 * W_000));
+      acc[45] += fma_t(eby101 * ebz011, W_011, fma_t(eby101 * ebz010, W_010, fma_t(eby100 * ebz011, W_001, eby100 * ebz010 * W_000)));
+      acc[54] += fma_t(ebx011 * ebz101, W_101, fma_t(ebx011 * ebz100, W_100, fma_t(ebx010 * ebz101, W_001, ebx010 * ebz100 * W_000)));
+      acc[63] += fma_t(eby011 * ebz101, W_011, fma_t(eby011 * ebz100, W_010, fma_t(eby010 * ebz101, W_001, eby010 * ebz100 * W_000)));
+      acc[72] += fma_t(ebz112, W_002, fma_t(ebz111, W_001, ebz110 * W_000));
+    }
+    {
+      const T W_000 = fma_t(ekp01_110, R0_110, fma_t(ekp01_100, R0_100, fma_t(ekp01_010, R0_010, ekp01_000 * R0_000)));
+      const T W_001 = fma_t(ekp01_110, R0_111, fma_t(ekp01_100, R0_101, fma_t(ekp01_010, R0_011, ekp01_000 * R0_001)));
+      const T W_010 = fma_t(ekp01_110, R0_120, fma_t(ekp01_100, R0_110, fma_t(ekp01_010, R0_020, ekp01_000 * R0_010)));
+      const T W_100 = fma_t(ekp01_110, R0_210, fma_t(ekp01_100, R0_200, fma_t(ekp01_010, R0_110, ekp01_000 * R0_100)));
+      const T W_002 = fma_t(ekp01_110, R0_112, fma_t(ekp01_100, R0_102, fma_t(ekp01_010, R0_012, ekp01_000 * R0_002)));
+      const T W_011 = fma_t(ekp01_110, R0_121, fma_t(ekp01_100, R0_111, fma_t(ekp01_010, R0_021, ekp01_000 * R0_011)));
+      const T W_020 = fma_t(ekp01_110, R0_130, fma_t(ekp01_100, R0_120, fma_t(ekp01_010, R0_030, ekp01_000 * R0_020)));
+      const T W_101 = fma_t(ekp01_110, R0_211, fma_t(ekp01_100, R0_201, fma_t(ekp01_010, R0_111, ekp01_000 * R0_101)));
+      const T W_110 = fma_t(ekp01_110, R0_220, fma_t(ekp01_100, R0_210, fma_t(ekp01_010, R0_120, ekp01_000 * R0_110)));
+      const T W_200 = fma_t(ekp01_110, R0_310, fma_t(ekp01_100, R0_300, fma_t(ekp01_010, R0_210, ekp01_000 * R0_200)));
+      acc[1] += fma_t(ebx112, W_200, fma_t(ebx111, W_100, ebx110 * W_000));
+      acc[10] += fma_t(ebx101 * eby011, W_110, fma_t(ebx101 * eby010, W_100, fma_t(ebx100 * eby011, W_010, ebx100 * eby010 * W_000)));
+      acc[19] += fma_t(ebx101 * ebz011, W_101, fma_t(ebx101 * ebz010, W_100, fma_t(ebx100 * ebz011, W_001, ebx100 * ebz010 * W_000)));
+      acc[28] += fma_t(ebx011 * eby101, W_110, fma_t(ebx011 * eby100, W_100, fma_t(ebx010 * eby101, W_010, ebx010 * eby100 * W_000)));
+      acc[37] += fma_t(eby112, W_020, fma_t(eby111, W_010, eby110 * W_000));
+      acc[46] += fma_t(eby101 * ebz011, W_011, fma_t(eby101 * ebz010, W_010, fma_t(eby100 * ebz011, W_001, eby100 * ebz010 * W_000)));
+      acc[55] += fma_t(ebx011 * ebz101, W_101, fma_t(ebx011 * ebz100, W_100, fma_t(ebx010 * ebz101, W_001, ebx010 * ebz100 * W_000)));
+      acc[64] += fma_t(eby011 * ebz101, W_011, fma_t(eby011 * ebz100, W_010, fma_t(eby010 * ebz101, W_001, eby010 * ebz100 * W_000)));
+      acc[73] += fma_t(ebz112, W_002, fma_t(ebz111, W_001, ebz110 * W_000));
+    }
+    {
+      const T W_000 = fma_t(ekp02_101, R0_101, fma_t(ekp02_100, R0_100, fma_t(ekp02_001, R0_001, ekp02_000 * R0_000)));
+      const T W_001 = fma_t(ekp02_101, R0_102, fma_t(ekp02_100, R0_101, fma_t(ekp02_001, R0_002, ekp02_000 * R0_001)));
+      const T W_010 = fma_t(ekp02_101, R0_111, fma_t(ekp02_100, R0_110, fma_t(ekp02_001, R0_011, ekp02_000 * R0_010)));
+      const T W_100 = fma_t(ekp02_101, R0_201, fma_t(ekp02_100, R0_200, fma_t(ekp02_001, R0_101, ekp02_000 * R0_100)));
+      const T W_002 = fma_t(ekp02_101, R0_103, fma_t(ekp02_100, R0_102, fma_t(ekp02_001, R0_003, ekp02_000 * R0_002)));
+      const T W_011 = fma_t(ekp02_101, R0_112, fma_t(ekp02_100, R0_111, fma_t(ekp02_001, R0_012, ekp02_000 * R0_011)));
+      const T W_020 = fma_t(ekp02_101, R0_121, fma_t(ekp02_100, R0_120, fma_t(ekp02_001, R0_021, ekp02_000 * R0_020)));
+      const T W_101 = fma_t(ekp02_101, R0_202, fma_t(ekp02_100, R0_201, fma_t(ekp02_001, R0_102, ekp02_000 * R0_101)));
+      const T W_110 = fma_t(ekp02_101, R0_211, fma_t(ekp02_100, R0_210, fma_t(ekp02_001, R0_111, ekp02_000 * R0_110)));
+      const T W_200 = fma_t(ekp02_101, R0_301, fma_t(ekp02_100, R0_300, fma_t(ekp02_001, R0_201, ekp02_000 * R0_200)));
+      acc[2] += fma_t(ebx112, W_200, fma_t(ebx111, W_100, ebx110 * W_000));
+      acc[11] += fma_t(ebx101 * eby011, W_110, fma_t(ebx101 * eby010, W_100, fma_t(ebx100 * eby011, W_010, ebx100 * eby010 * W_000)));
+      acc[20] += fma_t(ebx101 * ebz011, W_101, fma_t(ebx101 * ebz010, W_100, fma_t(ebx100 * ebz011, W_001, ebx100 * ebz010 * W_000)));
+      acc[29] += fma_t(ebx011 * eby101, W_110, fma_t(ebx011 * eby100, W_100, fma_t(ebx010 * eby101, W_010, ebx010 * eby100 * W_000)));
+      acc[38] += fma_t(eby112, W_020, fma_t(eby111, W_010, eby110 * W_000));
+      acc[47] += fma_t(eby101 * ebz011, W_011, fma_t(eby101 * ebz010, W_010, fma_t(eby100 * ebz011, W_001, eby100 * ebz010 * W_000)));
+      acc[56] += fma_t(ebx011 * ebz101, W_101, fma_t(ebx011 * ebz100, W_100, fma_t(ebx010 * ebz101, W_001, ebx010 * ebz100 * W_000)));
+      acc[65] += fma_t(eby011 * ebz101, W_011, fma_t(eby011 * ebz100, W_010, fma_t(eby010 * ebz101, W_001, eby010 * ebz100 * W_000)));
+      acc[74] += fma_t(ebz112, W_002, fma_t(ebz111, W_001, ebz110 * W_000));
+    }
+    {
+      const T W_000 = fma_t(ekp10_110, R0_110, fma_t(ekp10_100, R0_100, fma_t(ekp10_010, R0_010, ekp10_000 * R0_000)));
+      const T W_001 = fma_t(ekp10_110, R0_111, fma_t(ekp10_100, R0_101, fma_t(ekp10_010, R0_011, ekp10_000 * R0_001)));
+      const T W_010 = fma_t(ekp10_110, R0_120, fma_t(ekp10_100, R0_110, fma_t(ekp10_010, R0_020, ekp10_000 * R0_010)));
+      const T W_100 = fma_t(ekp10_110, R0_210, fma_t(ekp10_100, R0_200, fma_t(ekp10_010, R0_110, ekp10_000 * R0_100)));
+      const T W_002 = fma_t(ekp10_110, R0_112, fma_t(ekp10_100, R0_102, fma_t(ekp10_010, R0_012, ekp10_000 * R0_002)));
+      const T W_011 = fma_t(ekp10_110, R0_121, fma_t(ekp10_100, R0_111, fma_t(ekp10_010, R0_021, ekp10_000 * R0_011)));
+      const T W_020 = fma_t(ekp10_110, R0_130, fma_t(ekp10_100, R0_120, fma_t(ekp10_010, R0_030, ekp10_000 * R0_020)));
+      const T W_101 = fma_t(ekp10_110, R0_211, fma_t(ekp10_100, R0_201, fma_t(ekp10_010, R0_111, ekp10_000 * R0_101)));
+      const T W_110 = fma_t(ekp10_110, R0_220, fma_t(ekp10_100, R0_210, fma_t(ekp10_010, R0_120, ekp10_000 * R0_110)));
+      const T W_200 = fma_t(ekp10_110, R0_310, fma_t(ekp10_100, R0_300, fma_t(ekp10_010, R0_210, ekp10_000 * R0_200)));
+      acc[3] += fma_t(ebx112, W_200, fma_t(ebx111, W_100, ebx110 * W_000));
+      acc[12] += fma_t(ebx101 * eby011, W_110, fma_t(ebx101 * eby010, W_100, fma_t(ebx100 * eby011, W_010, ebx100 * eby010 * W_000)));
+      acc[21] += fma_t(ebx101 * ebz011, W_101, fma_t(ebx101 * ebz010, W_100, fma_t(ebx100 * ebz011, W_001, ebx100 * ebz010 * W_000)));
+      acc[30] += fma_t(ebx011 * eby101, W_110, fma_t(ebx011 * eby100, W_100, fma_t(ebx010 * eby101, W_010, ebx010 * eby100 * W_000)));
+      acc[39] += fma_t(eby112, W_020, fma_t(eby111, W_010, eby110 * W_000));
+      acc[48] += fma_t(eby101 * ebz011, W_011, fma_t(eby101 * ebz010, W_010, fma_t(eby100 * ebz011, W_001, eby100 * ebz010 * W_000)));
+      acc[57] += fma_t(ebx011 * ebz101, W_101, fma_t(ebx011 * ebz100, W_100, fma_t(ebx010 * ebz101, W_001, ebx010 * ebz100 * W_000)));
+      acc[66] += fma_t(eby011 * ebz101, W_011, fma_t(eby011 * ebz100, W_010, fma_t(eby010 * ebz101, W_001, eby010 * ebz100 * W_000)));
+      acc[75] += fma_t(ebz112, W_002, fma_t(ebz111, W_001, ebz110 * W_000));
+    }
+    {
+      const T W_000 = fma_t(ekp11_020, R0_020, fma_t(ekp11_010, R0_010, ekp11_000 * R0_000));
+      const T W_001 = fma_t(ekp11_020, R0_021, fma_t(ekp11_010, R0_011, ekp11_000 * R0_001));
+      const T W_010 = fma_t(ekp11_020, R0_030, fma_t(ekp11_010, R0_020, ekp11_000 * R0_010));
+      const T W_100 = fma_t(ekp11_020, R0_120, fma_t(ekp11_010, R0_110, ekp11_000 * R0_100));
+      const T W_002 = fma_t(ekp11_020, R0_022, fma_t(ekp11_010, R0_012, ekp11_000 * R0_002));
+      const T W_011 = fma_t(ekp11_020, R0_031, fma_t(ekp11_010, R0_021, ekp11_000 * R0_011));
+      const T W_020 = fma_t(ekp11_020, R0_040, fma_t(ekp11_010, R0_030, ekp11_000 * R0_020));
+      const T W_101 = fma_t(ekp11_020, R0_121, fma_t(ekp11_010, R0_111, ekp11_000 * R0_101));
+      const T W_110 = fma_t(ekp11_020, R0_130, fma_t(ekp11_010, R0_120, ekp11_000 * R0_110));
+      const T W_200 = fma_t(ekp11_020, R0_220, fma_t(ekp11_010, R0_210, ekp11_000 * R0_200));
+      acc[4] += fma_t(ebx112, W_200, fma_t(ebx111, W_100, ebx110 * W_000));
+      acc[13] += fma_t(ebx101 * eby011, W_110, fma_t(ebx101 * eby010, W_100, fma_t(ebx100 * eby011, W_010, ebx100 * eby010 * W_000)));
+      acc[22] += fma_t(ebx101 * ebz011, W_101, fma_t(ebx101 * ebz010, W_100, fma_t(ebx100 * ebz011, W_001, ebx100 * ebz010 * W_000)));
+      acc[31] += fma_t(ebx011 * eby101, W_110, fma_t(ebx011 * eby100, W_100, fma_t(ebx010 * eby101, W_010, ebx010 * eby100 * W_000)));
+      acc[40] += fma_t(eby112, W_020, fma_t(eby111, W_010, eby110 * W_000));
+      acc[49] += fma_t(eby101 * ebz011, W_011, fma_t(eby101 * ebz010, W_010, fma_t(eby100 * ebz011, W_001, eby100 * ebz010 * W_000)));
+      acc[58] += fma_t(ebx011 * ebz101, W_101, fma_t(ebx011 * ebz100, W_100, fma_t(ebx010 * ebz101, W_001, ebx010 * ebz100 * W_000)));
+      acc[67] += fma_t(eby011 * ebz101, W_011, fma_t(eby011 * ebz100, W_010, fma_t(eby010 * ebz101, W_001, eby010 * ebz100 * W_000)));
+      acc[76] += fma_t(ebz112, W_002, fma_t(ebz111, W_001, ebz110 * W_000));
+    }
+    {
+      const T W_000 = fma_t(ekp12_011, R0_011, fma_t(ekp12_010, R0_010, fma_t(ekp12_001, R0_001, ekp12_000 * R0_000)));
+      const T W_001 = fma_t(ekp12_011, R0_012, fma_t(ekp12_010, R0_011, fma_t(ekp12_001, R0_002, ekp12_000 * R0_001)));
+      const T W_010 = fma_t(ekp12_011, R0_021, fma_t(ekp12_010, R0_020, fma_t(ekp12_001, R0_011, ekp12_000 * R0_010)));
+      const T W_100 = fma_t(ekp12_011, R0_111, fma_t(ekp12_010, R0_110, fma_t(ekp12_001, R0_101, ekp12_000 * R0_100)));
+      const T W_002 = fma_t(ekp12_011, R0_013, fma_t(ekp12_010, R0_012, fma_t(ekp12_001, R0_003, ekp12_000 * R0_002)));
+      const T W_011 = fma_t(ekp12_011, R0_022, fma_t(ekp12_010, R0_021, fma_t(ekp12_001, R0_012, ekp12_000 * R0_011)));
+      const T W_020 = fma_t(ekp12_011, R0_031, fma_t(ekp12_010, R0_030, fma_t(ekp12_001, R0_021, ekp12_000 * R0_020)));
+      const T W_101 = fma_t(ekp12_011, R0_112, fma_t(ekp12_010, R0_111, fma_t(ekp12_001, R0_102, ekp12_000 * R0_101)));
+      const T W_110 = fma_t(ekp12_011, R0_121, fma_t(ekp12_010, R0_120, fma_t(ekp12_001, R0_111, ekp12_000 * R0_110)));
+      const T W_200 = fma_t(ekp12_011, R0_211, fma_t(ekp12_010, R0_210, fma_t(ekp12_001, R0_201, ekp12_000 * R0_200)));
+      acc[5] += fma_t(ebx112, W_200, fma_t(ebx111, W_100, ebx110 * W_000));
+      acc[14] += fma_t(ebx101 * eby011, W_110, fma_t(ebx101 * eby010, W_100, fma_t(ebx100 * eby011, W_010, ebx100 * eby010 * W_000)));
+      acc[23] += fma_t(ebx101 * ebz011, W_101, fma_t(ebx101 * ebz010, W_100, fma_t(ebx100 * ebz011, W_001, ebx100 * ebz010 * W_000)));
+      acc[32] += fma_t(ebx011 * eby101, W_110, fma_t(ebx011 * eby100, W_100, fma_t(ebx010 * eby101, W_010, ebx010 * eby100 * W_000)));
+      acc[41] += fma_t(eby112, W_020, fma_t(eby111, W_010, eby110 * W_000));
+      acc[50] += fma_t(eby101 * ebz011, W_011, fma_t(eby101 * ebz010, W_010, fma_t(eby100 * ebz011, W_001, eby100 * ebz010 * W_000)));
+      acc[59] += fma_t(ebx011 * ebz101, W_101, fma_t(ebx011 * ebz100, W_100, fma_t(ebx010 * ebz101, W_001, ebx010 * ebz100 * W_000)));
+      acc[68] += fma_t(eby011 * ebz101, W_011, fma_t(eby011 * ebz100, W_010, fma_t(eby010 * ebz101, W_001, eby010 * ebz100 * W_000)));
+      acc[77] += fma_t(ebz112, W_002, fma_t(ebz111, W_001, ebz110 * W_000));
+    }
+    {
+      const T W_000 = fma_t(ekp20_101, R0_101, fma_t(ekp20_100, R0_100, fma_t(ekp20_001, R0_001, ekp20_000 * R0_000)));
+      const T W_001 = fma_t(ekp20_101, R0_102, fma_t(ekp20_100, R0_101, fma_t(ekp20_001, R0_002, ekp20_000 * R0_001)));
+      const T W_010 = fma_t(ekp20_101, R0_111, fma_t(ekp20_100, R0_110, fma_t(ekp20_001, R0_011, ekp20_000 * R0_010)));
+      const T W_100 = fma_t(ekp20_101, R0_201, fma_t(ekp20_100, R0_200, fma_t(ekp20_001, R0_101, ekp20_000 * R0_100)));
+      const T W_002 = fma_t(ekp20_101, R0_103, fma_t(ekp20_100, R0_102, fma_t(ekp20_001, R0_003, ekp20_000 * R0_002)));
+      const T W_011 = fma_t(ekp20_101, R0_112, fma_t(ekp20_100, R0_111, fma_t(ekp20_001, R0_012, ekp20_000 * R0_011)));
+      const T W_020 = fma_t(ekp20_101, R0_121, fma_t(ekp20_100, R0_120, fma_t(ekp20_001, R0_021, ekp20_000 * R0_020)));
+      const T W_101 = fma_t(ekp20_101, R0_202, fma_t(ekp20_100, R0_201, fma_t(ekp20_001, R0_102, ekp20_000 * R0_101)));
+      const T W_110 = fma_t(ekp20_101, R0_211, fma_t(ekp20_100, R0_210, fma_t(ekp20_001, R0_111, ekp20_000 * R0_110)));
+      const T W_200 = fma_t(ekp20_101, R0_301, fma_t(ekp20_100, R0_300, fma_t(ekp20_001, R0_201, ekp20_000 * R0_200)));
+      acc[6] += fma_t(ebx112, W_200, fma_t(ebx111, W_100, ebx110 * W_000));
+      acc[15] += fma_t(ebx101 * eby011, W_110, fma_t(ebx101 * eby010, W_100, fma_t(ebx100 * eby011, W_010, ebx100 * eby010 * W_000)));
+      acc[24] += fma_t(ebx101 * ebz011, W_101, fma_t(ebx101 * ebz010, W_100, fma_t(ebx100 * ebz011, W_001, ebx100 * ebz010 * W_000)));
+      acc[33] += fma_t(ebx011 * eby101, W_110, fma_t(ebx011 * eby100, W_100, fma_t(ebx010 * eby101, W_010, ebx010 * eby100 * W_000)));
+      acc[42] += fma_t(eby112, W_020, fma_t(eby111, W_010, eby110 * W_000));
+      acc[51] += fma_t(eby101 * ebz011, W_011, fma_t(eby101 * ebz010, W_010, fma_t(eby100 * ebz011, W_001, eby100 * ebz010 * W_000)));
+      acc[60] += fma_t(ebx011 * ebz101, W_101, fma_t(ebx011 * ebz100, W_100, fma_t(ebx010 * ebz101, W_001, ebx010 * ebz100 * W_000)));
+      acc[69] += fma_t(eby011 * ebz101, W_011, fma_t(eby011 * ebz100, W_010, fma_t(eby010 * ebz101, W_001, eby010 * ebz100 * W_000)));
+      acc[78] += fma_t(ebz112, W_002, fma_t(ebz111, W_001, ebz110 * W_000));
+    }
+    {
+      const T W_000 = fma_t(ekp21_011, R0_011, fma_t(ekp21_010, R0_010, fma_t(ekp21_001, R0_001, ekp21_000 * R0_000)));
+      const T W_001 = fma_t(ekp21_011, R0_012, fma_t(ekp21_010, R0_011, fma_t(ekp21_001, R0_002, ekp21_000 * R0_001)));
+      const T W_010 = fma_t(ekp21_011, R0_021, fma_t(ekp21_010, R0_020, fma_t(ekp21_001, R0_011, ekp21_000 * R0_010)));
+      const T W_100 = fma_t(ekp21_011, R0_111, fma_t(ekp21_010, R0_110, fma_t(ekp21_001, R0_101, ekp21_000 * R0_100)));
+      const T W_002 = fma_t(ekp21_011, R0_013, fma_t(ekp21_010, R0_012, fma_t(ekp21_001, R0_003, ekp21_000 * R0_002)));
+      const T W_011 = fma_t(ekp21_011, R0_022, fma_t(ekp21_010, R0_021, fma_t(ekp21_001, R0_012, ekp21_000 * R0_011)));
+      const T W_020 = fma_t(ekp21_011, R0_031, fma_t(ekp21_010, R0_030, fma_t(ekp21_001, R0_021, ekp21_000 * R0_020)));
+      const T W_101 = fma_t(ekp21_011, R0_112, fma_t(ekp21_010, R0_111, fma_t(ekp21_001, R0_102, ekp21_000 * R0_101)));
+      const T W_110 = fma_t(ekp21_011, R0_121, fma_t(ekp21_010, R0_120, fma_t(ekp21_001, R0_111, ekp21_000 * R0_110)));
+      const T W_200 = fma_t(ekp21_011, R0_211, fma_t(ekp21_010, R0_210, fma_t(ekp21_001, R0_201, ekp21_000 * R0_200)));
+      acc[7] += fma_t(ebx112, W_200, fma_t(ebx111, W_100, ebx110 * W_000));
+      acc[16] += fma_t(ebx101 * eby011, W_110, fma_t(ebx101 * eby010, W_100, fma_t(ebx100 * eby011, W_010, ebx100 * eby010 * W_000)));
+      acc[25] += fma_t(ebx101 * ebz011, W_101, fma_t(ebx101 * ebz010, W_100, fma_t(ebx100 * ebz011, W_001, ebx100 * ebz010 * W_000)));
+      acc[34] += fma_t(ebx011 * eby101, W_110, fma_t(ebx011 * eby100, W_100, fma_t(ebx010 * eby101, W_010, ebx010 * eby100 * W_000)));
+      acc[43] += fma_t(eby112, W_020, fma_t(eby111, W_010, eby110 * W_000));
+      acc[52] += fma_t(eby101 * ebz011, W_011, fma_t(eby101 * ebz010, W_010, fma_t(eby100 * ebz011, W_001, eby100 * ebz010 * W_000)));
+      acc[61] += fma_t(ebx011 * ebz101, W_101, fma_t(ebx011 * ebz100, W_100, fma_t(ebx010 * ebz101, W_001, ebx010 * ebz100 * W_000)));
+      acc[70] += fma_t(eby011 * ebz101, W_011, fma_t(eby011 * ebz100, W_010, fma_t(eby010 * ebz101, W_001, eby010 * ebz100 * W_000)));
+      acc[79] += fma_t(ebz112, W_002, fma_t(ebz111, W_001, ebz110 * W_000));
+    }
+    {
+      const T W_000 = fma_t(ekp22_002, R0_002, fma_t(ekp22_001, R0_001, ekp22_000 * R0_000));
+      const T W_001 = fma_t(ekp22_002, R0_003, fma_t(ekp22_001, R0_002, ekp22_000 * R0_001));
+      const T W_010 = fma_t(ekp22_002, R0_012, fma_t(ekp22_001, R0_011, ekp22_000 * R0_010));
+      const T W_100 = fma_t(ekp22_002, R0_102, fma_t(ekp22_001, R0_101, ekp22_000 * R0_100));
+      const T W_002 = fma_t(ekp22_002, R0_004, fma_t(ekp22_001, R0_003, ekp22_000 * R0_002));
+      const T W_011 = fma_t(ekp22_002, R0_013, fma_t(ekp22_001, R0_012, ekp22_000 * R0_011));
+      const T W_020 = fma_t(ekp22_002, R0_022, fma_t(ekp22_001, R0_021, ekp22_000 * R0_020));
+      const T W_101 = fma_t(ekp22_002, R0_103, fma_t(ekp22_001, R0_102, ekp22_000 * R0_101));
+      const T W_110 = fma_t(ekp22_002, R0_112, fma_t(ekp22_001, R0_111, ekp22_000 * R0_110));
+      const T W_200 = fma_t(ekp22_002, R0_202, fma_t(ekp22_001, R0_201, ekp22_000 * R0_200));
+      acc[8] += fma_t(ebx112, W_200, fma_t(ebx111, W_100, ebx110 * W_000));
+      acc[17] += fma_t(ebx101 * eby011, W_110, fma_t(ebx101 * eby010, W_100, fma_t(ebx100 * eby011, W_010, ebx100 * eby010 * W_000)));
+      acc[26] += fma_t(ebx101 * ebz011, W_101, fma_t(ebx101 * ebz010, W_100, fma_t(ebx100 * ebz011, W_001, ebx100 * ebz010 * W_000)));
+      acc[35] += fma_t(ebx011 * eby101, W_110, fma_t(ebx011 * eby100, W_100, fma_t(ebx010 * eby101, W_010, ebx010 * eby100 * W_000)));
+      acc[44] += fma_t(eby112, W_020, fma_t(eby111, W_010, eby110 * W_000));
+      acc[53] += fma_t(eby101 * ebz011, W_011, fma_t(eby101 * ebz010, W_010, fma_t(eby100 * ebz011, W_001, eby100 * ebz010 * W_000)));
+      acc[62] += fma_t(ebx011 * ebz101, W_101, fma_t(ebx011 * ebz100, W_100, fma_t(ebx010 * ebz101, W_001, ebx010 * ebz100 * W_000)));
+      acc[71] += fma_t(eby011 * ebz101, W_011, fma_t(eby011 * ebz100, W_010, fma_t(eby010 * ebz101, W_001, eby010 * ebz100 * W_000)));
+      acc[80] += fma_t(ebz112, W_002, fma_t(ebz111, W_001, ebz110 * W_000));
+    }
+  }
+}

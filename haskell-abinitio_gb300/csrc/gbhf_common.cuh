@@ -1,0 +1,84 @@
+// Shared device-side definitions for libgbhf (sm_103a).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#define TWO_PI_2P5 34.98683665524972   // 2 pi^(5/2)
+#define GBHF_PI 3.141592653589793
+
+// Boys tables: F_m(T_j) on a uniform grid, row j holds m = 0 .. BOYS_NCOL-1.
+#define BOYS_NCOL 16
+// FP64: spacing 0.05 up to 38, 7-term Taylor about the nearest node.
+#define BOYS64_H 0.05
+#define BOYS64_TMAX 38.0
+#define BOYS64_NROW 762
+#define BOYS64_NTERM 7
+// FP32: spacing 0.1 up to 20, 5-term Taylor about the nearest node.
+#define BOYS32_H 0.1f
+#define BOYS32_TMAX 20.0f
+#define BOYS32_NROW 202
+#define BOYS32_NTERM 5
+
+// Bra primitive-pair fields (shared-memory staging and global SoA layout).
+enum {
+  BRA_P = 0, BRA_INVP, BRA_PX, BRA_PY, BRA_PZ, BRA_PAX, BRA_PAY, BRA_PAZ,
+  BRA_PBX, BRA_PBY, BRA_PBZ, BRA_K, BRA_NFIELD
+};
+#define BRA_STRIDE 40   // >= max primitive pairs per shell pair (6 x 6 = 36)
+#define KMAX_PRIM_PAIRS 36
+
+template <typename T> __device__ __forceinline__ T rsqrt_t(T x);
+template <> __device__ __forceinline__ double rsqrt_t<double>(double x) { return rsqrt(x); }
+template <> __device__ __forceinline__ float rsqrt_t<float>(float x) { return rsqrtf(x); }
+
+template <typename T> __device__ __forceinline__ T fma_t(T a, T b, T c);
+template <> __device__ __forceinline__ double fma_t<double>(double a, double b, double c) { return fma(a, b, c); }
+template <> __device__ __forceinline__ float fma_t<float>(float a, float b, float c) { return fmaf(a, b, c); }
+
+// F_0..F_L(T) from the table by Taylor expansion about the nearest node;
+// asymptotic form F_0 = sqrt(pi/T)/2, F_m = F_(m-1) (2m-1)/(2T) beyond TMAX
+// (the neglected exp(-T) term is below 4e-17 there for FP64, 2e-9 for FP32).
+template <typename T, int L> struct BoysCfg;
+template <int L> struct BoysCfg<double, L> {
+  static constexpr double H = BOYS64_H, TMAX = BOYS64_TMAX;
+  static constexpr int NT = BOYS64_NTERM;
+};
+template <int L> struct BoysCfg<float, L> {
+  static constexpr float H = BOYS32_H, TMAX = BOYS32_TMAX;
+  static constexpr int NT = BOYS32_NTERM;
+};
+
+template <typename T, int L>
+__device__ __forceinline__ void boys_eval(T t, const T* __restrict__ tab, T* F) {
+  using C = BoysCfg<T, L>;
+  if (t < T(C::TMAX)) {
+    const int j = (int)(t * T(1.0 / C::H) + T(0.5));
+    const T dx = T(j) * T(C::H) - t;   // = -(t - T_j)
+    T y[C::NT];
+    y[0] = T(1);
+#pragma unroll
+    for (int k = 1; k < C::NT; ++k) y[k] = y[k - 1] * dx * T(1.0 / k);
+    const T* row = tab + j * BOYS_NCOL;
+    T v[L + C::NT];
+#pragma unroll
+    for (int m = 0; m < L + C::NT; ++m) v[m] = __ldg(row + m);
+#pragma unroll
+    for (int m = 0; m <= L; ++m) {
+      T s = T(0);
+#pragma unroll
+      for (int k = C::NT - 1; k >= 0; --k) s = fma_t(y[k], v[m + k], s);
+      F[m] = s;
+    }
+  } else {
+    const T r = rsqrt_t(t);
+    F[0] = T(0.886226925452758) * r;
+    const T h = T(0.5) * r * r;
+#pragma unroll
+    for (int m = 1; m <= L; ++m) F[m] = F[m - 1] * T(2 * m - 1) * h;
+  }
+}
+
+// Error codes written by kernels into the context's device status word.
+#define GBHF_DEV_ERR_TIMEOUT 1
+#define GBHF_DEV_ERR_NOTCONV 2
+#define GBHF_DEV_ERR_BOUNDS 4

@@ -1,0 +1,219 @@
+// Host-side context and internal interfaces of libgbhf.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/gbhf.h"
+#include "gbhf_common.cuh"
+
+namespace gbhf {
+
+// Device buffer with RAII free (no copies).
+template <typename T>
+struct DBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  DBuf() = default;
+  DBuf(const DBuf&) = delete;
+  DBuf& operator=(const DBuf&) = delete;
+  ~DBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  cudaError_t alloc(size_t count) {
+    if (count <= n && p) return cudaSuccess;
+    release();
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+    if (e == cudaSuccess) n = count;
+    return e;
+  }
+};
+
+struct Shell {
+  int atom, L, np, ncomp, f0;   // f0: first basis function (components contiguous, x,y,z order)
+  std::vector<double> expo, coef;
+};
+
+// Number of shell-pair classes with L <= 1: (s,s), (p,s), (p,p).
+constexpr int NPCLS = 3;
+// Quartet combos (bra class >= ket class).
+constexpr int NCOMBO = 6;
+constexpr int COMBO_BRA[NCOMBO] = {0, 1, 1, 2, 2, 2};
+constexpr int COMBO_KET[NCOMBO] = {0, 0, 1, 0, 1, 2};
+
+struct Segment {
+  int start, end, K;   // global pair indices [start, end), primitive pairs per pair
+  int data_off;        // offset of this segment's ket-layout primitive data
+};
+
+struct Basis {
+  int natoms = 0, nbf = 0;
+  std::vector<double> xyz, Z;
+  // CGF description as given
+  std::vector<int> cgf_atom, cgf_lxyz, cgf_nprim;
+  std::vector<double> prim_coef, prim_exp;
+  std::vector<int> cgf_off;
+  std::vector<Shell> shells;
+  int maxL = 0;
+  bool shells_ok = false;   // every CGF grouped into a complete s or p shell
+  std::string shell_msg;
+};
+
+// Shell-pair data on the device, in the order used by the J/K kernels:
+// class 0 pairs, then class 1, then class 2; inside a class grouped by
+// primitive-pair count (segments), inside a segment by Schwarz bound descending.
+struct PairData {
+  int npairs = 0;
+  int cls_start[NPCLS + 1] = {0, 0, 0, 0};
+  std::vector<Segment> segs[NPCLS];
+  std::vector<int> hA, hB, hK, hPoff, hSeg;  // host copies
+  std::vector<double> hQ;
+  DBuf<int> A, B, K, poff, kseg;             // kseg: segment index (global list)
+  DBuf<double> Q;
+  DBuf<int4> seg_info;                       // (start, end, K, data_off) per segment, all classes
+  int nseg_total = 0;
+  int seg_cls_start[NPCLS + 1] = {0, 0, 0, 0};
+  // primitive-pair data: bra layout (pair-contiguous) and ket layout
+  // (segment-transposed: prim k of pair j at data_off + k*len + (j-start)).
+  DBuf<double> bra64, ket64;   // BRA_NFIELD arrays of length nprimpairs each
+  DBuf<float> bra32, ket32;
+  size_t nprim_pairs = 0;
+};
+
+struct TaskLists {
+  DBuf<int> item_count;    // per (combo, bra) item: [n64, n32]
+  DBuf<int> item_off;      // exclusive scan
+  DBuf<int4> tasks64, tasks32;
+  DBuf<int> ranges;        // per combo: start64, end64, start32, end32
+  DBuf<int> counters;      // per combo & precision: work-queue heads
+  DBuf<unsigned long long> stats;  // per combo: shell quartets, fn quartets, prim quartets (64, 32)
+  int nitems = 0;
+  std::vector<int> combo_item_start;   // host: first item of each combo
+  double thr_all = -1, thr64 = -1;     // thresholds the current lists were built for
+  int hranges[4 * 6] = {0};            // host copy of ranges
+  DBuf<int> f0;                        // first basis function per shell
+};
+
+struct JacobiWork {
+  DBuf<double> A, V, rot, red, t1, t2, t3;
+  DBuf<int> partner, sweeps;
+  DBuf<unsigned> bar;
+  int grid = 0;
+  int last_sweeps = 0;
+};
+
+struct Profile {
+  bool events = false;
+  double jk_ms64 = 0, jk_ms32 = 0, dense_ms = 0;
+  double prim64 = 0, prim32 = 0, shellq = 0, fnq = 0;
+  long long launches = 0;
+};
+
+}  // namespace gbhf
+
+struct gbhf_ctx {
+  int device = 0;
+  int nsm = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  gbhf::Basis basis;
+  bool have_grid = false;
+  gbhf::DBuf<double> boys_ref;   // 15 x 1001 reference grid
+  gbhf::DBuf<double> boys64;     // exact FP64 table
+  gbhf::DBuf<float> boys32;      // exact FP32 table
+  // basis on device (function level, for 1-e integrals and canonical ERIs)
+  gbhf::DBuf<double> d_xyz, d_Z, d_coef, d_exp;
+  gbhf::DBuf<int> d_fn;          // per CGF: atom, lx, ly, lz, np, off (6 ints)
+  bool basis_dev = false;
+  gbhf::PairData pairs;
+  bool pairs_ready = false;
+  gbhf::TaskLists tasks;
+  // dense work buffers (n*n doubles)
+  gbhf::DBuf<double> w[24];
+  gbhf::JacobiWork jac;
+  gbhf::DBuf<float> dfloat;
+  gbhf::DBuf<int> dev_status;
+  gbhf::DBuf<unsigned> barrier;
+  gbhf::DBuf<double> small;
+  gbhf::Profile prof;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+};
+
+namespace gbhf {
+
+// error helpers
+gbhf_status fail(gbhf_ctx* c, gbhf_status s, const std::string& msg);
+gbhf_status cuda_fail(gbhf_ctx* c, cudaError_t e, const char* where);
+#define GBHF_CUDA(ctx, call)                                        \
+  do {                                                              \
+    cudaError_t e__ = (call);                                       \
+    if (e__ != cudaSuccess) return gbhf::cuda_fail(ctx, e__, #call); \
+  } while (0)
+#define GBHF_TRY(call)                   \
+  do {                                   \
+    gbhf_status s__ = (call);            \
+    if (s__ != GBHF_OK) return s__;      \
+  } while (0)
+
+inline void count_launch(gbhf_ctx* c, int n = 1) { c->prof.launches += n; }
+
+// Work slot `slot` of the context with at least `count` doubles (nullptr on
+// allocation failure).  Slots 0-9: SCF driver; 10-12: diagonalHF and
+// symmOrtho; 13-14: DIIS error; 15-23: API entry points.
+inline double* ws(gbhf_ctx* c, int slot, size_t count) {
+  if (c->w[slot].alloc(count) != cudaSuccess) return nullptr;
+  return c->w[slot].p;
+}
+#define GBHF_WS(ctx, var, slot, count)                                                      \
+  double* var = gbhf::ws(ctx, slot, count);                                                 \
+  if (!var) return gbhf::fail(ctx, GBHF_ERR_CUDA, "device allocation failed (work buffer)")
+
+// setup.cu
+gbhf_status build_basis(gbhf_ctx* c, int n_atoms, const double* xyz, const double* Z, int n_cgf,
+                        const int* cgf_atom, const int* cgf_lxyz, const int* cgf_nprim, const double* coef,
+                        const double* expo);
+gbhf_status ensure_boys_tables(gbhf_ctx* c);
+gbhf_status ensure_pairs(gbhf_ctx* c);
+
+// onee.cu
+gbhf_status onee_matrices(gbhf_ctx* c, bool ref, double* d_S, double* d_H);   // flat (N(N+1)/2), device
+// eri_canon.cu
+gbhf_status eri_canonical_dev(gbhf_ctx* c, bool ref, double* d_eri);
+gbhf_status fock_canonical_dev(gbhf_ctx* c, const double* d_H, const double* d_D, const double* d_eri, double* d_F);
+gbhf_status boys_dev(gbhf_ctx* c, bool ref, int mmax, int n, const double* d_x, double* d_out);
+gbhf_status boys_ref_grid_dev(gbhf_ctx* c, double* d_grid);
+gbhf_status schwarz_pairs_dev(gbhf_ctx* c, const int* d_A, const int* d_B, int npairs, double* d_Q);
+// jk.cu
+// G_acc (n*n) += sym(G''(D)), D square n*n.  w = screening weight.
+gbhf_status jk_build(gbhf_ctx* c, const double* d_Dsq, double* d_G, int precision, double schwarz,
+                     double mixed_cutoff, double weight);
+// linalg.cu
+gbhf_status gemm(gbhf_ctx* c, bool ta, bool tb, int m, int n, int k, double alpha, const double* A, int lda,
+                 const double* B, int ldb, double beta, double* C, int ldc);
+gbhf_status eigh(gbhf_ctx* c, int n, const double* d_A, double* d_evals, double* d_evecs, const double* d_V0);
+gbhf_status flat_to_square(gbhf_ctx* c, int n, const double* d_flat, double* d_sq);
+gbhf_status square_to_flat(gbhf_ctx* c, int n, const double* d_sq, double* d_flat);
+gbhf_status symm_ortho_dev(gbhf_ctx* c, int n, const double* d_S, double* d_X);
+gbhf_status diagonal_hf_dev(gbhf_ctx* c, int n, const double* d_Fsq, const double* d_X, int nocc, double* d_C,
+                            double* d_Dsq, double* d_eps, double* d_Cprime_warm);
+gbhf_status diis_error_dev(gbhf_ctx* c, int n, const double* d_F, const double* d_S, const double* d_D,
+                           const double* d_X, double* d_e);
+gbhf_status gauss_elem_dev_call(gbhf_ctx* c, int m, const double* h_a, const double* h_b, double* h_x, bool* ok);
+// scf.cu
+gbhf_status scf_run(gbhf_ctx* c, const gbhf_scf_opts* o, gbhf_result* r);
+gbhf_status dot_matrices(gbhf_ctx* c, int n2, int k, const double* const* mats, const double* d_e,
+                         double* d_out);
+gbhf_status lincomb(gbhf_ctx* c, int n2, int k, const double* const* mats, const double* coefs, double* d_out);
+gbhf_status reduce_stats(gbhf_ctx* c, int n, const double* d_e, const double* d_H, const double* d_F,
+                         const double* d_Dnew, const double* d_Dold, double* host_out4);
+gbhf_status axpby(gbhf_ctx* c, size_t n, double a, const double* x, double b, const double* y, double* out);
+gbhf_status add_sym(gbhf_ctx* c, int n, const double* d_H, const double* d_Gpp, double* d_out);
+gbhf_status max_abs(gbhf_ctx* c, size_t n, const double* d_x, double* host_out);
+gbhf_status to_float(gbhf_ctx* c, size_t n, const double* d_x, float* d_y);
+
+}  // namespace gbhf

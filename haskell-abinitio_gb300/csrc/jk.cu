@@ -1,0 +1,560 @@
+// Direct J/K Fock build: screened task lists and per-class ERI+scatter kernels.
+//
+// Unique shell quartets (AB|CD): bra pair of class X, ket pair of class Y
+// with X >= Y, and within one class ket index <= bra index, which visits
+// each quartet of the 8-fold permutation orbit once.  With the degeneracy
+// weight s = (A==B ? 1/2 : 1)(C==D ? 1/2 : 1)(AB==CD ? 1/2 : 1) every
+// component integral v = (ab|cd) adds, to a non-symmetric accumulator G'',
+//   G''_ab += 2 s v D_cd,  G''_cd += 2 s v D_ab,
+//   G''_ac -= s v D_bd/2,  G''_bc -= s v D_ad/2,  G''_ad -= s v D_bc/2,  G''_bd -= s v D_ac/2,
+// and G = G'' + G''^T equals J - K/2 of the reference's calcGmatrix
+// (HartreeFock/HartreeFock.hs:225-241): G_ab = sum_kl D_lk [(ab|kl) - (al|kb)/2].
+//
+// Work decomposition: a task is (bra pair, <= 32 consecutive kets of one ket
+// segment); one warp runs one task, lane = ket.  Kets inside a segment share
+// the primitive-pair count, so lanes do equal work; the segment is sorted by
+// Schwarz bound, so the kets that pass Q_bra Q_ket w >= cutoff form a prefix
+// found by binary search, and the FP64/FP32 split of mixed precision is a
+// second prefix boundary.  Warps pull tasks from a per-kernel atomic counter
+// (no waiting on other warps).
+#include <algorithm>
+#include <cstring>
+
+#include <type_traits>
+
+#include "gbhf_internal.h"
+
+namespace gbhf {
+
+constexpr int ncart_c(int L) { return (L + 1) * (L + 2) / 2; }
+
+template <typename T, int N>
+struct RegAcc {
+  T v[N];
+  __device__ __forceinline__ T& operator[](int i) { return v[i]; }
+  __device__ __forceinline__ void zero() {
+#pragma unroll
+    for (int i = 0; i < N; ++i) v[i] = T(0);
+  }
+  __device__ __forceinline__ T get(int i) const { return v[i]; }
+};
+
+template <int N>
+struct SmemAcc {
+  double* p;   // this thread's column, stride blockDim (128)
+  __device__ __forceinline__ double& operator[](int i) { return p[i * 128]; }
+  __device__ __forceinline__ void zero() {
+#pragma unroll 4
+    for (int i = 0; i < N; ++i) p[i * 128] = 0.0;
+  }
+  __device__ __forceinline__ double get(int i) const { return p[i * 128]; }
+};
+
+}  // namespace gbhf
+
+#include "eri_gen.cuh"
+
+namespace gbhf {
+
+template <typename T>
+struct JKArgs {
+  const int4* tasks;
+  const int* range;    // [start, end)
+  int* counter;
+  const int* pA;
+  const int* pB;
+  const int* pK;
+  const int* poff;
+  const int* kseg;
+  const int4* seg;
+  const T* bra;
+  const T* ket;
+  long long npp;
+  const int* shell_f0;
+  const T* D;
+  int n;
+  double* G;
+  const T* boys;
+  unsigned long long* stats;   // [shell quartets, fn quartets, prim quartets]
+};
+
+template <int LA, int LB, int LC, int LD>
+struct ClassFn;
+
+#define GBHF_CLASS_FN(la, lb, lc, ld, name)                                                              \
+  template <>                                                                                            \
+  struct ClassFn<la, lb, lc, ld> {                                                                       \
+    template <typename T, typename Acc>                                                                  \
+    static __device__ __forceinline__ void run(const T* sb, int nbra, T q, T invq, T Qx, T Qy, T Qz, T QCx, \
+                                               T QCy, T QCz, T QDx, T QDy, T QDz, T Kcd, const T* boys,   \
+                                               Acc& acc) {                                               \
+      eri_ketprim_##name<T, Acc>(sb, nbra, q, invq, Qx, Qy, Qz, QCx, QCy, QCz, QDx, QDy, QDz, Kcd, boys, acc); \
+    }                                                                                                    \
+  };
+GBHF_CLASS_FN(0, 0, 0, 0, ssss)
+GBHF_CLASS_FN(1, 0, 0, 0, psss)
+GBHF_CLASS_FN(1, 0, 1, 0, psps)
+GBHF_CLASS_FN(1, 1, 0, 0, ppss)
+GBHF_CLASS_FN(1, 1, 1, 0, ppps)
+GBHF_CLASS_FN(1, 1, 1, 1, pppp)
+
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+constexpr int JK_THREADS = 128;
+constexpr int JK_WARPS = JK_THREADS / 32;
+
+template <int LA, int LB, int LC, int LD, typename T, bool SACC>
+__global__ void __launch_bounds__(JK_THREADS) k_jk(JKArgs<T> a) {
+  constexpr int NA = ncart_c(LA), NB = ncart_c(LB), NC = ncart_c(LC), ND = ncart_c(LD);
+  constexpr int NAB = NA * NB, NCD = NC * ND, NOUT = NAB * NCD;
+  __shared__ T sbra[JK_WARPS][BRA_NFIELD * BRA_STRIDE];
+  __shared__ T sDab[JK_WARPS][NAB > 1 ? NAB : 1];
+  extern __shared__ double sacc_dyn[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int start = a.range[0];
+  const int ntask = a.range[1] - start;
+  unsigned long long cnt_q = 0, cnt_p = 0;
+  using AccT = typename std::conditional<SACC, SmemAcc<NOUT>, RegAcc<T, NOUT>>::type;
+  AccT acc;
+  if constexpr (SACC) acc.p = sacc_dyn + threadIdx.x;
+  const long long npp = a.npp;
+  const int n = a.n;
+  while (true) {
+    int t = 0;
+    if (lane == 0) t = atomicAdd(a.counter, 1);
+    t = __shfl_sync(0xffffffffu, t, 0);
+    if (t >= ntask) break;
+    const int4 task = a.tasks[start + t];
+    const int ib = task.x;
+    const int jk = task.y + lane;
+    const bool active = lane < task.z;
+    const int Kb = a.pK[ib], pb0 = a.poff[ib];
+    for (int idx = lane; idx < BRA_NFIELD * Kb; idx += 32) {
+      const int f = idx / Kb, k = idx - f * Kb;
+      sbra[warp][f * BRA_STRIDE + k] = a.bra[(long long)f * npp + pb0 + k];
+    }
+    const int A = a.pA[ib], B = a.pB[ib];
+    const int a0 = a.shell_f0[A], b0 = a.shell_f0[B];
+    if (lane < NAB) sDab[warp][lane] = a.D[(long long)(a0 + lane / NB) * n + b0 + lane % NB];
+    __syncwarp();
+    acc.zero();
+    int C = 0, Dd = 0, c0 = 0, d0 = 0;
+    if (active) {
+      C = a.pA[jk];
+      Dd = a.pB[jk];
+      c0 = a.shell_f0[C];
+      d0 = a.shell_f0[Dd];
+      const int4 sg = a.seg[a.kseg[jk]];
+      const int K = sg.z, len = sg.y - sg.x;
+      const long long base = (long long)sg.w + (jk - sg.x);
+      for (int kc = 0; kc < K; ++kc) {
+        const long long idx = base + (long long)kc * len;
+        const T q = a.ket[BRA_P * npp + idx];
+        const T invq = a.ket[BRA_INVP * npp + idx];
+        const T Qx = a.ket[BRA_PX * npp + idx], Qy = a.ket[BRA_PY * npp + idx], Qz = a.ket[BRA_PZ * npp + idx];
+        T QCx = 0, QCy = 0, QCz = 0, QDx = 0, QDy = 0, QDz = 0;
+        if (LC >= 1) {
+          QCx = a.ket[BRA_PAX * npp + idx];
+          QCy = a.ket[BRA_PAY * npp + idx];
+          QCz = a.ket[BRA_PAZ * npp + idx];
+        }
+        if (LD >= 1) {
+          QDx = a.ket[BRA_PBX * npp + idx];
+          QDy = a.ket[BRA_PBY * npp + idx];
+          QDz = a.ket[BRA_PBZ * npp + idx];
+        }
+        const T Kcd = a.ket[BRA_K * npp + idx];
+        ClassFn<LA, LB, LC, LD>::template run<T, AccT>(sbra[warp], Kb, q, invq, Qx, Qy, Qz, QCx, QCy, QCz, QDx,
+                                                       QDy, QDz, Kcd, a.boys, acc);
+      }
+      cnt_q += 1;
+      cnt_p += (unsigned long long)Kb * K;
+    }
+    // ---- scatter into G'' (FP64 atomics)
+    const T s = (A == B ? T(0.5) : T(1)) * (C == Dd ? T(0.5) : T(1)) * (ib == jk ? T(0.5) : T(1));
+    T dcd[NCD];
+#pragma unroll
+    for (int ic = 0; ic < NC; ++ic)
+#pragma unroll
+      for (int id = 0; id < ND; ++id) dcd[ic * ND + id] = active ? a.D[(long long)(c0 + ic) * n + d0 + id] : T(0);
+    // J_ab (warp reduce over kets)
+#pragma unroll
+    for (int ab = 0; ab < NAB; ++ab) {
+      T v = 0;
+#pragma unroll
+      for (int cd = 0; cd < NCD; ++cd) v = fma_t(acc.get(ab * NCD + cd), dcd[cd], v);
+      v = warp_sum(v);
+      if (lane == 0) atomicAdd(&a.G[(long long)(a0 + ab / NB) * n + b0 + ab % NB], double(T(2) * s * v));
+    }
+    if (active) {
+      // J_cd
+#pragma unroll
+      for (int cd = 0; cd < NCD; ++cd) {
+        T v = 0;
+#pragma unroll
+        for (int ab = 0; ab < NAB; ++ab) v = fma_t(acc.get(ab * NCD + cd), sDab[warp][ab], v);
+        atomicAdd(&a.G[(long long)(c0 + cd / ND) * n + d0 + cd % ND], double(T(2) * s * v));
+      }
+      const T ks = T(-0.5) * s;
+      // K_ac -= sum_bd v D_bd ; K_ad -= sum_bc v D_bc
+#pragma unroll
+      for (int ia = 0; ia < NA; ++ia) {
+#pragma unroll
+        for (int ic = 0; ic < NC; ++ic) {
+          T v = 0;
+#pragma unroll
+          for (int ibb = 0; ibb < NB; ++ibb)
+#pragma unroll
+            for (int id = 0; id < ND; ++id)
+              v = fma_t(acc.get((ia * NB + ibb) * NCD + ic * ND + id), a.D[(long long)(b0 + ibb) * n + d0 + id], v);
+          atomicAdd(&a.G[(long long)(a0 + ia) * n + c0 + ic], double(ks * v));
+        }
+#pragma unroll
+        for (int id = 0; id < ND; ++id) {
+          T v = 0;
+#pragma unroll
+          for (int ibb = 0; ibb < NB; ++ibb)
+#pragma unroll
+            for (int ic = 0; ic < NC; ++ic)
+              v = fma_t(acc.get((ia * NB + ibb) * NCD + ic * ND + id), a.D[(long long)(b0 + ibb) * n + c0 + ic], v);
+          atomicAdd(&a.G[(long long)(a0 + ia) * n + d0 + id], double(ks * v));
+        }
+      }
+      // K_bc -= sum_ad v D_ad ; K_bd -= sum_ac v D_ac
+#pragma unroll
+      for (int ibb = 0; ibb < NB; ++ibb) {
+#pragma unroll
+        for (int ic = 0; ic < NC; ++ic) {
+          T v = 0;
+#pragma unroll
+          for (int ia = 0; ia < NA; ++ia)
+#pragma unroll
+            for (int id = 0; id < ND; ++id)
+              v = fma_t(acc.get((ia * NB + ibb) * NCD + ic * ND + id), a.D[(long long)(a0 + ia) * n + d0 + id], v);
+          atomicAdd(&a.G[(long long)(b0 + ibb) * n + c0 + ic], double(ks * v));
+        }
+#pragma unroll
+        for (int id = 0; id < ND; ++id) {
+          T v = 0;
+#pragma unroll
+          for (int ia = 0; ia < NA; ++ia)
+#pragma unroll
+            for (int ic = 0; ic < NC; ++ic)
+              v = fma_t(acc.get((ia * NB + ibb) * NCD + ic * ND + id), a.D[(long long)(a0 + ia) * n + c0 + ic], v);
+          atomicAdd(&a.G[(long long)(b0 + ibb) * n + d0 + id], double(ks * v));
+        }
+      }
+    }
+    __syncwarp();
+  }
+  // statistics (one atomic per warp and counter)
+  cnt_q = (unsigned long long)warp_sum((double)cnt_q);
+  cnt_p = (unsigned long long)warp_sum((double)cnt_p);
+  if (lane == 0 && a.stats) {
+    atomicAdd(&a.stats[0], cnt_q);
+    atomicAdd(&a.stats[1], cnt_q * (unsigned long long)(NOUT));
+    atomicAdd(&a.stats[2], cnt_p);
+  }
+}
+
+// ------------------------------------------------------------ task lists ----
+
+struct TaskGenArgs {
+  int nitems;
+  const int* item_combo_start;   // NCOMBO+1 item offsets
+  const int* cls_start;          // NPCLS+1
+  const int* seg_cls_start;      // NPCLS+1
+  const int4* seg;
+  const double* Q;
+  double thr_all, thr64;         // cutoff / weight, mixed cutoff / weight
+  int* count;                    // 2 per item
+  const int* off64;              // exclusive scans (nitems + 1)
+  const int* off32;
+  int4* tasks64;
+  int4* tasks32;
+};
+
+__device__ __forceinline__ int count_ge(const double* Q, int lo, int hi, double thr) {
+  // Q descending on [lo, hi): number of entries with Q >= thr
+  int a = lo, b = hi;
+  while (a < b) {
+    int m = (a + b) >> 1;
+    if (Q[m] >= thr) a = m + 1;
+    else b = m;
+  }
+  return a - lo;
+}
+
+template <bool FILL>
+__global__ void k_tasks(TaskGenArgs g) {
+  const int it = blockIdx.x * blockDim.x + threadIdx.x;
+  if (it >= g.nitems) return;
+  int k = 0;
+  while (k + 1 < NCOMBO && it >= g.item_combo_start[k + 1]) ++k;
+  const int X = k >= 3 ? 2 : (k >= 1 ? 1 : 0);   // combos (0,0) (1,0) (1,1) (2,0) (2,1) (2,2)
+  const int Y = k - X * (X + 1) / 2;
+  const int i = g.cls_start[X] + (it - g.item_combo_start[k]);
+  const double qi = g.Q[i];
+  int n64 = 0, n32 = 0;
+  int w64 = FILL ? g.off64[it] : 0, w32 = FILL ? g.off32[it] : 0;
+  if (qi > 0) {
+    const double ta = g.thr_all / qi, t64 = g.thr64 / qi;
+    for (int sidx = g.seg_cls_start[Y]; sidx < g.seg_cls_start[Y + 1]; ++sidx) {
+      const int4 s = g.seg[sidx];
+      int hi = s.y;
+      if (X == Y && hi > i + 1) hi = i + 1;
+      if (hi <= s.x) continue;
+      const int keep = count_ge(g.Q, s.x, hi, ta);
+      int k64 = count_ge(g.Q, s.x, s.x + keep, t64);
+      const int k32 = keep - k64;
+      if (FILL) {
+        for (int o = 0; o < k64; o += 32)
+          g.tasks64[w64++] = make_int4(i, s.x + o, min(32, k64 - o), 0);
+        for (int o = 0; o < k32; o += 32) g.tasks32[w32++] = make_int4(i, s.x + k64 + o, min(32, k32 - o), 0);
+      } else {
+        n64 += (k64 + 31) / 32;
+        n32 += (k32 + 31) / 32;
+      }
+    }
+  }
+  if (!FILL) {
+    g.count[2 * it] = n64;
+    g.count[2 * it + 1] = n32;
+  }
+}
+
+// Exclusive scan of count[2*i+which] into off (nitems+1 entries), one block.
+__global__ void k_scan2(int n, const int* __restrict__ count, int* __restrict__ off64, int* __restrict__ off32) {
+  __shared__ int s64[1024], s32[1024];
+  const int t = threadIdx.x;
+  const int chunk = (n + 1023) / 1024;
+  const int lo = min(n, t * chunk), hi = min(n, lo + chunk);
+  int a = 0, b = 0;
+  for (int i = lo; i < hi; ++i) {
+    a += count[2 * i];
+    b += count[2 * i + 1];
+  }
+  s64[t] = a;
+  s32[t] = b;
+  __syncthreads();
+  for (int o = 1; o < 1024; o <<= 1) {
+    int va = t >= o ? s64[t - o] : 0, vb = t >= o ? s32[t - o] : 0;
+    __syncthreads();
+    s64[t] += va;
+    s32[t] += vb;
+    __syncthreads();
+  }
+  int ra = s64[t] - a, rb = s32[t] - b;
+  for (int i = lo; i < hi; ++i) {
+    off64[i] = ra;
+    off32[i] = rb;
+    ra += count[2 * i];
+    rb += count[2 * i + 1];
+  }
+  if (t == 1023) {
+    off64[n] = s64[1023];
+    off32[n] = s32[1023];
+  }
+}
+
+__global__ void k_ranges(const int* item_combo_start, const int* off64, const int* off32, int* ranges) {
+  const int k = threadIdx.x;
+  if (k >= NCOMBO) return;
+  ranges[4 * k + 0] = off64[item_combo_start[k]];
+  ranges[4 * k + 1] = off64[item_combo_start[k + 1]];
+  ranges[4 * k + 2] = off32[item_combo_start[k]];
+  ranges[4 * k + 3] = off32[item_combo_start[k + 1]];
+}
+
+static gbhf_status build_tasks(gbhf_ctx* c, double thr_all, double thr64, int* h_ranges) {
+  PairData& P = c->pairs;
+  TaskLists& TL = c->tasks;
+  std::vector<int> ics(NCOMBO + 1, 0);
+  for (int k = 0; k < NCOMBO; ++k) {
+    const int X = COMBO_BRA[k];
+    ics[k + 1] = ics[k] + (P.cls_start[X + 1] - P.cls_start[X]);
+  }
+  TL.nitems = ics[NCOMBO];
+  TL.combo_item_start = ics;
+  const int ni = TL.nitems;
+  DBuf<int> d_ics, d_cls, d_scs;
+  GBHF_CUDA(c, d_ics.alloc(NCOMBO + 1));
+  GBHF_CUDA(c, d_cls.alloc(NPCLS + 1));
+  GBHF_CUDA(c, d_scs.alloc(NPCLS + 1));
+  GBHF_CUDA(c, cudaMemcpyAsync(d_ics.p, ics.data(), (NCOMBO + 1) * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  GBHF_CUDA(c, cudaMemcpyAsync(d_cls.p, P.cls_start, (NPCLS + 1) * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  GBHF_CUDA(c, cudaMemcpyAsync(d_scs.p, P.seg_cls_start, (NPCLS + 1) * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  GBHF_CUDA(c, TL.item_count.alloc(2 * (size_t)std::max(ni, 1)));
+  GBHF_CUDA(c, TL.item_off.alloc(2 * ((size_t)ni + 1)));
+  GBHF_CUDA(c, TL.ranges.alloc(4 * NCOMBO));
+  GBHF_CUDA(c, TL.counters.alloc(2 * NCOMBO));
+  GBHF_CUDA(c, TL.stats.alloc(3 * 2 * NCOMBO));
+  int* off64 = TL.item_off.p;
+  int* off32 = TL.item_off.p + ni + 1;
+  TaskGenArgs g;
+  g.nitems = ni;
+  g.item_combo_start = d_ics.p;
+  g.cls_start = d_cls.p;
+  g.seg_cls_start = d_scs.p;
+  g.seg = P.seg_info.p;
+  g.Q = P.Q.p;
+  g.thr_all = thr_all;
+  g.thr64 = thr64;
+  g.count = TL.item_count.p;
+  g.off64 = off64;
+  g.off32 = off32;
+  g.tasks64 = nullptr;
+  g.tasks32 = nullptr;
+  if (ni > 0) {
+    k_tasks<false><<<(ni + 127) / 128, 128, 0, c->stream>>>(g);
+    count_launch(c);
+  }
+  k_scan2<<<1, 1024, 0, c->stream>>>(ni, TL.item_count.p, off64, off32);
+  count_launch(c);
+  int tot[2];
+  GBHF_CUDA(c, cudaMemcpyAsync(&tot[0], off64 + ni, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  GBHF_CUDA(c, cudaMemcpyAsync(&tot[1], off32 + ni, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
+  GBHF_CUDA(c, TL.tasks64.alloc(std::max(tot[0], 1)));
+  GBHF_CUDA(c, TL.tasks32.alloc(std::max(tot[1], 1)));
+  g.tasks64 = TL.tasks64.p;
+  g.tasks32 = TL.tasks32.p;
+  if (ni > 0) {
+    k_tasks<true><<<(ni + 127) / 128, 128, 0, c->stream>>>(g);
+    count_launch(c);
+  }
+  k_ranges<<<1, 32, 0, c->stream>>>(d_ics.p, off64, off32, TL.ranges.p);
+  count_launch(c);
+  GBHF_CUDA(c, cudaGetLastError());
+  GBHF_CUDA(c, cudaMemcpyAsync(h_ranges, TL.ranges.p, 4 * NCOMBO * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
+  return GBHF_OK;
+}
+
+template <int LA, int LB, int LC, int LD, typename T, bool SACC>
+static gbhf_status launch_class(gbhf_ctx* c, int combo, int prec, const T* D, double* G, const T* bra, const T* ket,
+                                const T* boys, const int* f0, int ntask) {
+  if (ntask <= 0) return GBHF_OK;
+  constexpr int NOUT = ncart_c(LA) * ncart_c(LB) * ncart_c(LC) * ncart_c(LD);
+  const size_t smem = SACC ? (size_t)NOUT * JK_THREADS * sizeof(double) : 0;
+  auto kern = k_jk<LA, LB, LC, LD, T, SACC>;
+  static bool attr_set = false;
+  if (SACC && !attr_set) {
+    GBHF_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr_set = true;
+  }
+  int per_sm = 0;
+  GBHF_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, JK_THREADS, smem));
+  per_sm = std::max(per_sm, 1);
+  int grid = std::min(c->nsm * per_sm, (ntask + JK_WARPS - 1) / JK_WARPS);
+  PairData& P = c->pairs;
+  JKArgs<T> a;
+  a.tasks = prec == 0 ? c->tasks.tasks64.p : c->tasks.tasks32.p;
+  a.range = c->tasks.ranges.p + 4 * combo + 2 * prec;
+  a.counter = c->tasks.counters.p + 2 * combo + prec;
+  a.pA = P.A.p;
+  a.pB = P.B.p;
+  a.pK = P.K.p;
+  a.poff = P.poff.p;
+  a.kseg = P.kseg.p;
+  a.seg = P.seg_info.p;
+  a.bra = bra;
+  a.ket = ket;
+  a.npp = (long long)P.nprim_pairs;
+  a.shell_f0 = f0;
+  a.D = D;
+  a.n = c->basis.nbf;
+  a.G = G;
+  a.boys = boys;
+  a.stats = c->tasks.stats.p + 3 * (2 * combo + prec);
+  kern<<<grid, JK_THREADS, smem, c->stream>>>(a);
+  count_launch(c);
+  GBHF_CUDA(c, cudaGetLastError());
+  return GBHF_OK;
+}
+
+gbhf_status jk_build(gbhf_ctx* c, const double* d_Dsq, double* d_G, int precision, double schwarz,
+                     double mixed_cutoff, double weight) {
+  GBHF_TRY(ensure_pairs(c));
+  const int n = c->basis.nbf;
+  TaskLists& st = c->tasks;
+  if (!st.f0.p || st.f0.n < c->basis.shells.size()) {
+    std::vector<int> f0(c->basis.shells.size());
+    for (size_t s = 0; s < f0.size(); ++s) f0[s] = c->basis.shells[s].f0;
+    GBHF_CUDA(c, st.f0.alloc(f0.size()));
+    GBHF_CUDA(c, cudaMemcpyAsync(st.f0.p, f0.data(), f0.size() * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  }
+  if (!(weight > 0)) weight = 1e-300;
+  const double thr_all = schwarz / weight;
+  const double thr64 = precision == GBHF_PREC_FP64 ? 0.0 : mixed_cutoff / weight;
+  if (thr_all != st.thr_all || thr64 != st.thr64 || !c->tasks.tasks64.p) {
+    GBHF_TRY(build_tasks(c, thr_all, thr64, st.hranges));
+    st.thr_all = thr_all;
+    st.thr64 = thr64;
+  }
+  GBHF_CUDA(c, cudaMemsetAsync(c->tasks.counters.p, 0, 2 * NCOMBO * sizeof(int), c->stream));
+  GBHF_CUDA(c, cudaMemsetAsync(c->tasks.stats.p, 0, 6 * NCOMBO * sizeof(unsigned long long), c->stream));
+  bool any32 = false;
+  for (int k = 0; k < NCOMBO; ++k) any32 |= st.hranges[4 * k + 3] > st.hranges[4 * k + 2];
+  if (any32) {
+    GBHF_CUDA(c, c->dfloat.alloc((size_t)n * n));
+    GBHF_TRY(to_float(c, (size_t)n * n, d_Dsq, c->dfloat.p));
+  }
+  PairData& P = c->pairs;
+  const int* f0 = st.f0.p;
+  int nt[NCOMBO][2];
+  for (int k = 0; k < NCOMBO; ++k) {
+    nt[k][0] = st.hranges[4 * k + 1] - st.hranges[4 * k + 0];
+    nt[k][1] = st.hranges[4 * k + 3] - st.hranges[4 * k + 2];
+  }
+  const bool ev = c->prof.events;
+  if (ev) GBHF_CUDA(c, cudaEventRecord(c->ev[0], c->stream));
+  // FP64 kernels (heaviest class first)
+  GBHF_TRY((launch_class<1, 1, 1, 1, double, true>(c, 5, 0, d_Dsq, d_G, P.bra64.p, P.ket64.p, c->boys64.p, f0, nt[5][0])));
+  GBHF_TRY((launch_class<1, 1, 1, 0, double, false>(c, 4, 0, d_Dsq, d_G, P.bra64.p, P.ket64.p, c->boys64.p, f0, nt[4][0])));
+  GBHF_TRY((launch_class<1, 1, 0, 0, double, false>(c, 3, 0, d_Dsq, d_G, P.bra64.p, P.ket64.p, c->boys64.p, f0, nt[3][0])));
+  GBHF_TRY((launch_class<1, 0, 1, 0, double, false>(c, 2, 0, d_Dsq, d_G, P.bra64.p, P.ket64.p, c->boys64.p, f0, nt[2][0])));
+  GBHF_TRY((launch_class<1, 0, 0, 0, double, false>(c, 1, 0, d_Dsq, d_G, P.bra64.p, P.ket64.p, c->boys64.p, f0, nt[1][0])));
+  GBHF_TRY((launch_class<0, 0, 0, 0, double, false>(c, 0, 0, d_Dsq, d_G, P.bra64.p, P.ket64.p, c->boys64.p, f0, nt[0][0])));
+  if (ev) GBHF_CUDA(c, cudaEventRecord(c->ev[1], c->stream));
+  if (any32) {
+    const float* Df = c->dfloat.p;
+    GBHF_TRY((launch_class<1, 1, 1, 1, float, false>(c, 5, 1, Df, d_G, P.bra32.p, P.ket32.p, c->boys32.p, f0, nt[5][1])));
+    GBHF_TRY((launch_class<1, 1, 1, 0, float, false>(c, 4, 1, Df, d_G, P.bra32.p, P.ket32.p, c->boys32.p, f0, nt[4][1])));
+    GBHF_TRY((launch_class<1, 1, 0, 0, float, false>(c, 3, 1, Df, d_G, P.bra32.p, P.ket32.p, c->boys32.p, f0, nt[3][1])));
+    GBHF_TRY((launch_class<1, 0, 1, 0, float, false>(c, 2, 1, Df, d_G, P.bra32.p, P.ket32.p, c->boys32.p, f0, nt[2][1])));
+    GBHF_TRY((launch_class<1, 0, 0, 0, float, false>(c, 1, 1, Df, d_G, P.bra32.p, P.ket32.p, c->boys32.p, f0, nt[1][1])));
+    GBHF_TRY((launch_class<0, 0, 0, 0, float, false>(c, 0, 1, Df, d_G, P.bra32.p, P.ket32.p, c->boys32.p, f0, nt[0][1])));
+  }
+  if (ev) GBHF_CUDA(c, cudaEventRecord(c->ev[2], c->stream));
+  // statistics
+  unsigned long long hs[6 * NCOMBO];
+  GBHF_CUDA(c, cudaMemcpyAsync(hs, c->tasks.stats.p, sizeof(hs), cudaMemcpyDeviceToHost, c->stream));
+  GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
+  for (int k = 0; k < NCOMBO; ++k)
+    for (int p = 0; p < 2; ++p) {
+      const unsigned long long* s = hs + 3 * (2 * k + p);
+      c->prof.shellq += (double)s[0];
+      c->prof.fnq += (double)s[1];
+      (p == 0 ? c->prof.prim64 : c->prof.prim32) += (double)s[2];
+    }
+  if (ev) {
+    float m64 = 0, m32 = 0;
+    GBHF_CUDA(c, cudaEventElapsedTime(&m64, c->ev[0], c->ev[1]));
+    GBHF_CUDA(c, cudaEventElapsedTime(&m32, c->ev[1], c->ev[2]));
+    c->prof.jk_ms64 += m64;
+    c->prof.jk_ms32 += m32;
+  }
+  return GBHF_OK;
+}
+
+}  // namespace gbhf

@@ -1,0 +1,712 @@
+// Dense FP64 linear algebra for the SCF: DMMA GEMM (mma.sync m8n8k4 f64),
+// cooperative parallel Jacobi eigen-solver, DIIS helpers and reductions.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "gbhf_internal.h"
+
+namespace gbhf {
+
+// ------------------------------------------------------------------ GEMM ----
+// C = alpha * op(A) * op(B) + beta * C, row-major.  op(A) is m x k (A stored
+// m x k, or k x m when ta), op(B) is k x n.  CTA tile 64x64, 4 warps of 32x32,
+// each warp a 4x4 grid of 8x8 DMMA tiles, k-step 16.
+constexpr int GT = 64, GK = 16;
+
+__device__ __forceinline__ void dmma(double& d0, double& d1, double a, double b) {
+  asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0,%1}, {%2}, {%3}, {%0,%1};\n"
+               : "+d"(d0), "+d"(d1)
+               : "d"(a), "d"(b));
+}
+
+__global__ void __launch_bounds__(128) k_dgemm(bool ta, bool tb, int m, int n, int k, double alpha,
+                                               const double* __restrict__ A, int lda, const double* __restrict__ B,
+                                               int ldb, double beta, double* __restrict__ C, int ldc) {
+  __shared__ double As[GT][GK + 1];
+  __shared__ double Bs[GK][GT + 2];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int row0 = blockIdx.y * GT, col0 = blockIdx.x * GT;
+  const int wr = (warp >> 1) * 32, wc = (warp & 1) * 32;
+  double acc[4][4][2];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j][0] = acc[i][j][1] = 0.0;
+  for (int kk = 0; kk < k; kk += GK) {
+    // A tile: 64 x 16
+    for (int idx = tid; idx < GT * GK; idx += 128) {
+      int r, cc;
+      if (!ta) {
+        r = idx / GK;
+        cc = idx % GK;
+      } else {
+        cc = idx / GT;
+        r = idx % GT;
+      }
+      const int gr = row0 + r, gk = kk + cc;
+      double v = 0.0;
+      if (gr < m && gk < k) v = ta ? A[(long)gk * lda + gr] : A[(long)gr * lda + gk];
+      As[r][cc] = v;
+    }
+    // B tile: 16 x 64
+    for (int idx = tid; idx < GK * GT; idx += 128) {
+      int r, cc;
+      if (!tb) {
+        r = idx / GT;
+        cc = idx % GT;
+      } else {
+        cc = idx / GK;
+        r = idx % GK;
+      }
+      const int gk = kk + r, gc = col0 + cc;
+      double v = 0.0;
+      if (gk < k && gc < n) v = tb ? B[(long)gc * ldb + gk] : B[(long)gk * ldb + gc];
+      Bs[r][cc] = v;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k4 = 0; k4 < GK; k4 += 4) {
+      double af[4], bf[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) af[i] = As[wr + i * 8 + (lane >> 2)][k4 + (lane & 3)];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) bf[j] = Bs[k4 + (lane & 3)][wc + j * 8 + (lane >> 2)];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) dmma(acc[i][j][0], acc[i][j][1], af[i], bf[j]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int r = row0 + wr + i * 8 + (lane >> 2);
+        const int cc = col0 + wc + j * 8 + 2 * (lane & 3) + h;
+        if (r < m && cc < n) {
+          double* p = C + (long)r * ldc + cc;
+          *p = alpha * acc[i][j][h] + (beta == 0.0 ? 0.0 : beta * *p);
+        }
+      }
+}
+
+gbhf_status gemm(gbhf_ctx* c, bool ta, bool tb, int m, int n, int k, double alpha, const double* A, int lda,
+                 const double* B, int ldb, double beta, double* C, int ldc) {
+  if (m <= 0 || n <= 0) return GBHF_OK;
+  dim3 grid((n + GT - 1) / GT, (m + GT - 1) / GT);
+  k_dgemm<<<grid, 128, 0, c->stream>>>(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+  count_launch(c);
+  GBHF_CUDA(c, cudaGetLastError());
+  return GBHF_OK;
+}
+
+// ------------------------------------------------------- small kernels ----
+__global__ void k_flat_to_square(int n, const double* __restrict__ f, double* __restrict__ s) {
+  const int i = blockIdx.y, j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  const int a = min(i, j), b = max(i, j);
+  s[(long)i * n + j] = f[(long)a * n - (long)a * (a - 1) / 2 + (b - a)];
+}
+
+__global__ void k_square_to_flat(int n, const double* __restrict__ s, double* __restrict__ f) {
+  const int i = blockIdx.y, j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n || j < i) return;
+  f[(long)i * n - (long)i * (i - 1) / 2 + (j - i)] = s[(long)i * n + j];
+}
+
+gbhf_status flat_to_square(gbhf_ctx* c, int n, const double* d_flat, double* d_sq) {
+  k_flat_to_square<<<dim3((n + 127) / 128, n), 128, 0, c->stream>>>(n, d_flat, d_sq);
+  count_launch(c);
+  GBHF_CUDA(c, cudaGetLastError());
+  return GBHF_OK;
+}
+
+gbhf_status square_to_flat(gbhf_ctx* c, int n, const double* d_sq, double* d_flat) {
+  k_square_to_flat<<<dim3((n + 127) / 128, n), 128, 0, c->stream>>>(n, d_sq, d_flat);
+  count_launch(c);
+  GBHF_CUDA(c, cudaGetLastError());
+  return GBHF_OK;
+}
+
+__global__ void k_axpby(size_t n, double a, const double* __restrict__ x, double b, const double* __restrict__ y,
+                        double* __restrict__ out) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    out[i] = a * x[i] + (b == 0.0 ? 0.0 : b * y[i]);
+}
+
+gbhf_status axpby(gbhf_ctx* c, size_t n, double a, const double* x, double b, const double* y, double* out) {
+  int blocks = (int)std::min<size_t>((n + 255) / 256, (size_t)c->nsm * 8);
+  k_axpby<<<std::max(blocks, 1), 256, 0, c->stream>>>(n, a, x, b, y ? y : x, out);
+  count_launch(c);
+  GBHF_CUDA(c, cudaGetLastError());
+  return GBHF_OK;
+}
+
+// out = H + G + G^T (all square)
+__global__ void k_add_sym(int n, const double* __restrict__ H, const double* __restrict__ G, double* __restrict__ out) {
+  const int i = blockIdx.y, j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  const long ij = (long)i * n + j, ji = (long)j * n + i;
+  out[ij] = (H ? H[ij] : 0.0) + G[ij] + G[ji];
+}
+
+gbhf_status add_sym(gbhf_ctx* c, int n, const double* d_H, const double* d_Gpp, double* d_out) {
+  k_add_sym<<<dim3((n + 127) / 128, n), 128, 0, c->stream>>>(n, d_H, d_Gpp, d_out);
+  count_launch(c);
+  GBHF_CUDA(c, cudaGetLastError());
+  return GBHF_OK;
+}
+
+// e = M - M^T
+__global__ void k_antisym(int n, const double* __restrict__ M, double* __restrict__ e) {
+  const int i = blockIdx.y, j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  e[(long)i * n + j] = M[(long)i * n + j] - M[(long)j * n + i];
+}
+
+__global__ void k_to_float(size_t n, const double* __restrict__ x, float* __restrict__ y) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    y[i] = (float)x[i];
+}
+
+gbhf_status to_float(gbhf_ctx* c, size_t n, const double* d_x, float* d_y) {
+  int blocks = (int)std::min<size_t>((n + 255) / 256, (size_t)c->nsm * 8);
+  k_to_float<<<std::max(blocks, 1), 256, 0, c->stream>>>(n, d_x, d_y);
+  count_launch(c);
+  GBHF_CUDA(c, cudaGetLastError());
+  return GBHF_OK;
+}
+
+// Block reduction helper (sum or max) into a double.
+__device__ __forceinline__ double block_reduce(double v, bool is_max) {
+  __shared__ double sh[32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    double w = __shfl_xor_sync(0xffffffffu, v, o);
+    v = is_max ? fmax(v, w) : v + w;
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) sh[wid] = v;
+  __syncthreads();
+  const int nw = (blockDim.x + 31) / 32;
+  v = threadIdx.x < nw ? sh[threadIdx.x] : (is_max ? 0.0 : 0.0);
+  if (wid == 0) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      double w = __shfl_xor_sync(0xffffffffu, v, o);
+      v = is_max ? fmax(v, w) : v + w;
+    }
+  }
+  return v;
+}
+
+// out[0] = max|e|, out[1] = 1/2 sum Dnew(H+F) (when H,F given), out[2] = sum (Dnew-Dold)^2,
+// out[3] = sum(D (H + F)) with Dold.  Single block.
+__global__ void k_stats(int n, const double* __restrict__ e, const double* __restrict__ H, const double* __restrict__ F,
+                        const double* __restrict__ Dn, const double* __restrict__ Do, double* __restrict__ out) {
+  double mx = 0, en = 0, dd = 0, eo = 0;
+  const long nn = (long)n * n;
+  for (long i = threadIdx.x; i < nn; i += blockDim.x) {
+    if (e) mx = fmax(mx, fabs(e[i]));
+    if (H && F && Dn) en += Dn[i] * (H[i] + F[i]);
+    if (H && F && Do) eo += Do[i] * (H[i] + F[i]);
+    if (Dn && Do) {
+      const double d = Dn[i] - Do[i];
+      dd += d * d;
+    }
+  }
+  mx = block_reduce(mx, true);
+  __syncthreads();
+  en = block_reduce(en, false);
+  __syncthreads();
+  dd = block_reduce(dd, false);
+  __syncthreads();
+  eo = block_reduce(eo, false);
+  if (threadIdx.x == 0) {
+    out[0] = mx;
+    out[1] = 0.5 * en;
+    out[2] = dd;
+    out[3] = 0.5 * eo;
+  }
+}
+
+gbhf_status reduce_stats(gbhf_ctx* c, int n, const double* d_e, const double* d_H, const double* d_F,
+                         const double* d_Dnew, const double* d_Dold, double* host_out4) {
+  GBHF_CUDA(c, c->small.alloc(64));
+  k_stats<<<1, 1024, 0, c->stream>>>(n, d_e, d_H, d_F, d_Dnew, d_Dold, c->small.p);
+  count_launch(c);
+  GBHF_CUDA(c, cudaGetLastError());
+  GBHF_CUDA(c, cudaMemcpyAsync(host_out4, c->small.p, 4 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
+  return GBHF_OK;
+}
+
+__global__ void k_max_abs(size_t n, const double* __restrict__ x, double* out) {
+  double m = 0;
+  for (size_t i = threadIdx.x; i < n; i += blockDim.x) m = fmax(m, fabs(x[i]));
+  m = block_reduce(m, true);
+  if (threadIdx.x == 0) *out = m;
+}
+
+gbhf_status max_abs(gbhf_ctx* c, size_t n, const double* d_x, double* host_out) {
+  GBHF_CUDA(c, c->small.alloc(64));
+  k_max_abs<<<1, 1024, 0, c->stream>>>(n, d_x, c->small.p + 8);
+  count_launch(c);
+  GBHF_CUDA(c, cudaMemcpyAsync(host_out, c->small.p + 8, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
+  return GBHF_OK;
+}
+
+// out[j] = sum_i mats[j][i] * e[i], j < k  (DIIS B-matrix row; tr(e_j^T e) = sum e_j (.) e)
+struct MatPtrs {
+  const double* p[16];
+};
+__global__ void k_dots(size_t n2, int k, MatPtrs mats, const double* __restrict__ e, double* __restrict__ out) {
+  const int j = blockIdx.x;
+  if (j >= k) return;
+  const double* m = mats.p[j];
+  double s = 0;
+  for (size_t i = threadIdx.x; i < n2; i += blockDim.x) s += m[i] * e[i];
+  s = block_reduce(s, false);
+  if (threadIdx.x == 0) out[j] = s;
+}
+
+gbhf_status dot_matrices(gbhf_ctx* c, int n2, int k, const double* const* mats, const double* d_e, double* d_out) {
+  if (k > 16) return fail(c, GBHF_ERR_BAD_INPUT, "too many DIIS vectors");
+  MatPtrs mp;
+  for (int j = 0; j < k; ++j) mp.p[j] = mats[j];
+  k_dots<<<k, 512, 0, c->stream>>>((size_t)n2, k, mp, d_e, d_out);
+  count_launch(c);
+  GBHF_CUDA(c, cudaGetLastError());
+  return GBHF_OK;
+}
+
+// out = sum_j coefs[j] * mats[j]  (coefs in device memory)
+__global__ void k_lincomb(size_t n2, int k, MatPtrs mats, const double* __restrict__ coefs, double* __restrict__ out) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n2; i += (size_t)gridDim.x * blockDim.x) {
+    double s = 0;
+    for (int j = 0; j < k; ++j) s += coefs[j] * mats.p[j][i];
+    out[i] = s;
+  }
+}
+
+gbhf_status lincomb(gbhf_ctx* c, int n2, int k, const double* const* mats, const double* coefs, double* d_out) {
+  if (k > 16) return fail(c, GBHF_ERR_BAD_INPUT, "too many DIIS vectors");
+  MatPtrs mp;
+  for (int j = 0; j < k; ++j) mp.p[j] = mats[j];
+  int blocks = std::max(1, std::min((n2 + 255) / 256, c->nsm * 8));
+  k_lincomb<<<blocks, 256, 0, c->stream>>>((size_t)n2, k, mp, coefs, d_out);
+  count_launch(c);
+  GBHF_CUDA(c, cudaGetLastError());
+  return GBHF_OK;
+}
+
+// gaussElem (NumericalTools/GaussElimination.hs:42-98), single thread: unpivoted
+// elimination over all pivots, failure when a row of the eliminated matrix has
+// no |entry| > 1e-6 or any entry is NaN/Inf, then back substitution.
+__device__ bool gauss_elem_dev(int m, double* a, double* b, double* x) {
+  for (int k = 0; k < m; ++k) {
+    const double piv = a[k * m + k];
+    for (int i = k + 1; i < m; ++i) {
+      const double alpha = a[i * m + k] / piv;
+      for (int j = m - 1; j >= k; --j) a[i * m + j] = a[i * m + j] - alpha * a[k * m + j];
+      b[i] = b[i] - alpha * b[k];
+    }
+  }
+  for (int i = 0; i < m; ++i) {
+    bool any = false;
+    for (int j = 0; j < m; ++j) {
+      const double v = a[i * m + j];
+      if (isnan(v) || isinf(v)) return false;
+      if (fabs(v) > 1e-6) any = true;
+    }
+    if (!any) return false;
+  }
+  for (int k = m - 1; k >= 0; --k) {
+    double s = 0;
+    for (int j = k + 1; j < m; ++j) s += x[j] * a[k * m + j];
+    x[k] = (b[k] - s) * (1.0 / a[k * m + k]);
+  }
+  return true;
+}
+
+// Note: the reference evaluates alpha = mtx[i][k]/mtx[k][k] from the matrix
+// before the pivot step for every j; updating j from m-1 down to k keeps
+// a[i][k] unchanged until its own (last) update, which reproduces that.
+
+__global__ void k_gauss(int m, const double* __restrict__ a_in, const double* __restrict__ b_in, double* __restrict__ x,
+                        int* ok) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double a[81], b[9];
+  for (int i = 0; i < m * m; ++i) a[i] = a_in[i];
+  for (int i = 0; i < m; ++i) b[i] = b_in[i];
+  *ok = gauss_elem_dev(m, a, b, x) ? 1 : 0;
+}
+
+gbhf_status gauss_elem_dev_call(gbhf_ctx* c, int m, const double* h_a, const double* h_b, double* h_x, bool* ok) {
+  if (m < 1 || m > 9) return fail(c, GBHF_ERR_BAD_INPUT, "gauss elimination: 1 <= m <= 9");
+  GBHF_CUDA(c, c->small.alloc(256));
+  double* da = c->small.p + 16;
+  double* db = da + 81;
+  double* dx = db + 9;
+  int* dok = (int*)(dx + 9);
+  GBHF_CUDA(c, cudaMemcpyAsync(da, h_a, m * m * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  GBHF_CUDA(c, cudaMemcpyAsync(db, h_b, m * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  k_gauss<<<1, 32, 0, c->stream>>>(m, da, db, dx, dok);
+  count_launch(c);
+  int hok = 0;
+  GBHF_CUDA(c, cudaMemcpyAsync(h_x, dx, m * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  GBHF_CUDA(c, cudaMemcpyAsync(&hok, dok, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
+  *ok = hok != 0;
+  return GBHF_OK;
+}
+
+// --------------------------------------------------------------- Jacobi ----
+// Parallel cyclic Jacobi (round-robin ordering) in one cooperative launch.
+// The grid barrier spins with an iteration limit; on timeout it raises
+// GBHF_DEV_ERR_TIMEOUT in *status and every block leaves.
+constexpr long long BARRIER_SPIN_LIMIT = 1ll << 24;
+
+__device__ bool grid_barrier(unsigned* count, unsigned* gen, int* status) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    volatile unsigned* vgen = gen;
+    const unsigned g = *vgen;
+    __threadfence();
+    const unsigned arrived = atomicAdd(count, 1u);
+    if (arrived == gridDim.x - 1) {
+      atomicExch(count, 0u);
+      __threadfence();
+      atomicAdd(gen, 1u);
+    } else {
+      long long it = 0;
+      while (*vgen == g) {
+        if (++it > BARRIER_SPIN_LIMIT || *((volatile int*)status) & GBHF_DEV_ERR_TIMEOUT) {
+          atomicOr(status, GBHF_DEV_ERR_TIMEOUT);
+          ok = 0;
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+struct JacobiArgs {
+  int n, m;            // matrix size, padded even size
+  double* A;           // m x m (padded with zeros), destroyed
+  double* V;           // n x m accumulated rotations (rows n)
+  double* rot;         // per index: alpha, beta (2*m)
+  int* partner;        // per index
+  double* red;         // reduction scratch (2 doubles)
+  unsigned* bar;       // barrier count, generation
+  int* status;
+  int max_sweeps;
+  double tol;          // relative off-diagonal Frobenius tolerance
+  int* sweeps_out;
+};
+
+__device__ __forceinline__ void pair_of(int r, int k, int m, int& p, int& q) {
+  // circle method: index m-1 fixed, others rotate
+  if (k == 0) {
+    p = r % (m - 1);
+    q = m - 1;
+  } else {
+    p = (r + k) % (m - 1);
+    q = (r - k + (m - 1)) % (m - 1);
+  }
+  if (p > q) {
+    int t = p;
+    p = q;
+    q = t;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_jacobi(JacobiArgs a) {
+  const int m = a.m, n = a.n, half = m / 2;
+  const long gt = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  const long gs = (long)gridDim.x * blockDim.x;
+  unsigned* cnt = a.bar;
+  unsigned* gen = a.bar + 1;
+  // Frobenius norm^2 of A (fixed under rotations)
+  if (gt == 0) {
+    a.red[0] = 0;
+    a.red[1] = 0;
+  }
+  if (!grid_barrier(cnt, gen, a.status)) return;
+  {
+    double s = 0;
+    for (long i = gt; i < (long)m * m; i += gs) s += a.A[i] * a.A[i];
+    s = block_reduce(s, false);
+    if (threadIdx.x == 0) atomicAdd(&a.red[0], s);
+  }
+  if (!grid_barrier(cnt, gen, a.status)) return;
+  const double fro2 = a.red[0];
+  int sweep = 0;
+  for (; sweep < a.max_sweeps; ++sweep) {
+    // convergence test on the off-diagonal norm
+    if (gt == 0) a.red[1] = 0;
+    if (!grid_barrier(cnt, gen, a.status)) return;
+    {
+      double s = 0;
+      for (long i = gt; i < (long)m * m; i += gs) {
+        const long r = i / m, cc = i % m;
+        if (r != cc) s += a.A[i] * a.A[i];
+      }
+      s = block_reduce(s, false);
+      if (threadIdx.x == 0) atomicAdd(&a.red[1], s);
+    }
+    if (!grid_barrier(cnt, gen, a.status)) return;
+    const double off2 = a.red[1];
+    if (off2 <= a.tol * a.tol * fro2 || off2 == 0.0) break;
+    for (int r = 0; r < m - 1; ++r) {
+      // phase A: rotation per pair
+      for (long k = gt; k < half; k += gs) {
+        int p, q;
+        pair_of(r, (int)k, m, p, q);
+        const double app = a.A[(long)p * m + p], aqq = a.A[(long)q * m + q], apq = a.A[(long)p * m + q];
+        double c = 1.0, s = 0.0, t = 0.0;
+        if (apq != 0.0 && fabs(apq) > 1e-300 && !(fabs(apq) < 1e-18 * fmax(fabs(app), fabs(aqq)))) {
+          const double theta = (aqq - app) / (2.0 * apq);
+          if (fabs(theta) > 1e150) {
+            t = 0.5 / theta;
+          } else {
+            t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+          }
+          c = rsqrt(t * t + 1.0);
+          s = t * c;
+        }
+        a.rot[2 * p] = c;
+        a.rot[2 * p + 1] = -s;
+        a.rot[2 * q] = c;
+        a.rot[2 * q + 1] = s;
+        a.partner[p] = q;
+        a.partner[q] = p;
+        // stash t for the exact diagonal update (index p slot of red area is not used)
+        a.rot[2 * m + k] = t;
+      }
+      if (!grid_barrier(cnt, gen, a.status)) return;
+      // phase B: 2x2 block updates of A (upper block triangle) and V columns
+      const long nblk = (long)half * half;
+      for (long idx = gt; idx < nblk + (long)n * half; idx += gs) {
+        if (idx < nblk) {
+          const int P = (int)(idx / half), Qb = (int)(idx % half);
+          if (Qb < P) continue;
+          int p1, q1, p2, q2;
+          pair_of(r, P, m, p1, q1);
+          pair_of(r, Qb, m, p2, q2);
+          if (P == Qb) {
+            const double t = a.rot[2 * m + P];
+            const double apq = a.A[(long)p1 * m + q1];
+            a.A[(long)p1 * m + p1] -= t * apq;
+            a.A[(long)q1 * m + q1] += t * apq;
+            if (t != 0.0) {
+              a.A[(long)p1 * m + q1] = 0.0;
+              a.A[(long)q1 * m + p1] = 0.0;
+            }
+          } else {
+            const int ii[2] = {p1, q1}, jj[2] = {p2, q2};
+            double old[2][2];
+            for (int x = 0; x < 2; ++x)
+              for (int y = 0; y < 2; ++y) old[x][y] = a.A[(long)ii[x] * m + jj[y]];
+            for (int x = 0; x < 2; ++x) {
+              const double al_i = a.rot[2 * ii[x]], be_i = a.rot[2 * ii[x] + 1];
+              for (int y = 0; y < 2; ++y) {
+                const double al_j = a.rot[2 * jj[y]], be_j = a.rot[2 * jj[y] + 1];
+                const double v = al_i * al_j * old[x][y] + al_i * be_j * old[x][1 - y] + be_i * al_j * old[1 - x][y] +
+                                 be_i * be_j * old[1 - x][1 - y];
+                a.A[(long)ii[x] * m + jj[y]] = v;
+                a.A[(long)jj[y] * m + ii[x]] = v;
+              }
+            }
+          }
+        } else {
+          const long v = idx - nblk;
+          const int row = (int)(v / half), P = (int)(v % half);
+          int p, q;
+          pair_of(r, P, m, p, q);
+          const double vp = a.V[(long)row * m + p], vq = a.V[(long)row * m + q];
+          a.V[(long)row * m + p] = a.rot[2 * p] * vp + a.rot[2 * p + 1] * vq;
+          a.V[(long)row * m + q] = a.rot[2 * q] * vq + a.rot[2 * q + 1] * vp;
+        }
+      }
+      if (!grid_barrier(cnt, gen, a.status)) return;
+    }
+  }
+  if (gt == 0) {
+    *a.sweeps_out = sweep;
+    if (sweep >= a.max_sweeps) atomicOr(a.status, GBHF_DEV_ERR_NOTCONV);
+  }
+}
+
+// ascending sort of the diagonal with the matching columns
+__global__ void k_sort_eig(int n, int m, const double* __restrict__ A, const double* __restrict__ V,
+                           double* __restrict__ evals, double* __restrict__ evecs) {
+  // one block; rank by (value, index)
+  __shared__ double sv[1024];
+  __shared__ int rank[1024];
+  for (int i = threadIdx.x; i < n; i += blockDim.x) sv[i] = A[(long)i * m + i];
+  __syncthreads();
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    int r = 0;
+    const double vi = sv[i];
+    for (int j = 0; j < n; ++j) {
+      const double vj = sv[j];
+      if (vj < vi || (vj == vi && j < i)) ++r;
+    }
+    rank[i] = r;
+    evals[r] = vi;
+  }
+  __syncthreads();
+  for (long idx = threadIdx.x; idx < (long)n * n; idx += blockDim.x) {
+    const int row = (int)(idx / n), col = (int)(idx % n);
+    evecs[(long)row * n + rank[col]] = V[(long)row * m + col];
+  }
+}
+
+__global__ void k_jacobi_init(int n, int m, const double* __restrict__ Ain, double* __restrict__ A,
+                              double* __restrict__ V) {
+  for (long idx = blockIdx.x * (long)blockDim.x + threadIdx.x; idx < (long)m * m; idx += (long)gridDim.x * blockDim.x) {
+    const int i = (int)(idx / m), j = (int)(idx % m);
+    A[idx] = (i < n && j < n) ? Ain[(long)i * n + j] : 0.0;
+    if (i < n) V[(long)i * m + j] = (i == j) ? 1.0 : 0.0;
+  }
+}
+
+// d_evecs (n x n): eigenvectors of A in columns, ascending eigenvalues.
+gbhf_status eigh(gbhf_ctx* c, int n, const double* d_A, double* d_evals, double* d_evecs, const double* d_V0) {
+  if (n <= 0 || n > 1024) return fail(c, GBHF_ERR_UNSUPPORTED, "eigen-solve supports 1 <= n <= 1024");
+  JacobiWork& w = c->jac;
+  const int mm = std::max(2, n + (n & 1));
+  GBHF_CUDA(c, w.A.alloc((size_t)mm * mm));
+  GBHF_CUDA(c, w.V.alloc((size_t)n * mm));
+  GBHF_CUDA(c, w.rot.alloc(3 * (size_t)mm));
+  GBHF_CUDA(c, w.red.alloc(4));
+  GBHF_CUDA(c, w.partner.alloc(mm));
+  GBHF_CUDA(c, w.sweeps.alloc(1));
+  GBHF_CUDA(c, w.bar.alloc(2));
+  GBHF_CUDA(c, c->dev_status.alloc(1));
+  GBHF_CUDA(c, cudaMemsetAsync(w.bar.p, 0, 2 * sizeof(unsigned), c->stream));
+  GBHF_CUDA(c, cudaMemsetAsync(c->dev_status.p, 0, sizeof(int), c->stream));
+  // optional warm start: A' = V0^T A V0 (V0 orthogonal), eigenvectors = V0 * W
+  const double* src = d_A;
+  GBHF_CUDA(c, w.t1.alloc((size_t)n * n));
+  GBHF_CUDA(c, w.t2.alloc((size_t)n * n));
+  GBHF_CUDA(c, w.t3.alloc((size_t)n * n));
+  if (d_V0) {
+    GBHF_TRY(gemm(c, false, false, n, n, n, 1.0, d_A, n, d_V0, n, 0.0, w.t1.p, n));
+    GBHF_TRY(gemm(c, true, false, n, n, n, 1.0, d_V0, n, w.t1.p, n, 0.0, w.t2.p, n));
+    src = w.t2.p;
+  }
+  k_jacobi_init<<<std::max(1, std::min(c->nsm * 4, (mm * mm + 255) / 256)), 256, 0, c->stream>>>(n, mm, src, w.A.p,
+                                                                                                   w.V.p);
+  count_launch(c);
+  JacobiArgs a;
+  a.n = n;
+  a.m = mm;
+  a.A = w.A.p;
+  a.V = w.V.p;
+  a.rot = w.rot.p;
+  a.partner = w.partner.p;
+  a.red = w.red.p;
+  a.bar = w.bar.p;
+  a.status = c->dev_status.p;
+  a.max_sweeps = 40;
+  a.tol = 1e-14;
+  a.sweeps_out = w.sweeps.p;
+  if (w.grid == 0) {
+    int per_sm = 0;
+    GBHF_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_jacobi, 256, 0));
+    w.grid = std::max(1, c->nsm * std::min(per_sm, 2));
+  }
+  const long work = (long)(mm / 2) * (mm / 2) + (long)n * (mm / 2);
+  const int grid = (int)std::max(1L, std::min<long>(w.grid, (work + 255) / 256));
+  void* args[] = {&a};
+  GBHF_CUDA(c, cudaLaunchCooperativeKernel((void*)k_jacobi, dim3(grid), dim3(256), args, 0, c->stream));
+  count_launch(c);
+  double* vec_out = d_V0 ? w.t3.p : d_evecs;
+  k_sort_eig<<<1, 1024, 0, c->stream>>>(n, mm, w.A.p, w.V.p, d_evals, vec_out);
+  count_launch(c);
+  if (d_V0) GBHF_TRY(gemm(c, false, false, n, n, n, 1.0, d_V0, n, w.t3.p, n, 0.0, d_evecs, n));
+  int st = 0, sweeps = 0;
+  GBHF_CUDA(c, cudaMemcpyAsync(&st, c->dev_status.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  GBHF_CUDA(c, cudaMemcpyAsync(&sweeps, w.sweeps.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
+  GBHF_CUDA(c, cudaGetLastError());
+  w.last_sweeps = sweeps;
+  if (st & GBHF_DEV_ERR_TIMEOUT) return fail(c, GBHF_ERR_DEVICE_TIMEOUT, "Jacobi grid barrier timed out");
+  if (st & GBHF_DEV_ERR_NOTCONV) return fail(c, GBHF_ERR_NOT_CONVERGED, "Jacobi eigen-solver did not converge");
+  return GBHF_OK;
+}
+
+// X = U s^-1/2 U^T (symmOrtho, HartreeFock/BasisOrthogonalization.hs:26-34)
+__global__ void k_scale_cols(int n, const double* __restrict__ U, const double* __restrict__ s, double* __restrict__ out) {
+  const int i = blockIdx.y, j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  out[(long)i * n + j] = U[(long)i * n + j] * (1.0 / sqrt(s[j]));
+}
+
+gbhf_status symm_ortho_dev(gbhf_ctx* c, int n, const double* d_S, double* d_X) {
+  const size_t nn = (size_t)n * n;
+  GBHF_WS(c, U, 10, nn);
+  GBHF_WS(c, s, 11, (size_t)n);
+  GBHF_WS(c, T, 12, nn);
+  GBHF_TRY(eigh(c, n, d_S, s, U, nullptr));
+  k_scale_cols<<<dim3((n + 127) / 128, n), 128, 0, c->stream>>>(n, U, s, T);
+  count_launch(c);
+  GBHF_TRY(gemm(c, false, true, n, n, n, 1.0, T, n, U, n, 0.0, d_X, n));
+  GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
+  return GBHF_OK;
+}
+
+// diagonalHF (HartreeFock/HartreeFock.hs:263-273) with square F in:
+// F' = X^T F X, eigen-solve (warm-started from d_Cp when given; d_Cp receives
+// the new C'), C = X C', D = 2 C_occ C_occ^T (calcDensity, :195-208).
+gbhf_status diagonal_hf_dev(gbhf_ctx* c, int n, const double* d_Fsq, const double* d_X, int nocc, double* d_C,
+                            double* d_Dsq, double* d_eps, double* d_Cp) {
+  const size_t nn = (size_t)n * n;
+  GBHF_WS(c, T1, 10, nn);
+  GBHF_WS(c, Fp, 11, nn);
+  GBHF_WS(c, Cp, 12, nn);
+  GBHF_TRY(gemm(c, true, false, n, n, n, 1.0, d_X, n, d_Fsq, n, 0.0, T1, n));
+  GBHF_TRY(gemm(c, false, false, n, n, n, 1.0, T1, n, d_X, n, 0.0, Fp, n));
+  GBHF_TRY(eigh(c, n, Fp, d_eps, Cp, d_Cp));
+  if (d_Cp) GBHF_CUDA(c, cudaMemcpyAsync(d_Cp, Cp, nn * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+  GBHF_TRY(gemm(c, false, false, n, n, n, 1.0, d_X, n, Cp, n, 0.0, d_C, n));
+  if (nocc > 0) {
+    GBHF_TRY(gemm(c, false, true, n, n, nocc, 2.0, d_C, n, d_C, n, 0.0, d_Dsq, n));
+  } else {
+    GBHF_CUDA(c, cudaMemsetAsync(d_Dsq, 0, nn * sizeof(double), c->stream));
+  }
+  return GBHF_OK;
+}
+
+// calcErrorMtx (HartreeFock/DIIS.hs:119-132): e = X^T (F D S - S D F) X, with
+// S D F = (F D S)^T for symmetric F, D, S.
+gbhf_status diis_error_dev(gbhf_ctx* c, int n, const double* d_F, const double* d_S, const double* d_D,
+                           const double* d_X, double* d_e) {
+  const size_t nn = (size_t)n * n;
+  GBHF_WS(c, T1, 13, nn);
+  GBHF_WS(c, T2, 14, nn);
+  GBHF_TRY(gemm(c, false, false, n, n, n, 1.0, d_D, n, d_S, n, 0.0, T1, n));   // DS
+  GBHF_TRY(gemm(c, false, false, n, n, n, 1.0, d_F, n, T1, n, 0.0, T2, n));    // FDS
+  k_antisym<<<dim3((n + 127) / 128, n), 128, 0, c->stream>>>(n, T2, T1);         // FDS - SDF
+  count_launch(c);
+  GBHF_TRY(gemm(c, false, false, n, n, n, 1.0, T1, n, d_X, n, 0.0, T2, n));    // e X
+  GBHF_TRY(gemm(c, true, false, n, n, n, 1.0, d_X, n, T2, n, 0.0, d_e, n));    // X^T e X
+  return GBHF_OK;
+}
+
+}  // namespace gbhf

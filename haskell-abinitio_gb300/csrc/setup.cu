@@ -1,0 +1,320 @@
+// Basis upload, Boys tables and shell-pair data for the direct J/K build.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+
+#include "gbhf_internal.h"
+
+namespace gbhf {
+
+gbhf_status fail(gbhf_ctx* c, gbhf_status s, const std::string& msg) {
+  if (c) c->err = msg;
+  return s;
+}
+
+gbhf_status cuda_fail(gbhf_ctx* c, cudaError_t e, const char* where) {
+  std::string m = std::string("CUDA error ") + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ") in " + where;
+  return fail(c, GBHF_ERR_CUDA, m);
+}
+
+static int ncart(int L) { return (L + 1) * (L + 2) / 2; }
+
+// Group CGFs into shells: consecutive CGFs on one atom with the same total
+// angular momentum and identical exponents, in the Cartesian order x, y, z
+// (the order createCGF emits, BasisSet/FetchBasis.hs:50-59).
+static void group_shells(Basis& b) {
+  b.shells.clear();
+  b.shells_ok = true;
+  b.maxL = 0;
+  const int n = b.nbf;
+  int i = 0;
+  static const int px[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+  while (i < n) {
+    const int* l = &b.cgf_lxyz[3 * i];
+    const int L = l[0] + l[1] + l[2];
+    b.maxL = std::max(b.maxL, L);
+    Shell s;
+    s.atom = b.cgf_atom[i];
+    s.L = L;
+    s.np = b.cgf_nprim[i];
+    s.ncomp = ncart(L);
+    s.f0 = i;
+    s.expo.assign(b.prim_exp.begin() + b.cgf_off[i], b.prim_exp.begin() + b.cgf_off[i] + s.np);
+    s.coef.assign(b.prim_coef.begin() + b.cgf_off[i], b.prim_coef.begin() + b.cgf_off[i] + s.np);
+    bool ok = L <= 1;
+    int take = (L <= 1) ? s.ncomp : 1;
+    if (i + take > n) ok = false;
+    for (int c = 0; ok && c < take; ++c) {
+      const int j = i + c;
+      const int* lj = &b.cgf_lxyz[3 * j];
+      if (b.cgf_atom[j] != s.atom || b.cgf_nprim[j] != s.np) ok = false;
+      if (ok && L == 1 && !(lj[0] == px[c][0] && lj[1] == px[c][1] && lj[2] == px[c][2])) ok = false;
+      for (int k = 0; ok && k < s.np; ++k)
+        if (b.prim_exp[b.cgf_off[j] + k] != s.expo[k] || b.prim_coef[b.cgf_off[j] + k] != s.coef[k]) ok = false;
+    }
+    if (!ok) {
+      if (b.shells_ok) {
+        b.shell_msg = "basis function " + std::to_string(i) +
+                      " does not start a complete s or p shell (components x,y,z, shared primitives)";
+      }
+      b.shells_ok = false;
+      s.ncomp = 1;
+      take = 1;
+    }
+    b.shells.push_back(std::move(s));
+    i += take;
+  }
+}
+
+gbhf_status build_basis(gbhf_ctx* c, int n_atoms, const double* xyz, const double* Z, int n_cgf, const int* cgf_atom,
+                        const int* cgf_lxyz, const int* cgf_nprim, const double* coef, const double* expo) {
+  if (n_atoms <= 0 || n_cgf <= 0 || !xyz || !Z || !cgf_atom || !cgf_lxyz || !cgf_nprim || !coef || !expo)
+    return fail(c, GBHF_ERR_BAD_INPUT, "gbhf_set_basis: empty basis or null pointer");
+  Basis b;
+  b.natoms = n_atoms;
+  b.nbf = n_cgf;
+  b.xyz.assign(xyz, xyz + 3 * n_atoms);
+  b.Z.assign(Z, Z + n_atoms);
+  b.cgf_atom.assign(cgf_atom, cgf_atom + n_cgf);
+  b.cgf_lxyz.assign(cgf_lxyz, cgf_lxyz + 3 * n_cgf);
+  b.cgf_nprim.assign(cgf_nprim, cgf_nprim + n_cgf);
+  b.cgf_off.resize(n_cgf + 1);
+  b.cgf_off[0] = 0;
+  for (int i = 0; i < n_cgf; ++i) {
+    if (cgf_atom[i] < 0 || cgf_atom[i] >= n_atoms)
+      return fail(c, GBHF_ERR_BAD_INPUT, "gbhf_set_basis: CGF atom index out of range");
+    if (cgf_nprim[i] <= 0 || cgf_nprim[i] > 6)
+      return fail(c, GBHF_ERR_BAD_INPUT, "gbhf_set_basis: 1..6 primitives per CGF supported");
+    for (int x = 0; x < 3; ++x)
+      if (cgf_lxyz[3 * i + x] < 0 || cgf_lxyz[3 * i + x] > 2)
+        return fail(c, GBHF_ERR_BAD_INPUT, "gbhf_set_basis: Cartesian exponent out of range (s, p, d only)");
+    if (cgf_lxyz[3 * i] + cgf_lxyz[3 * i + 1] + cgf_lxyz[3 * i + 2] > 2)
+      return fail(c, GBHF_ERR_BAD_INPUT, "gbhf_set_basis: angular momentum above d");
+    b.cgf_off[i + 1] = b.cgf_off[i] + cgf_nprim[i];
+  }
+  const int nprim = b.cgf_off[n_cgf];
+  b.prim_coef.assign(coef, coef + nprim);
+  b.prim_exp.assign(expo, expo + nprim);
+  for (int k = 0; k < nprim; ++k)
+    if (!(expo[k] > 0) || !std::isfinite(coef[k]))
+      return fail(c, GBHF_ERR_BAD_INPUT, "gbhf_set_basis: exponents must be positive and coefficients finite");
+  for (int k = 0; k < 3 * n_atoms; ++k)
+    if (!std::isfinite(xyz[k])) return fail(c, GBHF_ERR_BAD_INPUT, "gbhf_set_basis: non-finite coordinate");
+  group_shells(b);
+  c->basis = std::move(b);
+  const Basis& B = c->basis;
+  // device copies (function level)
+  std::vector<int> fn(6 * n_cgf);
+  for (int i = 0; i < n_cgf; ++i) {
+    fn[6 * i] = B.cgf_atom[i];
+    fn[6 * i + 1] = B.cgf_lxyz[3 * i];
+    fn[6 * i + 2] = B.cgf_lxyz[3 * i + 1];
+    fn[6 * i + 3] = B.cgf_lxyz[3 * i + 2];
+    fn[6 * i + 4] = B.cgf_nprim[i];
+    fn[6 * i + 5] = B.cgf_off[i];
+  }
+  GBHF_CUDA(c, c->d_xyz.alloc(3 * n_atoms));
+  GBHF_CUDA(c, c->d_Z.alloc(n_atoms));
+  GBHF_CUDA(c, c->d_fn.alloc(6 * n_cgf));
+  GBHF_CUDA(c, c->d_coef.alloc(nprim));
+  GBHF_CUDA(c, c->d_exp.alloc(nprim));
+  GBHF_CUDA(c, cudaMemcpyAsync(c->d_xyz.p, B.xyz.data(), 3 * n_atoms * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  GBHF_CUDA(c, cudaMemcpyAsync(c->d_Z.p, B.Z.data(), n_atoms * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  GBHF_CUDA(c, cudaMemcpyAsync(c->d_fn.p, fn.data(), 6 * n_cgf * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  GBHF_CUDA(c, cudaMemcpyAsync(c->d_coef.p, B.prim_coef.data(), nprim * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  GBHF_CUDA(c, cudaMemcpyAsync(c->d_exp.p, B.prim_exp.data(), nprim * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
+  c->basis_dev = true;
+  c->pairs_ready = false;
+  return GBHF_OK;
+}
+
+// Exact Boys function by the power series
+//   F_m(x) = exp(-x) sum_k (2x)^k / ((2m+1)(2m+3)...(2m+2k+1))
+// in long double (all terms positive, so no cancellation).
+static double boys_series(int m, double xd) {
+  long double x = xd;
+  long double term = 1.0L / (2 * m + 1), sum = term;
+  for (int k = 1; k < 4000; ++k) {
+    term *= 2 * x / (2 * m + 2 * k + 1);
+    sum += term;
+    if (term < sum * 1e-22L) break;
+  }
+  return (double)(expl(-x) * sum);
+}
+
+gbhf_status ensure_boys_tables(gbhf_ctx* c) {
+  if (c->boys64.p && c->boys32.p) return GBHF_OK;
+  std::vector<double> t64((size_t)BOYS64_NROW * BOYS_NCOL);
+  std::vector<float> t32((size_t)BOYS32_NROW * BOYS_NCOL);
+  for (int j = 0; j < BOYS64_NROW; ++j)
+    for (int m = 0; m < BOYS_NCOL; ++m) t64[(size_t)j * BOYS_NCOL + m] = boys_series(m, j * BOYS64_H);
+  for (int j = 0; j < BOYS32_NROW; ++j) {
+    const float tj = (float)j * BOYS32_H;   // the node the device forms in float
+    for (int m = 0; m < BOYS_NCOL; ++m) t32[(size_t)j * BOYS_NCOL + m] = (float)boys_series(m, (double)tj);
+  }
+  GBHF_CUDA(c, c->boys64.alloc(t64.size()));
+  GBHF_CUDA(c, c->boys32.alloc(t32.size()));
+  GBHF_CUDA(c, cudaMemcpyAsync(c->boys64.p, t64.data(), t64.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  GBHF_CUDA(c, cudaMemcpyAsync(c->boys32.p, t32.data(), t32.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+  GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
+  return GBHF_OK;
+}
+
+static int pair_class(int la, int lb) { return la == 0 ? 0 : (lb == 0 ? 1 : 2); }
+
+gbhf_status ensure_pairs(gbhf_ctx* c) {
+  if (c->pairs_ready) return GBHF_OK;
+  const Basis& b = c->basis;
+  if (!c->basis_dev) return fail(c, GBHF_ERR_BAD_INPUT, "no basis set");
+  if (!b.shells_ok || b.maxL > 1)
+    return fail(c, GBHF_ERR_UNSUPPORTED,
+                "direct J/K kernels need complete s/p shells: " + (b.shell_msg.empty() ? std::string("d functions present") : b.shell_msg));
+  GBHF_TRY(ensure_boys_tables(c));
+  const int ns = (int)b.shells.size();
+  // 1. all pairs (la > lb, or la == lb and A >= B)
+  std::vector<int> A, B;
+  for (int a = 0; a < ns; ++a)
+    for (int bb = 0; bb < ns; ++bb) {
+      const int la = b.shells[a].L, lb = b.shells[bb].L;
+      if (la > lb || (la == lb && a >= bb)) {
+        A.push_back(a);
+        B.push_back(bb);
+      }
+    }
+  const int np = (int)A.size();
+  // 2. Schwarz bounds on the device
+  std::vector<double> Q(np);
+  {
+    DBuf<int> dA, dB;
+    DBuf<double> dQ;
+    GBHF_CUDA(c, dA.alloc(np));
+    GBHF_CUDA(c, dB.alloc(np));
+    GBHF_CUDA(c, dQ.alloc(np));
+    GBHF_CUDA(c, cudaMemcpyAsync(dA.p, A.data(), np * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    GBHF_CUDA(c, cudaMemcpyAsync(dB.p, B.data(), np * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    GBHF_TRY(schwarz_pairs_dev(c, dA.p, dB.p, np, dQ.p));
+    GBHF_CUDA(c, cudaMemcpy(Q.data(), dQ.p, np * sizeof(double), cudaMemcpyDeviceToHost));
+  }
+  // 3. order: class, then primitive-pair count descending, then Q descending
+  std::vector<int> order(np);
+  std::iota(order.begin(), order.end(), 0);
+  auto K_of = [&](int t) { return b.shells[A[t]].np * b.shells[B[t]].np; };
+  auto cls_of = [&](int t) { return pair_class(b.shells[A[t]].L, b.shells[B[t]].L); };
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+    int cx = cls_of(x), cy = cls_of(y);
+    if (cx != cy) return cx < cy;
+    int kx = K_of(x), ky = K_of(y);
+    if (kx != ky) return kx > ky;
+    if (Q[x] != Q[y]) return Q[x] > Q[y];
+    return x < y;
+  });
+  PairData& P = c->pairs;
+  P.npairs = np;
+  P.hA.resize(np);
+  P.hB.resize(np);
+  P.hK.resize(np);
+  P.hQ.resize(np);
+  P.hPoff.resize(np);
+  P.hSeg.resize(np);
+  for (int cl = 0; cl < NPCLS; ++cl) P.segs[cl].clear();
+  for (int cl = 0; cl <= NPCLS; ++cl) P.cls_start[cl] = np;
+  size_t poff = 0;
+  for (int t = 0; t < np; ++t) {
+    const int o = order[t];
+    P.hA[t] = A[o];
+    P.hB[t] = B[o];
+    P.hK[t] = K_of(o);
+    P.hQ[t] = Q[o];
+    P.hPoff[t] = (int)poff;
+    poff += P.hK[t];
+    const int cl = cls_of(o);
+    if (P.cls_start[cl] == np) P.cls_start[cl] = t;
+    auto& sg = P.segs[cl];
+    if (sg.empty() || sg.back().K != P.hK[t]) sg.push_back({t, t + 1, P.hK[t], 0});
+    else sg.back().end = t + 1;
+  }
+  for (int cl = NPCLS - 1; cl >= 0; --cl)
+    if (P.cls_start[cl] == np && cl + 1 <= NPCLS) P.cls_start[cl] = P.cls_start[cl + 1];
+  P.nprim_pairs = poff;
+  // segment table (global) and ket-layout offsets
+  std::vector<int4> seginfo;
+  size_t koff = 0;
+  for (int cl = 0; cl < NPCLS; ++cl) {
+    P.seg_cls_start[cl] = (int)seginfo.size();
+    for (auto& s : P.segs[cl]) {
+      s.data_off = (int)koff;
+      koff += (size_t)(s.end - s.start) * s.K;
+      for (int t = s.start; t < s.end; ++t) P.hSeg[t] = (int)seginfo.size();
+      seginfo.push_back(make_int4(s.start, s.end, s.K, s.data_off));
+    }
+  }
+  P.seg_cls_start[NPCLS] = (int)seginfo.size();
+  P.nseg_total = (int)seginfo.size();
+  // 4. primitive-pair data
+  const size_t npp = poff;
+  std::vector<double> bra((size_t)BRA_NFIELD * npp), ket((size_t)BRA_NFIELD * npp);
+  for (int t = 0; t < np; ++t) {
+    const Shell &sa = b.shells[P.hA[t]], &sb = b.shells[P.hB[t]];
+    const double* RA = &b.xyz[3 * sa.atom];
+    const double* RB = &b.xyz[3 * sb.atom];
+    const int4 sg = seginfo[P.hSeg[t]];
+    const int seglen = sg.y - sg.x;
+    int k = 0;
+    for (int ia = 0; ia < sa.np; ++ia)
+      for (int ib = 0; ib < sb.np; ++ib, ++k) {
+        const double ea = sa.expo[ia], eb = sb.expo[ib];
+        const double p = ea + eb, mu = ea * eb / p;
+        double f[BRA_NFIELD];
+        double r2 = 0;
+        f[BRA_P] = p;
+        f[BRA_INVP] = 1.0 / p;
+        for (int x = 0; x < 3; ++x) {
+          const double Px = (ea * RA[x] + eb * RB[x]) / p;
+          f[BRA_PX + x] = Px;
+          f[BRA_PAX + x] = Px - RA[x];
+          f[BRA_PBX + x] = Px - RB[x];
+          r2 += (RA[x] - RB[x]) * (RA[x] - RB[x]);
+        }
+        f[BRA_K] = sa.coef[ia] * sb.coef[ib] * std::exp(-mu * r2);
+        const size_t bidx = (size_t)P.hPoff[t] + k;
+        const size_t kidx = (size_t)sg.w + (size_t)k * seglen + (t - sg.x);
+        for (int fl = 0; fl < BRA_NFIELD; ++fl) {
+          bra[(size_t)fl * npp + bidx] = f[fl];
+          ket[(size_t)fl * npp + kidx] = f[fl];
+        }
+      }
+  }
+  std::vector<float> bra32(bra.begin(), bra.end()), ket32(ket.begin(), ket.end());
+  GBHF_CUDA(c, P.A.alloc(np));
+  GBHF_CUDA(c, P.B.alloc(np));
+  GBHF_CUDA(c, P.K.alloc(np));
+  GBHF_CUDA(c, P.poff.alloc(np));
+  GBHF_CUDA(c, P.kseg.alloc(np));
+  GBHF_CUDA(c, P.Q.alloc(np));
+  GBHF_CUDA(c, P.seg_info.alloc(seginfo.size()));
+  GBHF_CUDA(c, P.bra64.alloc(bra.size()));
+  GBHF_CUDA(c, P.ket64.alloc(ket.size()));
+  GBHF_CUDA(c, P.bra32.alloc(bra.size()));
+  GBHF_CUDA(c, P.ket32.alloc(ket.size()));
+  auto up = [&](void* d, const void* h, size_t bytes) {
+    return cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, c->stream);
+  };
+  GBHF_CUDA(c, up(P.A.p, P.hA.data(), np * sizeof(int)));
+  GBHF_CUDA(c, up(P.B.p, P.hB.data(), np * sizeof(int)));
+  GBHF_CUDA(c, up(P.K.p, P.hK.data(), np * sizeof(int)));
+  GBHF_CUDA(c, up(P.poff.p, P.hPoff.data(), np * sizeof(int)));
+  GBHF_CUDA(c, up(P.kseg.p, P.hSeg.data(), np * sizeof(int)));
+  GBHF_CUDA(c, up(P.Q.p, P.hQ.data(), np * sizeof(double)));
+  GBHF_CUDA(c, up(P.seg_info.p, seginfo.data(), seginfo.size() * sizeof(int4)));
+  GBHF_CUDA(c, up(P.bra64.p, bra.data(), bra.size() * sizeof(double)));
+  GBHF_CUDA(c, up(P.ket64.p, ket.data(), ket.size() * sizeof(double)));
+  GBHF_CUDA(c, up(P.bra32.p, bra32.data(), bra32.size() * sizeof(float)));
+  GBHF_CUDA(c, up(P.ket32.p, ket32.data(), ket32.size() * sizeof(float)));
+  GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
+  c->pairs_ready = true;
+  return GBHF_OK;
+}
+
+}  // namespace gbhf

@@ -1,0 +1,137 @@
+"""Seeded synthetic water clusters and the single-water test geometry.
+
+No public benchmark set exists for the reference (it publishes no numbers), so
+the workloads are seeded water clusters:
+
+* monomer r(OH) = 0.9572 A, angle HOH = 104.52 deg, atom order O, H, H;
+* sites on a 3.0 A cubic grid, the first n sites of the smallest k^3 >= n cube
+  in lexicographic (i, j, k) order;
+* per monomer a uniform random rotation (Shoemake's quaternion construction)
+  and a uniform +-0.3 A translation jitter on each axis; the monomer is drawn
+  again while any O-O distance to an already placed monomer is below 2.6 A;
+* ``numpy.random.default_rng(seed)``; Angstrom -> bohr by dividing by
+  0.529177 as ``angstrom2AU`` does (Units.hs:12-13).
+
+Because libm trigonometry may differ in the last bit between machines, the
+generated clusters are committed in ``data/water_clusters.json`` (made by
+``write_cluster_file``) and the workloads read that file.
+"""
+from __future__ import annotations
+
+import json
+import math
+from functools import lru_cache
+from pathlib import Path
+
+import numpy as np
+
+from .basis import ANGSTROM_TO_BOHR, make_atoms
+
+R_OH = 0.9572
+THETA_HOH = math.radians(104.52)
+GRID = 3.0
+JITTER = 0.3
+MIN_OO = 2.6
+
+# Workload seeds: (H2O)16 -> 0, (H2O)8 -> 1, 256 conformers -> 2, (H2O)64 -> 3.
+SEEDS = {"w16": 0, "w8": 1, "batch256": 2, "w64": 3}
+
+# Single water, bohr: O (0,0,0); H (0,+-1.4305,1.1093).
+WATER_BOHR = np.array([[0.0, 0.0, 0.0], [0.0, 1.4305, 1.1093], [0.0, -1.4305, 1.1093]])
+
+
+def _monomer():
+    h = R_OH
+    s, c = math.sin(THETA_HOH / 2), math.cos(THETA_HOH / 2)
+    return np.array([[0.0, 0.0, 0.0], [h * s, 0.0, h * c], [-h * s, 0.0, h * c]])
+
+
+def _rotation(u):
+    """Shoemake (1992) uniform quaternion from three uniforms -> rotation matrix."""
+    u1, u2, u3 = u
+    q = np.array([math.sqrt(1 - u1) * math.sin(2 * math.pi * u2),
+                  math.sqrt(1 - u1) * math.cos(2 * math.pi * u2),
+                  math.sqrt(u1) * math.sin(2 * math.pi * u3),
+                  math.sqrt(u1) * math.cos(2 * math.pi * u3)])
+    x, y, z, w = q
+    return np.array([
+        [1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)],
+        [2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)],
+        [2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)]])
+
+
+def _sites(n):
+    k = 1
+    while k ** 3 < n:
+        k += 1
+    out = [(i, j, l) for i in range(k) for j in range(k) for l in range(k)]
+    return np.array(out[:n], dtype=np.float64) * GRID
+
+
+def water_cluster(n, rng):
+    """Coordinates (3n, 3) in bohr of a seeded (H2O)_n cluster."""
+    mono = _monomer()
+    placed_o = []
+    atoms = []
+    for site in _sites(n):
+        while True:
+            rot = _rotation(rng.random(3))
+            shift = site + rng.uniform(-JITTER, JITTER, size=3)
+            xyz = mono @ rot.T + shift
+            if all(np.linalg.norm(xyz[0] - o) >= MIN_OO for o in placed_o):
+                break
+        placed_o.append(xyz[0])
+        atoms.append(xyz)
+    return np.concatenate(atoms, axis=0) * ANGSTROM_TO_BOHR
+
+
+def generate_all():
+    out = {}
+    for name, n in (("w16", 16), ("w8", 8), ("w64", 64)):
+        out[name] = water_cluster(n, np.random.default_rng(SEEDS[name])).tolist()
+    rng = np.random.default_rng(SEEDS["batch256"])
+    sizes = [int(v) for v in rng.integers(1, 13, size=256)]
+    out["batch256"] = [water_cluster(n, rng).tolist() for n in sizes]
+    return out
+
+
+def write_cluster_file(path=None):
+    path = Path(path) if path else Path(__file__).with_name("data") / "water_clusters.json"
+    data = generate_all()
+    path.write_text(json.dumps({k: v for k, v in data.items()}, separators=(",", ":")))
+    return path
+
+
+@lru_cache(maxsize=None)
+def _cluster_file():
+    return json.loads((Path(__file__).with_name("data") / "water_clusters.json").read_text())
+
+
+def cluster_coords(name, index=None):
+    d = _cluster_file()[name]
+    return np.asarray(d if index is None else d[index], dtype=np.float64)
+
+
+def water_labels(n_waters):
+    return ["O", "H", "H"] * n_waters
+
+
+def water_atoms(basis="sto-3g", variant="text"):
+    """The single-water workload (bohr geometry above)."""
+    return make_atoms(["O", "H", "H"], WATER_BOHR, basis, variant)
+
+
+def cluster_atoms(name, basis="6-31g", variant="text", index=None):
+    xyz = cluster_coords(name, index)
+    return make_atoms(water_labels(len(xyz) // 3), xyz, basis, variant)
+
+
+def batch_workload(variant="text"):
+    """The 256-conformer batch: STO-3G for even index, 6-31G for odd index."""
+    confs = _cluster_file()["batch256"]
+    return [make_atoms(water_labels(len(c) // 3), c, "sto-3g" if i % 2 == 0 else "6-31g", variant)
+            for i, c in enumerate(confs)]
+
+
+if __name__ == "__main__":
+    print(write_cluster_file())
