@@ -1,0 +1,293 @@
+"""Benchmark: SCF seconds per molecule and ERI quartets/s on one GB300.
+
+Workload: (H2O)16 RHF/6-31G (208 basis functions, seeded geometry, EMSL
+basis), mixed FP32/FP64 direct SCF (FP32 for quartets with Schwarz bound
+below 1e-4, Schwarz cutoff 1e-12, incremental dD Fock builds, core guess,
+DIIS with 6 vectors, converged to dE < 1e-10 and RMS dD < 1e-8).  One step
+is one complete SCF of the molecule, including the screening setup, with the
+basis already on the device; the plain FP64 GPU SCF is run once beside it and
+both energies are reported.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gbhf|reference]
+
+--impl reference times the CPU implementation (the FP64 oracle, a
+restatement of the reference's numerics; the Haskell original cannot be
+built here) on the same workload.  For N > 1 (torchrun), each rank runs its
+own replica of the molecule (independent molecules, no data exchange) and
+rank 0 prints the whole-job number.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT / "haskell-abinitio_gb300"))
+sys.path.insert(0, str(ROOT / "oracle"))
+
+METRIC = "SCF s/molecule & ERI quartets/s: mixed vs FP64 on one GB300 at |ΔE|≤1e-6 Eh"
+WORKLOAD = "(H2O)16 RHF/6-31G, 208 basis functions, seeded water cluster (seed 0)"
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo", rank=rank, world_size=world)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(world, v):
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(v)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.lines = []
+        if self.proc:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for l in getattr(self, "lines", []):
+            p = [x.strip() for x in l.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx.append(float(p[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["clock sampling unavailable"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def load_measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    return json.loads(p.read_text()) if p.exists() else {}
+
+
+def traffic_profile():
+    p = ROOT / "profiles" / "traffic.json"
+    return json.loads(p.read_text()) if p.exists() else {}
+
+
+def oracle_sample(fb, n_iter):
+    """CPU oracle: setup + one full direct Fock build + one diagonalisation, all host threads."""
+    import numpy as np
+    import oracle as O
+    nth = O.lib().orc_num_threads()
+    t0 = time.perf_counter()
+    ob = O.OracleBasis(fb)
+    core = ob.hcore(False)
+    s = ob.overlap(False)
+    x = O.symm_ortho(O.tri_to_square(s))
+    _, d, _ = O.diagonal_hf(core, x, fb.n_occupied)
+    t1 = time.perf_counter()
+    f, st = ob.fock_direct(core, d, 1e-12)
+    err = O.calc_error_mtx(f, s, d, x)
+    O.diagonal_hf(f, x, fb.n_occupied)
+    t2 = time.perf_counter()
+    setup, per_iter = t1 - t0, t2 - t1
+    return {"setup_s": setup, "iteration_s": per_iter, "threads": nth, "fn_quartet_stats": st.tolist(),
+            "estimate": setup + n_iter * per_iter, "max_err": float(np.max(np.abs(err)))}
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    import oracle as O
+    from gbhf import basis as B, molecules as M
+    fb = B.flatten(M.cluster_atoms("w16", "6-31g"))
+    rec = json.loads((ROOT / "tests" / "golden" / "clusters.json").read_text()).get("w16_631g", {})
+    n_iter = int(rec.get("iterations", 17))
+    for _ in range(args.warmup):
+        oracle_sample(fb, n_iter)
+    times = []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        times.append(oracle_sample(fb, n_iter)["estimate"])
+    wall = time.perf_counter() - t0
+    v = statistics.mean(times)
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "s/molecule", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * wall / args.steps,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": WORKLOAD, "precision": "FP64 (CPU)",
+                                            "parallelism": "OpenMP, all host threads"},
+            "cpu_baseline": {"value": v, "unit": "s/molecule", "cores": O.lib().orc_num_threads(),
+                             "kind": "port",
+                             "sample": f"per step: setup + 1 direct Fock build + DIIS error + diagonalisation "
+                                       f"of the FP64 oracle, SCF time = setup + {n_iter} x iteration "
+                                       f"({n_iter} = the oracle's own iteration count for this molecule)"},
+            "e2e": {"value": v, "unit": "s/molecule", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_gbhf(args, world, rank, local):
+    import numpy as np
+    from gbhf import _lib, basis as B, molecules as M
+    from gbhf.flops_model import F_ALG
+    ctx = _lib.Context(local)
+    fb = B.flatten(M.cluster_atoms("w16", "6-31g"))
+    mixed = _lib.baseline_opts(precision=_lib.PREC_MIXED, incremental=1, final_fp64=0)
+    fp64 = _lib.baseline_opts(precision=_lib.PREC_FP64, incremental=0, final_fp64=0)
+
+    def step(opts, matrices=False):
+        ctx.set_basis(fb)
+        ctx.event_record(0)
+        r = ctx.scf(opts, want_matrices=matrices)
+        ctx.event_record(1)
+        return r, ctx.event_elapsed(0, 1)
+
+    for _ in range(max(args.warmup, 3)):
+        step(mixed)
+    # plain FP64 GPU SCF, once (reported beside the headline)
+    r64, t64 = step(fp64)
+    barrier(world)
+    ctx.profile_reset(events=True)
+    times = []
+    with ClockSampler(local) as clk:
+        barrier(world)
+        for _ in range(args.steps):
+            ctx.flush_l2()
+            r, ms = step(mixed)
+            times.append(ms)
+        barrier(world)
+    prof = ctx.profile_read()
+    cls = ctx.profile_classes()
+    total_ms = max_over_ranks(world, sum(times))
+    value = total_ms / 1e3 / (args.steps * world)
+    # end to end: host basis in, every result matrix back to host memory
+    e2e_t = []
+    h2d = sum(a.nbytes for a in (fb.xyz, fb.charge, fb.cgf_atom, fb.cgf_lxyz, fb.cgf_nprim, fb.prim_coef,
+                                 fb.prim_exp))
+    n = fb.n_cgf
+    d2h = 8 * (2 * n * (n + 1) // 2 + n * n + n) + 8
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        ctx.set_basis(fb)
+        ctx.scf(mixed, want_matrices=True)
+        e2e_t.append(time.perf_counter() - t0)
+    e2e_v = max_over_ranks(world, sum(e2e_t)) / (args.steps * world)
+    if rank != 0:
+        return
+    # roofline of the dominant J/K kernel class
+    dom = max(cls.items(), key=lambda kv: kv[1]["ms"])
+    (cname, prec), st = dom
+    flops = st["prim_quartets"] * F_ALG[cname]
+    achieved = flops / (st["ms"] * 1e-3) / 1e12 if st["ms"] > 0 else 0.0
+    peak64, peak32 = ctx.peak_flops(_lib.PREC_FP64), ctx.peak_flops(_lib.PREC_MIXED)
+    peak = peak64 if prec == "fp64" else peak32
+    prof_tr = traffic_profile().get(f"{cname}_{prec}")
+    jk_ms = prof["jk_ms_fp64"] + prof["jk_ms_fp32"]
+    fnq_step = prof["fn_quartets"] / args.steps
+    line = {
+        "metric": METRIC, "value": value, "unit": "s/molecule", "n_gpus": world, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": total_ms / args.steps, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+        "data": "synthetic (seeded water cluster, EMSL 6-31G)",
+        "config": {"workload": WORKLOAD, "n_basis": n, "precision": "mixed: FP32 ERIs below Schwarz bound 1e-4, "
+                   "FP64 Fock accumulation, DIIS and eigen-solve", "schwarz_cutoff": 1e-12,
+                   "incremental_fock": True, "l2": "flushed (256 MiB write) before every timed step",
+                   "parallelism": f"{world} independent replica(s), one per GPU"},
+        "energy": r["energy"], "iterations": r["iterations"],
+        "fp64": {"s_per_molecule": t64 / 1e3, "energy": r64["energy"], "iterations": r64["iterations"],
+                 "delta_e_mixed_vs_fp64": r["energy"] - r64["energy"],
+                 "speedup_mixed_vs_fp64": (t64 / 1e3) / value if value > 0 else None},
+        "eri_quartets_per_s": fnq_step / (total_ms / args.steps / 1e3),
+        "eri_quartets_per_step": fnq_step,
+        "eri_quartets_unscreened": (n * (n + 1) // 2) ** 2,
+        "eri_fp32_fraction": r["eri_fp32_fraction"],
+        "jk_ms_per_step": jk_ms / args.steps,
+        "gpu_launches": int(prof["launches"]),
+        "roofline": {"kernel": f"k_jk<{cname}, {prec}>", "bound": f"{prec} CUDA-core pipe", "achieved": achieved,
+                     "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
+                     "peak_source": f"FMA microbenchmark on this GPU (FP64 {peak64:.2f}, FP32 {peak32:.1f} TFLOP/s); "
+                                    "MEASURED_PEAKS.json holds only HBM and bf16 tensor peaks",
+                     "flops_per_launch": flops / args.steps, "traffic": prof_tr},
+        "classes": {f"{k[0]}_{k[1]}": v for k, v in cls.items() if v["ms"] > 0},
+        "clocks": clk.summary(),
+        "e2e": {"value": e2e_v, "unit": "s/molecule", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+    }
+    peaks = load_measured_peaks()
+    if peaks:
+        line["measured_peaks"] = {"hbm_gbs": peaks.get("hbm_gbs"), "bf16_tflops": peaks.get("bf16_tflops")}
+    if world == 1 and not args.no_cpu_baseline:
+        cb = oracle_sample(fb, r64["iterations"])
+        line["cpu_baseline"] = {"value": cb["estimate"], "unit": "s/molecule", "cores": cb["threads"], "kind": "port",
+                                "sample": f"FP64 oracle on the host: setup + 1 direct Fock build + DIIS error + "
+                                          f"diagonalisation, SCF time = setup + {r64['iterations']} x iteration "
+                                          f"(the FP64 GPU SCF's iteration count)"}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gbhf", choices=["gbhf", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_gbhf(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -72,6 +72,8 @@ gbhf_status gbhf_create(gbhf_ctx** out, int device) {
     return GBHF_ERR_CUDA;
   }
   for (auto& e : c->ev) cudaEventCreate(&e);
+  for (auto& e : c->evc) cudaEventCreate(&e);
+  for (auto& e : c->evu) cudaEventCreate(&e);
   *out = c;
   return GBHF_OK;
 }
@@ -81,6 +83,10 @@ gbhf_status gbhf_destroy(gbhf_ctx* c) {
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
   for (auto& e : c->ev)
+    if (e) cudaEventDestroy(e);
+  for (auto& e : c->evc)
+    if (e) cudaEventDestroy(e);
+  for (auto& e : c->evu)
     if (e) cudaEventDestroy(e);
   cudaStream_t s = c->stream;
   delete c;   // frees device buffers

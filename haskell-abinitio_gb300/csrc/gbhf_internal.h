@@ -97,6 +97,7 @@ struct TaskLists {
   double thr_all = -1, thr64 = -1;     // thresholds the current lists were built for
   int hranges[4 * 6] = {0};            // host copy of ranges
   DBuf<int> f0;                        // first basis function per shell
+  long f0_gen = -1;                    // basis generation f0 was uploaded for
 };
 
 struct JacobiWork {
@@ -112,6 +113,7 @@ struct Profile {
   double jk_ms64 = 0, jk_ms32 = 0, dense_ms = 0;
   double prim64 = 0, prim32 = 0, shellq = 0, fnq = 0;
   long long launches = 0;
+  double cls[6][2][4] = {};   // per combo and precision: shell q, fn q, prim q, ms
 };
 
 }  // namespace gbhf
@@ -130,6 +132,7 @@ struct gbhf_ctx {
   gbhf::DBuf<double> d_xyz, d_Z, d_coef, d_exp;
   gbhf::DBuf<int> d_fn;          // per CGF: atom, lx, ly, lz, np, off (6 ints)
   bool basis_dev = false;
+  long basis_gen = 0;            // incremented by every gbhf_set_basis
   gbhf::PairData pairs;
   bool pairs_ready = false;
   gbhf::TaskLists tasks;
@@ -142,6 +145,9 @@ struct gbhf_ctx {
   gbhf::DBuf<double> small;
   gbhf::Profile prof;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  cudaEvent_t evc[13] = {};      // per-class J/K launch boundaries (profiling)
+  cudaEvent_t evu[8] = {};       // user slots (gbhf_event_record)
+  gbhf::DBuf<unsigned char> flush;
 };
 
 namespace gbhf {

@@ -192,8 +192,8 @@ __global__ void __launch_bounds__(JK_THREADS) k_jk(JKArgs<T> a) {
       T v = 0;
 #pragma unroll
       for (int cd = 0; cd < NCD; ++cd) v = fma_t(acc.get(ab * NCD + cd), dcd[cd], v);
-      v = warp_sum(v);
-      if (lane == 0) atomicAdd(&a.G[(long long)(a0 + ab / NB) * n + b0 + ab % NB], double(T(2) * s * v));
+      v = warp_sum(T(2) * s * v);   // s depends on the lane's ket: apply before the reduction
+      if (lane == 0) atomicAdd(&a.G[(long long)(a0 + ab / NB) * n + b0 + ab % NB], double(v));
     }
     if (active) {
       // J_cd
@@ -487,7 +487,8 @@ gbhf_status jk_build(gbhf_ctx* c, const double* d_Dsq, double* d_G, int precisio
   GBHF_TRY(ensure_pairs(c));
   const int n = c->basis.nbf;
   TaskLists& st = c->tasks;
-  if (!st.f0.p || st.f0.n < c->basis.shells.size()) {
+  if (st.f0_gen != c->basis_gen) {
+    st.f0_gen = c->basis_gen;
     std::vector<int> f0(c->basis.shells.size());
     for (size_t s = 0; s < f0.size(); ++s) f0[s] = c->basis.shells[s].f0;
     GBHF_CUDA(c, st.f0.alloc(f0.size()));
@@ -517,25 +518,47 @@ gbhf_status jk_build(gbhf_ctx* c, const double* d_Dsq, double* d_G, int precisio
     nt[k][1] = st.hranges[4 * k + 3] - st.hranges[4 * k + 2];
   }
   const bool ev = c->prof.events;
-  if (ev) GBHF_CUDA(c, cudaEventRecord(c->ev[0], c->stream));
-  // FP64 kernels (heaviest class first)
-  GBHF_TRY((launch_class<1, 1, 1, 1, double, true>(c, 5, 0, d_Dsq, d_G, P.bra64.p, P.ket64.p, c->boys64.p, f0, nt[5][0])));
-  GBHF_TRY((launch_class<1, 1, 1, 0, double, false>(c, 4, 0, d_Dsq, d_G, P.bra64.p, P.ket64.p, c->boys64.p, f0, nt[4][0])));
-  GBHF_TRY((launch_class<1, 1, 0, 0, double, false>(c, 3, 0, d_Dsq, d_G, P.bra64.p, P.ket64.p, c->boys64.p, f0, nt[3][0])));
-  GBHF_TRY((launch_class<1, 0, 1, 0, double, false>(c, 2, 0, d_Dsq, d_G, P.bra64.p, P.ket64.p, c->boys64.p, f0, nt[2][0])));
-  GBHF_TRY((launch_class<1, 0, 0, 0, double, false>(c, 1, 0, d_Dsq, d_G, P.bra64.p, P.ket64.p, c->boys64.p, f0, nt[1][0])));
-  GBHF_TRY((launch_class<0, 0, 0, 0, double, false>(c, 0, 0, d_Dsq, d_G, P.bra64.p, P.ket64.p, c->boys64.p, f0, nt[0][0])));
-  if (ev) GBHF_CUDA(c, cudaEventRecord(c->ev[1], c->stream));
-  if (any32) {
-    const float* Df = c->dfloat.p;
-    GBHF_TRY((launch_class<1, 1, 1, 1, float, false>(c, 5, 1, Df, d_G, P.bra32.p, P.ket32.p, c->boys32.p, f0, nt[5][1])));
-    GBHF_TRY((launch_class<1, 1, 1, 0, float, false>(c, 4, 1, Df, d_G, P.bra32.p, P.ket32.p, c->boys32.p, f0, nt[4][1])));
-    GBHF_TRY((launch_class<1, 1, 0, 0, float, false>(c, 3, 1, Df, d_G, P.bra32.p, P.ket32.p, c->boys32.p, f0, nt[3][1])));
-    GBHF_TRY((launch_class<1, 0, 1, 0, float, false>(c, 2, 1, Df, d_G, P.bra32.p, P.ket32.p, c->boys32.p, f0, nt[2][1])));
-    GBHF_TRY((launch_class<1, 0, 0, 0, float, false>(c, 1, 1, Df, d_G, P.bra32.p, P.ket32.p, c->boys32.p, f0, nt[1][1])));
-    GBHF_TRY((launch_class<0, 0, 0, 0, float, false>(c, 0, 1, Df, d_G, P.bra32.p, P.ket32.p, c->boys32.p, f0, nt[0][1])));
+  // heaviest class first; FP64 lists, then FP32 lists
+  static const int order[NCOMBO] = {5, 4, 3, 2, 1, 0};
+  int ne = 0;
+  int ev_combo[12], ev_prec[12];
+  if (ev) GBHF_CUDA(c, cudaEventRecord(c->evc[ne], c->stream));
+  for (int prec = 0; prec < 2; ++prec) {
+    if (prec == 1 && !any32) break;
+    const double* D64 = d_Dsq;
+    const float* D32 = c->dfloat.p;
+    for (int oi = 0; oi < NCOMBO; ++oi) {
+      const int k = order[oi];
+      if (nt[k][prec] <= 0) continue;
+      gbhf_status s = GBHF_OK;
+      if (prec == 0) {
+        switch (k) {
+          case 5: s = launch_class<1, 1, 1, 1, double, true>(c, 5, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boys64.p, f0, nt[5][0]); break;
+          case 4: s = launch_class<1, 1, 1, 0, double, false>(c, 4, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boys64.p, f0, nt[4][0]); break;
+          case 3: s = launch_class<1, 1, 0, 0, double, false>(c, 3, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boys64.p, f0, nt[3][0]); break;
+          case 2: s = launch_class<1, 0, 1, 0, double, false>(c, 2, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boys64.p, f0, nt[2][0]); break;
+          case 1: s = launch_class<1, 0, 0, 0, double, false>(c, 1, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boys64.p, f0, nt[1][0]); break;
+          default: s = launch_class<0, 0, 0, 0, double, false>(c, 0, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boys64.p, f0, nt[0][0]); break;
+        }
+      } else {
+        switch (k) {
+          case 5: s = launch_class<1, 1, 1, 1, float, false>(c, 5, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boys32.p, f0, nt[5][1]); break;
+          case 4: s = launch_class<1, 1, 1, 0, float, false>(c, 4, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boys32.p, f0, nt[4][1]); break;
+          case 3: s = launch_class<1, 1, 0, 0, float, false>(c, 3, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boys32.p, f0, nt[3][1]); break;
+          case 2: s = launch_class<1, 0, 1, 0, float, false>(c, 2, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boys32.p, f0, nt[2][1]); break;
+          case 1: s = launch_class<1, 0, 0, 0, float, false>(c, 1, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boys32.p, f0, nt[1][1]); break;
+          default: s = launch_class<0, 0, 0, 0, float, false>(c, 0, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boys32.p, f0, nt[0][1]); break;
+        }
+      }
+      if (s != GBHF_OK) return s;
+      if (ev) {
+        ev_combo[ne] = k;
+        ev_prec[ne] = prec;
+        ++ne;
+        GBHF_CUDA(c, cudaEventRecord(c->evc[ne], c->stream));
+      }
+    }
   }
-  if (ev) GBHF_CUDA(c, cudaEventRecord(c->ev[2], c->stream));
   // statistics
   unsigned long long hs[6 * NCOMBO];
   GBHF_CUDA(c, cudaMemcpyAsync(hs, c->tasks.stats.p, sizeof(hs), cudaMemcpyDeviceToHost, c->stream));
@@ -546,13 +569,15 @@ gbhf_status jk_build(gbhf_ctx* c, const double* d_Dsq, double* d_G, int precisio
       c->prof.shellq += (double)s[0];
       c->prof.fnq += (double)s[1];
       (p == 0 ? c->prof.prim64 : c->prof.prim32) += (double)s[2];
+      c->prof.cls[k][p][0] += (double)s[0];
+      c->prof.cls[k][p][1] += (double)s[1];
+      c->prof.cls[k][p][2] += (double)s[2];
     }
-  if (ev) {
-    float m64 = 0, m32 = 0;
-    GBHF_CUDA(c, cudaEventElapsedTime(&m64, c->ev[0], c->ev[1]));
-    GBHF_CUDA(c, cudaEventElapsedTime(&m32, c->ev[1], c->ev[2]));
-    c->prof.jk_ms64 += m64;
-    c->prof.jk_ms32 += m32;
+  for (int e = 0; e < ne; ++e) {
+    float ms = 0;
+    GBHF_CUDA(c, cudaEventElapsedTime(&ms, c->evc[e], c->evc[e + 1]));
+    c->prof.cls[ev_combo[e]][ev_prec[e]][3] += ms;
+    (ev_prec[e] == 0 ? c->prof.jk_ms64 : c->prof.jk_ms32) += ms;
   }
   return GBHF_OK;
 }

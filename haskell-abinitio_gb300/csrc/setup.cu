@@ -127,6 +127,9 @@ gbhf_status build_basis(gbhf_ctx* c, int n_atoms, const double* xyz, const doubl
   GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
   c->basis_dev = true;
   c->pairs_ready = false;
+  c->basis_gen += 1;
+  c->tasks.thr_all = -1;
+  c->tasks.thr64 = -1;
   return GBHF_OK;
 }
 

@@ -94,6 +94,11 @@ def load():
                                 _dp, _ip, _ip, _dp]),
         "gbhf_profile_reset": (st, [_vp, C.c_int]),
         "gbhf_profile_read": (st, [_vp, _dp, C.c_int]),
+        "gbhf_profile_classes": (st, [_vp, _dp]),
+        "gbhf_event_record": (st, [_vp, C.c_int]),
+        "gbhf_event_elapsed": (st, [_vp, C.c_int, C.c_int, _dp]),
+        "gbhf_flush_l2": (st, [_vp]),
+        "gbhf_peak_flops": (st, [_vp, C.c_int, _dp]),
     }
     for name, (res, args) in sigs.items():
         f = getattr(L, name)
@@ -305,3 +310,32 @@ class Context:
         keys = ("jk_ms_fp64", "jk_ms_fp32", "prim_quartets_fp64", "prim_quartets_fp32", "shell_quartets",
                 "fn_quartets", "launches", "dense_ms")
         return dict(zip(keys, v.tolist()))
+
+    CLASSES = ("ssss", "psss", "psps", "ppss", "ppps", "pppp")
+
+    def profile_classes(self):
+        """{(class, 'fp64'|'fp32'): dict(shell_quartets, fn_quartets, prim_quartets, ms)}"""
+        v = np.zeros(48)
+        self._check(self.L.gbhf_profile_classes(self.h, _d(v)))
+        out = {}
+        for k, name in enumerate(self.CLASSES):
+            for p, prec in enumerate(("fp64", "fp32")):
+                q = v[(k * 2 + p) * 4:(k * 2 + p) * 4 + 4]
+                out[(name, prec)] = dict(shell_quartets=q[0], fn_quartets=q[1], prim_quartets=q[2], ms=q[3])
+        return out
+
+    def event_record(self, slot):
+        self._check(self.L.gbhf_event_record(self.h, slot))
+
+    def event_elapsed(self, a, b):
+        ms = C.c_double(0)
+        self._check(self.L.gbhf_event_elapsed(self.h, a, b, C.byref(ms)))
+        return ms.value
+
+    def flush_l2(self):
+        self._check(self.L.gbhf_flush_l2(self.h))
+
+    def peak_flops(self, precision):
+        t = C.c_double(0)
+        self._check(self.L.gbhf_peak_flops(self.h, precision, C.byref(t)))
+        return t.value

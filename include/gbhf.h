@@ -204,6 +204,18 @@ gbhf_status gbhf_scf_batch(gbhf_ctx* ctx, int n_mol, const int* atom_off, const 
  * total library kernel launches, dense linear-algebra milliseconds. */
 gbhf_status gbhf_profile_reset(gbhf_ctx* ctx, int enable_events);
 gbhf_status gbhf_profile_read(gbhf_ctx* ctx, double* stats, int n_stats);
+/* Per ERI class (ss|ss, ps|ss, ps|ps, pp|ss, pp|ps, pp|pp) and precision
+ * (FP64, FP32) since the last reset: out[(class*2+prec)*4 + k], k = shell
+ * quartets, function quartets, primitive quartets, kernel milliseconds. */
+gbhf_status gbhf_profile_classes(gbhf_ctx* ctx, double* out48);
+/* CUDA events on the context stream (slots 0..7) and the time between two. */
+gbhf_status gbhf_event_record(gbhf_ctx* ctx, int slot);
+gbhf_status gbhf_event_elapsed(gbhf_ctx* ctx, int slot_start, int slot_end, double* ms);
+/* Overwrite a device buffer larger than L2 (256 MiB) on the context stream. */
+gbhf_status gbhf_flush_l2(gbhf_ctx* ctx);
+/* Measured FMA throughput of this GPU's CUDA cores (TFLOP/s, 2 flops per
+ * FMA) for precision GBHF_PREC_FP64 or GBHF_PREC_MIXED (= FP32). */
+gbhf_status gbhf_peak_flops(gbhf_ctx* ctx, int precision, double* tflops);
 
 #ifdef __cplusplus
 }

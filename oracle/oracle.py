@@ -448,6 +448,7 @@ class SCFOptions:
     schwarz: float = 1e-12
     charge: float = 0.0
     direct: bool = False           # shell-based direct Fock instead of stored ERIs
+    stop_rule: str = ""            # "reference" | "energy"; default follows ref_compat
 
     @staticmethod
     def reference():
@@ -482,6 +483,7 @@ def scf(fb, opts: Optional[SCFOptions] = None, grid=None):
     opts = opts or SCFOptions.reference()
     ob = OracleBasis(fb, grid)
     ref = opts.ref_compat
+    ref_stop = (opts.stop_rule or ("reference" if ref else "energy")) == "reference"
     occupied = int(math.floor((float(fb.charge.sum()) - opts.charge) / 2.0))
     e_nn = nuclear_rep(fb.xyz, fb.charge)
     core = ob.hcore(ref)
@@ -512,7 +514,7 @@ def scf(fb, opts: Optional[SCFOptions] = None, grid=None):
         err = calc_error_mtx(f, s, density, x)
         f_diis, dat, switch = diis_driver(err, f, dat, step, switch, opts.diis_start)
         c, new_density, eps = diagonal_hf(f_diis, x, occupied)
-        if ref:
+        if ref_stop:
             etot = variational_e(core, f_diis, new_density) + e_nn
             energies.append(etot)
             if step != 0 and np.max(np.abs(err)) < opts.conv_error:
