@@ -249,6 +249,9 @@ def run_gbhf(args, world, rank, local):
         "eri_quartets_unscreened": (n * (n + 1) // 2) ** 2,
         "eri_fp32_fraction": r["eri_fp32_fraction"],
         "jk_ms_per_step": jk_ms / args.steps,
+        "phases_ms_per_step": {k: prof[k] / args.steps for k in ("ms_setup", "ms_fock", "ms_diis", "ms_diag",
+                                                                  "ms_other")},
+        "jacobi_sweeps_per_call": prof["jacobi_sweeps"] / max(prof["jacobi_calls"], 1),
         "gpu_launches": int(prof["launches"]),
         "roofline": {"kernel": f"k_jk<{cname}, {prec}>", "bound": f"{prec} CUDA-core pipe", "achieved": achieved,
                      "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak if peak else None,

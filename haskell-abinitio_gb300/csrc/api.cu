@@ -426,9 +426,11 @@ gbhf_status gbhf_profile_reset(gbhf_ctx* c, int enable_events) {
 gbhf_status gbhf_profile_read(gbhf_ctx* c, double* stats, int n_stats) {
   CTX_CHECK(c);
   if (!stats) return fail(c, GBHF_ERR_BAD_INPUT, "null pointer");
-  const double v[8] = {c->prof.jk_ms64, c->prof.jk_ms32, c->prof.prim64, c->prof.prim32,
-                       c->prof.shellq,  c->prof.fnq,     (double)c->prof.launches, c->prof.dense_ms};
-  for (int i = 0; i < n_stats && i < 8; ++i) stats[i] = v[i];
+  const double v[15] = {c->prof.jk_ms64,   c->prof.jk_ms32,  c->prof.prim64,        c->prof.prim32,
+                        c->prof.shellq,    c->prof.fnq,      (double)c->prof.launches, c->prof.dense_ms,
+                        c->prof.ph_setup,  c->prof.ph_fock,  c->prof.ph_diis,       c->prof.ph_diag,
+                        c->prof.ph_other,  c->prof.jacobi_sweeps, c->prof.jacobi_calls};
+  for (int i = 0; i < n_stats && i < 15; ++i) stats[i] = v[i];
   return GBHF_OK;
 }
 

@@ -21,7 +21,7 @@ __device__ __forceinline__ void eri_ketprim_ssss(const T* __restrict__ sb, int n
     const T rs = rsqrt_t(ppq);
     const T alpha = p * q * (rs * rs);
     const T Tb = alpha * (X * X + Y * Y + Z * Z);
-    const T pref = T(TWO_PI_2P5) * Kab * Kcd * invp * invq * rs;
+    const T pref = Kab * Kcd * rs;   // K holds sqrt(2 pi^2.5) c c exp(-mu R^2) / p
     T F[1];
     boys_eval<T, 0>(Tb, boys, F);
     const T m2a = T(-2) * alpha;
@@ -56,7 +56,7 @@ __device__ __forceinline__ void eri_ketprim_psss(const T* __restrict__ sb, int n
     const T rs = rsqrt_t(ppq);
     const T alpha = p * q * (rs * rs);
     const T Tb = alpha * (X * X + Y * Y + Z * Z);
-    const T pref = T(TWO_PI_2P5) * Kab * Kcd * invp * invq * rs;
+    const T pref = Kab * Kcd * rs;   // K holds sqrt(2 pi^2.5) c c exp(-mu R^2) / p
     T F[2];
     boys_eval<T, 1>(Tb, boys, F);
     const T m2a = T(-2) * alpha;
@@ -118,7 +118,7 @@ __device__ __forceinline__ void eri_ketprim_psps(const T* __restrict__ sb, int n
     const T rs = rsqrt_t(ppq);
     const T alpha = p * q * (rs * rs);
     const T Tb = alpha * (X * X + Y * Y + Z * Z);
-    const T pref = T(TWO_PI_2P5) * Kab * Kcd * invp * invq * rs;
+    const T pref = Kab * Kcd * rs;   // K holds sqrt(2 pi^2.5) c c exp(-mu R^2) / p
     T F[3];
     boys_eval<T, 2>(Tb, boys, F);
     const T m2a = T(-2) * alpha;
@@ -199,7 +199,7 @@ __device__ __forceinline__ void eri_ketprim_ppss(const T* __restrict__ sb, int n
     const T rs = rsqrt_t(ppq);
     const T alpha = p * q * (rs * rs);
     const T Tb = alpha * (X * X + Y * Y + Z * Z);
-    const T pref = T(TWO_PI_2P5) * Kab * Kcd * invp * invq * rs;
+    const T pref = Kab * Kcd * rs;   // K holds sqrt(2 pi^2.5) c c exp(-mu R^2) / p
     T F[3];
     boys_eval<T, 2>(Tb, boys, F);
     const T m2a = T(-2) * alpha;
@@ -300,7 +300,7 @@ __device__ __forceinline__ void eri_ketprim_ppps(const T* __restrict__ sb, int n
     const T rs = rsqrt_t(ppq);
     const T alpha = p * q * (rs * rs);
     const T Tb = alpha * (X * X + Y * Y + Z * Z);
-    const T pref = T(TWO_PI_2P5) * Kab * Kcd * invp * invq * rs;
+    const T pref = Kab * Kcd * rs;   // K holds sqrt(2 pi^2.5) c c exp(-mu R^2) / p
     T F[4];
     boys_eval<T, 3>(Tb, boys, F);
     const T m2a = T(-2) * alpha;
@@ -506,7 +506,7 @@ __device__ __forceinline__ void eri_ketprim_pppp(const T* __restrict__ sb, int n
     const T rs = rsqrt_t(ppq);
     const T alpha = p * q * (rs * rs);
     const T Tb = alpha * (X * X + Y * Y + Z * Z);
-    const T pref = T(TWO_PI_2P5) * Kab * Kcd * invp * invq * rs;
+    const T pref = Kab * Kcd * rs;   // K holds sqrt(2 pi^2.5) c c exp(-mu R^2) / p
     T F[5];
     boys_eval<T, 4>(Tb, boys, F);
     const T m2a = T(-2) * alpha;

@@ -48,25 +48,29 @@ template <int L> struct BoysCfg<float, L> {
   static constexpr int NT = BOYS32_NTERM;
 };
 
+// Horner form used by the J/K kernels: row j holds, for m = 0..BOYSH_LMAX and
+// k = 0..NT-1, G[m*NT + k] = F_(m+k)(T_j) / k!, so that
+// F_m(t) = sum_k G[m*NT+k] (T_j - t)^k costs NT-1 FMAs per m.
+#define BOYSH_LMAX 4
+#define BOYSH64_STRIDE 36   // (BOYSH_LMAX+1) * 7 = 35, padded
+#define BOYSH32_STRIDE 28   // (BOYSH_LMAX+1) * 5 = 25, padded
+template <typename T> struct BoysHStride;
+template <> struct BoysHStride<double> { static constexpr int S = BOYSH64_STRIDE; };
+template <> struct BoysHStride<float> { static constexpr int S = BOYSH32_STRIDE; };
+
 template <typename T, int L>
 __device__ __forceinline__ void boys_eval(T t, const T* __restrict__ tab, T* F) {
   using C = BoysCfg<T, L>;
+  static_assert(L <= BOYSH_LMAX, "Horner Boys table holds m <= BOYSH_LMAX");
   if (t < T(C::TMAX)) {
     const int j = (int)(t * T(1.0 / C::H) + T(0.5));
     const T dx = T(j) * T(C::H) - t;   // = -(t - T_j)
-    T y[C::NT];
-    y[0] = T(1);
-#pragma unroll
-    for (int k = 1; k < C::NT; ++k) y[k] = y[k - 1] * dx * T(1.0 / k);
-    const T* row = tab + j * BOYS_NCOL;
-    T v[L + C::NT];
-#pragma unroll
-    for (int m = 0; m < L + C::NT; ++m) v[m] = __ldg(row + m);
+    const T* row = tab + j * BoysHStride<T>::S;
 #pragma unroll
     for (int m = 0; m <= L; ++m) {
-      T s = T(0);
+      T s = __ldg(row + m * C::NT + C::NT - 1);
 #pragma unroll
-      for (int k = C::NT - 1; k >= 0; --k) s = fma_t(y[k], v[m + k], s);
+      for (int k = C::NT - 2; k >= 0; --k) s = fma_t(s, dx, __ldg(row + m * C::NT + k));
       F[m] = s;
     }
   } else {

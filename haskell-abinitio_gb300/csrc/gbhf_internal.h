@@ -114,6 +114,8 @@ struct Profile {
   double prim64 = 0, prim32 = 0, shellq = 0, fnq = 0;
   long long launches = 0;
   double cls[6][2][4] = {};   // per combo and precision: shell q, fn q, prim q, ms
+  // host wall-clock per SCF phase (ms): setup, Fock, DIIS, diagonalisation, other; Jacobi sweeps
+  double ph_setup = 0, ph_fock = 0, ph_diis = 0, ph_diag = 0, ph_other = 0, jacobi_sweeps = 0, jacobi_calls = 0;
 };
 
 }  // namespace gbhf
@@ -128,6 +130,8 @@ struct gbhf_ctx {
   gbhf::DBuf<double> boys_ref;   // 15 x 1001 reference grid
   gbhf::DBuf<double> boys64;     // exact FP64 table
   gbhf::DBuf<float> boys32;      // exact FP32 table
+  gbhf::DBuf<double> boysh64;    // Horner tables for the J/K kernels
+  gbhf::DBuf<float> boysh32;
   // basis on device (function level, for 1-e integrals and canonical ERIs)
   gbhf::DBuf<double> d_xyz, d_Z, d_coef, d_exp;
   gbhf::DBuf<int> d_fn;          // per CGF: atom, lx, ly, lz, np, off (6 ints)

@@ -212,7 +212,7 @@ def gen_class(la, lb, lc, ld):
     w("    const T rs = rsqrt_t(ppq);")
     w("    const T alpha = p * q * (rs * rs);")
     w("    const T Tb = alpha * (X * X + Y * Y + Z * Z);")
-    w("    const T pref = T(TWO_PI_2P5) * Kab * Kcd * invp * invq * rs;")
+    w("    const T pref = Kab * Kcd * rs;   // K holds sqrt(2 pi^2.5) c c exp(-mu R^2) / p")
     w(f"    T F[{L + 1}];")
     w(f"    boys_eval<T, {L}>(Tb, boys, F);")
     w("    const T m2a = T(-2) * alpha;")

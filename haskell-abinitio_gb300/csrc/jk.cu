@@ -533,21 +533,21 @@ gbhf_status jk_build(gbhf_ctx* c, const double* d_Dsq, double* d_G, int precisio
       gbhf_status s = GBHF_OK;
       if (prec == 0) {
         switch (k) {
-          case 5: s = launch_class<1, 1, 1, 1, double, true>(c, 5, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boys64.p, f0, nt[5][0]); break;
-          case 4: s = launch_class<1, 1, 1, 0, double, false>(c, 4, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boys64.p, f0, nt[4][0]); break;
-          case 3: s = launch_class<1, 1, 0, 0, double, false>(c, 3, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boys64.p, f0, nt[3][0]); break;
-          case 2: s = launch_class<1, 0, 1, 0, double, false>(c, 2, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boys64.p, f0, nt[2][0]); break;
-          case 1: s = launch_class<1, 0, 0, 0, double, false>(c, 1, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boys64.p, f0, nt[1][0]); break;
-          default: s = launch_class<0, 0, 0, 0, double, false>(c, 0, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boys64.p, f0, nt[0][0]); break;
+          case 5: s = launch_class<1, 1, 1, 1, double, true>(c, 5, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boysh64.p, f0, nt[5][0]); break;
+          case 4: s = launch_class<1, 1, 1, 0, double, false>(c, 4, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boysh64.p, f0, nt[4][0]); break;
+          case 3: s = launch_class<1, 1, 0, 0, double, false>(c, 3, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boysh64.p, f0, nt[3][0]); break;
+          case 2: s = launch_class<1, 0, 1, 0, double, false>(c, 2, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boysh64.p, f0, nt[2][0]); break;
+          case 1: s = launch_class<1, 0, 0, 0, double, false>(c, 1, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boysh64.p, f0, nt[1][0]); break;
+          default: s = launch_class<0, 0, 0, 0, double, false>(c, 0, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boysh64.p, f0, nt[0][0]); break;
         }
       } else {
         switch (k) {
-          case 5: s = launch_class<1, 1, 1, 1, float, false>(c, 5, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boys32.p, f0, nt[5][1]); break;
-          case 4: s = launch_class<1, 1, 1, 0, float, false>(c, 4, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boys32.p, f0, nt[4][1]); break;
-          case 3: s = launch_class<1, 1, 0, 0, float, false>(c, 3, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boys32.p, f0, nt[3][1]); break;
-          case 2: s = launch_class<1, 0, 1, 0, float, false>(c, 2, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boys32.p, f0, nt[2][1]); break;
-          case 1: s = launch_class<1, 0, 0, 0, float, false>(c, 1, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boys32.p, f0, nt[1][1]); break;
-          default: s = launch_class<0, 0, 0, 0, float, false>(c, 0, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boys32.p, f0, nt[0][1]); break;
+          case 5: s = launch_class<1, 1, 1, 1, float, false>(c, 5, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boysh32.p, f0, nt[5][1]); break;
+          case 4: s = launch_class<1, 1, 1, 0, float, false>(c, 4, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boysh32.p, f0, nt[4][1]); break;
+          case 3: s = launch_class<1, 1, 0, 0, float, false>(c, 3, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boysh32.p, f0, nt[3][1]); break;
+          case 2: s = launch_class<1, 0, 1, 0, float, false>(c, 2, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boysh32.p, f0, nt[2][1]); break;
+          case 1: s = launch_class<1, 0, 0, 0, float, false>(c, 1, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boysh32.p, f0, nt[1][1]); break;
+          default: s = launch_class<0, 0, 0, 0, float, false>(c, 0, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boysh32.p, f0, nt[0][1]); break;
         }
       }
       if (s != GBHF_OK) return s;

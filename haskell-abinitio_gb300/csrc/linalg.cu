@@ -5,6 +5,7 @@
 #include <vector>
 
 #include "gbhf_internal.h"
+#include "jacobi.cuh"
 
 namespace gbhf {
 
@@ -404,20 +405,6 @@ __device__ bool grid_barrier(unsigned* count, unsigned* gen, int* status) {
   return s_ok != 0;
 }
 
-struct JacobiArgs {
-  int n, m;            // matrix size, padded even size
-  double* A;           // m x m (padded with zeros), destroyed
-  double* V;           // n x m accumulated rotations (rows n)
-  double* rot;         // per index: alpha, beta (2*m)
-  int* partner;        // per index
-  double* red;         // reduction scratch (2 doubles)
-  unsigned* bar;       // barrier count, generation
-  int* status;
-  int max_sweeps;
-  double tol;          // relative off-diagonal Frobenius tolerance
-  int* sweeps_out;
-};
-
 __device__ __forceinline__ void pair_of(int r, int k, int m, int& p, int& q) {
   // circle method: index m-1 fixed, others rotate
   if (k == 0) {
@@ -646,6 +633,8 @@ gbhf_status eigh(gbhf_ctx* c, int n, const double* d_A, double* d_evals, double*
   GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
   GBHF_CUDA(c, cudaGetLastError());
   w.last_sweeps = sweeps;
+  c->prof.jacobi_sweeps += sweeps;
+  c->prof.jacobi_calls += 1;
   if (st & GBHF_DEV_ERR_TIMEOUT) return fail(c, GBHF_ERR_DEVICE_TIMEOUT, "Jacobi grid barrier timed out");
   if (st & GBHF_DEV_ERR_NOTCONV) return fail(c, GBHF_ERR_NOT_CONVERGED, "Jacobi eigen-solver did not converge");
   return GBHF_OK;

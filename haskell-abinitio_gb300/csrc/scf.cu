@@ -3,6 +3,7 @@
 // scalars (max|e|, energy, RMS dD, DIIS dot products) to take the branch
 // decisions of the reference driver.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <vector>
 
@@ -111,6 +112,11 @@ gbhf_status scf_run(gbhf_ctx* c, const gbhf_scf_opts* o, gbhf_result* r) {
   GBHF_WS(c, Dnew, 20, nn);
   GBHF_WS(c, Dref, 21, nn);
   GBHF_WS(c, coefs, 22, 32);
+  using clk = std::chrono::steady_clock;
+  auto ms_since = [](clk::time_point t0) {
+    return std::chrono::duration<double, std::milli>(clk::now() - t0).count();
+  };
+  auto t_phase = clk::now();
   // one-electron matrices and orthogonaliser
   GBHF_TRY(onee_matrices(c, ref, fS, fH));
   GBHF_TRY(flat_to_square(c, n, fS, S));
@@ -184,7 +190,10 @@ gbhf_status scf_run(gbhf_ctx* c, const gbhf_scf_opts* o, gbhf_result* r) {
   const double* last_fuse = F;
   double hstats[4];
   const double prim64_0 = c->prof.prim64, prim32_0 = c->prof.prim32, shq0 = c->prof.shellq, fnq0 = c->prof.fnq;
+  GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
+  c->prof.ph_setup += ms_since(t_phase);
   for (step = 0; step < o->max_iter; ++step) {
+    t_phase = clk::now();
     // ---- Fock matrix of the current density
     if (ref) {
       GBHF_TRY(square_to_flat(c, n, D, fD));
@@ -214,6 +223,9 @@ gbhf_status scf_run(gbhf_ctx* c, const gbhf_scf_opts* o, gbhf_result* r) {
       GBHF_TRY(axpby(c, nn, 1.0, H, 1.0, Gacc, F));
       fock_builds += 1;
     }
+    GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
+    c->prof.ph_fock += ms_since(t_phase);
+    t_phase = clk::now();
     // ---- DIIS error and extrapolation (DIIS.hs:55-132)
     GBHF_TRY(diis_error_dev(c, n, F, S, D, X, E));
     double maxe = 0;
@@ -295,11 +307,17 @@ gbhf_status scf_run(gbhf_ctx* c, const gbhf_scf_opts* o, gbhf_result* r) {
       }
       GBHF_TRY(prepend());
     }
+    GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
+    c->prof.ph_diis += ms_since(t_phase);
+    t_phase = clk::now();
     // ---- diagonalise the (extrapolated) Fock matrix
     GBHF_TRY(diagonal_hf_dev(c, n, Fuse, X, nocc, Cm, Dnew, eps, Cp));
-    last_fuse = (ref || o->ref_stop_rule) ? Fuse : F;
+    last_fuse = o->ref_stop_rule ? Fuse : F;
+    GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
+    c->prof.ph_diag += ms_since(t_phase);
+    t_phase = clk::now();
     // ---- energies and convergence
-    if (ref || o->ref_stop_rule) {
+    if (o->ref_stop_rule) {
       GBHF_TRY(reduce_stats(c, n, nullptr, H, Fuse, Dnew, D, hstats));
       energy = hstats[1] + enuc;   // variationalE with F_DIIS and the new density
       converged = step != 0 && maxe < o->conv_error;
@@ -309,6 +327,7 @@ gbhf_status scf_run(gbhf_ctx* c, const gbhf_scf_opts* o, gbhf_result* r) {
       const double rms = std::sqrt(hstats[2] / (double)nn);
       converged = have_prev && std::fabs(energy - e_prev) < o->conv_energy && rms < o->conv_density;
     }
+    c->prof.ph_other += ms_since(t_phase);
     e_prev = energy;
     have_prev = true;
     GBHF_CUDA(c, cudaMemcpyAsync(D, Dnew, nn * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));

@@ -148,7 +148,7 @@ static double boys_series(int m, double xd) {
 }
 
 gbhf_status ensure_boys_tables(gbhf_ctx* c) {
-  if (c->boys64.p && c->boys32.p) return GBHF_OK;
+  if (c->boys64.p && c->boys32.p && c->boysh64.p && c->boysh32.p) return GBHF_OK;
   std::vector<double> t64((size_t)BOYS64_NROW * BOYS_NCOL);
   std::vector<float> t32((size_t)BOYS32_NROW * BOYS_NCOL);
   for (int j = 0; j < BOYS64_NROW; ++j)
@@ -157,10 +157,34 @@ gbhf_status ensure_boys_tables(gbhf_ctx* c) {
     const float tj = (float)j * BOYS32_H;   // the node the device forms in float
     for (int m = 0; m < BOYS_NCOL; ++m) t32[(size_t)j * BOYS_NCOL + m] = (float)boys_series(m, (double)tj);
   }
+  // Horner tables: G[j][m*NT + k] = F_(m+k)(T_j) / k!
+  std::vector<double> h64((size_t)BOYS64_NROW * BOYSH64_STRIDE, 0.0);
+  std::vector<float> h32((size_t)BOYS32_NROW * BOYSH32_STRIDE, 0.0f);
+  for (int j = 0; j < BOYS64_NROW; ++j) {
+    double inv_fact = 1.0;
+    for (int k = 0; k < BOYS64_NTERM; ++k) {
+      if (k > 0) inv_fact /= k;
+      for (int m = 0; m <= BOYSH_LMAX; ++m)
+        h64[(size_t)j * BOYSH64_STRIDE + m * BOYS64_NTERM + k] = t64[(size_t)j * BOYS_NCOL + m + k] * inv_fact;
+    }
+  }
+  for (int j = 0; j < BOYS32_NROW; ++j) {
+    const double tj = (double)((float)j * BOYS32_H);
+    double inv_fact = 1.0;
+    for (int k = 0; k < BOYS32_NTERM; ++k) {
+      if (k > 0) inv_fact /= k;
+      for (int m = 0; m <= BOYSH_LMAX; ++m)
+        h32[(size_t)j * BOYSH32_STRIDE + m * BOYS32_NTERM + k] = (float)(boys_series(m + k, tj) * inv_fact);
+    }
+  }
   GBHF_CUDA(c, c->boys64.alloc(t64.size()));
   GBHF_CUDA(c, c->boys32.alloc(t32.size()));
+  GBHF_CUDA(c, c->boysh64.alloc(h64.size()));
+  GBHF_CUDA(c, c->boysh32.alloc(h32.size()));
   GBHF_CUDA(c, cudaMemcpyAsync(c->boys64.p, t64.data(), t64.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
   GBHF_CUDA(c, cudaMemcpyAsync(c->boys32.p, t32.data(), t32.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+  GBHF_CUDA(c, cudaMemcpyAsync(c->boysh64.p, h64.data(), h64.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  GBHF_CUDA(c, cudaMemcpyAsync(c->boysh32.p, h32.data(), h32.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream));
   GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
   return GBHF_OK;
 }
@@ -280,7 +304,9 @@ gbhf_status ensure_pairs(gbhf_ctx* c) {
           f[BRA_PBX + x] = Px - RB[x];
           r2 += (RA[x] - RB[x]) * (RA[x] - RB[x]);
         }
-        f[BRA_K] = sa.coef[ia] * sb.coef[ib] * std::exp(-mu * r2);
+        // K' = sqrt(2 pi^(5/2)) c_a c_b exp(-mu |AB|^2) / p: the product of a bra and a
+        // ket K' times 1/sqrt(p+q) is the whole ERI prefactor
+        f[BRA_K] = std::sqrt(TWO_PI_2P5) * sa.coef[ia] * sb.coef[ib] * std::exp(-mu * r2) / p;
         const size_t bidx = (size_t)P.hPoff[t] + k;
         const size_t kidx = (size_t)sg.w + (size_t)k * seglen + (t - sg.x);
         for (int fl = 0; fl < BRA_NFIELD; ++fl) {

@@ -69,9 +69,16 @@ def test_exact_mode_fp64_energy(ctx, name, make):
 
 def test_cluster_fixture_energies(ctx):
     for name, rec in golden("clusters.json").items():
-        ctx.set_basis(B.flatten(M.cluster_atoms("batch256", rec["basis"], index=rec["batch_index"])))
-        r = ctx.scf(_lib.baseline_opts())
+        if "batch_index" in rec:
+            atoms = M.cluster_atoms("batch256", rec["basis"], index=rec["batch_index"])
+        else:
+            atoms = M.cluster_atoms(rec["cluster"], rec["basis"])
+        ctx.set_basis(B.flatten(atoms))
+        r = ctx.scf(_lib.baseline_opts(), want_matrices=False)
         assert abs(r["energy"] - rec["energy"]) < 1e-8, name
+        # mixed precision (FP32 below Schwarz bound 1e-4, incremental builds) within 1e-6
+        rm = ctx.scf(_lib.baseline_opts(precision=_lib.PREC_MIXED, incremental=1), want_matrices=False)
+        assert abs(rm["energy"] - rec["energy"]) < 1e-6, name
 
 
 def test_mixed_precision_energy_w8(ctx):
