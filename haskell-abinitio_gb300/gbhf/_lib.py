@@ -82,6 +82,7 @@ def load():
         "gbhf_fock": (st, [_vp, C.c_int, C.c_int, C.c_double, C.c_double, _dp, _dp, _dp]),
         "gbhf_symm_ortho": (st, [_vp, C.c_int, _dp, _dp]),
         "gbhf_eigen_solve": (st, [_vp, C.c_int, _dp, _dp, _dp]),
+        "gbhf_eigen_solve_noalloc": (st, [C.c_int, _vp, _vp, _vp, _vp]),
         "gbhf_diagonal_hf": (st, [_vp, C.c_int, _dp, _dp, C.c_int, _dp, _dp, _dp]),
         "gbhf_diis_error": (st, [_vp, C.c_int, _dp, _dp, _dp, _dp, _dp]),
         "gbhf_diis_extrapolate": (st, [_vp, C.c_int, C.c_int, _dp, _dp, _dp, _ip]),

@@ -154,6 +154,23 @@ gbhf_status gbhf_symm_ortho(gbhf_ctx* ctx, int n, const double* s_square, double
  * ascending, eigenvectors as columns of the N*N row-major output. */
 gbhf_status gbhf_eigen_solve(gbhf_ctx* ctx, int n, const double* a_square, double* evals, double* evecs);
 
+/* Eigen-solve that allocates nothing.  No counterpart in the reference: it
+ * exists for callers that must not allocate device memory during the call,
+ * e.g. code running inside another framework's custom-call hook, where that
+ * framework owns every buffer.  d_a (n x n, row-major, symmetric), d_evals (n)
+ * and d_evecs (n x n, eigenvectors as columns, eigenvalues ascending) are
+ * device pointers owned by the caller; `stream` is a cudaStream_t (NULL =
+ * the default stream) and the call returns after that stream has finished the
+ * work.  The solver's working memory is one static device array sized for
+ * n <= GBHF_NOALLOC_EIGEN_MAX_N (about 1 MiB, held by every GPU that loads
+ * the library until the process exits); larger n returns GBHF_ERR_BAD_INPUT.
+ * The first call on a device resolves that array's device address and the
+ * launch geometry; make that first call before any stream capture.  All calls
+ * share the array, so calls that overlap on the GPU (other host threads or
+ * streams) race: serialise them. */
+#define GBHF_NOALLOC_EIGEN_MAX_N 256
+gbhf_status gbhf_eigen_solve_noalloc(int n, const double* d_a, double* d_evals, double* d_evecs, void* stream);
+
 /* diagonalHF (HartreeFock/HartreeFock.hs:263-273): X^T F X, eigen-solve,
  * C = X C', density P = 2 C_occ C_occ^T (calcDensity, :195-208). */
 gbhf_status gbhf_diagonal_hf(gbhf_ctx* ctx, int n, const double* f_flat, const double* x_square, int n_occupied,
