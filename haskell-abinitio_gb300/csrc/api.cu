@@ -88,6 +88,9 @@ gbhf_status gbhf_destroy(gbhf_ctx* c) {
     if (e) cudaEventDestroy(e);
   for (auto& e : c->evu)
     if (e) cudaEventDestroy(e);
+  for (gbhf_ctx* w : c->pool) gbhf_destroy(w);
+  c->pool.clear();
+  cudaSetDevice(c->device);
   cudaStream_t s = c->stream;
   delete c;   // frees device buffers
   if (s) cudaStreamDestroy(s);
@@ -397,23 +400,44 @@ gbhf_status gbhf_scf(gbhf_ctx* c, const gbhf_scf_opts* opts, gbhf_result* result
 gbhf_status gbhf_gradient(gbhf_ctx* c, int precision, double schwarz_cutoff, const double* d_flat,
                           const double* w_flat, double* grad) {
   CTX_CHECK(c);
-  (void)precision;
-  (void)schwarz_cutoff;
-  (void)d_flat;
-  (void)w_flat;
-  (void)grad;
-  return fail(c, GBHF_ERR_UNSUPPORTED, "gradient kernels not built yet");
-}
-
-gbhf_status gbhf_scf_batch(gbhf_ctx* c, int n_mol, const int* atom_off, const int* cgf_off, const double* xyz_bohr,
-                           const double* charges, const int* cgf_atom, const int* cgf_lxyz, const int* cgf_nprim,
-                           const double* prim_coef, const double* prim_exp, const gbhf_scf_opts* opts,
-                           double* energies, int* iterations, int* converged, double* grads) {
-  CTX_CHECK(c);
-  (void)n_mol; (void)atom_off; (void)cgf_off; (void)xyz_bohr; (void)charges; (void)cgf_atom; (void)cgf_lxyz;
-  (void)cgf_nprim; (void)prim_coef; (void)prim_exp; (void)opts; (void)energies; (void)iterations;
-  (void)converged; (void)grads;
-  return fail(c, GBHF_ERR_UNSUPPORTED, "batched SCF not built yet");
+  (void)precision;   // derivative integrals are evaluated in FP64 for either precision
+  if (!need_basis(c)) return GBHF_ERR_BAD_INPUT;
+  if (!grad || !(schwarz_cutoff >= 0)) return fail(c, GBHF_ERR_BAD_INPUT, "bad arguments");
+  if ((d_flat == nullptr) != (w_flat == nullptr))
+    return fail(c, GBHF_ERR_BAD_INPUT, "give both D and W, or neither (use the last SCF)");
+  const int n = c->basis.nbf, na = c->basis.natoms;
+  const size_t nn = (size_t)n * n, ntri = (size_t)n * (n + 1) / 2;
+  GBHF_WS(c, D, 15, nn);
+  GBHF_WS(c, W, 16, nn);
+  GBHF_WS(c, t, 17, std::max(ntri, (size_t)n));
+  if (d_flat) {
+    GBHF_CUDA(c, cudaMemcpyAsync(t, d_flat, ntri * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    GBHF_TRY(flat_to_square(c, n, t, D));
+    GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
+    GBHF_CUDA(c, cudaMemcpyAsync(t, w_flat, ntri * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    GBHF_TRY(flat_to_square(c, n, t, W));
+  } else {
+    if (c->last_gen != c->basis_gen || c->last_nocc < 0)
+      return fail(c, GBHF_ERR_BAD_INPUT, "no converged SCF for this basis: run gbhf_scf first or pass D and W");
+    // orbitals of the converged Fock matrix -> W; D from the SCF
+    GBHF_WS(c, S, 18, nn);
+    GBHF_WS(c, X, 19, nn);
+    GBHF_WS(c, Cm, 20, nn);
+    GBHF_WS(c, Dt, 21, nn);
+    GBHF_TRY(onee_matrices(c, false, t, nullptr));
+    GBHF_TRY(flat_to_square(c, n, t, S));
+    int it = 0;
+    GBHF_TRY(inv_sqrt_dev(c, n, S, X, &it));
+    GBHF_WS(c, eps, 22, (size_t)n);
+    GBHF_TRY(diagonal_hf_dev(c, n, c->last_F.p, X, c->last_nocc, Cm, Dt, eps, nullptr));
+    GBHF_TRY(energy_weighted_density(c, n, c->last_nocc, Cm, eps, W));
+    // D and W from the same orbitals
+    GBHF_CUDA(c, cudaMemcpyAsync(D, Dt, nn * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+  }
+  DBuf<double> g;
+  GBHF_CUDA(c, g.alloc(3 * (size_t)na));
+  GBHF_TRY(gradient_dev(c, D, W, schwarz_cutoff, g.p));
+  return download(c, grad, g.p, 3 * (size_t)na * sizeof(double));
 }
 
 gbhf_status gbhf_profile_reset(gbhf_ctx* c, int enable_events) {

@@ -143,6 +143,12 @@ struct gbhf_ctx {
   // dense work buffers (n*n doubles)
   gbhf::DBuf<double> w[24];
   gbhf::JacobiWork jac;
+  // state of the last SCF (for the gradient): density, Fock matrix, occupation
+  gbhf::DBuf<double> last_D, last_F;
+  int last_nocc = -1;
+  long last_gen = -1;
+  // worker contexts of gbhf_scf_batch (owned; destroyed with this context)
+  std::vector<gbhf_ctx*> pool;
   gbhf::DBuf<float> dfloat;
   gbhf::DBuf<int> dev_status;
   gbhf::DBuf<unsigned> barrier;
@@ -202,6 +208,10 @@ gbhf_status schwarz_pairs_dev(gbhf_ctx* c, const int* d_A, const int* d_B, int n
 // G_acc (n*n) += sym(G''(D)), D square n*n.  w = screening weight.
 gbhf_status jk_build(gbhf_ctx* c, const double* d_Dsq, double* d_G, int precision, double schwarz,
                      double mixed_cutoff, double weight);
+// Q of every pair in [cls_start[cl], cls_start[cl+1]) (pairs grouped by class,
+// bra-layout primitive data at d_poff), FP64 class code.
+gbhf_status schwarz_classes_dev(gbhf_ctx* c, const int* cls_start, const int* d_K, const int* d_poff,
+                                const double* d_bra, long long npp, double* d_Q);
 // linalg.cu
 gbhf_status gemm(gbhf_ctx* c, bool ta, bool tb, int m, int n, int k, double alpha, const double* A, int lda,
                  const double* B, int ldb, double beta, double* C, int ldc);
@@ -209,6 +219,11 @@ gbhf_status eigh(gbhf_ctx* c, int n, const double* d_A, double* d_evals, double*
 gbhf_status flat_to_square(gbhf_ctx* c, int n, const double* d_flat, double* d_sq);
 gbhf_status square_to_flat(gbhf_ctx* c, int n, const double* d_sq, double* d_flat);
 gbhf_status symm_ortho_dev(gbhf_ctx* c, int n, const double* d_S, double* d_X);
+// S^-1/2 by Newton-Schulz (GEMMs only); density by canonical purification.
+gbhf_status inv_sqrt_dev(gbhf_ctx* c, int n, const double* d_S, double* d_X, int* iters);
+gbhf_status purify(gbhf_ctx* c, int n, int ne, const double* d_F, double* d_P, double* err_out);
+gbhf_status density_purified_dev(gbhf_ctx* c, int n, const double* d_Fsq, const double* d_X, int nocc,
+                                 double* d_Dsq);
 gbhf_status diagonal_hf_dev(gbhf_ctx* c, int n, const double* d_Fsq, const double* d_X, int nocc, double* d_C,
                             double* d_Dsq, double* d_eps, double* d_Cprime_warm);
 gbhf_status diis_error_dev(gbhf_ctx* c, int n, const double* d_F, const double* d_S, const double* d_D,
@@ -216,6 +231,10 @@ gbhf_status diis_error_dev(gbhf_ctx* c, int n, const double* d_F, const double* 
 gbhf_status gauss_elem_dev_call(gbhf_ctx* c, int m, const double* h_a, const double* h_b, double* h_x, bool* ok);
 // scf.cu
 gbhf_status scf_run(gbhf_ctx* c, const gbhf_scf_opts* o, gbhf_result* r);
+// grad.cu: D, W square on the device; gradient (3*natoms) on the device
+gbhf_status gradient_dev(gbhf_ctx* c, const double* d_D, const double* d_W, double schwarz, double* d_grad);
+gbhf_status energy_weighted_density(gbhf_ctx* c, int n, int nocc, const double* d_C, const double* d_eps,
+                                    double* d_W);
 gbhf_status dot_matrices(gbhf_ctx* c, int n2, int k, const double* const* mats, const double* d_e,
                          double* d_out);
 gbhf_status lincomb(gbhf_ctx* c, int n2, int k, const double* const* mats, const double* coefs, double* d_out);

@@ -266,6 +266,59 @@ __global__ void __launch_bounds__(JK_THREADS) k_jk(JKArgs<T> a) {
   }
 }
 
+// ------------------------------------------------------- Schwarz bounds ----
+// Q_AB = sqrt(max_ab (ab|ab)) for the pairs of one class (bra = ket = pair),
+// with the generated FP64 class code; one thread per pair, its primitive
+// pairs staged in its own slice of shared memory.
+constexpr int SCHWARZ_THREADS = 8;   // 8 x 3840 B of staged primitives per block
+
+template <int LA, int LB>
+__global__ void __launch_bounds__(SCHWARZ_THREADS) k_schwarz_cls(int p0, int p1, const int* __restrict__ pK,
+                                                                  const int* __restrict__ poff,
+                                                                  const double* __restrict__ bra, long long npp,
+                                                                  const double* __restrict__ boys,
+                                                                  double* __restrict__ Q) {
+  constexpr int NA = ncart_c(LA), NB = ncart_c(LB), NAB = NA * NB;
+  __shared__ double sb[SCHWARZ_THREADS][BRA_NFIELD * BRA_STRIDE];
+  const int t = p0 + blockIdx.x * SCHWARZ_THREADS + threadIdx.x;
+  if (t >= p1) return;
+  const int K = pK[t];
+  const long long o = poff[t];
+  double* s = sb[threadIdx.x];
+  for (int f = 0; f < BRA_NFIELD; ++f)
+    for (int k = 0; k < K; ++k) s[f * BRA_STRIDE + k] = bra[f * npp + o + k];
+  RegAcc<double, NAB * NAB> acc;
+  acc.zero();
+  for (int k = 0; k < K; ++k) {
+    auto g = [&](int f) { return s[f * BRA_STRIDE + k]; };
+    ClassFn<LA, LB, LA, LB>::template run<double, RegAcc<double, NAB * NAB>>(
+        s, K, g(BRA_P), g(BRA_INVP), g(BRA_PX), g(BRA_PY), g(BRA_PZ), g(BRA_PAX), g(BRA_PAY), g(BRA_PAZ),
+        g(BRA_PBX), g(BRA_PBY), g(BRA_PBZ), g(BRA_K), boys, acc);
+  }
+  double mx = 0;
+#pragma unroll
+  for (int ab = 0; ab < NAB; ++ab) mx = fmax(mx, fabs(acc.get(ab * NAB + ab)));
+  Q[t] = sqrt(mx);
+}
+
+gbhf_status schwarz_classes_dev(gbhf_ctx* c, const int* cls_start, const int* d_K, const int* d_poff,
+                                const double* d_bra, long long npp, double* d_Q) {
+  for (int cl = 0; cl < NPCLS; ++cl) {
+    const int p0 = cls_start[cl], p1 = cls_start[cl + 1];
+    if (p1 <= p0) continue;
+    const int blocks = (p1 - p0 + SCHWARZ_THREADS - 1) / SCHWARZ_THREADS;
+    if (cl == 0)
+      k_schwarz_cls<0, 0><<<blocks, SCHWARZ_THREADS, 0, c->stream>>>(p0, p1, d_K, d_poff, d_bra, npp, c->boysh64.p, d_Q);
+    else if (cl == 1)
+      k_schwarz_cls<1, 0><<<blocks, SCHWARZ_THREADS, 0, c->stream>>>(p0, p1, d_K, d_poff, d_bra, npp, c->boysh64.p, d_Q);
+    else
+      k_schwarz_cls<1, 1><<<blocks, SCHWARZ_THREADS, 0, c->stream>>>(p0, p1, d_K, d_poff, d_bra, npp, c->boysh64.p, d_Q);
+    count_launch(c);
+    GBHF_CUDA(c, cudaGetLastError());
+  }
+  return GBHF_OK;
+}
+
 // ------------------------------------------------------------ task lists ----
 
 struct TaskGenArgs {

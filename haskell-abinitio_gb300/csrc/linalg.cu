@@ -95,12 +95,107 @@ __global__ void __launch_bounds__(128) k_dgemm(bool ta, bool tb, int m, int n, i
       }
 }
 
+// Small-matrix variant: 32x32 C tile per CTA (4 warps of 16x16 = 2x2 DMMA
+// tiles), K split over gridDim.z slices whose partial products are added
+// with FP64 atomics into C (pre-scaled by beta), so that N ~ 200 matrices
+// still occupy every SM.
+constexpr int ST = 32, SK = 16;
+
+__global__ void __launch_bounds__(128) k_dgemm_split(bool ta, bool tb, int m, int n, int k, int kslice,
+                                                     double alpha, const double* __restrict__ A, int lda,
+                                                     const double* __restrict__ B, int ldb, double* __restrict__ C,
+                                                     int ldc) {
+  __shared__ double As[ST][SK + 1];
+  __shared__ double Bs[SK][ST + 2];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int row0 = blockIdx.y * ST, col0 = blockIdx.x * ST;
+  const int k0 = blockIdx.z * kslice, k1 = min(k, k0 + kslice);
+  const int wr = (warp >> 1) * 16, wc = (warp & 1) * 16;
+  double acc[2][2][2] = {};
+  for (int kk = k0; kk < k1; kk += SK) {
+    for (int idx = tid; idx < ST * SK; idx += 128) {
+      int r, cc;
+      if (!ta) {
+        r = idx / SK;
+        cc = idx % SK;
+      } else {
+        cc = idx / ST;
+        r = idx % ST;
+      }
+      const int gr = row0 + r, gk = kk + cc;
+      double v = 0.0;
+      if (gr < m && gk < k1) v = ta ? A[(long)gk * lda + gr] : A[(long)gr * lda + gk];
+      As[r][cc] = v;
+    }
+    for (int idx = tid; idx < SK * ST; idx += 128) {
+      int r, cc;
+      if (!tb) {
+        r = idx / ST;
+        cc = idx % ST;
+      } else {
+        cc = idx / SK;
+        r = idx % SK;
+      }
+      const int gk = kk + r, gc = col0 + cc;
+      double v = 0.0;
+      if (gk < k1 && gc < n) v = tb ? B[(long)gc * ldb + gk] : B[(long)gk * ldb + gc];
+      Bs[r][cc] = v;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k4 = 0; k4 < SK; k4 += 4) {
+      double af[2], bf[2];
+#pragma unroll
+      for (int i = 0; i < 2; ++i) af[i] = As[wr + i * 8 + (lane >> 2)][k4 + (lane & 3)];
+#pragma unroll
+      for (int j = 0; j < 2; ++j) bf[j] = Bs[k4 + (lane & 3)][wc + j * 8 + (lane >> 2)];
+#pragma unroll
+      for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 2; ++j) dmma(acc[i][j][0], acc[i][j][1], af[i], bf[j]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < 2; ++j)
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int r = row0 + wr + i * 8 + (lane >> 2);
+        const int cc = col0 + wc + j * 8 + 2 * (lane & 3) + h;
+        if (r < m && cc < n) atomicAdd(C + (long)r * ldc + cc, alpha * acc[i][j][h]);
+      }
+}
+
+__global__ void k_scale_matrix(int m, int n, double beta, double* __restrict__ C, int ldc) {
+  const int r = blockIdx.y, cc = blockIdx.x * blockDim.x + threadIdx.x;
+  if (cc >= n) return;
+  double* p = C + (long)r * ldc + cc;
+  *p = beta == 0.0 ? 0.0 : beta * *p;
+}
+
 gbhf_status gemm(gbhf_ctx* c, bool ta, bool tb, int m, int n, int k, double alpha, const double* A, int lda,
                  const double* B, int ldb, double beta, double* C, int ldc) {
   if (m <= 0 || n <= 0) return GBHF_OK;
-  dim3 grid((n + GT - 1) / GT, (m + GT - 1) / GT);
-  k_dgemm<<<grid, 128, 0, c->stream>>>(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
-  count_launch(c);
+  const long tiles64 = (long)((n + GT - 1) / GT) * ((m + GT - 1) / GT);
+  if (tiles64 >= 2L * c->nsm) {
+    dim3 grid((n + GT - 1) / GT, (m + GT - 1) / GT);
+    k_dgemm<<<grid, 128, 0, c->stream>>>(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+    count_launch(c);
+    GBHF_CUDA(c, cudaGetLastError());
+    return GBHF_OK;
+  }
+  const int tiles = ((n + ST - 1) / ST) * ((m + ST - 1) / ST);
+  int splits = std::max(1, (2 * c->nsm + tiles - 1) / tiles);
+  splits = std::min(splits, std::max(1, (k + 4 * SK - 1) / (4 * SK)));   // at least 4 k-steps per slice
+  int kslice = (k + splits - 1) / splits;
+  kslice = (kslice + SK - 1) / SK * SK;
+  splits = std::max(1, (k + kslice - 1) / kslice);
+  k_scale_matrix<<<dim3((n + 127) / 128, m), 128, 0, c->stream>>>(m, n, beta, C, ldc);
+  k_dgemm_split<<<dim3((n + ST - 1) / ST, (m + ST - 1) / ST, splits), 128, 0, c->stream>>>(
+      ta, tb, m, n, k, kslice, alpha, A, lda, B, ldb, C, ldc);
+  count_launch(c, 2);
   GBHF_CUDA(c, cudaGetLastError());
   return GBHF_OK;
 }
@@ -637,6 +732,246 @@ gbhf_status eigh(gbhf_ctx* c, int n, const double* d_A, double* d_evals, double*
   c->prof.jacobi_calls += 1;
   if (st & GBHF_DEV_ERR_TIMEOUT) return fail(c, GBHF_ERR_DEVICE_TIMEOUT, "Jacobi grid barrier timed out");
   if (st & GBHF_DEV_ERR_NOTCONV) return fail(c, GBHF_ERR_NOT_CONVERGED, "Jacobi eigen-solver did not converge");
+  return GBHF_OK;
+}
+
+// --------------------------------------------- GEMM-only matrix functions ----
+// Gershgorin interval and trace of a symmetric matrix: out = {lo, hi, trace}.
+__global__ void k_gershgorin(int n, const double* __restrict__ A, double* __restrict__ out) {
+  double lo = 1e300, hi = -1e300, tr = 0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    double r = 0;
+    const double* row = A + (long)i * n;
+    for (int j = 0; j < n; ++j)
+      if (j != i) r += fabs(row[j]);
+    lo = fmin(lo, row[i] - r);
+    hi = fmax(hi, row[i] + r);
+    tr += row[i];
+  }
+  __shared__ double s_lo[32], s_hi[32], s_tr[32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    lo = fmin(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+    hi = fmax(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    tr += __shfl_xor_sync(0xffffffffu, tr, o);
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if (lane == 0) {
+    s_lo[wid] = lo;
+    s_hi[wid] = hi;
+    s_tr[wid] = tr;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < nw; ++w) {
+      lo = fmin(lo, s_lo[w]);
+      hi = fmax(hi, s_hi[w]);
+      tr += s_tr[w];
+    }
+    out[0] = lo;
+    out[1] = hi;
+    out[2] = tr;
+  }
+}
+
+// P0 = (lambda/n)(mu I - F) + (ne/n) I with mu = tr F / n and
+// lambda = min(ne/(hi - mu), (n - ne)/(mu - lo))  (canonical purification start).
+__global__ void k_purify_init(int n, int ne, const double* __restrict__ F, const double* __restrict__ g,
+                              double* __restrict__ P) {
+  const int i = blockIdx.y, j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  const double lo = g[0], hi = g[1], mu = g[2] / n;
+  double lam = 1e300;
+  if (hi - mu > 0) lam = fmin(lam, ne / (hi - mu));
+  if (mu - lo > 0) lam = fmin(lam, (n - ne) / (mu - lo));
+  if (!(lam < 1e300)) lam = 0;
+  const double f = F[(long)i * n + j];
+  P[(long)i * n + j] = (lam / n) * ((i == j ? mu : 0.0) - f) + (i == j ? (double)ne / n : 0.0);
+}
+
+// traces of P, P^2, P^3 (diagonals) -> coefficients of the next iterate
+// P' = a P + b P^2 + d P^3 and the idempotency error tr(P - P^2) in coef[3].
+__global__ void k_purify_coef(int n, const double* __restrict__ P, const double* __restrict__ P2,
+                              const double* __restrict__ P3, double* __restrict__ coef) {
+  double t1 = 0, t2 = 0, t3 = 0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    t1 += P[(long)i * n + i];
+    t2 += P2[(long)i * n + i];
+    t3 += P3[(long)i * n + i];
+  }
+  __shared__ double s[3][32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    t1 += __shfl_xor_sync(0xffffffffu, t1, o);
+    t2 += __shfl_xor_sync(0xffffffffu, t2, o);
+    t3 += __shfl_xor_sync(0xffffffffu, t3, o);
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if (lane == 0) {
+    s[0][wid] = t1;
+    s[1][wid] = t2;
+    s[2][wid] = t3;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < nw; ++w) {
+      t1 += s[0][w];
+      t2 += s[1][w];
+      t3 += s[2][w];
+    }
+    const double den = t1 - t2, num = t2 - t3;
+    double a, b, d;
+    if (!(fabs(den) > 1e-300)) {   // already idempotent: keep P
+      a = 1;
+      b = 0;
+      d = 0;
+    } else {
+      const double cc = num / den;
+      if (cc >= 0.5) {
+        a = 0;
+        b = (1 + cc) / cc;
+        d = -1 / cc;
+      } else {
+        a = (1 - 2 * cc) / (1 - cc);
+        b = (1 + cc) / (1 - cc);
+        d = -1 / (1 - cc);
+      }
+    }
+    coef[0] = a;
+    coef[1] = b;
+    coef[2] = d;
+    coef[3] = den;
+  }
+}
+
+// Canonical purification (Palser & Manolopoulos, Phys. Rev. B 58, 12704 (1998)):
+// the spectral projector onto the ne lowest eigenvectors of the symmetric F,
+// by trace-conserving cubic polynomials of P, two GEMMs per step.  Returns the
+// idempotency error tr(P - P^2) of the result.
+gbhf_status purify(gbhf_ctx* c, int n, int ne, const double* d_F, double* d_P, double* err_out) {
+  const size_t nn = (size_t)n * n;
+  GBHF_WS(c, P2, 23, nn);
+  double* P3 = c->jac.t1.p;
+  GBHF_CUDA(c, c->jac.t1.alloc(nn));
+  P3 = c->jac.t1.p;
+  GBHF_CUDA(c, c->small.alloc(64));
+  double* g = c->small.p + 32;
+  double* coef = c->small.p + 40;
+  k_gershgorin<<<1, 1024, 0, c->stream>>>(n, d_F, g);
+  k_purify_init<<<dim3((n + 127) / 128, n), 128, 0, c->stream>>>(n, ne, d_F, g, d_P);
+  count_launch(c, 2);
+  double err = 1.0;
+  const int max_iter = 200;
+  for (int it = 0; it < max_iter; ++it) {
+    GBHF_TRY(gemm(c, false, false, n, n, n, 1.0, d_P, n, d_P, n, 0.0, P2, n));
+    GBHF_TRY(gemm(c, false, false, n, n, n, 1.0, d_P, n, P2, n, 0.0, P3, n));
+    k_purify_coef<<<1, 1024, 0, c->stream>>>(n, d_P, P2, P3, coef);
+    count_launch(c);
+    const double* mats[3] = {d_P, P2, P3};
+    GBHF_TRY(lincomb(c, (int)nn, 3, mats, coef, d_P));
+    if (it % 4 == 3 || it == max_iter - 1) {
+      GBHF_CUDA(c, cudaMemcpyAsync(&err, coef + 3, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+      GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
+      if (std::fabs(err) < 1e-11 * std::max(1, ne)) break;
+    }
+  }
+  if (err_out) *err_out = err;
+  if (!(std::fabs(err) < 1e-6 * std::max(1, ne)))
+    return fail(c, GBHF_ERR_NOT_CONVERGED, "density purification did not converge");
+  return GBHF_OK;
+}
+
+// Density of the ne lowest orbitals of F (AO basis) in the orthogonalised
+// basis: D = X (2 P) X^T with P the projector of F' = X^T F X.
+gbhf_status density_purified_dev(gbhf_ctx* c, int n, const double* d_Fsq, const double* d_X, int nocc,
+                                 double* d_Dsq) {
+  const size_t nn = (size_t)n * n;
+  GBHF_WS(c, T1, 10, nn);
+  GBHF_WS(c, Fp, 11, nn);
+  GBHF_WS(c, P, 12, nn);
+  GBHF_TRY(gemm(c, true, false, n, n, n, 1.0, d_X, n, d_Fsq, n, 0.0, T1, n));
+  GBHF_TRY(gemm(c, false, false, n, n, n, 1.0, T1, n, d_X, n, 0.0, Fp, n));
+  if (nocc <= 0) {
+    GBHF_CUDA(c, cudaMemsetAsync(d_Dsq, 0, nn * sizeof(double), c->stream));
+    return GBHF_OK;
+  }
+  double err = 0;
+  GBHF_TRY(purify(c, n, nocc, Fp, P, &err));
+  GBHF_TRY(gemm(c, false, false, n, n, n, 2.0, d_X, n, P, n, 0.0, T1, n));
+  GBHF_TRY(gemm(c, false, true, n, n, n, 1.0, T1, n, d_X, n, 0.0, d_Dsq, n));
+  return GBHF_OK;
+}
+
+// 3I - M
+__global__ void k_three_minus(int n, const double* __restrict__ M, double* __restrict__ out) {
+  const int i = blockIdx.y, j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  out[(long)i * n + j] = (i == j ? 3.0 : 0.0) - M[(long)i * n + j];
+}
+
+__global__ void k_ns_init(int n, const double* __restrict__ S, const double* __restrict__ g, double* __restrict__ Y,
+                          double* __restrict__ Z) {
+  const int i = blockIdx.y, j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  const double scale = 1.0 / g[1];
+  Y[(long)i * n + j] = S[(long)i * n + j] * scale;
+  Z[(long)i * n + j] = i == j ? 1.0 : 0.0;
+}
+
+__global__ void k_ns_err(int n, const double* __restrict__ T, double* out) {
+  double m = 0;
+  for (long idx = threadIdx.x; idx < (long)n * n; idx += blockDim.x) {
+    const long i = idx / n, j = idx % n;
+    m = fmax(m, fabs(T[idx] - (i == j ? 1.0 : 0.0)));
+  }
+  m = block_reduce(m, true);
+  if (threadIdx.x == 0) *out = m;
+}
+
+__global__ void k_ns_finish(int n, const double* __restrict__ g, const double* __restrict__ Z, double* __restrict__ X) {
+  const int i = blockIdx.y, j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  X[(long)i * n + j] = Z[(long)i * n + j] / sqrt(g[1]);
+}
+
+// S^(-1/2) by the coupled Newton-Schulz iteration (Higham, "Functions of
+// Matrices", 2008, eq. 6.35): Y0 = S/c, Z0 = I, M = 3I - Z Y,
+// Y <- Y M / 2, Z <- M Z / 2; Z -> (S/c)^(-1/2).  c bounds the spectrum
+// (Gershgorin), so S/c has eigenvalues in (0, 1].
+gbhf_status inv_sqrt_dev(gbhf_ctx* c, int n, const double* d_S, double* d_X, int* iters) {
+  const size_t nn = (size_t)n * n;
+  GBHF_WS(c, Y, 10, nn);
+  GBHF_WS(c, Z, 11, nn);
+  GBHF_WS(c, T, 12, nn);
+  GBHF_WS(c, M, 23, nn);
+  GBHF_CUDA(c, c->small.alloc(64));
+  double* g = c->small.p + 32;
+  double* e = c->small.p + 44;
+  k_gershgorin<<<1, 1024, 0, c->stream>>>(n, d_S, g);
+  k_ns_init<<<dim3((n + 127) / 128, n), 128, 0, c->stream>>>(n, d_S, g, Y, Z);
+  count_launch(c, 2);
+  double err = 1;
+  int it = 0;
+  for (; it < 100; ++it) {
+    GBHF_TRY(gemm(c, false, false, n, n, n, 1.0, Z, n, Y, n, 0.0, T, n));
+    if (it % 3 == 2) {
+      k_ns_err<<<1, 1024, 0, c->stream>>>(n, T, e);
+      count_launch(c);
+      GBHF_CUDA(c, cudaMemcpyAsync(&err, e, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+      GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
+      if (err < 1e-14) break;
+    }
+    k_three_minus<<<dim3((n + 127) / 128, n), 128, 0, c->stream>>>(n, T, M);
+    count_launch(c);
+    GBHF_TRY(gemm(c, false, false, n, n, n, 0.5, Y, n, M, n, 0.0, T, n));
+    std::swap(Y, T);
+    GBHF_TRY(gemm(c, false, false, n, n, n, 0.5, M, n, Z, n, 0.0, T, n));
+    std::swap(Z, T);
+  }
+  if (iters) *iters = it;
+  if (!(err < 1e-10)) return fail(c, GBHF_ERR_NOT_CONVERGED, "Newton-Schulz S^-1/2 did not converge");
+  k_ns_finish<<<dim3((n + 127) / 128, n), 128, 0, c->stream>>>(n, g, Z, d_X);
+  count_launch(c);
   return GBHF_OK;
 }
 

@@ -121,7 +121,21 @@ gbhf_status scf_run(gbhf_ctx* c, const gbhf_scf_opts* o, gbhf_result* r) {
   GBHF_TRY(onee_matrices(c, ref, fS, fH));
   GBHF_TRY(flat_to_square(c, n, fS, S));
   GBHF_TRY(flat_to_square(c, n, fH, H));
-  GBHF_TRY(symm_ortho_dev(c, n, S, X));
+  // Reference mode: symmOrtho as the reference writes it (U s^-1/2 U^T by an
+  // eigen-solve); exact mode: the same S^-1/2 by Newton-Schulz (GEMMs only).
+  if (ref) {
+    GBHF_TRY(symm_ortho_dev(c, n, S, X));
+  } else {
+    int ns_iters = 0;
+    GBHF_TRY(inv_sqrt_dev(c, n, S, X, &ns_iters));
+  }
+  // Per-iteration density: reference mode diagonalises (diagonalHF); exact
+  // mode takes the same projector by canonical purification and diagonalises
+  // once at the end for the orbitals.
+  auto new_density = [&](const double* Fsq, double* Dout) -> gbhf_status {
+    if (ref) return diagonal_hf_dev(c, n, Fsq, X, nocc, Cm, Dout, eps, Cp);
+    return density_purified_dev(c, n, Fsq, X, nocc, Dout);
+  };
   // stored ERIs for the reference path (and the Harris guess)
   DBuf<double> eri;
   const long long P = (long long)ntri;
@@ -166,10 +180,10 @@ gbhf_status scf_run(gbhf_ctx* c, const gbhf_scf_opts* o, gbhf_result* r) {
     k_harris<<<(unsigned)((ntri + 127) / 128), 128, 0, c->stream>>>((long)ntri, nocc, d1.p, d2.p, eri.p, fH, fD);
     count_launch(c);
     GBHF_TRY(flat_to_square(c, n, fD, Fd));
-    GBHF_TRY(diagonal_hf_dev(c, n, Fd, X, nocc, Cm, D, eps, Cp));
+    GBHF_TRY(new_density(Fd, D));
     GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
   } else {
-    GBHF_TRY(diagonal_hf_dev(c, n, H, X, nocc, Cm, D, eps, Cp));
+    GBHF_TRY(new_density(H, D));
   }
   if (!ref) eri.release();
   // DIIS history buffers: slots in c->w beyond the driver's
@@ -311,7 +325,7 @@ gbhf_status scf_run(gbhf_ctx* c, const gbhf_scf_opts* o, gbhf_result* r) {
     c->prof.ph_diis += ms_since(t_phase);
     t_phase = clk::now();
     // ---- diagonalise the (extrapolated) Fock matrix
-    GBHF_TRY(diagonal_hf_dev(c, n, Fuse, X, nocc, Cm, Dnew, eps, Cp));
+    GBHF_TRY(new_density(Fuse, Dnew));
     last_fuse = o->ref_stop_rule ? Fuse : F;
     GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
     c->prof.ph_diag += ms_since(t_phase);
@@ -341,6 +355,17 @@ gbhf_status scf_run(gbhf_ctx* c, const gbhf_scf_opts* o, gbhf_result* r) {
       }
       break;
     }
+  }
+  // keep the converged state for gbhf_gradient
+  GBHF_CUDA(c, c->last_D.alloc(nn));
+  GBHF_CUDA(c, c->last_F.alloc(nn));
+  GBHF_CUDA(c, cudaMemcpyAsync(c->last_D.p, D, nn * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+  GBHF_CUDA(c, cudaMemcpyAsync(c->last_F.p, last_fuse, nn * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+  c->last_nocc = nocc;
+  c->last_gen = c->basis_gen;
+  if (r && !ref && (r->coeff || r->orb_energies)) {
+    // orbitals of the last diagonalised Fock matrix (one eigen-solve per SCF)
+    GBHF_TRY(diagonal_hf_dev(c, n, last_fuse, X, nocc, Cm, Dnew, eps, Cp));
   }
   if (r) {
     r->energy = energy;

@@ -191,6 +191,33 @@ gbhf_status ensure_boys_tables(gbhf_ctx* c) {
 
 static int pair_class(int la, int lb) { return la == 0 ? 0 : (lb == 0 ? 1 : 2); }
 
+// Fields of every primitive pair of shells (A, B), out[k*BRA_NFIELD + field],
+// k = ia*np_B + ib.  K' = sqrt(2 pi^(5/2)) c_a c_b exp(-mu |AB|^2) / p, so the
+// product of a bra and a ket K' times 1/sqrt(p+q) is the whole ERI prefactor.
+static void pair_prims(const Basis& b, int A, int B, double* out) {
+  const Shell &sa = b.shells[A], &sb = b.shells[B];
+  const double* RA = &b.xyz[3 * sa.atom];
+  const double* RB = &b.xyz[3 * sb.atom];
+  double r2 = 0;
+  for (int x = 0; x < 3; ++x) r2 += (RA[x] - RB[x]) * (RA[x] - RB[x]);
+  int k = 0;
+  for (int ia = 0; ia < sa.np; ++ia)
+    for (int ib = 0; ib < sb.np; ++ib, ++k) {
+      const double ea = sa.expo[ia], eb = sb.expo[ib];
+      const double p = ea + eb, mu = ea * eb / p;
+      double* f = out + (size_t)k * BRA_NFIELD;
+      f[BRA_P] = p;
+      f[BRA_INVP] = 1.0 / p;
+      for (int x = 0; x < 3; ++x) {
+        const double Px = (ea * RA[x] + eb * RB[x]) / p;
+        f[BRA_PX + x] = Px;
+        f[BRA_PAX + x] = Px - RA[x];
+        f[BRA_PBX + x] = Px - RB[x];
+      }
+      f[BRA_K] = std::sqrt(TWO_PI_2P5) * sa.coef[ia] * sb.coef[ib] * std::exp(-mu * r2) / p;
+    }
+}
+
 gbhf_status ensure_pairs(gbhf_ctx* c) {
   if (c->pairs_ready) return GBHF_OK;
   const Basis& b = c->basis;
@@ -211,18 +238,47 @@ gbhf_status ensure_pairs(gbhf_ctx* c) {
       }
     }
   const int np = (int)A.size();
-  // 2. Schwarz bounds on the device
+  // 2. Schwarz bounds on the device, pairs grouped by class (class code, FP64)
   std::vector<double> Q(np);
   {
-    DBuf<int> dA, dB;
-    DBuf<double> dQ;
-    GBHF_CUDA(c, dA.alloc(np));
-    GBHF_CUDA(c, dB.alloc(np));
+    std::vector<int> ord0(np);
+    std::iota(ord0.begin(), ord0.end(), 0);
+    std::stable_sort(ord0.begin(), ord0.end(), [&](int x, int y) {
+      return pair_class(b.shells[A[x]].L, b.shells[B[x]].L) < pair_class(b.shells[A[y]].L, b.shells[B[y]].L);
+    });
+    int cs0[NPCLS + 1];
+    for (int cl = 0; cl <= NPCLS; ++cl) cs0[cl] = np;
+    std::vector<int> K0(np), off0(np);
+    size_t npp0 = 0;
+    for (int t = np - 1; t >= 0; --t)
+      cs0[pair_class(b.shells[A[ord0[t]]].L, b.shells[B[ord0[t]]].L)] = t;
+    for (int cl = NPCLS - 1; cl >= 0; --cl)
+      if (cs0[cl] == np) cs0[cl] = cs0[cl + 1];
+    for (int t = 0; t < np; ++t) {
+      K0[t] = b.shells[A[ord0[t]]].np * b.shells[B[ord0[t]]].np;
+      off0[t] = (int)npp0;
+      npp0 += K0[t];
+    }
+    std::vector<double> bra0((size_t)BRA_NFIELD * npp0), f(BRA_NFIELD * KMAX_PRIM_PAIRS);
+    for (int t = 0; t < np; ++t) {
+      pair_prims(b, A[ord0[t]], B[ord0[t]], f.data());
+      for (int k = 0; k < K0[t]; ++k)
+        for (int fl = 0; fl < BRA_NFIELD; ++fl) bra0[(size_t)fl * npp0 + off0[t] + k] = f[k * BRA_NFIELD + fl];
+    }
+    DBuf<int> dK, doff;
+    DBuf<double> dQ, dbra;
+    GBHF_CUDA(c, dK.alloc(np));
+    GBHF_CUDA(c, doff.alloc(np));
     GBHF_CUDA(c, dQ.alloc(np));
-    GBHF_CUDA(c, cudaMemcpyAsync(dA.p, A.data(), np * sizeof(int), cudaMemcpyHostToDevice, c->stream));
-    GBHF_CUDA(c, cudaMemcpyAsync(dB.p, B.data(), np * sizeof(int), cudaMemcpyHostToDevice, c->stream));
-    GBHF_TRY(schwarz_pairs_dev(c, dA.p, dB.p, np, dQ.p));
-    GBHF_CUDA(c, cudaMemcpy(Q.data(), dQ.p, np * sizeof(double), cudaMemcpyDeviceToHost));
+    GBHF_CUDA(c, dbra.alloc(bra0.size()));
+    GBHF_CUDA(c, cudaMemcpyAsync(dK.p, K0.data(), np * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    GBHF_CUDA(c, cudaMemcpyAsync(doff.p, off0.data(), np * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    GBHF_CUDA(c, cudaMemcpyAsync(dbra.p, bra0.data(), bra0.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    GBHF_TRY(schwarz_classes_dev(c, cs0, dK.p, doff.p, dbra.p, (long long)npp0, dQ.p));
+    std::vector<double> Q0(np);
+    GBHF_CUDA(c, cudaMemcpyAsync(Q0.data(), dQ.p, np * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
+    for (int t = 0; t < np; ++t) Q[ord0[t]] = Q0[t];
   }
   // 3. order: class, then primitive-pair count descending, then Q descending
   std::vector<int> order(np);
@@ -282,38 +338,20 @@ gbhf_status ensure_pairs(gbhf_ctx* c) {
   // 4. primitive-pair data
   const size_t npp = poff;
   std::vector<double> bra((size_t)BRA_NFIELD * npp), ket((size_t)BRA_NFIELD * npp);
+  std::vector<double> fbuf(BRA_NFIELD * KMAX_PRIM_PAIRS);
   for (int t = 0; t < np; ++t) {
-    const Shell &sa = b.shells[P.hA[t]], &sb = b.shells[P.hB[t]];
-    const double* RA = &b.xyz[3 * sa.atom];
-    const double* RB = &b.xyz[3 * sb.atom];
+    pair_prims(b, P.hA[t], P.hB[t], fbuf.data());
     const int4 sg = seginfo[P.hSeg[t]];
     const int seglen = sg.y - sg.x;
-    int k = 0;
-    for (int ia = 0; ia < sa.np; ++ia)
-      for (int ib = 0; ib < sb.np; ++ib, ++k) {
-        const double ea = sa.expo[ia], eb = sb.expo[ib];
-        const double p = ea + eb, mu = ea * eb / p;
-        double f[BRA_NFIELD];
-        double r2 = 0;
-        f[BRA_P] = p;
-        f[BRA_INVP] = 1.0 / p;
-        for (int x = 0; x < 3; ++x) {
-          const double Px = (ea * RA[x] + eb * RB[x]) / p;
-          f[BRA_PX + x] = Px;
-          f[BRA_PAX + x] = Px - RA[x];
-          f[BRA_PBX + x] = Px - RB[x];
-          r2 += (RA[x] - RB[x]) * (RA[x] - RB[x]);
-        }
-        // K' = sqrt(2 pi^(5/2)) c_a c_b exp(-mu |AB|^2) / p: the product of a bra and a
-        // ket K' times 1/sqrt(p+q) is the whole ERI prefactor
-        f[BRA_K] = std::sqrt(TWO_PI_2P5) * sa.coef[ia] * sb.coef[ib] * std::exp(-mu * r2) / p;
-        const size_t bidx = (size_t)P.hPoff[t] + k;
-        const size_t kidx = (size_t)sg.w + (size_t)k * seglen + (t - sg.x);
-        for (int fl = 0; fl < BRA_NFIELD; ++fl) {
-          bra[(size_t)fl * npp + bidx] = f[fl];
-          ket[(size_t)fl * npp + kidx] = f[fl];
-        }
+    for (int k = 0; k < P.hK[t]; ++k) {
+      const double* f = fbuf.data() + (size_t)k * BRA_NFIELD;
+      const size_t bidx = (size_t)P.hPoff[t] + k;
+      const size_t kidx = (size_t)sg.w + (size_t)k * seglen + (t - sg.x);
+      for (int fl = 0; fl < BRA_NFIELD; ++fl) {
+        bra[(size_t)fl * npp + bidx] = f[fl];
+        ket[(size_t)fl * npp + kidx] = f[fl];
       }
+    }
   }
   std::vector<float> bra32(bra.begin(), bra.end()), ket32(ket.begin(), ket.end());
   GBHF_CUDA(c, P.A.alloc(np));

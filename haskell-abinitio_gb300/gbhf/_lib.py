@@ -301,6 +301,47 @@ class Context:
         self._check(s)
         return out
 
+    def scf_batch(self, flats, opts=None, gradients=False):
+        """SCF of many molecules (list of FlatBasis) in one call; returns
+        (energies, iterations, converged, gradients or None)."""
+        opts = opts or baseline_opts()
+        ao, co = [0], [0]
+        xyz, z, catom, lx, npr, pc, pe = [], [], [], [], [], [], []
+        for fb in flats:
+            catom.append(np.asarray(fb.cgf_atom, np.int32) + ao[-1])
+            ao.append(ao[-1] + int(fb.n_atoms))
+            co.append(co[-1] + int(fb.n_cgf))
+            xyz.append(fb.xyz.ravel()); z.append(fb.charge); lx.append(fb.cgf_lxyz.ravel())
+            npr.append(fb.cgf_nprim); pc.append(fb.prim_coef); pe.append(fb.prim_exp)
+        arrs = [np.asarray(ao, np.int32), np.asarray(co, np.int32), _f64(np.concatenate(xyz)),
+                _f64(np.concatenate(z)), np.ascontiguousarray(np.concatenate(catom), np.int32),
+                np.ascontiguousarray(np.concatenate(lx), np.int32),
+                np.ascontiguousarray(np.concatenate(npr), np.int32), _f64(np.concatenate(pc)),
+                _f64(np.concatenate(pe))]
+        nm = len(flats)
+        e = np.zeros(nm)
+        it = np.zeros(nm, np.int32)
+        cv = np.zeros(nm, np.int32)
+        g = np.zeros(3 * ao[-1]) if gradients else None
+        s = self.L.gbhf_scf_batch(self.h, nm, _i(arrs[0]), _i(arrs[1]), _d(arrs[2]), _d(arrs[3]), _i(arrs[4]),
+                                  _i(arrs[5]), _i(arrs[6]), _d(arrs[7]), _d(arrs[8]), C.byref(opts), _d(e), _i(it),
+                                  _i(cv), _d(g) if gradients else None)
+        self._check(s)
+        grads = [g[3 * ao[k]:3 * ao[k + 1]].reshape(-1, 3) for k in range(nm)] if gradients else None
+        return e, it, cv.astype(bool), grads
+
+    def gradient(self, d_flat=None, w_flat=None, schwarz=1e-12, precision=PREC_FP64, n_atoms=None):
+        """dE/dR (n_atoms, 3) in hartree/bohr.  Without D and W: the last SCF's."""
+        na = n_atoms if n_atoms is not None else self._keep[1].size
+        g = np.zeros(3 * na)
+        if d_flat is None:
+            s = self.L.gbhf_gradient(self.h, precision, schwarz, None, None, _d(g))
+        else:
+            d, w = _f64(d_flat), _f64(w_flat)
+            s = self.L.gbhf_gradient(self.h, precision, schwarz, _d(d), _d(w), _d(g))
+        self._check(s)
+        return g.reshape(na, 3)
+
     # -- measurement ------------------------------------------------------
     def profile_reset(self, events=True):
         self._check(self.L.gbhf_profile_reset(self.h, 1 if events else 0))
