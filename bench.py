@@ -2,8 +2,9 @@
 
 Workload: (H2O)16 RHF/6-31G (208 basis functions, seeded geometry, EMSL
 basis), mixed FP32/FP64 direct SCF (FP32 for quartets with Schwarz bound
-below 1e-4, Schwarz cutoff 1e-12, incremental dD Fock builds, core guess,
-DIIS with 6 vectors, converged to dE < 1e-10 and RMS dD < 1e-8).  One step
+below 1e-4, Schwarz cutoff 1e-12, incremental dD Fock builds, superposition-
+of-atomic-densities guess, DIIS with 6 vectors, converged to dE < 1e-10 and
+RMS dD < 1e-8).  One step
 is one complete SCF of the molecule, including the screening setup, with the
 basis already on the device; the plain FP64 GPU SCF is run once beside it and
 both energies are reported.
@@ -132,7 +133,7 @@ def oracle_sample(fb, n_iter):
     core = ob.hcore(False)
     s = ob.overlap(False)
     x = O.symm_ortho(O.tri_to_square(s))
-    _, d, _ = O.diagonal_hf(core, x, fb.n_occupied)
+    d = O.sad_density(fb)
     t1 = time.perf_counter()
     f, st = ob.fock_direct(core, d, 1e-12)
     err = O.calc_error_mtx(f, s, d, x)
@@ -150,7 +151,7 @@ def run_reference(args, world, rank):
     from gbhf import basis as B, molecules as M
     fb = B.flatten(M.cluster_atoms("w16", "6-31g"))
     rec = json.loads((ROOT / "tests" / "golden" / "clusters.json").read_text()).get("w16_631g", {})
-    n_iter = int(rec.get("iterations", 17))
+    n_iter = int(rec.get("iterations_sad", rec.get("iterations", 17)))
     for _ in range(args.warmup):
         oracle_sample(fb, n_iter)
     times = []
@@ -194,7 +195,7 @@ def run_gbhf(args, world, rank, local):
     # plain FP64 GPU SCF, once (reported beside the headline)
     r64, t64 = step(fp64)
     barrier(world)
-    ctx.profile_reset(events=True)
+    ctx.profile_reset(events=False)
     times = []
     with ClockSampler(local) as clk:
         barrier(world)
@@ -204,7 +205,13 @@ def run_gbhf(args, world, rank, local):
             times.append(ms)
         barrier(world)
     prof = ctx.profile_read()
+    # per-class kernel times: one more SCF with an event around every J/K
+    # launch (the class launches then run one after another on one stream)
+    ctx.profile_reset(events=True)
+    ctx.flush_l2()
+    r_prof, ms_prof = step(mixed)
     cls = ctx.profile_classes()
+    prof_cls = ctx.profile_read()
     total_ms = max_over_ranks(world, sum(times))
     value = total_ms / 1e3 / (args.steps * world)
     # end to end: host basis in, every result matrix back to host memory
@@ -221,7 +228,7 @@ def run_gbhf(args, world, rank, local):
     e2e_v = max_over_ranks(world, sum(e2e_t)) / (args.steps * world)
     if rank != 0:
         return
-    # roofline of the dominant J/K kernel class
+    # roofline of the dominant J/K kernel class (profiling SCF)
     dom = max(cls.items(), key=lambda kv: kv[1]["ms"])
     (cname, prec), st = dom
     flops = st["prim_quartets"] * F_ALG[cname]
@@ -229,7 +236,7 @@ def run_gbhf(args, world, rank, local):
     peak64, peak32 = ctx.peak_flops(_lib.PREC_FP64), ctx.peak_flops(_lib.PREC_MIXED)
     peak = peak64 if prec == "fp64" else peak32
     prof_tr = traffic_profile().get(f"{cname}_{prec}")
-    jk_ms = prof["jk_ms_fp64"] + prof["jk_ms_fp32"]
+    jk_ms = prof_cls["jk_ms_fp64"] + prof_cls["jk_ms_fp32"]
     fnq_step = prof["fn_quartets"] / args.steps
     line = {
         "metric": METRIC, "value": value, "unit": "s/molecule", "n_gpus": world, "steps": args.steps,
@@ -248,12 +255,14 @@ def run_gbhf(args, world, rank, local):
         "eri_quartets_per_step": fnq_step,
         "eri_quartets_unscreened": (n * (n + 1) // 2) ** 2,
         "eri_fp32_fraction": r["eri_fp32_fraction"],
-        "jk_ms_per_step": jk_ms / args.steps,
+        "jk_ms_serialized_profiling_scf": jk_ms, "profiling_scf_ms": ms_prof,
         "phases_ms_per_step": {k: prof[k] / args.steps for k in ("ms_setup", "ms_fock", "ms_diis", "ms_diag",
                                                                   "ms_other")},
         "jacobi_sweeps_per_call": prof["jacobi_sweeps"] / max(prof["jacobi_calls"], 1),
         "gpu_launches": int(prof["launches"]),
         "roofline": {"kernel": f"k_jk<{cname}, {prec}>", "bound": f"{prec} CUDA-core pipe", "achieved": achieved,
+                     "timing": "CUDA events around each launch of this class in one profiling SCF run after "
+                               "the timed steps (class launches serialised on one stream)",
                      "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
                      "peak_source": f"FMA microbenchmark on this GPU (FP64 {peak64:.2f}, FP32 {peak32:.1f} TFLOP/s); "
                                     "MEASURED_PEAKS.json holds only HBM and bf16 tensor peaks",
@@ -274,17 +283,176 @@ def run_gbhf(args, world, rank, local):
     print(json.dumps(line), flush=True)
 
 
+def run_batch(args, world, rank, local):
+    """256 seeded conformers (H2O)_n, n in [1, 12], STO-3G (even) / 6-31G (odd):
+    mixed-precision SCF + analytic gradient for every molecule in batched calls,
+    versus one-at-a-time plain FP64 SCFs (timed on a sample and scaled)."""
+    import numpy as np
+    from gbhf import _lib, basis as B, molecules as M, replicas
+    ctx = _lib.Context(local)
+    mols = M.batch_workload()
+    flats = [B.flatten(a) for a in mols]
+    mine = replicas.shard([f.n_cgf ** 4 for f in flats], world, rank)
+    sub = [flats[i] for i in mine]
+    mixed = _lib.baseline_opts(precision=_lib.PREC_MIXED, incremental=1)
+    ctx.scf_batch(sub[:16], mixed, gradients=True)          # warm-up (worker pool, tables)
+    barrier(world)
+    ctx.event_record(0)
+    t0 = time.perf_counter()
+    e, it, cv, g = ctx.scf_batch(sub, mixed, gradients=True)
+    wall = time.perf_counter() - t0
+    wall = max_over_ranks(world, wall)
+    # one-at-a-time FP64 on every 8th molecule of this rank, scaled to the shard
+    fp64 = _lib.baseline_opts()
+    sample = list(range(0, len(sub), 8))
+    t_single, de = 0.0, []
+    for k in sample:
+        t1 = time.perf_counter()
+        ctx.set_basis(sub[k])
+        r = ctx.scf(fp64, want_matrices=False)
+        t_single += time.perf_counter() - t1
+        de.append(abs(r["energy"] - e[k]))
+    single_est = t_single * len(sub) / max(len(sample), 1)
+    if rank != 0:
+        return
+    n_total = len(flats)
+    line = {"workload": "batch256", "metric": "molecules/s (mixed SCF + analytic gradient, batched)",
+            "value": n_total / wall, "unit": "molecules/s", "n_gpus": world, "wall_s": wall,
+            "converged": int(cv.sum()) * world, "molecules": n_total,
+            "fp64_one_at_a_time_molecules_per_s": len(sub) / single_est if single_est > 0 else None,
+            "speedup_vs_fp64_one_at_a_time": single_est / wall * world if wall > 0 else None,
+            "max_abs_delta_e_mixed_vs_fp64_sample": float(max(de)) if de else None,
+            "sample": f"FP64 one-at-a-time timed on {len(sample)} of {len(sub)} molecules and scaled",
+            "data": "synthetic (256 seeded water conformers)", "dtype": "f32+f64", "higher_is_better": True}
+    print(json.dumps(line), flush=True)
+
+
+def run_gradient(args, world, rank, local):
+    """(H2O)8 RHF/6-31G analytic gradient: FP64 and mixed, checked against
+    central finite differences (1e-4 bohr) of the GPU SCF energy on all 72
+    Cartesian coordinates."""
+    import numpy as np
+    from gbhf import _lib, basis as B, molecules as M
+    ctx = _lib.Context(local)
+    xyz = M.cluster_coords("w8")
+    labels = M.water_labels(len(xyz) // 3)
+    tight = dict(conv_energy=1e-12, conv_density=1e-10, max_iter=200)
+
+    def setup(p):
+        ctx.set_basis(B.flatten(B.make_atoms(labels, p, "6-31g")))
+
+    setup(xyz)
+    ctx.scf(_lib.baseline_opts(**tight), want_matrices=False)
+    ctx.event_record(0)
+    r64 = ctx.scf(_lib.baseline_opts(**tight), want_matrices=False)
+    g64 = ctx.gradient()
+    ctx.event_record(1)
+    t64 = ctx.event_elapsed(0, 1)
+    ctx.event_record(2)
+    rmx = ctx.scf(_lib.baseline_opts(precision=_lib.PREC_MIXED, incremental=1, **tight), want_matrices=False)
+    gmx = ctx.gradient(precision=_lib.PREC_MIXED)
+    ctx.event_record(3)
+    tmx = ctx.event_elapsed(2, 3)
+    n_coords = len(xyz) * 3 if not args.quick else 6
+    fd_err = 0.0
+    h = 1e-4
+    for idx in range(n_coords):
+        a, x = divmod(idx, 3)
+        e = []
+        for s in (1, -1):
+            p = xyz.copy()
+            p[a, x] += s * h
+            setup(p)
+            e.append(ctx.scf(_lib.baseline_opts(**tight), want_matrices=False)["energy"])
+        fd = (e[0] - e[1]) / (2 * h)
+        fd_err = max(fd_err, abs(fd - g64[a, x]))
+    if rank != 0:
+        return
+    line = {"workload": "grad8", "metric": "analytic RHF/6-31G gradient of (H2O)8", "n_basis": 104,
+            "fp64_scf_plus_gradient_s": t64 / 1e3, "mixed_scf_plus_gradient_s": tmx / 1e3,
+            "max_abs_grad_fd_error": fd_err, "fd_coordinates": n_coords, "fd_step_bohr": h,
+            "max_abs_grad_mixed_vs_fp64": float(np.max(np.abs(gmx - g64))),
+            "translational_invariance": float(np.max(np.abs(g64.sum(axis=0)))),
+            "energy_fp64": r64["energy"], "energy_mixed": rmx["energy"], "unit": "hartree/bohr"}
+    print(json.dumps(line), flush=True)
+
+
+def run_large(args, world, rank, local):
+    """(H2O)64 RHF/6-31G (832 functions): mixed direct SCF with incremental
+    builds, then the analytic gradient; the plain FP64 GPU SCF beside it."""
+    from gbhf import _lib, basis as B, molecules as M
+    from gbhf.flops_model import F_ALG
+    ctx = _lib.Context(local)
+    fb = B.flatten(M.cluster_atoms("w64", "6-31g"))
+    ctx.set_basis(fb)
+    ctx.profile_reset(events=True)
+    ctx.event_record(0)
+    rmx = ctx.scf(_lib.baseline_opts(precision=_lib.PREC_MIXED, incremental=1), want_matrices=False)
+    ctx.event_record(1)
+    tmx = ctx.event_elapsed(0, 1)
+    prof = ctx.profile_read()
+    cls = ctx.profile_classes()
+    g = ctx.gradient()
+    ctx.event_record(2)
+    tg = ctx.event_elapsed(1, 2)
+    out = {"workload": "w64", "n_basis": fb.n_cgf, "mixed_scf_s": tmx / 1e3, "gradient_s": tg / 1e3,
+           "energy_mixed": rmx["energy"], "iterations": rmx["iterations"],
+           "eri_quartets_per_s": prof["fn_quartets"] / (tmx / 1e3),
+           "jk_ms": prof["jk_ms_fp64"] + prof["jk_ms_fp32"], "phases_ms": {k: prof[k] for k in (
+               "ms_setup", "ms_fock", "ms_diis", "ms_diag", "ms_other")},
+           "eri_quartets_unscreened": (fb.n_cgf * (fb.n_cgf + 1) // 2) ** 2,
+           "fp32_fraction": rmx["eri_fp32_fraction"],
+           "classes": {f"{k[0]}_{k[1]}": v for k, v in cls.items() if v["ms"] > 0}}
+    if not args.quick:
+        ctx.set_basis(fb)
+        ctx.event_record(3)
+        r64 = ctx.scf(_lib.baseline_opts(), want_matrices=False)
+        ctx.event_record(4)
+        out["fp64_scf_s"] = ctx.event_elapsed(3, 4) / 1e3
+        out["energy_fp64"] = r64["energy"]
+        out["delta_e_mixed_vs_fp64"] = rmx["energy"] - r64["energy"]
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+
+
+def run_fock_case(args, world, rank, local):
+    """Profiling case: one mixed-precision full direct Fock build of (H2O)16/6-31G
+    for a seeded symmetric density (every J/K class launched once per precision)."""
+    import numpy as np
+    from gbhf import _lib, basis as B, molecules as M
+    ctx = _lib.Context(local)
+    fb = B.flatten(M.cluster_atoms("w16", "6-31g"))
+    ctx.set_basis(fb)
+    n = fb.n_cgf
+    h = ctx.hcore(_lib.MODE_EXACT)
+    d = np.random.default_rng(2).standard_normal((n, n)) * 0.05
+    d = (d + d.T)[np.triu_indices(n)]
+    f = ctx.fock(h, d, _lib.MODE_EXACT, _lib.PREC_MIXED, 1e-12, 1e-4)
+    if rank == 0:
+        print(json.dumps({"workload": "fock", "n_basis": n, "checksum": float(np.abs(f).sum())}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gbhf", choices=["gbhf", "reference"])
+    ap.add_argument("--workload", default="w16", choices=["w16", "batch256", "grad8", "w64", "fock"])
+    ap.add_argument("--quick", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     world, rank, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, world, rank)
+    elif args.workload == "batch256":
+        run_batch(args, world, rank, local)
+    elif args.workload == "grad8":
+        run_gradient(args, world, rank, local)
+    elif args.workload == "w64":
+        run_large(args, world, rank, local)
+    elif args.workload == "fock":
+        run_fock_case(args, world, rank, local)
     else:
         run_gbhf(args, world, rank, local)
     if world > 1:

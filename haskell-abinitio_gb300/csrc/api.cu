@@ -74,6 +74,17 @@ gbhf_status gbhf_create(gbhf_ctx** out, int device) {
   for (auto& e : c->ev) cudaEventCreate(&e);
   for (auto& e : c->evc) cudaEventCreate(&e);
   for (auto& e : c->evu) cudaEventCreate(&e);
+  for (int i = 0; i < gbhf_ctx::NSIDE; ++i) {
+    if (cudaStreamCreateWithFlags(&c->side[i], cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->join_ev[i], cudaEventDisableTiming) != cudaSuccess) {
+      gbhf_destroy(c);
+      return GBHF_ERR_CUDA;
+    }
+  }
+  if (cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming) != cudaSuccess) {
+    gbhf_destroy(c);
+    return GBHF_ERR_CUDA;
+  }
   *out = c;
   return GBHF_OK;
 }
@@ -88,8 +99,18 @@ gbhf_status gbhf_destroy(gbhf_ctx* c) {
     if (e) cudaEventDestroy(e);
   for (auto& e : c->evu)
     if (e) cudaEventDestroy(e);
+  for (int i = 0; i < gbhf_ctx::NSIDE; ++i) {
+    if (c->side[i]) {
+      cudaStreamSynchronize(c->side[i]);
+      cudaStreamDestroy(c->side[i]);
+    }
+    if (c->join_ev[i]) cudaEventDestroy(c->join_ev[i]);
+  }
+  if (c->fork_ev) cudaEventDestroy(c->fork_ev);
   for (gbhf_ctx* w : c->pool) gbhf_destroy(w);
   c->pool.clear();
+  if (c->sad_ctx) gbhf_destroy(c->sad_ctx);
+  c->sad_ctx = nullptr;
   cudaSetDevice(c->device);
   cudaStream_t s = c->stream;
   delete c;   // frees device buffers
@@ -244,6 +265,21 @@ gbhf_status gbhf_eigen_solve(gbhf_ctx* c, int n, const double* a_square, double*
   return download(c, evecs, V, nn * sizeof(double));
 }
 
+gbhf_status gbhf_sad_density(gbhf_ctx* c, double* density_flat) {
+  CTX_CHECK(c);
+  if (!c->basis_dev) return fail(c, GBHF_ERR_BAD_INPUT, "no basis set");
+  if (!density_flat) return fail(c, GBHF_ERR_BAD_INPUT, "null output");
+  const int n = c->basis.nbf;
+  const size_t nn = (size_t)n * n, ntri = (size_t)n * (n + 1) / 2;
+  GBHF_WS(c, Dsq, 15, nn);
+  GBHF_WS(c, fD, 16, ntri);
+  GBHF_TRY(sad_density(c, Dsq));
+  GBHF_TRY(square_to_flat(c, n, Dsq, fD));
+  GBHF_TRY(download(c, density_flat, fD, ntri * sizeof(double)));
+  GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
+  return GBHF_OK;
+}
+
 gbhf_status gbhf_diagonal_hf(gbhf_ctx* c, int n, const double* f_flat, const double* x_square, int n_occupied,
                              double* coeff, double* density_flat, double* orb_energies) {
   CTX_CHECK(c);
@@ -375,7 +411,7 @@ void gbhf_scf_opts_baseline(gbhf_scf_opts* o) {
   std::memset(o, 0, sizeof(*o));
   o->mode = GBHF_MODE_EXACT;
   o->precision = GBHF_PREC_FP64;
-  o->guess = GBHF_GUESS_CORE;
+  o->guess = GBHF_GUESS_SAD;
   o->diis_size = 6;
   o->max_iter = 100;
   o->incremental = 0;

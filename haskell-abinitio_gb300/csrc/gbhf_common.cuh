@@ -27,9 +27,40 @@ enum {
 #define BRA_STRIDE 40   // >= max primitive pairs per shell pair (6 x 6 = 36)
 #define KMAX_PRIM_PAIRS 36
 
+// 1/sqrt(x) in FP64 with few FP64-pipe instructions (that pipe is 1/64 of the
+// FP32 rate on this GPU): x is truncated to single precision by moving its
+// exponent and top mantissa bits (integer ops), the single-precision estimate
+// rsqrtf (relative error ~2^-21 with the truncation) is widened the same way,
+// and one second-order Newton (Householder) step y (1 + e/2 + 3e^2/8),
+// e = 1 - x y^2, brings it to ~1 ulp (the neglected term is ~(5/16) e^3).
+// Valid for positive normal x with 2^-126 < x < 2^127 (every caller passes an
+// exponent sum or a Boys argument >= 20).
+__device__ __forceinline__ double rsqrt_d(double x) {
+  const int hi = __double2hiint(x);
+  const float xf = __int_as_float((hi - 0x38000000) << 3);
+  const int yb = __float_as_int(rsqrtf(xf));
+  const double y = __hiloint2double((yb >> 3) + 0x38000000, yb << 29);
+  const double e = fma(-x, y * y, 1.0);
+  return fma(y * e, fma(0.375, e, 0.5), y);
+}
+
 template <typename T> __device__ __forceinline__ T rsqrt_t(T x);
-template <> __device__ __forceinline__ double rsqrt_t<double>(double x) { return rsqrt(x); }
+template <> __device__ __forceinline__ double rsqrt_t<double>(double x) { return rsqrt_d(x); }
 template <> __device__ __forceinline__ float rsqrt_t<float>(float x) { return rsqrtf(x); }
+
+// Nearest integer j of x (0 <= x < 2^22), returned as j and as the exact
+// floating-point value of j: adding 1.5 * 2^52 (1.5 * 2^23 for float) leaves j in
+// the low mantissa bits of the sum, with no float<->int conversion instruction.
+__device__ __forceinline__ double round_node(double x, int& j) {
+  const double r = x + 6755399441055744.0;
+  j = __double2loint(r);
+  return r - 6755399441055744.0;
+}
+__device__ __forceinline__ float round_node(float x, int& j) {
+  const float r = x + 12582912.0f;
+  j = __float_as_int(r) - 0x4B400000;
+  return r - 12582912.0f;
+}
 
 template <typename T> __device__ __forceinline__ T fma_t(T a, T b, T c);
 template <> __device__ __forceinline__ double fma_t<double>(double a, double b, double c) { return fma(a, b, c); }
@@ -63,8 +94,9 @@ __device__ __forceinline__ void boys_eval(T t, const T* __restrict__ tab, T* F) 
   using C = BoysCfg<T, L>;
   static_assert(L <= BOYSH_LMAX, "Horner Boys table holds m <= BOYSH_LMAX");
   if (t < T(C::TMAX)) {
-    const int j = (int)(t * T(1.0 / C::H) + T(0.5));
-    const T dx = T(j) * T(C::H) - t;   // = -(t - T_j)
+    int j;
+    const T node = round_node(t * T(1.0 / C::H), j);
+    const T dx = node * T(C::H) - t;   // = -(t - T_j)
     const T* row = tab + j * BoysHStride<T>::S;
 #pragma unroll
     for (int m = 0; m <= L; ++m) {

@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <map>
 #include <string>
 #include <vector>
 
@@ -97,6 +98,8 @@ struct TaskLists {
   double thr_all = -1, thr64 = -1;     // thresholds the current lists were built for
   int hranges[4 * 6] = {0};            // host copy of ranges
   DBuf<int> f0;                        // first basis function per shell
+  DBuf<int> nc;                        // components per shell
+  DBuf<double> blk, row, pw, pb, sw;   // density weights (incremental builds)
   long f0_gen = -1;                    // basis generation f0 was uploaded for
 };
 
@@ -149,6 +152,9 @@ struct gbhf_ctx {
   long last_gen = -1;
   // worker contexts of gbhf_scf_batch (owned; destroyed with this context)
   std::vector<gbhf_ctx*> pool;
+  // SAD guess: atomic densities by atom key, and the context that computes them
+  std::map<std::string, std::vector<double>> sad_cache;
+  gbhf_ctx* sad_ctx = nullptr;
   gbhf::DBuf<float> dfloat;
   gbhf::DBuf<int> dev_status;
   gbhf::DBuf<unsigned> barrier;
@@ -157,6 +163,11 @@ struct gbhf_ctx {
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   cudaEvent_t evc[13] = {};      // per-class J/K launch boundaries (profiling)
   cudaEvent_t evu[8] = {};       // user slots (gbhf_event_record)
+  // side streams of the J/K build: the class kernels of one build run
+  // concurrently so that the tail of one persistent launch overlaps the next
+  static constexpr int NSIDE = 4;
+  cudaStream_t side[NSIDE] = {};
+  cudaEvent_t fork_ev = nullptr, join_ev[NSIDE] = {};
   gbhf::DBuf<unsigned char> flush;
 };
 
@@ -206,8 +217,10 @@ gbhf_status boys_ref_grid_dev(gbhf_ctx* c, double* d_grid);
 gbhf_status schwarz_pairs_dev(gbhf_ctx* c, const int* d_A, const int* d_B, int npairs, double* d_Q);
 // jk.cu
 // G_acc (n*n) += sym(G''(D)), D square n*n.  w = screening weight.
+// local_weights: screen and choose precision with per-pair |D| weights (D is a
+// density change); otherwise a uniform weight `weight`.
 gbhf_status jk_build(gbhf_ctx* c, const double* d_Dsq, double* d_G, int precision, double schwarz,
-                     double mixed_cutoff, double weight);
+                     double mixed_cutoff, double weight, bool local_weights = false);
 // Q of every pair in [cls_start[cl], cls_start[cl+1]) (pairs grouped by class,
 // bra-layout primitive data at d_poff), FP64 class code.
 gbhf_status schwarz_classes_dev(gbhf_ctx* c, const int* cls_start, const int* d_K, const int* d_poff,
@@ -231,6 +244,8 @@ gbhf_status diis_error_dev(gbhf_ctx* c, int n, const double* d_F, const double* 
 gbhf_status gauss_elem_dev_call(gbhf_ctx* c, int m, const double* h_a, const double* h_b, double* h_x, bool* ok);
 // scf.cu
 gbhf_status scf_run(gbhf_ctx* c, const gbhf_scf_opts* o, gbhf_result* r);
+// sad.cu: superposition-of-atomic-densities guess (n x n square, device)
+gbhf_status sad_density(gbhf_ctx* c, double* d_D);
 // grad.cu: D, W square on the device; gradient (3*natoms) on the device
 gbhf_status gradient_dev(gbhf_ctx* c, const double* d_D, const double* d_W, double schwarz, double* d_grad);
 gbhf_status energy_weighted_density(gbhf_ctx* c, int n, int nocc, const double* d_C, const double* d_eps,

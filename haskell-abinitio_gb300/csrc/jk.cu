@@ -111,6 +111,8 @@ __device__ __forceinline__ double warp_sum(double v) {
 
 constexpr int JK_THREADS = 128;
 constexpr int JK_WARPS = JK_THREADS / 32;
+// Upper bound on the primitive quartets one lane evaluates in one task.
+constexpr int JK_LANE_PRIMS = 256;
 
 template <int LA, int LB, int LC, int LD, typename T, bool SACC>
 __global__ void __launch_bounds__(JK_THREADS) k_jk(JKArgs<T> a) {
@@ -137,7 +139,8 @@ __global__ void __launch_bounds__(JK_THREADS) k_jk(JKArgs<T> a) {
     const int ib = task.x;
     const int jk = task.y + lane;
     const bool active = lane < task.z;
-    const int Kb = a.pK[ib], pb0 = a.poff[ib];
+    // bra primitives [kb0, kb1) of pair ib
+    const int kb0 = task.w & 0xffff, Kb = (task.w >> 16) - kb0, pb0 = a.poff[ib] + kb0;
     for (int idx = lane; idx < BRA_NFIELD * Kb; idx += 32) {
       const int f = idx / Kb, k = idx - f * Kb;
       sbra[warp][f * BRA_STRIDE + k] = a.bra[(long long)f * npp + pb0 + k];
@@ -176,7 +179,7 @@ __global__ void __launch_bounds__(JK_THREADS) k_jk(JKArgs<T> a) {
         ClassFn<LA, LB, LC, LD>::template run<T, AccT>(sbra[warp], Kb, q, invq, Qx, Qy, Qz, QCx, QCy, QCz, QDx,
                                                        QDy, QDz, Kcd, a.boys, acc);
       }
-      cnt_q += 1;
+      cnt_q += kb0 == 0;
       cnt_p += (unsigned long long)Kb * K;
     }
     // ---- scatter into G'' (FP64 atomics)
@@ -328,7 +331,10 @@ struct TaskGenArgs {
   const int* seg_cls_start;      // NPCLS+1
   const int4* seg;
   const double* Q;
+  const int* pK;                 // primitive pairs per shell pair
   double thr_all, thr64;         // cutoff / weight, mixed cutoff / weight
+  const double* pw;              // per-pair density weight (local mode) or nullptr
+  const double* sw;              // per-segment max of pw (local mode)
   int* count;                    // 2 per item
   const int* off64;              // exclusive scans (nitems + 1)
   const int* off32;
@@ -359,23 +365,35 @@ __global__ void k_tasks(TaskGenArgs g) {
   const double qi = g.Q[i];
   int n64 = 0, n32 = 0;
   int w64 = FILL ? g.off64[it] : 0, w32 = FILL ? g.off32[it] : 0;
+  const double wi = g.pw ? g.pw[i] : 1.0;
+  const int kb = g.pK[i];
   if (qi > 0) {
-    const double ta = g.thr_all / qi, t64 = g.thr64 / qi;
     for (int sidx = g.seg_cls_start[Y]; sidx < g.seg_cls_start[Y + 1]; ++sidx) {
       const int4 s = g.seg[sidx];
+      // bound of (bra|ket) contributions: Q_bra Q_ket max(w_bra, max w over the ket segment)
+      const double w = g.pw ? fmax(wi, g.sw[sidx]) : 1.0;
+      if (!(w > 0)) continue;
+      const double ta = g.thr_all / (qi * w), t64 = g.thr64 / (qi * w);
       int hi = s.y;
       if (X == Y && hi > i + 1) hi = i + 1;
       if (hi <= s.x) continue;
       const int keep = count_ge(g.Q, s.x, hi, ta);
       int k64 = count_ge(g.Q, s.x, s.x + keep, t64);
       const int k32 = keep - k64;
+      // split the bra primitives so that one lane handles at most
+      // ~JK_LANE_PRIMS primitive quartets per task (bounds the launch tail)
+      const int nch0 = min(kb, (kb * s.z + JK_LANE_PRIMS - 1) / JK_LANE_PRIMS);
+      const int cs = (kb + nch0 - 1) / nch0;
+      const int nch = (kb + cs - 1) / cs;
       if (FILL) {
-        for (int o = 0; o < k64; o += 32)
-          g.tasks64[w64++] = make_int4(i, s.x + o, min(32, k64 - o), 0);
-        for (int o = 0; o < k32; o += 32) g.tasks32[w32++] = make_int4(i, s.x + k64 + o, min(32, k32 - o), 0);
+        for (int ch = 0; ch < nch; ++ch) {
+          const int w = (ch * cs) | (min(kb, (ch + 1) * cs) << 16);
+          for (int o = 0; o < k64; o += 32) g.tasks64[w64++] = make_int4(i, s.x + o, min(32, k64 - o), w);
+          for (int o = 0; o < k32; o += 32) g.tasks32[w32++] = make_int4(i, s.x + k64 + o, min(32, k32 - o), w);
+        }
       } else {
-        n64 += (k64 + 31) / 32;
-        n32 += (k32 + 31) / 32;
+        n64 += nch * ((k64 + 31) / 32);
+        n32 += nch * ((k32 + 31) / 32);
       }
     }
   }
@@ -428,7 +446,79 @@ __global__ void k_ranges(const int* item_combo_start, const int* off64, const in
   ranges[4 * k + 3] = off32[item_combo_start[k + 1]];
 }
 
-static gbhf_status build_tasks(gbhf_ctx* c, double thr_all, double thr64, int* h_ranges) {
+// Density weights for incremental builds: per shell-pair block max |dD|, per
+// shell row max, per pair w = max(block, row A, row B), per ket segment the
+// max block weight of its pairs.
+__global__ void k_block_max(int ns, const int* __restrict__ f0, const int* __restrict__ nc,
+                            const double* __restrict__ D, int n, double* __restrict__ blk) {
+  const int A = blockIdx.y, B = blockIdx.x * blockDim.x + threadIdx.x;
+  if (B >= ns) return;
+  double m = 0;
+  for (int a = 0; a < nc[A]; ++a)
+    for (int b = 0; b < nc[B]; ++b) m = fmax(m, fabs(D[(long)(f0[A] + a) * n + f0[B] + b]));
+  blk[(long)A * ns + B] = m;
+}
+
+__global__ void k_row_max(int ns, const double* __restrict__ blk, double* __restrict__ row) {
+  const int A = blockIdx.x * blockDim.x + threadIdx.x;
+  if (A >= ns) return;
+  double m = 0;
+  for (int B = 0; B < ns; ++B) m = fmax(m, blk[(long)A * ns + B]);
+  row[A] = m;
+}
+
+// A quartet (AB|CD) feeds J_AB (dD_CD), J_CD (dD_AB) and K_AC, K_AD, K_BC, K_BD
+// (dD_BD, dD_BC, dD_AD, dD_AC); every exchange block holds a bra shell, so
+// max(pw[bra], pb[ket]) bounds all six density factors.
+__global__ void k_pair_weight(int np, int ns, const int* __restrict__ pA, const int* __restrict__ pB,
+                              const double* __restrict__ blk, const double* __restrict__ row, double* __restrict__ pw,
+                              double* __restrict__ pb) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= np) return;
+  const int A = pA[p], B = pB[p];
+  const double b = blk[(long)A * ns + B];
+  pw[p] = fmax(b, fmax(row[A], row[B]));
+  pb[p] = b;
+}
+
+__global__ void k_seg_max(int nseg, const int4* __restrict__ seg, const double* __restrict__ pw, double* __restrict__ sw) {
+  const int s = blockIdx.x;
+  if (s >= nseg) return;
+  const int4 g = seg[s];
+  double m = 0;
+  for (int p = g.x + threadIdx.x; p < g.y; p += blockDim.x) m = fmax(m, pw[p]);
+  __shared__ double sh[32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) m = fmax(m, sh[w]);
+    sw[s] = m;
+  }
+}
+
+static gbhf_status density_weights(gbhf_ctx* c, const double* d_dD) {
+  TaskLists& st = c->tasks;
+  PairData& P = c->pairs;
+  const int ns = (int)c->basis.shells.size(), n = c->basis.nbf;
+  GBHF_CUDA(c, st.blk.alloc((size_t)ns * ns));
+  GBHF_CUDA(c, st.row.alloc(ns));
+  GBHF_CUDA(c, st.pw.alloc(std::max(P.npairs, 1)));
+  GBHF_CUDA(c, st.pb.alloc(std::max(P.npairs, 1)));
+  GBHF_CUDA(c, st.sw.alloc(std::max(P.nseg_total, 1)));
+  k_block_max<<<dim3((ns + 127) / 128, ns), 128, 0, c->stream>>>(ns, st.f0.p, st.nc.p, d_dD, n, st.blk.p);
+  k_row_max<<<(ns + 127) / 128, 128, 0, c->stream>>>(ns, st.blk.p, st.row.p);
+  k_pair_weight<<<(P.npairs + 127) / 128, 128, 0, c->stream>>>(P.npairs, ns, P.A.p, P.B.p, st.blk.p, st.row.p,
+                                                               st.pw.p, st.pb.p);
+  if (P.nseg_total > 0) k_seg_max<<<P.nseg_total, 256, 0, c->stream>>>(P.nseg_total, P.seg_info.p, st.pb.p, st.sw.p);
+  count_launch(c, 4);
+  GBHF_CUDA(c, cudaGetLastError());
+  return GBHF_OK;
+}
+
+static gbhf_status build_tasks(gbhf_ctx* c, double thr_all, double thr64, int* h_ranges, const double* pw = nullptr,
+                               const double* sw = nullptr) {
   PairData& P = c->pairs;
   TaskLists& TL = c->tasks;
   std::vector<int> ics(NCOMBO + 1, 0);
@@ -460,8 +550,11 @@ static gbhf_status build_tasks(gbhf_ctx* c, double thr_all, double thr64, int* h
   g.seg_cls_start = d_scs.p;
   g.seg = P.seg_info.p;
   g.Q = P.Q.p;
+  g.pK = P.K.p;
   g.thr_all = thr_all;
   g.thr64 = thr64;
+  g.pw = pw;
+  g.sw = sw;
   g.count = TL.item_count.p;
   g.off64 = off64;
   g.off32 = off32;
@@ -494,8 +587,8 @@ static gbhf_status build_tasks(gbhf_ctx* c, double thr_all, double thr64, int* h
 }
 
 template <int LA, int LB, int LC, int LD, typename T, bool SACC>
-static gbhf_status launch_class(gbhf_ctx* c, int combo, int prec, const T* D, double* G, const T* bra, const T* ket,
-                                const T* boys, const int* f0, int ntask) {
+static gbhf_status launch_class(gbhf_ctx* c, cudaStream_t strm, int combo, int prec, const T* D, double* G,
+                                const T* bra, const T* ket, const T* boys, const int* f0, int ntask) {
   if (ntask <= 0) return GBHF_OK;
   constexpr int NOUT = ncart_c(LA) * ncart_c(LB) * ncart_c(LC) * ncart_c(LD);
   const size_t smem = SACC ? (size_t)NOUT * JK_THREADS * sizeof(double) : 0;
@@ -529,31 +622,46 @@ static gbhf_status launch_class(gbhf_ctx* c, int combo, int prec, const T* D, do
   a.G = G;
   a.boys = boys;
   a.stats = c->tasks.stats.p + 3 * (2 * combo + prec);
-  kern<<<grid, JK_THREADS, smem, c->stream>>>(a);
+  kern<<<grid, JK_THREADS, smem, strm>>>(a);
   count_launch(c);
   GBHF_CUDA(c, cudaGetLastError());
   return GBHF_OK;
 }
 
 gbhf_status jk_build(gbhf_ctx* c, const double* d_Dsq, double* d_G, int precision, double schwarz,
-                     double mixed_cutoff, double weight) {
+                     double mixed_cutoff, double weight, bool local_weights) {
   GBHF_TRY(ensure_pairs(c));
   const int n = c->basis.nbf;
   TaskLists& st = c->tasks;
   if (st.f0_gen != c->basis_gen) {
     st.f0_gen = c->basis_gen;
-    std::vector<int> f0(c->basis.shells.size());
-    for (size_t s = 0; s < f0.size(); ++s) f0[s] = c->basis.shells[s].f0;
+    std::vector<int> f0(c->basis.shells.size()), nc(c->basis.shells.size());
+    for (size_t s = 0; s < f0.size(); ++s) {
+      f0[s] = c->basis.shells[s].f0;
+      nc[s] = c->basis.shells[s].ncomp;
+    }
     GBHF_CUDA(c, st.f0.alloc(f0.size()));
+    GBHF_CUDA(c, st.nc.alloc(nc.size()));
     GBHF_CUDA(c, cudaMemcpyAsync(st.f0.p, f0.data(), f0.size() * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    GBHF_CUDA(c, cudaMemcpyAsync(st.nc.p, nc.data(), nc.size() * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
   }
-  if (!(weight > 0)) weight = 1e-300;
-  const double thr_all = schwarz / weight;
-  const double thr64 = precision == GBHF_PREC_FP64 ? 0.0 : mixed_cutoff / weight;
-  if (thr_all != st.thr_all || thr64 != st.thr64 || !c->tasks.tasks64.p) {
-    GBHF_TRY(build_tasks(c, thr_all, thr64, st.hranges));
-    st.thr_all = thr_all;
-    st.thr64 = thr64;
+  if (local_weights) {
+    // incremental build: bounds weighted by the local size of the density change
+    GBHF_TRY(density_weights(c, d_Dsq));
+    const double t64 = precision == GBHF_PREC_FP64 ? 0.0 : mixed_cutoff;
+    GBHF_TRY(build_tasks(c, schwarz, t64, st.hranges, st.pw.p, st.sw.p));
+    st.thr_all = -1;   // lists no longer match a uniform weight
+    st.thr64 = -1;
+  } else {
+    if (!(weight > 0)) weight = 1e-300;
+    const double thr_all = schwarz / weight;
+    const double thr64 = precision == GBHF_PREC_FP64 ? 0.0 : mixed_cutoff / weight;
+    if (thr_all != st.thr_all || thr64 != st.thr64 || !c->tasks.tasks64.p) {
+      GBHF_TRY(build_tasks(c, thr_all, thr64, st.hranges));
+      st.thr_all = thr_all;
+      st.thr64 = thr64;
+    }
   }
   GBHF_CUDA(c, cudaMemsetAsync(c->tasks.counters.p, 0, 2 * NCOMBO * sizeof(int), c->stream));
   GBHF_CUDA(c, cudaMemsetAsync(c->tasks.stats.p, 0, 6 * NCOMBO * sizeof(unsigned long long), c->stream));
@@ -571,11 +679,19 @@ gbhf_status jk_build(gbhf_ctx* c, const double* d_Dsq, double* d_G, int precisio
     nt[k][1] = st.hranges[4 * k + 3] - st.hranges[4 * k + 2];
   }
   const bool ev = c->prof.events;
-  // heaviest class first; FP64 lists, then FP32 lists
+  // heaviest class first; FP64 lists, then FP32 lists.  Without per-class
+  // profiling events the launches go round-robin to the side streams: each is a
+  // persistent grid that fills the GPU, and the next one takes over SMs as the
+  // tail of the previous one drains.  With profiling events they run in order
+  // on the context stream so that each launch is timed alone.
   static const int order[NCOMBO] = {5, 4, 3, 2, 1, 0};
-  int ne = 0;
+  int ne = 0, nl = 0;
   int ev_combo[12], ev_prec[12];
   if (ev) GBHF_CUDA(c, cudaEventRecord(c->evc[ne], c->stream));
+  else {
+    GBHF_CUDA(c, cudaEventRecord(c->fork_ev, c->stream));
+    for (int i = 0; i < gbhf_ctx::NSIDE; ++i) GBHF_CUDA(c, cudaStreamWaitEvent(c->side[i], c->fork_ev, 0));
+  }
   for (int prec = 0; prec < 2; ++prec) {
     if (prec == 1 && !any32) break;
     const double* D64 = d_Dsq;
@@ -584,23 +700,25 @@ gbhf_status jk_build(gbhf_ctx* c, const double* d_Dsq, double* d_G, int precisio
       const int k = order[oi];
       if (nt[k][prec] <= 0) continue;
       gbhf_status s = GBHF_OK;
+      cudaStream_t strm = ev ? c->stream : c->side[nl % gbhf_ctx::NSIDE];
+      ++nl;
       if (prec == 0) {
         switch (k) {
-          case 5: s = launch_class<1, 1, 1, 1, double, true>(c, 5, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boysh64.p, f0, nt[5][0]); break;
-          case 4: s = launch_class<1, 1, 1, 0, double, false>(c, 4, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boysh64.p, f0, nt[4][0]); break;
-          case 3: s = launch_class<1, 1, 0, 0, double, false>(c, 3, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boysh64.p, f0, nt[3][0]); break;
-          case 2: s = launch_class<1, 0, 1, 0, double, false>(c, 2, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boysh64.p, f0, nt[2][0]); break;
-          case 1: s = launch_class<1, 0, 0, 0, double, false>(c, 1, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boysh64.p, f0, nt[1][0]); break;
-          default: s = launch_class<0, 0, 0, 0, double, false>(c, 0, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boysh64.p, f0, nt[0][0]); break;
+          case 5: s = launch_class<1, 1, 1, 1, double, true>(c, strm, 5, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boysh64.p, f0, nt[5][0]); break;
+          case 4: s = launch_class<1, 1, 1, 0, double, false>(c, strm, 4, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boysh64.p, f0, nt[4][0]); break;
+          case 3: s = launch_class<1, 1, 0, 0, double, false>(c, strm, 3, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boysh64.p, f0, nt[3][0]); break;
+          case 2: s = launch_class<1, 0, 1, 0, double, false>(c, strm, 2, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boysh64.p, f0, nt[2][0]); break;
+          case 1: s = launch_class<1, 0, 0, 0, double, false>(c, strm, 1, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boysh64.p, f0, nt[1][0]); break;
+          default: s = launch_class<0, 0, 0, 0, double, false>(c, strm, 0, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boysh64.p, f0, nt[0][0]); break;
         }
       } else {
         switch (k) {
-          case 5: s = launch_class<1, 1, 1, 1, float, false>(c, 5, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boysh32.p, f0, nt[5][1]); break;
-          case 4: s = launch_class<1, 1, 1, 0, float, false>(c, 4, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boysh32.p, f0, nt[4][1]); break;
-          case 3: s = launch_class<1, 1, 0, 0, float, false>(c, 3, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boysh32.p, f0, nt[3][1]); break;
-          case 2: s = launch_class<1, 0, 1, 0, float, false>(c, 2, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boysh32.p, f0, nt[2][1]); break;
-          case 1: s = launch_class<1, 0, 0, 0, float, false>(c, 1, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boysh32.p, f0, nt[1][1]); break;
-          default: s = launch_class<0, 0, 0, 0, float, false>(c, 0, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boysh32.p, f0, nt[0][1]); break;
+          case 5: s = launch_class<1, 1, 1, 1, float, false>(c, strm, 5, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boysh32.p, f0, nt[5][1]); break;
+          case 4: s = launch_class<1, 1, 1, 0, float, false>(c, strm, 4, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boysh32.p, f0, nt[4][1]); break;
+          case 3: s = launch_class<1, 1, 0, 0, float, false>(c, strm, 3, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boysh32.p, f0, nt[3][1]); break;
+          case 2: s = launch_class<1, 0, 1, 0, float, false>(c, strm, 2, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boysh32.p, f0, nt[2][1]); break;
+          case 1: s = launch_class<1, 0, 0, 0, float, false>(c, strm, 1, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boysh32.p, f0, nt[1][1]); break;
+          default: s = launch_class<0, 0, 0, 0, float, false>(c, strm, 0, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boysh32.p, f0, nt[0][1]); break;
         }
       }
       if (s != GBHF_OK) return s;
@@ -610,6 +728,12 @@ gbhf_status jk_build(gbhf_ctx* c, const double* d_Dsq, double* d_G, int precisio
         ++ne;
         GBHF_CUDA(c, cudaEventRecord(c->evc[ne], c->stream));
       }
+    }
+  }
+  if (!ev) {
+    for (int i = 0; i < gbhf_ctx::NSIDE; ++i) {
+      GBHF_CUDA(c, cudaEventRecord(c->join_ev[i], c->side[i]));
+      GBHF_CUDA(c, cudaStreamWaitEvent(c->stream, c->join_ev[i], 0));
     }
   }
   // statistics

@@ -182,6 +182,8 @@ gbhf_status scf_run(gbhf_ctx* c, const gbhf_scf_opts* o, gbhf_result* r) {
     GBHF_TRY(flat_to_square(c, n, fD, Fd));
     GBHF_TRY(new_density(Fd, D));
     GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
+  } else if (o->guess == GBHF_GUESS_SAD) {
+    GBHF_TRY(sad_density(c, D));
   } else {
     GBHF_TRY(new_density(H, D));
   }
@@ -228,7 +230,8 @@ gbhf_status scf_run(gbhf_ctx* c, const gbhf_scf_opts* o, gbhf_result* r) {
         double w = 0;
         GBHF_TRY(max_abs(c, nn, Dnew, &w));
         if (w > 0) {
-          GBHF_TRY(jk_build(c, Dnew, Gpp, precision, o->schwarz_cutoff, o->mixed_cutoff, w));
+          // per-pair weights from the local size of dD (tighter than the global max)
+          GBHF_TRY(jk_build(c, Dnew, Gpp, precision, o->schwarz_cutoff, o->mixed_cutoff, w, true));
           GBHF_TRY(add_sym(c, n, Gacc, Gpp, Gacc));
         }
         ++since_full;

@@ -19,7 +19,7 @@ STATUS = {0: "GBHF_OK", 1: "GBHF_ERR_BAD_INPUT", 2: "GBHF_ERR_NOT_CONVERGED", 3:
           8: "GBHF_ERR_INDEX"}
 MODE_REFERENCE, MODE_EXACT = 0, 1
 PREC_FP64, PREC_MIXED = 0, 1
-GUESS_HARRIS, GUESS_CORE = 0, 1
+GUESS_HARRIS, GUESS_CORE, GUESS_SAD = 0, 1, 2
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
@@ -84,6 +84,7 @@ def load():
         "gbhf_eigen_solve": (st, [_vp, C.c_int, _dp, _dp, _dp]),
         "gbhf_eigen_solve_noalloc": (st, [C.c_int, _vp, _vp, _vp, _vp]),
         "gbhf_diagonal_hf": (st, [_vp, C.c_int, _dp, _dp, C.c_int, _dp, _dp, _dp]),
+        "gbhf_sad_density": (st, [_vp, _dp]),
         "gbhf_diis_error": (st, [_vp, C.c_int, _dp, _dp, _dp, _dp, _dp]),
         "gbhf_diis_extrapolate": (st, [_vp, C.c_int, C.c_int, _dp, _dp, _dp, _ip]),
         "gbhf_gauss_elem": (st, [_vp, C.c_int, _dp, _dp, _dp]),
@@ -255,6 +256,12 @@ class Context:
         c, d, e = np.zeros((n, n)), np.zeros(n * (n + 1) // 2), np.zeros(n)
         self._check(self.L.gbhf_diagonal_hf(self.h, n, _d(f), _d(x), int(n_occupied), _d(c), _d(d), _d(e)))
         return c, d, e
+
+    def sad_density(self):
+        """Superposition-of-atomic-densities starting density (flat upper triangle)."""
+        d = np.zeros(self.n * (self.n + 1) // 2)
+        self._check(self.L.gbhf_sad_density(self.h, _d(d)))
+        return d
 
     def diis_error(self, f_flat, s_flat, d_flat, x_square):
         x = _f64(x_square)

@@ -56,7 +56,11 @@ typedef enum {
                           DIIS and the eigen-solve always FP64 */
 } gbhf_precision;
 
-typedef enum { GBHF_GUESS_HARRIS = 0, GBHF_GUESS_CORE = 1 } gbhf_guess;
+/* GBHF_GUESS_SAD (superposition of atomic densities: block-diagonal densities of
+ * spherically averaged free atoms) has no counterpart in the reference, which
+ * offers the Harris functional and the core Hamiltonian
+ * (HartreeFock/HartreeFock.hs:128-149). */
+typedef enum { GBHF_GUESS_HARRIS = 0, GBHF_GUESS_CORE = 1, GBHF_GUESS_SAD = 2 } gbhf_guess;
 
 /* SCF options.  gbhf_scf_opts_reference() fills the reference's constants
  * (HartreeFock.hs:78,81,87,113; DIIS.hs:58). */
@@ -170,6 +174,12 @@ gbhf_status gbhf_eigen_solve(gbhf_ctx* ctx, int n, const double* a_square, doubl
  * streams) race: serialise them. */
 #define GBHF_NOALLOC_EIGEN_MAX_N 256
 gbhf_status gbhf_eigen_solve_noalloc(int n, const double* d_a, double* d_evals, double* d_evecs, void* stream);
+
+/* Superposition-of-atomic-densities starting density of the context's basis
+ * (flat upper triangle, N(N+1)/2).  No counterpart in the reference (its guesses
+ * are harrisFunctional and the core Hamiltonian, HartreeFock/HartreeFock.hs:
+ * 128-149); it is the starting density of gbhf_scf with GBHF_GUESS_SAD. */
+gbhf_status gbhf_sad_density(gbhf_ctx* ctx, double* density_flat);
 
 /* diagonalHF (HartreeFock/HartreeFock.hs:263-273): X^T F X, eigen-solve,
  * C = X C', density P = 2 C_occ C_occ^T (calcDensity, :195-208). */

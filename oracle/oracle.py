@@ -14,6 +14,8 @@ below restates, step by step, the reference's Haskell driver:
 * ``diagonal_hf``       HartreeFock/HartreeFock.hs:263-273
 * ``variational_e``     HartreeFock/HartreeFock.hs:277-287
 * ``nuclear_rep``       HartreeFock/HartreeFock.hs:300-305
+* ``sad_density``       no reference counterpart: the superposition-of-atomic-
+                         densities guess of the library (restated for checking)
 * ``calc_error_mtx``, ``diis_driver``, ``diis``, ``update_diis``
                          HartreeFock/DIIS.hs:55-140
 * ``gauss_elem``        NumericalTools/GaussElimination.hs:42-98
@@ -435,10 +437,77 @@ def harris_guess_terms(eri, n_tri, occupied):
 
 # -------------------------------------------------------------- SCF driver ----
 
+def _atom_sub_basis(fb, a):
+    """Functions of atom ``a`` as a one-atom basis at the origin, with their indices."""
+    idx = np.where(fb.cgf_atom == a)[0]
+    off = np.concatenate([[0], np.cumsum(fb.cgf_nprim)])
+    coef = np.concatenate([fb.prim_coef[off[i]:off[i + 1]] for i in idx])
+    expo = np.concatenate([fb.prim_exp[off[i]:off[i + 1]] for i in idx])
+    sub = type(fb)(1, np.zeros((1, 3)), fb.charge[a:a + 1].astype(np.float64), len(idx),
+                   np.zeros(len(idx), np.int32), np.ascontiguousarray(fb.cgf_lxyz[idx], dtype=np.int32),
+                   np.ascontiguousarray(fb.cgf_nprim[idx], dtype=np.int32), coef, expo)
+    return sub, idx
+
+
+def fractional_occupations(eps, nel, tol=1e-5):
+    """Aufbau with 2 electrons per orbital; a partly filled set of orbitals
+    whose energies agree to ``tol`` shares its electrons equally."""
+    occ = np.zeros(len(eps))
+    left, i = float(nel), 0
+    while left > 1e-12 and i < len(eps):
+        j = i
+        while j + 1 < len(eps) and abs(eps[j + 1] - eps[i]) < tol:
+            j += 1
+        take = min(left, 2.0 * (j - i + 1))
+        occ[i:j + 1] = take / (j - i + 1)
+        left -= take
+        i = j + 1
+    return occ
+
+
+def atomic_density(fb1, max_iter=200):
+    """Spherically averaged fractional-occupation RHF density of one neutral
+    atom (square, in its own functions): Roothaan steps from the core
+    Hamiltonian, the first four averaged with the previous density, until
+    max|dD| < 1e-10."""
+    ob = OracleBasis(fb1)
+    h, s, eri = ob.hcore(False), ob.overlap(False), ob.eri_canonical(False)
+    x = symm_ortho(tri_to_square(s))
+    nel = float(fb1.charge.sum())
+    f, d = tri_to_square(h), None
+    for it in range(max_iter):
+        eps, cp = np.linalg.eigh(x.T @ f @ x)
+        c = x @ cp
+        dn = (c * fractional_occupations(eps, nel)) @ c.T
+        change = 1.0 if d is None else float(np.max(np.abs(dn - d)))
+        d = dn if (d is None or it >= 4) else 0.5 * (dn + d)
+        if change < 1e-10:
+            break
+        f = tri_to_square(fock_canonical(h, square_to_tri(d), eri))
+    return d
+
+
+def sad_density(fb):
+    """Superposition of atomic densities (flat upper triangle): block-diagonal
+    assembly of ``atomic_density`` for every atom, computed once per distinct
+    atom (charge and functions)."""
+    n = int(fb.n_cgf)
+    dens = np.zeros((n, n))
+    cache = {}
+    for a in range(int(fb.n_atoms)):
+        sub, idx = _atom_sub_basis(fb, a)
+        key = (float(sub.charge[0]), sub.cgf_lxyz.tobytes(), sub.cgf_nprim.tobytes(), sub.prim_coef.tobytes(),
+               sub.prim_exp.tobytes())
+        if key not in cache:
+            cache[key] = atomic_density(sub)
+        dens[np.ix_(idx, idx)] = cache[key]
+    return square_to_tri(dens)
+
+
 @dataclass
 class SCFOptions:
     ref_compat: bool = True        # reference numerics + reference driver rules
-    guess: str = "harris"          # "harris" | "core"
+    guess: str = "harris"          # "harris" | "core" | "sad"
     diis_size: int = 5             # vectors in the extrapolation (current + stored)
     max_iter: int = 30
     conv_error: float = 1e-7       # max|e| (reference rule, used when ref_compat)
@@ -503,6 +572,8 @@ def scf(fb, opts: Optional[SCFOptions] = None, grid=None):
             eri = ob.eri_canonical(ref)
         g = harris_guess_terms(eri, len(core), occupied)
         _, density, _ = diagonal_hf(core + g, x, occupied)
+    elif opts.guess == "sad":
+        density = sad_density(fb)
     else:
         _, density, _ = diagonal_hf(core, x, occupied)
     dat = DataDIIS(size=opts.diis_size)

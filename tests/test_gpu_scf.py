@@ -105,3 +105,24 @@ def test_not_converged_raises(ctx):
     ctx.generate_boys_grid()
     with pytest.raises(_lib.NotConverged):
         ctx.scf(_lib.reference_opts(max_iter=2))
+
+
+@pytest.mark.parametrize("basis,index", [("6-31g", 7), ("sto-3g", 20), ("sto-3g", 154)])
+def test_sad_density_matches_oracle(ctx, basis, index):
+    fb = B.flatten(M.cluster_atoms("batch256", basis, index=index))
+    ctx.set_basis(fb)
+    np.testing.assert_allclose(ctx.sad_density(), O.sad_density(fb), rtol=0, atol=1e-9)
+
+
+def test_sad_guess_converges_where_core_guess_does_not(ctx):
+    """Conformer 154 of the 256-molecule set, (H2O)7/STO-3G: the core guess with
+    DIIS from the first step oscillates past 100 steps (oracle and library
+    alike); the SAD guess converges to the oracle's energy."""
+    fb = B.flatten(M.cluster_atoms("batch256", "sto-3g", index=154))
+    ctx.set_basis(fb)
+    with pytest.raises(_lib.NotConverged):
+        ctx.scf(_lib.baseline_opts(guess=_lib.GUESS_CORE), want_matrices=False)
+    r = ctx.scf(_lib.baseline_opts(), want_matrices=False)
+    o = O.scf(fb, O.SCFOptions.baseline(guess="sad"))
+    assert r["converged"] and abs(r["energy"] - o.energy) < 1e-8
+    assert r["iterations"] <= 15
