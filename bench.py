@@ -392,10 +392,14 @@ def run_large(args, world, rank, local):
     tmx = ctx.event_elapsed(0, 1)
     prof = ctx.profile_read()
     cls = ctx.profile_classes()
-    g = ctx.gradient()
+    gmx = ctx.gradient(precision=_lib.PREC_MIXED)
     ctx.event_record(2)
     tg = ctx.event_elapsed(1, 2)
-    out = {"workload": "w64", "n_basis": fb.n_cgf, "mixed_scf_s": tmx / 1e3, "gradient_s": tg / 1e3,
+    g64 = ctx.gradient()
+    ctx.event_record(5)
+    tg64 = ctx.event_elapsed(2, 5)
+    out = {"workload": "w64", "n_basis": fb.n_cgf, "mixed_scf_s": tmx / 1e3, "gradient_mixed_s": tg / 1e3,
+           "gradient_fp64_s": tg64 / 1e3, "max_abs_grad_mixed_vs_fp64": float(abs(gmx - g64).max()),
            "energy_mixed": rmx["energy"], "iterations": rmx["iterations"],
            "eri_quartets_per_s": prof["fn_quartets"] / (tmx / 1e3),
            "jk_ms": prof["jk_ms_fp64"] + prof["jk_ms_fp32"], "phases_ms": {k: prof[k] for k in (

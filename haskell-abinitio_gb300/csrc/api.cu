@@ -18,6 +18,7 @@ gbhf_status check_ctx(gbhf_ctx* c) {
 }
 
 #define CTX_CHECK(c)                            \
+  gbhf::PoolScope pool_scope__(c);              \
   do {                                          \
     if (!(c)) return GBHF_ERR_BAD_INPUT;        \
     gbhf_status s0__ = check_ctx(c);            \
@@ -436,7 +437,8 @@ gbhf_status gbhf_scf(gbhf_ctx* c, const gbhf_scf_opts* opts, gbhf_result* result
 gbhf_status gbhf_gradient(gbhf_ctx* c, int precision, double schwarz_cutoff, const double* d_flat,
                           const double* w_flat, double* grad) {
   CTX_CHECK(c);
-  (void)precision;   // derivative integrals are evaluated in FP64 for either precision
+  if (precision != GBHF_PREC_FP64 && precision != GBHF_PREC_MIXED)
+    return fail(c, GBHF_ERR_BAD_INPUT, "precision must be GBHF_PREC_FP64 or GBHF_PREC_MIXED");
   if (!need_basis(c)) return GBHF_ERR_BAD_INPUT;
   if (!grad || !(schwarz_cutoff >= 0)) return fail(c, GBHF_ERR_BAD_INPUT, "bad arguments");
   if ((d_flat == nullptr) != (w_flat == nullptr))
@@ -472,7 +474,9 @@ gbhf_status gbhf_gradient(gbhf_ctx* c, int precision, double schwarz_cutoff, con
   }
   DBuf<double> g;
   GBHF_CUDA(c, g.alloc(3 * (size_t)na));
-  GBHF_TRY(gradient_dev(c, D, W, schwarz_cutoff, g.p));
+  // mixed precision: FP32 derivative integrals for quartets whose bound
+  // Q_ab Q_cd max(w)^2 is below 1e-4, the SCF's mixed cutoff
+  GBHF_TRY(gradient_dev(c, D, W, schwarz_cutoff, 1e-4, precision, g.p));
   return download(c, grad, g.p, 3 * (size_t)na * sizeof(double));
 }
 

@@ -22,6 +22,7 @@ extern "C" gbhf_status gbhf_scf_batch(gbhf_ctx* c, int n_mol, const int* atom_of
                                       int* iterations, int* converged, double* grads) {
   using namespace gbhf;
   if (!c) return GBHF_ERR_BAD_INPUT;
+  PoolScope pool_scope(c);
   if (cudaSetDevice(c->device) != cudaSuccess) return fail(c, GBHF_ERR_CUDA, "cudaSetDevice");
   c->err.clear();
   if (n_mol < 0 || (n_mol > 0 && (!atom_off || !cgf_off || !xyz_bohr || !charges || !cgf_atom || !cgf_lxyz ||

@@ -22,8 +22,14 @@
 // Bra primitive-pair fields (shared-memory staging and global SoA layout).
 enum {
   BRA_P = 0, BRA_INVP, BRA_PX, BRA_PY, BRA_PZ, BRA_PAX, BRA_PAY, BRA_PAZ,
-  BRA_PBX, BRA_PBY, BRA_PBZ, BRA_K, BRA_NFIELD
+  BRA_PBX, BRA_PBY, BRA_PBZ, BRA_K, BRA_AEXP, BRA_NFIELD
 };
+// Cartesian components of a shell of angular momentum L.
+constexpr int ncart_c(int L) { return (L + 1) * (L + 2) / 2; }
+
+// The J/K kernels stage the first BRA_NJK fields; BRA_AEXP (the exponent of
+// the pair's first primitive) is read by the gradient kernels only.
+#define BRA_NJK BRA_AEXP
 #define BRA_STRIDE 40   // >= max primitive pairs per shell pair (6 x 6 = 36)
 #define KMAX_PRIM_PAIRS 36
 
@@ -79,12 +85,17 @@ template <int L> struct BoysCfg<float, L> {
   static constexpr int NT = BOYS32_NTERM;
 };
 
-// Horner form used by the J/K kernels: row j holds, for m = 0..BOYSH_LMAX and
-// k = 0..NT-1, G[m*NT + k] = F_(m+k)(T_j) / k!, so that
-// F_m(t) = sum_k G[m*NT+k] (T_j - t)^k costs NT-1 FMAs per m.
-#define BOYSH_LMAX 4
-#define BOYSH64_STRIDE 36   // (BOYSH_LMAX+1) * 7 = 35, padded
-#define BOYSH32_STRIDE 28   // (BOYSH_LMAX+1) * 5 = 25, padded
+// Horner form used by the J/K and gradient kernels: row j holds, for
+// m = 0..BOYSH_LMAX and k = 0..NT-1, G[m*NT + k] = F_(m+k)(T_j) / k!, so that
+// F_m(t) = sum_k G[m*NT+k] (T_j - t)^k costs NT-1 FMAs per m, and in row
+// BOYSH_EXPROW the same expansion of exp(-t), G[k] = exp(-T_j) / k!.  For
+// orders L >= 2 only F_L and exp(-t) are expanded and the lower orders follow
+// by the downward recursion F_m = (2t F_(m+1) + exp(-t)) / (2m + 1), whose
+// terms are all positive.
+#define BOYSH_LMAX 5
+#define BOYSH_EXPROW (BOYSH_LMAX + 1)
+#define BOYSH64_STRIDE 50   // (BOYSH_LMAX+2) * 7 = 49, padded to 16 bytes
+#define BOYSH32_STRIDE 36   // (BOYSH_LMAX+2) * 5 = 35, padded
 template <typename T> struct BoysHStride;
 template <> struct BoysHStride<double> { static constexpr int S = BOYSH64_STRIDE; };
 template <> struct BoysHStride<float> { static constexpr int S = BOYSH32_STRIDE; };
@@ -98,12 +109,26 @@ __device__ __forceinline__ void boys_eval(T t, const T* __restrict__ tab, T* F) 
     const T node = round_node(t * T(1.0 / C::H), j);
     const T dx = node * T(C::H) - t;   // = -(t - T_j)
     const T* row = tab + j * BoysHStride<T>::S;
+    if constexpr (L <= 1) {
 #pragma unroll
-    for (int m = 0; m <= L; ++m) {
-      T s = __ldg(row + m * C::NT + C::NT - 1);
+      for (int m = 0; m <= L; ++m) {
+        T s = __ldg(row + m * C::NT + C::NT - 1);
 #pragma unroll
-      for (int k = C::NT - 2; k >= 0; --k) s = fma_t(s, dx, __ldg(row + m * C::NT + k));
-      F[m] = s;
+        for (int k = C::NT - 2; k >= 0; --k) s = fma_t(s, dx, __ldg(row + m * C::NT + k));
+        F[m] = s;
+      }
+    } else {
+      T s = __ldg(row + L * C::NT + C::NT - 1);
+      T e = __ldg(row + BOYSH_EXPROW * C::NT + C::NT - 1);
+#pragma unroll
+      for (int k = C::NT - 2; k >= 0; --k) {
+        s = fma_t(s, dx, __ldg(row + L * C::NT + k));
+        e = fma_t(e, dx, __ldg(row + BOYSH_EXPROW * C::NT + k));
+      }
+      F[L] = s;
+      const T t2 = t + t;
+#pragma unroll
+      for (int m = L - 1; m >= 0; --m) F[m] = fma_t(t2, F[m + 1], e) * T(1.0 / (2 * m + 1));
     }
   } else {
     const T r = rsqrt_t(t);

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <map>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -11,24 +12,110 @@
 
 namespace gbhf {
 
-// Device buffer with RAII free (no copies).
+// Per-context cache of device blocks.  cudaFree waits for the whole device,
+// so a buffer released by one context (one stream) would stall every other
+// context's work; instead released blocks go back to the pool of the context
+// that allocated them and are handed out again to later allocations of the
+// same context, whose work is ordered on the same stream.  Block sizes are
+// rounded up to 256 bytes and then to four steps per power of two.  The
+// blocks are freed when the context is destroyed (and all free blocks when an
+// allocation fails).
+struct DevPool {
+  std::map<size_t, std::vector<void*>> free_blocks;
+  std::vector<void*> all_blocks;
+  std::mutex mu;
+  static size_t round_size(size_t b) {
+    b = (b + 255) & ~(size_t)255;
+    size_t hi = 256;
+    while (hi < b) hi <<= 1;
+    if (hi <= 1024) return hi;
+    const size_t step = hi >> 3;   // hi/2 < b <= hi: steps of hi/8
+    return (b + step - 1) / step * step;
+  }
+  cudaError_t get(size_t bytes, void** out) {
+    {
+      std::lock_guard<std::mutex> lock(mu);
+      auto it = free_blocks.find(bytes);
+      if (it != free_blocks.end() && !it->second.empty()) {
+        *out = it->second.back();
+        it->second.pop_back();
+        return cudaSuccess;
+      }
+    }
+    cudaError_t e = cudaMalloc(out, bytes);
+    if (e == cudaErrorMemoryAllocation) {
+      (void)cudaGetLastError();
+      trim();
+      e = cudaMalloc(out, bytes);
+    }
+    if (e == cudaSuccess) {
+      std::lock_guard<std::mutex> lock(mu);
+      all_blocks.push_back(*out);
+    }
+    return e;
+  }
+  void put(void* p, size_t bytes) {
+    std::lock_guard<std::mutex> lock(mu);
+    free_blocks[bytes].push_back(p);
+  }
+  void trim() {
+    std::lock_guard<std::mutex> lock(mu);
+    for (auto& kv : free_blocks)
+      for (void* p : kv.second) {
+        cudaFree(p);
+        for (auto& q : all_blocks)
+          if (q == p) q = nullptr;
+      }
+    free_blocks.clear();
+  }
+  ~DevPool() {
+    for (void* p : all_blocks)
+      if (p) cudaFree(p);
+  }
+};
+
+// Pool used by allocations on this thread: set by every entry point for the
+// context it works on (PoolScope), null outside the library.
+extern thread_local DevPool* tls_pool;
+
+// Device buffer with RAII release (no copies); grows, never shrinks.
 template <typename T>
 struct DBuf {
   T* p = nullptr;
   size_t n = 0;
+  size_t bytes = 0;
+  DevPool* owner = nullptr;
   DBuf() = default;
   DBuf(const DBuf&) = delete;
   DBuf& operator=(const DBuf&) = delete;
   ~DBuf() { release(); }
   void release() {
-    if (p) cudaFree(p);
+    if (p) {
+      if (owner) owner->put(p, bytes);
+      else cudaFree(p);
+    }
     p = nullptr;
     n = 0;
+    bytes = 0;
+    owner = nullptr;
   }
   cudaError_t alloc(size_t count) {
     if (count <= n && p) return cudaSuccess;
     release();
     if (count == 0) count = 1;
+    DevPool* pool = tls_pool;
+    if (pool) {
+      const size_t b = DevPool::round_size(count * sizeof(T));
+      void* q = nullptr;
+      cudaError_t e = pool->get(b, &q);
+      if (e == cudaSuccess) {
+        p = static_cast<T*>(q);
+        n = b / sizeof(T);
+        bytes = b;
+        owner = pool;
+      }
+      return e;
+    }
     cudaError_t e = cudaMalloc(&p, count * sizeof(T));
     if (e == cudaSuccess) n = count;
     return e;
@@ -44,6 +131,7 @@ struct Shell {
 constexpr int NPCLS = 3;
 // Quartet combos (bra class >= ket class).
 constexpr int NCOMBO = 6;
+constexpr int NCOMBO_MAX = 9;   // all (bra class, ket class) combinations (gradient lists)
 constexpr int COMBO_BRA[NCOMBO] = {0, 1, 1, 2, 2, 2};
 constexpr int COMBO_KET[NCOMBO] = {0, 0, 1, 0, 1, 2};
 
@@ -96,9 +184,11 @@ struct TaskLists {
   int nitems = 0;
   std::vector<int> combo_item_start;   // host: first item of each combo
   double thr_all = -1, thr64 = -1;     // thresholds the current lists were built for
-  int hranges[4 * 6] = {0};            // host copy of ranges
+  int ncombo = 0;
+  int hranges[4 * NCOMBO_MAX] = {0};   // host copy of ranges
   DBuf<int> f0;                        // first basis function per shell
   DBuf<int> nc;                        // components per shell
+  DBuf<int> atom;                      // atom of each shell
   DBuf<double> blk, row, pw, pb, sw;   // density weights (incremental builds)
   long f0_gen = -1;                    // basis generation f0 was uploaded for
 };
@@ -124,6 +214,7 @@ struct Profile {
 }  // namespace gbhf
 
 struct gbhf_ctx {
+  gbhf::DevPool devpool;         // first member: destroyed after every buffer below
   int device = 0;
   int nsm = 0;
   cudaStream_t stream = nullptr;
@@ -143,6 +234,7 @@ struct gbhf_ctx {
   gbhf::PairData pairs;
   bool pairs_ready = false;
   gbhf::TaskLists tasks;
+  gbhf::TaskLists gtasks;        // gradient task lists
   // dense work buffers (n*n doubles)
   gbhf::DBuf<double> w[24];
   gbhf::JacobiWork jac;
@@ -172,6 +264,15 @@ struct gbhf_ctx {
 };
 
 namespace gbhf {
+
+// Makes `c`'s pool the allocation pool of this thread for the scope.
+struct PoolScope {
+  DevPool* prev;
+  explicit PoolScope(gbhf_ctx* c) : prev(tls_pool) {
+    if (c) tls_pool = &c->devpool;
+  }
+  ~PoolScope() { tls_pool = prev; }
+};
 
 // error helpers
 gbhf_status fail(gbhf_ctx* c, gbhf_status s, const std::string& msg);
@@ -219,6 +320,8 @@ gbhf_status schwarz_pairs_dev(gbhf_ctx* c, const int* d_A, const int* d_B, int n
 // G_acc (n*n) += sym(G''(D)), D square n*n.  w = screening weight.
 // local_weights: screen and choose precision with per-pair |D| weights (D is a
 // density change); otherwise a uniform weight `weight`.
+gbhf_status ensure_shell_arrays(gbhf_ctx* c);
+gbhf_status build_grad_tasks(gbhf_ctx* c, const double* d_D, double cutoff, double mixed_cutoff, int precision);
 gbhf_status jk_build(gbhf_ctx* c, const double* d_Dsq, double* d_G, int precision, double schwarz,
                      double mixed_cutoff, double weight, bool local_weights = false);
 // Q of every pair in [cls_start[cl], cls_start[cl+1]) (pairs grouped by class,
@@ -247,7 +350,8 @@ gbhf_status scf_run(gbhf_ctx* c, const gbhf_scf_opts* o, gbhf_result* r);
 // sad.cu: superposition-of-atomic-densities guess (n x n square, device)
 gbhf_status sad_density(gbhf_ctx* c, double* d_D);
 // grad.cu: D, W square on the device; gradient (3*natoms) on the device
-gbhf_status gradient_dev(gbhf_ctx* c, const double* d_D, const double* d_W, double schwarz, double* d_grad);
+gbhf_status gradient_dev(gbhf_ctx* c, const double* d_D, const double* d_W, double schwarz, double mixed_cutoff,
+                         int precision, double* d_grad);
 gbhf_status energy_weighted_density(gbhf_ctx* c, int n, int nocc, const double* d_C, const double* d_eps,
                                     double* d_W);
 gbhf_status dot_matrices(gbhf_ctx* c, int n2, int k, const double* const* mats, const double* d_e,

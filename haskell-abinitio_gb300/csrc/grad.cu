@@ -18,283 +18,337 @@
 
 #include "gbhf_internal.h"
 #include "gbhf_md.cuh"
+#include "grad_gen.cuh"
 
 namespace gbhf {
 
-namespace {
+// ----------------------------------------------------------- two-electron ----
+// Warp per task (bra shell pair, up to 32 kets of one segment, a range of bra
+// primitives), as the J/K kernels: the bra primitive pairs are staged in
+// shared memory, each lane runs the generated bra-derivative code for its ket
+// pair against them, and the warp reduces the six bra-centre components before
+// one set of atomics.  Summed over every ordered pair of shell pairs with
+// weights (2 - delta_AB)(2 - delta_CD), the bra-centre derivatives give the
+// whole two-electron gradient (the ket-centre terms of (P|Q) are the
+// bra-centre terms of (Q|P)).
 
-constexpr int GL = 6;          // R table dimension (L + 1 <= 5 for s, p quartets)
+constexpr int GR_THREADS = 128;
+constexpr int GR_WARPS = GR_THREADS / 32;
 
-// Hermite E per axis with i <= IA, j <= IB, t <= i + j; E^00_0 = 1.
-template <int IA, int IB>
-struct EAxT {
-  double v[IA + 1][IB + 1][IA + IB + 1];
-  __device__ __forceinline__ double get(int i, int j, int t) const {
-    if (i < 0 || j < 0 || t < 0 || t > i + j) return 0.0;
-    return v[i][j][t];
-  }
-  __device__ __forceinline__ void build(double hp, double pa, double pb) {
-#pragma unroll
-    for (int i = 0; i <= IA; ++i)
-#pragma unroll
-      for (int j = 0; j <= IB; ++j)
-#pragma unroll
-        for (int t = 0; t <= i + j; ++t) {
-          double val;
-          if (i == 0 && j == 0 && t == 0) val = 1.0;
-          else if (t == 0 && i >= 1) val = pa * get(i - 1, j, 0) + get(i - 1, j, 1);
-          else if (t == 0) val = pb * get(i, j - 1, 0) + get(i, j - 1, 1);
-          else val = (hp / t) * (i * get(i - 1, j, t - 1) + j * get(i, j - 1, t - 1));
-          v[i][j][t] = val;
-        }
-  }
+template <typename T, int N>
+struct GamReg {
+  T v[N];
+  __device__ __forceinline__ T get(int i) const { return v[i]; }
+  __device__ __forceinline__ void set(int i, T x) { v[i] = x; }
+};
+template <typename T, int N>
+struct GamSmem {   // per-thread column of a [N][GR_THREADS] shared array
+  T* p;
+  __device__ __forceinline__ T get(int i) const { return p[i * GR_THREADS]; }
+  __device__ __forceinline__ void set(int i, T x) { p[i * GR_THREADS] = x; }
 };
 
-__device__ __forceinline__ void comp_of(int L, int c, int* l) {
-  l[0] = l[1] = l[2] = 0;
-  if (L == 1) l[c] = 1;
-}
-
-// R^0_tuv up to total order L, stored R[t][u][v] with dims GL.
-__device__ void r_table(int L, double alpha, double X, double Y, double Z, const double* F, double* R) {
-  hermite_r<GL - 1>(L, alpha, X, Y, Z, F, R);
-}
-
-}  // namespace
-
-// Bra-side derivative contributions of one shell quartet (AB|CD):
-// gA[3], gB[3] += 4 s sum_prims sum_abcd Gamma_abcd d(ab|cd)/dA,B.
 template <int LA, int LB, int LC, int LD>
-__device__ void quartet_bra_grad(const double* RA, const double* RB, const double* RC, const double* RD,
-                                 const double* ea, const double* ca, int na_p, const double* eb, const double* cb,
-                                 int nb_p, const double* ec, const double* cc, int nc_p, const double* ed,
-                                 const double* cd, int nd_p, const double* Gamma, const double* tab, double wgt,
-                                 double* gA, double* gB) {
-  constexpr int NA = (LA + 1) * (LA + 2) / 2, NB = (LB + 1) * (LB + 2) / 2;
-  constexpr int NC = (LC + 1) * (LC + 2) / 2, ND = (LD + 1) * (LD + 2) / 2;
-  constexpr int L = LA + LB + LC + LD + 1;       // one order higher for the derivative
-  constexpr int HB = LA + LB + 1;                  // bra Hermite range (derivative)
-  double F[GL + 1];
-  double R[GL * GL * GL];
-  double ab2 = 0, cd2 = 0;
-  for (int x = 0; x < 3; ++x) {
-    ab2 += (RA[x] - RB[x]) * (RA[x] - RB[x]);
-    cd2 += (RC[x] - RD[x]) * (RC[x] - RD[x]);
-  }
-  for (int ia = 0; ia < na_p; ++ia)
-    for (int ib = 0; ib < nb_p; ++ib) {
-      const double a = ea[ia], b = eb[ib], p = a + b;
-      const double Kab = ca[ia] * cb[ib] * exp(-a * b / p * ab2);
-      double P[3];
-      EAxT<LA + 1, LB + 1> Eb[3];
-      for (int x = 0; x < 3; ++x) {
-        P[x] = (a * RA[x] + b * RB[x]) / p;
-        Eb[x].build(0.5 / p, P[x] - RA[x], P[x] - RB[x]);
-      }
-      for (int ic = 0; ic < nc_p; ++ic)
-        for (int id = 0; id < nd_p; ++id) {
-          const double c = ec[ic], d = ed[id], q = c + d;
-          const double Kcd = cc[ic] * cd[id] * exp(-c * d / q * cd2);
-          double Q[3];
-          EAxT<LC, LD> Ek[3];
-          for (int x = 0; x < 3; ++x) {
-            Q[x] = (c * RC[x] + d * RD[x]) / q;
-            Ek[x].build(0.5 / q, Q[x] - RC[x], Q[x] - RD[x]);
-          }
-          const double alpha = p * q / (p + q);
-          const double X = P[0] - Q[0], Y = P[1] - Q[1], Z = P[2] - Q[2];
-          boys_generic(false, nullptr, tab, L, alpha * (X * X + Y * Y + Z * Z), F);
-          r_table(L, alpha, X, Y, Z, F, R);
-          const double pref = wgt * 4.0 * 34.98683665524972 / (p * q * sqrt(p + q)) * Kab * Kcd;
-          // Y^{ab}_{tuv} = sum_cd Gamma_abcd W^{cd}_{tuv},  W^{cd}_{tuv} = sum (-1)^.. E^cd R
-          for (int ka = 0; ka < NA; ++ka)
-            for (int kb = 0; kb < NB; ++kb) {
-              int la[3], lb[3];
-              comp_of(LA, ka, la);
-              comp_of(LB, kb, lb);
-              // derivative bra Hermite range per axis: t <= la+lb+1
-              double Yv[HB + 1][HB + 1][HB + 1];
-              for (int t = 0; t <= HB; ++t)
-                for (int u = 0; u <= HB; ++u)
-                  for (int v = 0; v <= HB; ++v) Yv[t][u][v] = 0.0;
-              for (int kc = 0; kc < NC; ++kc)
-                for (int kd = 0; kd < ND; ++kd) {
-                  const double g = Gamma[((ka * NB + kb) * NC + kc) * ND + kd];
-                  if (g == 0.0) continue;
-                  int lc[3], ld[3];
-                  comp_of(LC, kc, lc);
-                  comp_of(LD, kd, ld);
-                  for (int t = 0; t <= la[0] + lb[0] + 1; ++t)
-                    for (int u = 0; u <= la[1] + lb[1] + 1; ++u)
-                      for (int v = 0; v <= la[2] + lb[2] + 1; ++v) {
-                        if (t + u + v > HB) continue;
-                        double w = 0;
-                        for (int tau = 0; tau <= lc[0] + ld[0]; ++tau)
-                          for (int nu = 0; nu <= lc[1] + ld[1]; ++nu)
-                            for (int phi = 0; phi <= lc[2] + ld[2]; ++phi) {
-                              const double e = Ek[0].get(lc[0], ld[0], tau) * Ek[1].get(lc[1], ld[1], nu) *
-                                               Ek[2].get(lc[2], ld[2], phi);
-                              const double r = R[((t + tau) * GL + (u + nu)) * GL + (v + phi)];
-                              w += ((tau + nu + phi) & 1) ? -e * r : e * r;
-                            }
-                        Yv[t][u][v] += g * w;
-                      }
-                }
-              // contract with differentiated bra E for the 3 axes of A and B
-              for (int dir = 0; dir < 3; ++dir) {
-                double sA = 0, sB = 0;
-                for (int t = 0; t <= la[0] + lb[0] + 1; ++t)
-                  for (int u = 0; u <= la[1] + lb[1] + 1; ++u)
-                    for (int v = 0; v <= la[2] + lb[2] + 1; ++v) {
-                      if (t + u + v > HB) continue;
-                      const int tt[3] = {t, u, v};
-                      double eA = 1, eB = 1;
-                      for (int x = 0; x < 3; ++x) {
-                        const int i = la[x], j = lb[x];
-                        if (x == dir) {
-                          eA *= 2 * a * Eb[x].get(i + 1, j, tt[x]) - i * Eb[x].get(i - 1, j, tt[x]);
-                          eB *= 2 * b * Eb[x].get(i, j + 1, tt[x]) - j * Eb[x].get(i, j - 1, tt[x]);
-                        } else {
-                          const double e = Eb[x].get(i, j, tt[x]);
-                          eA *= e;
-                          eB *= e;
-                        }
-                      }
-                      sA += eA * Yv[t][u][v];
-                      sB += eB * Yv[t][u][v];
-                    }
-                gA[dir] += pref * sA;
-                gB[dir] += pref * sB;
-              }
-            }
-        }
-    }
-}
+struct GradFn;
+#define GBHF_GRAD_FN(la, lb, lc, ld, name)                                                                      \
+  template <>                                                                                                  \
+  struct GradFn<la, lb, lc, ld> {                                                                              \
+    template <typename T, typename G>                                                                          \
+    static __device__ __forceinline__ void run(const T* sb, int nbra, T q, T invq, T Qx, T Qy, T Qz, T QCx,    \
+                                               T QCy, T QCz, T QDx, T QDy, T QDz, T Kcd, const T* boys,         \
+                                               const G& gam, T* g) {                                           \
+      grad_ketprim_##name<T, G>(sb, nbra, q, invq, Qx, Qy, Qz, QCx, QCy, QCz, QDx, QDy, QDz, Kcd, boys, gam, g); \
+    }                                                                                                          \
+  };
+GBHF_GRAD_FN(0, 0, 0, 0, ssss)
+GBHF_GRAD_FN(0, 0, 1, 0, ssps)
+GBHF_GRAD_FN(0, 0, 1, 1, sspp)
+GBHF_GRAD_FN(1, 0, 0, 0, psss)
+GBHF_GRAD_FN(1, 0, 1, 0, psps)
+GBHF_GRAD_FN(1, 0, 1, 1, pspp)
+GBHF_GRAD_FN(1, 1, 0, 0, ppss)
+GBHF_GRAD_FN(1, 1, 1, 0, ppps)
+GBHF_GRAD_FN(1, 1, 1, 1, pppp)
 
-struct GradShell {
-  int atom, L, np, f0;
-  int off;   // primitive offset into exps/coefs
-};
-
+template <typename T>
 struct GradArgs {
-  int nq;
-  const int4* quartets;      // (A, B, C, D) shells with A>=B pair ordering irrelevant
-  const double* qweight;     // degeneracy weight s per quartet
-  const GradShell* sh;
-  const double* exps;
-  const double* coefs;
-  const double* xyz;
-  const double* D;           // n x n
+  const int4* tasks;
+  const int* range;          // start, end of this class and precision
+  int* counter;
+  const int *pA, *pB, *pK, *poff, *kseg;
+  const int4* seg;
+  const T* bra;
+  const T* ket;
+  long long npp;
+  const int* shell_f0;
+  const int* shell_atom;
+  const T* D;                // n x n, this precision
   int n;
-  const double* tab;
+  const T* boys;
   double* grad;              // 3 * natoms
 };
 
-template <int LA, int LB, int LC, int LD>
-__device__ void quartet_grad(const GradArgs& g, int4 q, double wgt) {
-  constexpr int NA = (LA + 1) * (LA + 2) / 2, NB = (LB + 1) * (LB + 2) / 2;
-  constexpr int NC = (LC + 1) * (LC + 2) / 2, ND = (LD + 1) * (LD + 2) / 2;
-  const GradShell &A = g.sh[q.x], &B = g.sh[q.y], &C = g.sh[q.z], &Dd = g.sh[q.w];
-  const int n = g.n;
-  double Gam[NA * NB * NC * ND];
-  double GamT[NC * ND * NA * NB];
-  for (int a = 0; a < NA; ++a)
-    for (int b = 0; b < NB; ++b)
-      for (int c = 0; c < NC; ++c)
-        for (int d = 0; d < ND; ++d) {
-          const int fa = A.f0 + a, fb = B.f0 + b, fc = C.f0 + c, fd = Dd.f0 + d;
-          const double val = g.D[(long)fa * n + fb] * g.D[(long)fc * n + fd] -
-                             0.25 * (g.D[(long)fa * n + fc] * g.D[(long)fb * n + fd] +
-                                     g.D[(long)fa * n + fd] * g.D[(long)fb * n + fc]);
-          Gam[((a * NB + b) * NC + c) * ND + d] = val;
-          GamT[((c * ND + d) * NA + a) * NB + b] = val;
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+template <int LA, int LB, int LC, int LD, typename T, bool SG>
+__global__ void __launch_bounds__(GR_THREADS) k_grad_jk(GradArgs<T> a) {
+  constexpr int NA = ncart_c(LA), NB = ncart_c(LB), NC = ncart_c(LC), ND = ncart_c(LD);
+  constexpr int NAB = NA * NB, NCD = NC * ND, NOUT = NAB * NCD;
+  __shared__ T sbra[GR_WARPS][BRA_NFIELD * BRA_STRIDE];
+  __shared__ T sDab[GR_WARPS][NAB];
+  extern __shared__ double gsm_dyn[];
+  using GamT = typename std::conditional<SG, GamSmem<T, NOUT>, GamReg<T, NOUT>>::type;
+  GamT gam;
+  if constexpr (SG) gam.p = reinterpret_cast<T*>(gsm_dyn) + threadIdx.x;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int start = a.range[0];
+  const int ntask = a.range[1] - start;
+  const long long npp = a.npp;
+  const int n = a.n;
+  while (true) {
+    int t = 0;
+    if (lane == 0) t = atomicAdd(a.counter, 1);
+    t = __shfl_sync(0xffffffffu, t, 0);
+    if (t >= ntask) break;
+    const int4 task = a.tasks[start + t];
+    const int ib = task.x;
+    const int jk = task.y + lane;
+    const bool active = lane < task.z;
+    const int kb0 = task.w & 0xffff, Kb = (task.w >> 16) - kb0, pb0 = a.poff[ib] + kb0;
+    for (int idx = lane; idx < BRA_NFIELD * Kb; idx += 32) {
+      const int f = idx / Kb, k = idx - f * Kb;
+      sbra[warp][f * BRA_STRIDE + k] = a.bra[(long long)f * npp + pb0 + k];
+    }
+    const int A = a.pA[ib], B = a.pB[ib];
+    const int a0 = a.shell_f0[A], b0 = a.shell_f0[B];
+    if (lane < NAB) sDab[warp][lane] = a.D[(long long)(a0 + lane / NB) * n + b0 + lane % NB];
+    __syncwarp();
+    T g[6] = {0, 0, 0, 0, 0, 0};
+    T wgt = 0;
+    if (active) {
+      const int C = a.pA[jk], Dd = a.pB[jk];
+      const int c0 = a.shell_f0[C], d0 = a.shell_f0[Dd];
+      // Gamma_abcd = D_ab D_cd - (D_ac D_bd + D_ad D_bc) / 4
+#pragma unroll
+      for (int ia = 0; ia < NA; ++ia)
+#pragma unroll
+        for (int ibb = 0; ibb < NB; ++ibb)
+#pragma unroll
+          for (int ic = 0; ic < NC; ++ic)
+#pragma unroll
+            for (int id = 0; id < ND; ++id) {
+              const T dab = sDab[warp][ia * NB + ibb];
+              const T dcd = a.D[(long long)(c0 + ic) * n + d0 + id];
+              const T dac = a.D[(long long)(a0 + ia) * n + c0 + ic];
+              const T dbd = a.D[(long long)(b0 + ibb) * n + d0 + id];
+              const T dad = a.D[(long long)(a0 + ia) * n + d0 + id];
+              const T dbc = a.D[(long long)(b0 + ibb) * n + c0 + ic];
+              gam.set(((ia * NB + ibb) * NC + ic) * ND + id, dab * dcd - T(0.25) * (dac * dbd + dad * dbc));
+            }
+      const int4 sg = a.seg[a.kseg[jk]];
+      const int K = sg.z, len = sg.y - sg.x;
+      const long long base = (long long)sg.w + (jk - sg.x);
+      for (int kc = 0; kc < K; ++kc) {
+        const long long idx = base + (long long)kc * len;
+        const T q = a.ket[BRA_P * npp + idx];
+        const T invq = a.ket[BRA_INVP * npp + idx];
+        const T Qx = a.ket[BRA_PX * npp + idx], Qy = a.ket[BRA_PY * npp + idx], Qz = a.ket[BRA_PZ * npp + idx];
+        T QCx = 0, QCy = 0, QCz = 0, QDx = 0, QDy = 0, QDz = 0;
+        if (LC >= 1) {
+          QCx = a.ket[BRA_PAX * npp + idx];
+          QCy = a.ket[BRA_PAY * npp + idx];
+          QCz = a.ket[BRA_PAZ * npp + idx];
         }
-  double gA[3] = {0, 0, 0}, gB[3] = {0, 0, 0}, gC[3] = {0, 0, 0}, gD[3] = {0, 0, 0};
-  const double *RA = g.xyz + 3 * A.atom, *RB = g.xyz + 3 * B.atom, *RC = g.xyz + 3 * C.atom,
-               *RD = g.xyz + 3 * Dd.atom;
-  quartet_bra_grad<LA, LB, LC, LD>(RA, RB, RC, RD, g.exps + A.off, g.coefs + A.off, A.np, g.exps + B.off,
-                                   g.coefs + B.off, B.np, g.exps + C.off, g.coefs + C.off, C.np, g.exps + Dd.off,
-                                   g.coefs + Dd.off, Dd.np, Gam, g.tab, wgt, gA, gB);
-  quartet_bra_grad<LC, LD, LA, LB>(RC, RD, RA, RB, g.exps + C.off, g.coefs + C.off, C.np, g.exps + Dd.off,
-                                   g.coefs + Dd.off, Dd.np, g.exps + A.off, g.coefs + A.off, A.np, g.exps + B.off,
-                                   g.coefs + B.off, B.np, GamT, g.tab, wgt, gC, gD);
-  // orientation (AB|CD) gives the A and B derivatives, (CD|AB) the C and D ones
-  for (int x = 0; x < 3; ++x) {
-    atomicAdd(&g.grad[3 * A.atom + x], gA[x]);
-    atomicAdd(&g.grad[3 * B.atom + x], gB[x]);
-    atomicAdd(&g.grad[3 * C.atom + x], gC[x]);
-    atomicAdd(&g.grad[3 * Dd.atom + x], gD[x]);
+        if (LD >= 1) {
+          QDx = a.ket[BRA_PBX * npp + idx];
+          QDy = a.ket[BRA_PBY * npp + idx];
+          QDz = a.ket[BRA_PBZ * npp + idx];
+        }
+        const T Kcd = a.ket[BRA_K * npp + idx];
+        GradFn<LA, LB, LC, LD>::run(sbra[warp], Kb, q, invq, Qx, Qy, Qz, QCx, QCy, QCz, QDx, QDy, QDz, Kcd, a.boys,
+                                    gam, g);
+      }
+      wgt = (A == B ? T(1) : T(2)) * (C == Dd ? T(1) : T(2));
+    }
+#pragma unroll
+    for (int x = 0; x < 6; ++x) {
+      const double v = warp_sum_d(double(wgt * g[x]));
+      if (lane == 0) atomicAdd(&a.grad[3 * a.shell_atom[x < 3 ? A : B] + x % 3], v);
+    }
+    __syncwarp();
   }
 }
 
-__global__ void __launch_bounds__(128) k_grad_2e(GradArgs g) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= g.nq) return;
-  const int4 q = g.quartets[t];
-  const double w = g.qweight[t];
-  const int key = g.sh[q.x].L * 1000 + g.sh[q.y].L * 100 + g.sh[q.z].L * 10 + g.sh[q.w].L;
-  switch (key) {
-    case 0: quartet_grad<0, 0, 0, 0>(g, q, w); break;
-    case 1000: quartet_grad<1, 0, 0, 0>(g, q, w); break;
-    case 1010: quartet_grad<1, 0, 1, 0>(g, q, w); break;
-    case 1100: quartet_grad<1, 1, 0, 0>(g, q, w); break;
-    case 1110: quartet_grad<1, 1, 1, 0>(g, q, w); break;
-    case 1111: quartet_grad<1, 1, 1, 1>(g, q, w); break;
-    default: break;
+template <int LA, int LB, int LC, int LD, typename T>
+static gbhf_status launch_grad_class(gbhf_ctx* c, cudaStream_t strm, int combo, int prec, const T* D, const T* bra,
+                                     const T* ket, const T* boys, double* grad, int ntask) {
+  if (ntask <= 0) return GBHF_OK;
+  constexpr int NOUT = ncart_c(LA) * ncart_c(LB) * ncart_c(LC) * ncart_c(LD);
+  constexpr bool SG = sizeof(T) == 8 ? NOUT > 9 : NOUT > 27;   // Gamma in shared memory
+  const size_t smem = SG ? (size_t)NOUT * GR_THREADS * sizeof(T) : 0;
+  auto kern = k_grad_jk<LA, LB, LC, LD, T, SG>;
+  static bool attr_set = false;
+  if (SG && !attr_set) {
+    GBHF_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr_set = true;
   }
+  int per_sm = 0;
+  GBHF_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, GR_THREADS, smem));
+  per_sm = std::max(per_sm, 1);
+  const int grid = std::min(c->nsm * per_sm, (ntask + GR_WARPS - 1) / GR_WARPS);
+  PairData& P = c->pairs;
+  TaskLists& gt = c->gtasks;
+  GradArgs<T> a;
+  a.tasks = prec == 0 ? gt.tasks64.p : gt.tasks32.p;
+  a.range = gt.ranges.p + 4 * combo + 2 * prec;
+  a.counter = gt.counters.p + 2 * combo + prec;
+  a.pA = P.A.p;
+  a.pB = P.B.p;
+  a.pK = P.K.p;
+  a.poff = P.poff.p;
+  a.kseg = P.kseg.p;
+  a.seg = P.seg_info.p;
+  a.bra = bra;
+  a.ket = ket;
+  a.npp = (long long)P.nprim_pairs;
+  a.shell_f0 = c->tasks.f0.p;
+  a.shell_atom = c->tasks.atom.p;
+  a.D = D;
+  a.n = c->basis.nbf;
+  a.boys = boys;
+  a.grad = grad;
+  kern<<<grid, GR_THREADS, smem, strm>>>(a);
+  count_launch(c);
+  GBHF_CUDA(c, cudaGetLastError());
+  return GBHF_OK;
+}
+
+template <typename T>
+static gbhf_status launch_grad_combo(gbhf_ctx* c, cudaStream_t strm, int k, int prec, const T* D, const T* bra,
+                                     const T* ket, const T* boys, double* grad, int nt) {
+  switch (k) {   // (bra class, ket class) = (k / 3, k % 3); class 0 = ss, 1 = ps, 2 = pp
+    case 0: return launch_grad_class<0, 0, 0, 0, T>(c, strm, k, prec, D, bra, ket, boys, grad, nt);
+    case 1: return launch_grad_class<0, 0, 1, 0, T>(c, strm, k, prec, D, bra, ket, boys, grad, nt);
+    case 2: return launch_grad_class<0, 0, 1, 1, T>(c, strm, k, prec, D, bra, ket, boys, grad, nt);
+    case 3: return launch_grad_class<1, 0, 0, 0, T>(c, strm, k, prec, D, bra, ket, boys, grad, nt);
+    case 4: return launch_grad_class<1, 0, 1, 0, T>(c, strm, k, prec, D, bra, ket, boys, grad, nt);
+    case 5: return launch_grad_class<1, 0, 1, 1, T>(c, strm, k, prec, D, bra, ket, boys, grad, nt);
+    case 6: return launch_grad_class<1, 1, 0, 0, T>(c, strm, k, prec, D, bra, ket, boys, grad, nt);
+    case 7: return launch_grad_class<1, 1, 1, 0, T>(c, strm, k, prec, D, bra, ket, boys, grad, nt);
+    default: return launch_grad_class<1, 1, 1, 1, T>(c, strm, k, prec, D, bra, ket, boys, grad, nt);
+  }
+}
+
+// Two-electron gradient of D (n x n, device) into d_grad (accumulated).
+static gbhf_status grad_2e(gbhf_ctx* c, const double* d_D, double schwarz, double mixed_cutoff, int precision,
+                           double* d_grad) {
+  GBHF_TRY(build_grad_tasks(c, d_D, schwarz, mixed_cutoff, precision));
+  TaskLists& gt = c->gtasks;
+  const int n = c->basis.nbf;
+  bool any32 = false;
+  for (int k = 0; k < NCOMBO_MAX; ++k) any32 |= gt.hranges[4 * k + 3] > gt.hranges[4 * k + 2];
+  if (any32) {
+    GBHF_CUDA(c, c->dfloat.alloc((size_t)n * n));
+    GBHF_TRY(to_float(c, (size_t)n * n, d_D, c->dfloat.p));
+  }
+  GBHF_CUDA(c, cudaMemsetAsync(gt.counters.p, 0, 2 * NCOMBO_MAX * sizeof(int), c->stream));
+  GBHF_CUDA(c, cudaEventRecord(c->fork_ev, c->stream));
+  for (int i = 0; i < gbhf_ctx::NSIDE; ++i) GBHF_CUDA(c, cudaStreamWaitEvent(c->side[i], c->fork_ev, 0));
+  PairData& P = c->pairs;
+  int nl = 0;
+  static const int order[NCOMBO_MAX] = {8, 7, 5, 6, 4, 2, 3, 1, 0};   // heaviest first
+  for (int prec = 0; prec < 2; ++prec) {
+    if (prec == 1 && !any32) break;
+    for (int oi = 0; oi < NCOMBO_MAX; ++oi) {
+      const int k = order[oi];
+      const int nt = gt.hranges[4 * k + 2 * prec + 1] - gt.hranges[4 * k + 2 * prec];
+      if (nt <= 0) continue;
+      cudaStream_t strm = c->side[nl++ % gbhf_ctx::NSIDE];
+      if (prec == 0)
+        GBHF_TRY(launch_grad_combo<double>(c, strm, k, 0, d_D, P.bra64.p, P.ket64.p, c->boysh64.p, d_grad, nt));
+      else
+        GBHF_TRY(launch_grad_combo<float>(c, strm, k, 1, c->dfloat.p, P.bra32.p, P.ket32.p, c->boysh32.p, d_grad,
+                                          nt));
+    }
+  }
+  for (int i = 0; i < gbhf_ctx::NSIDE; ++i) {
+    GBHF_CUDA(c, cudaEventRecord(c->join_ev[i], c->side[i]));
+    GBHF_CUDA(c, cudaStreamWaitEvent(c->stream, c->join_ev[i], 0));
+  }
+  return GBHF_OK;
 }
 
 // ---------------------------------------------------------- one-electron ----
 // Thread per function pair (a <= b): D-weighted derivatives of T and V (with
-// the operator-centre term) and W-weighted derivatives of S.
-__global__ void k_grad_1e(int nbf, int natoms, const double* __restrict__ xyz, const double* __restrict__ Z,
-                          const int* __restrict__ fn, const double* __restrict__ coef, const double* __restrict__ expo,
-                          const double* __restrict__ tab, const double* __restrict__ D, const double* __restrict__ W,
-                          double* __restrict__ grad) {
+// the operator-centre term) and W-weighted derivatives of S.  Primitive pairs
+// whose weighted prefactor is below 1e-17 are skipped.  The operator-centre
+// terms of the block are summed in shared memory (when 3 * natoms fits) and
+// written with one atomic per atom component.
+constexpr int G1_THREADS = 64;
+constexpr int G1_SMEM_ATOMS = 2048;
+
+__global__ void __launch_bounds__(G1_THREADS) k_grad_1e(int nbf, int natoms, const double* __restrict__ xyz,
+                                                        const double* __restrict__ Z, const int* __restrict__ fn,
+                                                        const double* __restrict__ coef,
+                                                        const double* __restrict__ expo,
+                                                        const double* __restrict__ tab, const double* __restrict__ D,
+                                                        const double* __restrict__ W, double* __restrict__ grad) {
+  extern __shared__ double s_gc[];   // 3 * natoms when natoms <= G1_SMEM_ATOMS
+  const bool use_smem = natoms <= G1_SMEM_ATOMS;
+  if (use_smem)
+    for (int k = threadIdx.x; k < 3 * natoms; k += blockDim.x) s_gc[k] = 0.0;
+  __syncthreads();
   const int i = blockIdx.y;
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= nbf || j < i) return;
-  const DevFn f = load_fn(fn, i), gfn = load_fn(fn, j);
-  const double *A = xyz + 3 * f.atom, *B = xyz + 3 * gfn.atom;
-  const double mult = (i == j) ? 1.0 : 2.0;
-  const double dab = mult * D[(long)i * nbf + j], wab = mult * W[(long)i * nbf + j];
-  const int L = f.l[0] + f.l[1] + f.l[2] + gfn.l[0] + gfn.l[1] + gfn.l[2] + 1;
-  double gA[3] = {0, 0, 0};                    // d/dA of (D T - W S); d/dB = -d/dA
-  double F[MD_LMAX + 2];
-  double R[MD_D * MD_D * MD_D];
-  for (int p1 = 0; p1 < f.np; ++p1)
-    for (int p2 = 0; p2 < gfn.np; ++p2) {
-      const double c1 = coef[f.off + p1], a = expo[f.off + p1];
-      const double c2 = coef[gfn.off + p2], b = expo[gfn.off + p2];
-      const double p = a + b, mu = a * b / p;
-      const double cte = sqrt(GBHF_PI / p);
-      double P[3], s[3][3][5];
-      for (int x = 0; x < 3; ++x) {
-        P[x] = (a * A[x] + b * B[x]) / p;
-        const double ab = A[x] - B[x];
-        // table up to i+1 on A and j+2 on B (kinetic)
-        const double s00 = exp(-mu * ab * ab) * cte;
-        const double c = 1.0 / (2.0 * p);
-        const double pax = P[x] - A[x], pbx = P[x] - B[x];
-        for (int m = 0; m <= f.l[x] + 1; ++m)
-          for (int nn = 0; nn <= gfn.l[x] + 2; ++nn) {
-            double v;
-            if (m == 0 && nn == 0) v = s00;
-            else if (m == 0) v = pbx * s[x][0][nn - 1] + (nn >= 2 ? c * (nn - 1) * s[x][0][nn - 2] : 0.0);
-            else if (nn == 0) v = pax * s[x][m - 1][0] + (m >= 2 ? c * (m - 1) * s[x][m - 2][0] : 0.0);
-            else v = pax * s[x][m - 1][nn] + c * ((m >= 2 ? (m - 1) * s[x][m - 2][nn] : 0.0) + nn * s[x][m - 1][nn - 1]);
-            s[x][m][nn] = v;
-          }
-      }
-      auto S1 = [&](int x, int m, int nn) { return (m < 0 || nn < 0) ? 0.0 : s[x][m][nn]; };
-      auto T1 = [&](int x, int m, int nn) {   // kinetic 1-D term as in tab
-        if (m < 0) return 0.0;
-        return -2.0 * b * b * S1(x, m, nn + 2) + b * (2 * nn + 1) * S1(x, m, nn) -
-               (nn >= 2 ? 0.5 * nn * (nn - 1) * S1(x, m, nn - 2) : 0.0);
-      };
-      for (int dir = 0; dir < 3; ++dir) {
-        // d/dA_dir of S and T: replace axis dir factor by 2a f(i+1) - i f(i-1)
-        double dS = c1 * c2, dT = 0;
+  if (j < nbf && j >= i) {
+    const DevFn f = load_fn(fn, i), gfn = load_fn(fn, j);
+    const double *A = xyz + 3 * f.atom, *B = xyz + 3 * gfn.atom;
+    const double mult = (i == j) ? 1.0 : 2.0;
+    const double dab = mult * D[(long)i * nbf + j], wab = mult * W[(long)i * nbf + j];
+    const int L = f.l[0] + f.l[1] + f.l[2] + gfn.l[0] + gfn.l[1] + gfn.l[2] + 1;
+    double ab2 = 0;
+    for (int x = 0; x < 3; ++x) ab2 += (A[x] - B[x]) * (A[x] - B[x]);
+    double gA[3] = {0, 0, 0};   // d/dA of (D T - W S); d/dB = -d/dA
+    double vA[3] = {0, 0, 0}, vB[3] = {0, 0, 0};
+    double F[MD_LMAX + 2];
+    double R[MD_D * MD_D * MD_D];
+    for (int p1 = 0; p1 < f.np; ++p1)
+      for (int p2 = 0; p2 < gfn.np; ++p2) {
+        const double c1 = coef[f.off + p1], a = expo[f.off + p1];
+        const double c2 = coef[gfn.off + p2], b = expo[gfn.off + p2];
+        const double p = a + b, mu = a * b / p;
+        const double kab = c1 * c2 * exp(-mu * ab2);
+        if (fabs(kab) * (1.0 + p) * (fabs(dab) * (1.0 + p) + fabs(wab)) * (GBHF_PI / p) * sqrt(GBHF_PI / p) < 1e-17)
+          continue;
+        const double cte = sqrt(GBHF_PI / p);
+        double P[3], s[3][3][5];
+        for (int x = 0; x < 3; ++x) {
+          P[x] = (a * A[x] + b * B[x]) / p;
+          const double abx = A[x] - B[x];
+          // table up to i+1 on A and j+2 on B (kinetic)
+          const double s00 = exp(-mu * abx * abx) * cte;
+          const double c = 1.0 / (2.0 * p);
+          const double pax = P[x] - A[x], pbx = P[x] - B[x];
+          for (int m = 0; m <= f.l[x] + 1; ++m)
+            for (int nn = 0; nn <= gfn.l[x] + 2; ++nn) {
+              double v;
+              if (m == 0 && nn == 0) v = s00;
+              else if (m == 0) v = pbx * s[x][0][nn - 1] + (nn >= 2 ? c * (nn - 1) * s[x][0][nn - 2] : 0.0);
+              else if (nn == 0) v = pax * s[x][m - 1][0] + (m >= 2 ? c * (m - 1) * s[x][m - 2][0] : 0.0);
+              else v = pax * s[x][m - 1][nn] + c * ((m >= 2 ? (m - 1) * s[x][m - 2][nn] : 0.0) + nn * s[x][m - 1][nn - 1]);
+              s[x][m][nn] = v;
+            }
+        }
+        auto S1 = [&](int x, int m, int nn) { return (m < 0 || nn < 0) ? 0.0 : s[x][m][nn]; };
+        auto T1 = [&](int x, int m, int nn) {   // kinetic 1-D term
+          if (m < 0) return 0.0;
+          return -2.0 * b * b * S1(x, m, nn + 2) + b * (2 * nn + 1) * S1(x, m, nn) -
+                 (nn >= 2 ? 0.5 * nn * (nn - 1) * S1(x, m, nn - 2) : 0.0);
+        };
         double sx[3], tx[3], dsx[3], dtx[3];
         for (int x = 0; x < 3; ++x) {
           const int li = f.l[x], lj = gfn.l[x];
@@ -303,76 +357,101 @@ __global__ void k_grad_1e(int nbf, int natoms, const double* __restrict__ xyz, c
           dsx[x] = 2 * a * S1(x, li + 1, lj) - li * S1(x, li - 1, lj);
           dtx[x] = 2 * a * T1(x, li + 1, lj) - li * T1(x, li - 1, lj);
         }
-        dS = 1.0;
-        for (int x = 0; x < 3; ++x) dS *= (x == dir) ? dsx[x] : sx[x];
-        for (int k = 0; k < 3; ++k) {
-          double term = 1.0;
-          for (int x = 0; x < 3; ++x) {
-            if (x == k) term *= (x == dir) ? dtx[x] : tx[x];
-            else term *= (x == dir) ? dsx[x] : sx[x];
-          }
-          dT += term;
-        }
-        gA[dir] += c1 * c2 * (dab * dT - wab * dS);
-      }
-      // nuclear attraction: d/dA and d/dB of V^C, operator centre -(dA + dB)
-      EAx E[3];
-      for (int x = 0; x < 3; ++x) {
-        const double ab = A[x] - B[x];
-        e_axis(E[x], f.l[x] + 1 <= 2 ? f.l[x] + 1 : 2, gfn.l[x] + 1 <= 2 ? gfn.l[x] + 1 : 2, p, P[x] - A[x],
-               P[x] - B[x], exp(-mu * ab * ab));
-      }
-      for (int cn = 0; cn < natoms; ++cn) {
-        const double* Cc = xyz + 3 * cn;
-        const double PC[3] = {P[0] - Cc[0], P[1] - Cc[1], P[2] - Cc[2]};
-        boys_generic(false, nullptr, tab, L, p * (PC[0] * PC[0] + PC[1] * PC[1] + PC[2] * PC[2]), F);
-        hermite_r<MD_LMAX>(L, p, PC[0], PC[1], PC[2], F, R);
-        const double vpref = -Z[cn] * c1 * c2 * 2.0 * (GBHF_PI / p) * dab;
-        double dA[3] = {0, 0, 0}, dB[3] = {0, 0, 0};
         for (int dir = 0; dir < 3; ++dir) {
-          int hi[3];
-          for (int x = 0; x < 3; ++x) hi[x] = f.l[x] + gfn.l[x] + (x == dir ? 1 : 0);
-          for (int t = 0; t <= hi[0]; ++t)
-            for (int u = 0; u <= hi[1]; ++u)
-              for (int v = 0; v <= hi[2]; ++v) {
-                const int tt[3] = {t, u, v};
-                double eA = 1, eB = 1;
-                for (int x = 0; x < 3; ++x) {
-                  const int li = f.l[x], lj = gfn.l[x];
-                  if (x == dir) {
-                    eA *= 2 * a * E[x].get(li + 1, lj, tt[x]) - li * E[x].get(li - 1, lj, tt[x]);
-                    eB *= 2 * b * E[x].get(li, lj + 1, tt[x]) - lj * E[x].get(li, lj - 1, tt[x]);
-                  } else {
-                    const double e = E[x].get(li, lj, tt[x]);
-                    eA *= e;
-                    eB *= e;
-                  }
-                }
-                const double r = R[(t * MD_D + u) * MD_D + v];
-                dA[dir] += eA * r;
-                dB[dir] += eB * r;
-              }
+          // d/dA_dir of S and T: the axis-dir factor becomes 2a f(i+1) - i f(i-1)
+          double dS = 1.0, dT = 0;
+          for (int x = 0; x < 3; ++x) dS *= (x == dir) ? dsx[x] : sx[x];
+          for (int k = 0; k < 3; ++k) {
+            double term = 1.0;
+            for (int x = 0; x < 3; ++x) {
+              if (x == k) term *= (x == dir) ? dtx[x] : tx[x];
+              else term *= (x == dir) ? dsx[x] : sx[x];
+            }
+            dT += term;
+          }
+          gA[dir] += c1 * c2 * (dab * dT - wab * dS);
         }
+        if (fabs(kab) * fabs(dab) * (1.0 + p) * 2.0 * GBHF_PI / p < 1e-17) continue;
+        // nuclear attraction: d/dA and d/dB of V^C, operator centre -(dA + dB)
+        EAx E[3];
         for (int x = 0; x < 3; ++x) {
-          atomicAdd(&grad[3 * f.atom + x], vpref * dA[x]);
-          atomicAdd(&grad[3 * gfn.atom + x], vpref * dB[x]);
-          atomicAdd(&grad[3 * cn + x], -vpref * (dA[x] + dB[x]));
+          const double abx = A[x] - B[x];
+          e_axis(E[x], f.l[x] + 1 <= 2 ? f.l[x] + 1 : 2, gfn.l[x] + 1 <= 2 ? gfn.l[x] + 1 : 2, p, P[x] - A[x],
+                 P[x] - B[x], exp(-mu * abx * abx));
+        }
+        for (int cn = 0; cn < natoms; ++cn) {
+          const double* Cc = xyz + 3 * cn;
+          const double PC[3] = {P[0] - Cc[0], P[1] - Cc[1], P[2] - Cc[2]};
+          boys_generic(false, nullptr, tab, L, p * (PC[0] * PC[0] + PC[1] * PC[1] + PC[2] * PC[2]), F);
+          hermite_r<MD_LMAX>(L, p, PC[0], PC[1], PC[2], F, R);
+          const double vpref = -Z[cn] * c1 * c2 * 2.0 * (GBHF_PI / p) * dab;
+          double dA[3] = {0, 0, 0}, dB[3] = {0, 0, 0};
+          for (int dir = 0; dir < 3; ++dir) {
+            int hi[3];
+            for (int x = 0; x < 3; ++x) hi[x] = f.l[x] + gfn.l[x] + (x == dir ? 1 : 0);
+            for (int t = 0; t <= hi[0]; ++t)
+              for (int u = 0; u <= hi[1]; ++u)
+                for (int v = 0; v <= hi[2]; ++v) {
+                  const int tt[3] = {t, u, v};
+                  double eA = 1, eB = 1;
+                  for (int x = 0; x < 3; ++x) {
+                    const int li = f.l[x], lj = gfn.l[x];
+                    if (x == dir) {
+                      eA *= 2 * a * E[x].get(li + 1, lj, tt[x]) - li * E[x].get(li - 1, lj, tt[x]);
+                      eB *= 2 * b * E[x].get(li, lj + 1, tt[x]) - lj * E[x].get(li, lj - 1, tt[x]);
+                    } else {
+                      const double e = E[x].get(li, lj, tt[x]);
+                      eA *= e;
+                      eB *= e;
+                    }
+                  }
+                  const double r = R[(t * MD_D + u) * MD_D + v];
+                  dA[dir] += eA * r;
+                  dB[dir] += eB * r;
+                }
+          }
+          for (int x = 0; x < 3; ++x) {
+            vA[x] += vpref * dA[x];
+            vB[x] += vpref * dB[x];
+            const double gc = -vpref * (dA[x] + dB[x]);
+            if (use_smem) atomicAdd(&s_gc[3 * cn + x], gc);
+            else atomicAdd(&grad[3 * cn + x], gc);
+          }
         }
       }
+    for (int x = 0; x < 3; ++x) {
+      atomicAdd(&grad[3 * f.atom + x], gA[x] + vA[x]);
+      atomicAdd(&grad[3 * gfn.atom + x], -gA[x] + vB[x]);
     }
-  for (int x = 0; x < 3; ++x) {
-    atomicAdd(&grad[3 * f.atom + x], gA[x]);
-    atomicAdd(&grad[3 * gfn.atom + x], -gA[x]);
   }
+  __syncthreads();
+  if (use_smem)
+    for (int k = threadIdx.x; k < 3 * natoms; k += blockDim.x)
+      if (s_gc[k] != 0.0) atomicAdd(&grad[k], s_gc[k]);
 }
 
-}  // namespace gbhf
-
-using namespace gbhf;
+// Nuclear repulsion gradient, one thread per atom: -sum_L Z_K Z_L (R_K - R_L) / R_KL^3.
+__global__ void k_grad_nuc(int natoms, const double* __restrict__ xyz, const double* __restrict__ Z,
+                           double* __restrict__ grad) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= natoms) return;
+  double g[3] = {0, 0, 0};
+  for (int l = 0; l < natoms; ++l) {
+    if (l == k) continue;
+    double d[3], r2 = 0;
+    for (int x = 0; x < 3; ++x) {
+      d[x] = xyz[3 * k + x] - xyz[3 * l + x];
+      r2 += d[x] * d[x];
+    }
+    const double f = Z[k] * Z[l] / (r2 * sqrt(r2));
+    for (int x = 0; x < 3; ++x) g[x] -= f * d[x];
+  }
+  for (int x = 0; x < 3; ++x) grad[3 * k + x] += g[x];
+}
 
 // Host driver: D and W square (device), gradient into d_grad (3*natoms, device).
-namespace gbhf {
-gbhf_status gradient_dev(gbhf_ctx* c, const double* d_D, const double* d_W, double schwarz, double* d_grad) {
+gbhf_status gradient_dev(gbhf_ctx* c, const double* d_D, const double* d_W, double schwarz, double mixed_cutoff,
+                         int precision, double* d_grad) {
   const Basis& b = c->basis;
   if (!b.shells_ok || b.maxL > 1)
     return fail(c, GBHF_ERR_UNSUPPORTED, "gradient kernels need complete s/p shells");
@@ -380,84 +459,15 @@ gbhf_status gradient_dev(gbhf_ctx* c, const double* d_D, const double* d_W, doub
   GBHF_TRY(ensure_pairs(c));
   const int n = b.nbf, na = b.natoms;
   GBHF_CUDA(c, cudaMemsetAsync(d_grad, 0, 3 * na * sizeof(double), c->stream));
-  // one-electron terms
-  k_grad_1e<<<dim3((n + 63) / 64, n), 64, 0, c->stream>>>(n, na, c->d_xyz.p, c->d_Z.p, c->d_fn.p, c->d_coef.p,
-                                                          c->d_exp.p, c->boys64.p, d_D, d_W, d_grad);
-  count_launch(c);
+  k_grad_nuc<<<(na + 127) / 128, 128, 0, c->stream>>>(na, c->d_xyz.p, c->d_Z.p, d_grad);
+  const size_t smem1 = na <= G1_SMEM_ATOMS ? 3 * (size_t)na * sizeof(double) : 0;
+  if (smem1 > 48 * 1024)
+    GBHF_CUDA(c, cudaFuncSetAttribute(k_grad_1e, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1));
+  k_grad_1e<<<dim3((n + G1_THREADS - 1) / G1_THREADS, n), G1_THREADS, smem1, c->stream>>>(
+      n, na, c->d_xyz.p, c->d_Z.p, c->d_fn.p, c->d_coef.p, c->d_exp.p, c->boys64.p, d_D, d_W, d_grad);
+  count_launch(c, 2);
   GBHF_CUDA(c, cudaGetLastError());
-  // two-electron terms: unique shell quartets passing Schwarz
-  const PairData& P = c->pairs;
-  std::vector<int4> quart;
-  std::vector<double> wq;
-  for (int X = 0; X < NPCLS; ++X)
-    for (int i = P.cls_start[X]; i < P.cls_start[X + 1]; ++i)
-      for (int Y = 0; Y <= X; ++Y)
-        for (int j = P.cls_start[Y]; j < P.cls_start[Y + 1]; ++j) {
-          if (X == Y && j > i) break;
-          if (P.hQ[i] * P.hQ[j] < schwarz) continue;
-          const int A = P.hA[i], B = P.hB[i], C = P.hA[j], D = P.hB[j];
-          quart.push_back(make_int4(A, B, C, D));
-          wq.push_back((A == B ? 0.5 : 1.0) * (C == D ? 0.5 : 1.0) * (i == j ? 0.5 : 1.0));
-        }
-  const int nq = (int)quart.size();
-  std::vector<GradShell> sh(b.shells.size());
-  std::vector<double> ex, co;
-  for (size_t s = 0; s < b.shells.size(); ++s) {
-    sh[s].atom = b.shells[s].atom;
-    sh[s].L = b.shells[s].L;
-    sh[s].np = b.shells[s].np;
-    sh[s].f0 = b.shells[s].f0;
-    sh[s].off = (int)ex.size();
-    ex.insert(ex.end(), b.shells[s].expo.begin(), b.shells[s].expo.end());
-    co.insert(co.end(), b.shells[s].coef.begin(), b.shells[s].coef.end());
-  }
-  DBuf<int4> dq;
-  DBuf<double> dw, dex, dco;
-  DBuf<GradShell> dsh;
-  GBHF_CUDA(c, dq.alloc(std::max(nq, 1)));
-  GBHF_CUDA(c, dw.alloc(std::max(nq, 1)));
-  GBHF_CUDA(c, dex.alloc(ex.size()));
-  GBHF_CUDA(c, dco.alloc(co.size()));
-  GBHF_CUDA(c, dsh.alloc(sh.size()));
-  GBHF_CUDA(c, cudaMemcpyAsync(dq.p, quart.data(), nq * sizeof(int4), cudaMemcpyHostToDevice, c->stream));
-  GBHF_CUDA(c, cudaMemcpyAsync(dw.p, wq.data(), nq * sizeof(double), cudaMemcpyHostToDevice, c->stream));
-  GBHF_CUDA(c, cudaMemcpyAsync(dex.p, ex.data(), ex.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
-  GBHF_CUDA(c, cudaMemcpyAsync(dco.p, co.data(), co.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
-  GBHF_CUDA(c, cudaMemcpyAsync(dsh.p, sh.data(), sh.size() * sizeof(GradShell), cudaMemcpyHostToDevice, c->stream));
-  GradArgs g;
-  g.nq = nq;
-  g.quartets = dq.p;
-  g.qweight = dw.p;
-  g.sh = dsh.p;
-  g.exps = dex.p;
-  g.coefs = dco.p;
-  g.xyz = c->d_xyz.p;
-  g.D = d_D;
-  g.n = n;
-  g.tab = c->boys64.p;
-  g.grad = d_grad;
-  if (nq > 0) {
-    k_grad_2e<<<(nq + 127) / 128, 128, 0, c->stream>>>(g);
-    count_launch(c);
-    GBHF_CUDA(c, cudaGetLastError());
-  }
-  // nuclear repulsion: d/dR_K sum_{K<L} Z_K Z_L / R_KL
-  std::vector<double> gn(3 * na, 0.0);
-  for (int k = 0; k < na; ++k)
-    for (int l = 0; l < na; ++l) {
-      if (l == k) continue;
-      double d[3], r2 = 0;
-      for (int x = 0; x < 3; ++x) {
-        d[x] = b.xyz[3 * k + x] - b.xyz[3 * l + x];
-        r2 += d[x] * d[x];
-      }
-      const double r3 = r2 * std::sqrt(r2);
-      for (int x = 0; x < 3; ++x) gn[3 * k + x] -= b.Z[k] * b.Z[l] * d[x] / r3;
-    }
-  DBuf<double> dgn;
-  GBHF_CUDA(c, dgn.alloc(3 * na));
-  GBHF_CUDA(c, cudaMemcpyAsync(dgn.p, gn.data(), 3 * na * sizeof(double), cudaMemcpyHostToDevice, c->stream));
-  GBHF_TRY(axpby(c, 3 * (size_t)na, 1.0, d_grad, 1.0, dgn.p, d_grad));
+  GBHF_TRY(grad_2e(c, d_D, schwarz, mixed_cutoff, precision, d_grad));
   GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
   return GBHF_OK;
 }
@@ -484,4 +494,5 @@ gbhf_status energy_weighted_density(gbhf_ctx* c, int n, int nocc, const double* 
   GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
   return GBHF_OK;
 }
+
 }  // namespace gbhf

@@ -26,7 +26,6 @@
 
 namespace gbhf {
 
-constexpr int ncart_c(int L) { return (L + 1) * (L + 2) / 2; }
 
 template <typename T, int N>
 struct RegAcc {
@@ -118,7 +117,7 @@ template <int LA, int LB, int LC, int LD, typename T, bool SACC>
 __global__ void __launch_bounds__(JK_THREADS) k_jk(JKArgs<T> a) {
   constexpr int NA = ncart_c(LA), NB = ncart_c(LB), NC = ncart_c(LC), ND = ncart_c(LD);
   constexpr int NAB = NA * NB, NCD = NC * ND, NOUT = NAB * NCD;
-  __shared__ T sbra[JK_WARPS][BRA_NFIELD * BRA_STRIDE];
+  __shared__ T sbra[JK_WARPS][BRA_NJK * BRA_STRIDE];
   __shared__ T sDab[JK_WARPS][NAB > 1 ? NAB : 1];
   extern __shared__ double sacc_dyn[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -141,7 +140,7 @@ __global__ void __launch_bounds__(JK_THREADS) k_jk(JKArgs<T> a) {
     const bool active = lane < task.z;
     // bra primitives [kb0, kb1) of pair ib
     const int kb0 = task.w & 0xffff, Kb = (task.w >> 16) - kb0, pb0 = a.poff[ib] + kb0;
-    for (int idx = lane; idx < BRA_NFIELD * Kb; idx += 32) {
+    for (int idx = lane; idx < BRA_NJK * Kb; idx += 32) {
       const int f = idx / Kb, k = idx - f * Kb;
       sbra[warp][f * BRA_STRIDE + k] = a.bra[(long long)f * npp + pb0 + k];
     }
@@ -326,7 +325,11 @@ gbhf_status schwarz_classes_dev(gbhf_ctx* c, const int* cls_start, const int* d_
 
 struct TaskGenArgs {
   int nitems;
-  const int* item_combo_start;   // NCOMBO+1 item offsets
+  int ncombo;                    // quartet classes (bra pair class, ket pair class)
+  int cbra[NCOMBO_MAX], cket[NCOMBO_MAX];
+  int all_pairs;                 // every ordered (bra, ket) pair, else ket <= bra in one class
+  int square_w;                  // bound uses the squared density weight (gradient)
+  const int* item_combo_start;   // ncombo+1 item offsets
   const int* cls_start;          // NPCLS+1
   const int* seg_cls_start;      // NPCLS+1
   const int4* seg;
@@ -358,9 +361,8 @@ __global__ void k_tasks(TaskGenArgs g) {
   const int it = blockIdx.x * blockDim.x + threadIdx.x;
   if (it >= g.nitems) return;
   int k = 0;
-  while (k + 1 < NCOMBO && it >= g.item_combo_start[k + 1]) ++k;
-  const int X = k >= 3 ? 2 : (k >= 1 ? 1 : 0);   // combos (0,0) (1,0) (1,1) (2,0) (2,1) (2,2)
-  const int Y = k - X * (X + 1) / 2;
+  while (k + 1 < g.ncombo && it >= g.item_combo_start[k + 1]) ++k;
+  const int X = g.cbra[k], Y = g.cket[k];
   const int i = g.cls_start[X] + (it - g.item_combo_start[k]);
   const double qi = g.Q[i];
   int n64 = 0, n32 = 0;
@@ -371,11 +373,12 @@ __global__ void k_tasks(TaskGenArgs g) {
     for (int sidx = g.seg_cls_start[Y]; sidx < g.seg_cls_start[Y + 1]; ++sidx) {
       const int4 s = g.seg[sidx];
       // bound of (bra|ket) contributions: Q_bra Q_ket max(w_bra, max w over the ket segment)
-      const double w = g.pw ? fmax(wi, g.sw[sidx]) : 1.0;
+      double w = g.pw ? fmax(wi, g.sw[sidx]) : 1.0;
+      if (g.square_w) w *= w;
       if (!(w > 0)) continue;
       const double ta = g.thr_all / (qi * w), t64 = g.thr64 / (qi * w);
       int hi = s.y;
-      if (X == Y && hi > i + 1) hi = i + 1;
+      if (!g.all_pairs && X == Y && hi > i + 1) hi = i + 1;
       if (hi <= s.x) continue;
       const int keep = count_ge(g.Q, s.x, hi, ta);
       int k64 = count_ge(g.Q, s.x, s.x + keep, t64);
@@ -437,9 +440,9 @@ __global__ void k_scan2(int n, const int* __restrict__ count, int* __restrict__ 
   }
 }
 
-__global__ void k_ranges(const int* item_combo_start, const int* off64, const int* off32, int* ranges) {
+__global__ void k_ranges(int ncombo, const int* item_combo_start, const int* off64, const int* off32, int* ranges) {
   const int k = threadIdx.x;
-  if (k >= NCOMBO) return;
+  if (k >= ncombo) return;
   ranges[4 * k + 0] = off64[item_combo_start[k]];
   ranges[4 * k + 1] = off64[item_combo_start[k + 1]];
   ranges[4 * k + 2] = off32[item_combo_start[k]];
@@ -498,8 +501,7 @@ __global__ void k_seg_max(int nseg, const int4* __restrict__ seg, const double* 
   }
 }
 
-static gbhf_status density_weights(gbhf_ctx* c, const double* d_dD) {
-  TaskLists& st = c->tasks;
+static gbhf_status density_weights(gbhf_ctx* c, TaskLists& st, const double* d_dD) {
   PairData& P = c->pairs;
   const int ns = (int)c->basis.shells.size(), n = c->basis.nbf;
   GBHF_CUDA(c, st.blk.alloc((size_t)ns * ns));
@@ -507,7 +509,8 @@ static gbhf_status density_weights(gbhf_ctx* c, const double* d_dD) {
   GBHF_CUDA(c, st.pw.alloc(std::max(P.npairs, 1)));
   GBHF_CUDA(c, st.pb.alloc(std::max(P.npairs, 1)));
   GBHF_CUDA(c, st.sw.alloc(std::max(P.nseg_total, 1)));
-  k_block_max<<<dim3((ns + 127) / 128, ns), 128, 0, c->stream>>>(ns, st.f0.p, st.nc.p, d_dD, n, st.blk.p);
+  const TaskLists& sh = c->tasks;   // per-shell arrays
+  k_block_max<<<dim3((ns + 127) / 128, ns), 128, 0, c->stream>>>(ns, sh.f0.p, sh.nc.p, d_dD, n, st.blk.p);
   k_row_max<<<(ns + 127) / 128, 128, 0, c->stream>>>(ns, st.blk.p, st.row.p);
   k_pair_weight<<<(P.npairs + 127) / 128, 128, 0, c->stream>>>(P.npairs, ns, P.A.p, P.B.p, st.blk.p, st.row.p,
                                                                st.pw.p, st.pb.p);
@@ -517,34 +520,44 @@ static gbhf_status density_weights(gbhf_ctx* c, const double* d_dD) {
   return GBHF_OK;
 }
 
-static gbhf_status build_tasks(gbhf_ctx* c, double thr_all, double thr64, int* h_ranges, const double* pw = nullptr,
-                               const double* sw = nullptr) {
+// Quartet-class task lists of TL for the combos (cbra[k], cket[k]).
+static gbhf_status build_task_lists(gbhf_ctx* c, TaskLists& TL, int ncombo, const int* cbra, const int* cket,
+                                    bool all_pairs, bool square_w, double thr_all, double thr64, const double* pw,
+                                    const double* sw) {
   PairData& P = c->pairs;
-  TaskLists& TL = c->tasks;
-  std::vector<int> ics(NCOMBO + 1, 0);
-  for (int k = 0; k < NCOMBO; ++k) {
-    const int X = COMBO_BRA[k];
+  int* h_ranges = TL.hranges;
+  std::vector<int> ics(ncombo + 1, 0);
+  for (int k = 0; k < ncombo; ++k) {
+    const int X = cbra[k];
     ics[k + 1] = ics[k] + (P.cls_start[X + 1] - P.cls_start[X]);
   }
-  TL.nitems = ics[NCOMBO];
+  TL.nitems = ics[ncombo];
   TL.combo_item_start = ics;
+  TL.ncombo = ncombo;
   const int ni = TL.nitems;
   DBuf<int> d_ics, d_cls, d_scs;
-  GBHF_CUDA(c, d_ics.alloc(NCOMBO + 1));
+  GBHF_CUDA(c, d_ics.alloc(ncombo + 1));
   GBHF_CUDA(c, d_cls.alloc(NPCLS + 1));
   GBHF_CUDA(c, d_scs.alloc(NPCLS + 1));
-  GBHF_CUDA(c, cudaMemcpyAsync(d_ics.p, ics.data(), (NCOMBO + 1) * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  GBHF_CUDA(c, cudaMemcpyAsync(d_ics.p, ics.data(), (ncombo + 1) * sizeof(int), cudaMemcpyHostToDevice, c->stream));
   GBHF_CUDA(c, cudaMemcpyAsync(d_cls.p, P.cls_start, (NPCLS + 1) * sizeof(int), cudaMemcpyHostToDevice, c->stream));
   GBHF_CUDA(c, cudaMemcpyAsync(d_scs.p, P.seg_cls_start, (NPCLS + 1) * sizeof(int), cudaMemcpyHostToDevice, c->stream));
   GBHF_CUDA(c, TL.item_count.alloc(2 * (size_t)std::max(ni, 1)));
   GBHF_CUDA(c, TL.item_off.alloc(2 * ((size_t)ni + 1)));
-  GBHF_CUDA(c, TL.ranges.alloc(4 * NCOMBO));
-  GBHF_CUDA(c, TL.counters.alloc(2 * NCOMBO));
-  GBHF_CUDA(c, TL.stats.alloc(3 * 2 * NCOMBO));
+  GBHF_CUDA(c, TL.ranges.alloc(4 * ncombo));
+  GBHF_CUDA(c, TL.counters.alloc(2 * ncombo));
+  GBHF_CUDA(c, TL.stats.alloc(3 * 2 * ncombo));
   int* off64 = TL.item_off.p;
   int* off32 = TL.item_off.p + ni + 1;
   TaskGenArgs g;
   g.nitems = ni;
+  g.ncombo = ncombo;
+  for (int k = 0; k < NCOMBO_MAX; ++k) {
+    g.cbra[k] = k < ncombo ? cbra[k] : 0;
+    g.cket[k] = k < ncombo ? cket[k] : 0;
+  }
+  g.all_pairs = all_pairs ? 1 : 0;
+  g.square_w = square_w ? 1 : 0;
   g.item_combo_start = d_ics.p;
   g.cls_start = d_cls.p;
   g.seg_cls_start = d_scs.p;
@@ -578,11 +591,53 @@ static gbhf_status build_tasks(gbhf_ctx* c, double thr_all, double thr64, int* h
     k_tasks<true><<<(ni + 127) / 128, 128, 0, c->stream>>>(g);
     count_launch(c);
   }
-  k_ranges<<<1, 32, 0, c->stream>>>(d_ics.p, off64, off32, TL.ranges.p);
+  k_ranges<<<1, 32, 0, c->stream>>>(ncombo, d_ics.p, off64, off32, TL.ranges.p);
   count_launch(c);
   GBHF_CUDA(c, cudaGetLastError());
-  GBHF_CUDA(c, cudaMemcpyAsync(h_ranges, TL.ranges.p, 4 * NCOMBO * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  GBHF_CUDA(c, cudaMemcpyAsync(h_ranges, TL.ranges.p, 4 * ncombo * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
+  return GBHF_OK;
+}
+
+// J/K lists: the six classes with bra class >= ket class, unique quartets.
+static gbhf_status build_tasks(gbhf_ctx* c, double thr_all, double thr64, const double* pw = nullptr,
+                               const double* sw = nullptr) {
+  return build_task_lists(c, c->tasks, NCOMBO, COMBO_BRA, COMBO_KET, false, false, thr_all, thr64, pw, sw);
+}
+
+gbhf_status ensure_shell_arrays(gbhf_ctx* c) {
+  TaskLists& st = c->tasks;
+  if (st.f0_gen == c->basis_gen) return GBHF_OK;
+  const size_t ns = c->basis.shells.size();
+  std::vector<int> f0(ns), nc(ns), at(ns);
+  for (size_t s = 0; s < ns; ++s) {
+    f0[s] = c->basis.shells[s].f0;
+    nc[s] = c->basis.shells[s].ncomp;
+    at[s] = c->basis.shells[s].atom;
+  }
+  GBHF_CUDA(c, st.f0.alloc(ns));
+  GBHF_CUDA(c, st.nc.alloc(ns));
+  GBHF_CUDA(c, st.atom.alloc(ns));
+  GBHF_CUDA(c, cudaMemcpyAsync(st.f0.p, f0.data(), ns * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  GBHF_CUDA(c, cudaMemcpyAsync(st.nc.p, nc.data(), ns * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  GBHF_CUDA(c, cudaMemcpyAsync(st.atom.p, at.data(), ns * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
+  st.f0_gen = c->basis_gen;
+  return GBHF_OK;
+}
+
+// Gradient lists: all nine (bra class, ket class) combinations, every ordered
+// pair of shell pairs, bound Q_bra Q_ket max(w_bra, w_ket)^2 with the pair
+// weights of D (|Gamma_abcd| <= that squared weight).
+gbhf_status build_grad_tasks(gbhf_ctx* c, const double* d_D, double cutoff, double mixed_cutoff, int precision) {
+  GBHF_TRY(ensure_pairs(c));
+  GBHF_TRY(ensure_shell_arrays(c));
+  TaskLists& gt = c->gtasks;
+  GBHF_TRY(density_weights(c, gt, d_D));
+  static const int gb[NCOMBO_MAX] = {0, 0, 0, 1, 1, 1, 2, 2, 2};
+  static const int gk[NCOMBO_MAX] = {0, 1, 2, 0, 1, 2, 0, 1, 2};
+  const double t64 = precision == GBHF_PREC_FP64 ? 0.0 : mixed_cutoff;
+  GBHF_TRY(build_task_lists(c, gt, NCOMBO_MAX, gb, gk, true, true, cutoff, t64, gt.pw.p, gt.sw.p));
   return GBHF_OK;
 }
 
@@ -633,24 +688,12 @@ gbhf_status jk_build(gbhf_ctx* c, const double* d_Dsq, double* d_G, int precisio
   GBHF_TRY(ensure_pairs(c));
   const int n = c->basis.nbf;
   TaskLists& st = c->tasks;
-  if (st.f0_gen != c->basis_gen) {
-    st.f0_gen = c->basis_gen;
-    std::vector<int> f0(c->basis.shells.size()), nc(c->basis.shells.size());
-    for (size_t s = 0; s < f0.size(); ++s) {
-      f0[s] = c->basis.shells[s].f0;
-      nc[s] = c->basis.shells[s].ncomp;
-    }
-    GBHF_CUDA(c, st.f0.alloc(f0.size()));
-    GBHF_CUDA(c, st.nc.alloc(nc.size()));
-    GBHF_CUDA(c, cudaMemcpyAsync(st.f0.p, f0.data(), f0.size() * sizeof(int), cudaMemcpyHostToDevice, c->stream));
-    GBHF_CUDA(c, cudaMemcpyAsync(st.nc.p, nc.data(), nc.size() * sizeof(int), cudaMemcpyHostToDevice, c->stream));
-    GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
-  }
+  GBHF_TRY(ensure_shell_arrays(c));
   if (local_weights) {
     // incremental build: bounds weighted by the local size of the density change
-    GBHF_TRY(density_weights(c, d_Dsq));
+    GBHF_TRY(density_weights(c, st, d_Dsq));
     const double t64 = precision == GBHF_PREC_FP64 ? 0.0 : mixed_cutoff;
-    GBHF_TRY(build_tasks(c, schwarz, t64, st.hranges, st.pw.p, st.sw.p));
+    GBHF_TRY(build_tasks(c, schwarz, t64, st.pw.p, st.sw.p));
     st.thr_all = -1;   // lists no longer match a uniform weight
     st.thr64 = -1;
   } else {
@@ -658,7 +701,7 @@ gbhf_status jk_build(gbhf_ctx* c, const double* d_Dsq, double* d_G, int precisio
     const double thr_all = schwarz / weight;
     const double thr64 = precision == GBHF_PREC_FP64 ? 0.0 : mixed_cutoff / weight;
     if (thr_all != st.thr_all || thr64 != st.thr64 || !c->tasks.tasks64.p) {
-      GBHF_TRY(build_tasks(c, thr_all, thr64, st.hranges));
+      GBHF_TRY(build_tasks(c, thr_all, thr64));
       st.thr_all = thr_all;
       st.thr64 = thr64;
     }

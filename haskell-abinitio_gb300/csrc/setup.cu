@@ -8,6 +8,8 @@
 
 namespace gbhf {
 
+thread_local DevPool* tls_pool = nullptr;
+
 gbhf_status fail(gbhf_ctx* c, gbhf_status s, const std::string& msg) {
   if (c) c->err = msg;
   return s;
@@ -166,6 +168,7 @@ gbhf_status ensure_boys_tables(gbhf_ctx* c) {
       if (k > 0) inv_fact /= k;
       for (int m = 0; m <= BOYSH_LMAX; ++m)
         h64[(size_t)j * BOYSH64_STRIDE + m * BOYS64_NTERM + k] = t64[(size_t)j * BOYS_NCOL + m + k] * inv_fact;
+      h64[(size_t)j * BOYSH64_STRIDE + BOYSH_EXPROW * BOYS64_NTERM + k] = std::exp(-j * BOYS64_H) * inv_fact;
     }
   }
   for (int j = 0; j < BOYS32_NROW; ++j) {
@@ -175,6 +178,7 @@ gbhf_status ensure_boys_tables(gbhf_ctx* c) {
       if (k > 0) inv_fact /= k;
       for (int m = 0; m <= BOYSH_LMAX; ++m)
         h32[(size_t)j * BOYSH32_STRIDE + m * BOYS32_NTERM + k] = (float)(boys_series(m + k, tj) * inv_fact);
+      h32[(size_t)j * BOYSH32_STRIDE + BOYSH_EXPROW * BOYS32_NTERM + k] = (float)(std::exp(-tj) * inv_fact);
     }
   }
   GBHF_CUDA(c, c->boys64.alloc(t64.size()));
@@ -215,6 +219,7 @@ static void pair_prims(const Basis& b, int A, int B, double* out) {
         f[BRA_PBX + x] = Px - RB[x];
       }
       f[BRA_K] = std::sqrt(TWO_PI_2P5) * sa.coef[ia] * sb.coef[ib] * std::exp(-mu * r2) / p;
+      f[BRA_AEXP] = ea;
     }
 }
 

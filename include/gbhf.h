@@ -209,7 +209,11 @@ gbhf_status gbhf_scf(gbhf_ctx* ctx, const gbhf_scf_opts* opts, gbhf_result* resu
 
 /* Analytic RHF nuclear gradient (energyGradient, HartreeFock/Derivatives.hs:40-48,
  * which is dead code in the reference): dE/dR for density D and energy-weighted
- * density W (both flat), grad[3*atom + axis] in hartree/bohr. */
+ * density W (both flat), grad[3*atom + axis] in hartree/bohr.  With D and W
+ * NULL the last SCF of this basis is used.  Two-electron terms are screened at
+ * Q_ab Q_cd max(w)^2 < schwarz_cutoff (w: shell-block maxima of |D|); with
+ * GBHF_PREC_MIXED the quartets whose bound is below 1e-4 use FP32 derivative
+ * integrals. */
 gbhf_status gbhf_gradient(gbhf_ctx* ctx, int precision, double schwarz_cutoff, const double* d_flat,
                           const double* w_flat, double* grad);
 
