@@ -235,7 +235,7 @@ def run_gbhf(args, world, rank, local):
     achieved = flops / (st["ms"] * 1e-3) / 1e12 if st["ms"] > 0 else 0.0
     peak64, peak32 = ctx.peak_flops(_lib.PREC_FP64), ctx.peak_flops(_lib.PREC_MIXED)
     peak = peak64 if prec == "fp64" else peak32
-    prof_tr = traffic_profile().get(f"{cname}_{prec}")
+    prof_tr = traffic_profile().get(f"{cname}_{prec}", {}).get("dram_bytes_per_launch")
     jk_ms = prof_cls["jk_ms_fp64"] + prof_cls["jk_ms_fp32"]
     fnq_step = prof["fn_quartets"] / args.steps
     line = {
@@ -266,7 +266,10 @@ def run_gbhf(args, world, rank, local):
                      "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
                      "peak_source": f"FMA microbenchmark on this GPU (FP64 {peak64:.2f}, FP32 {peak32:.1f} TFLOP/s); "
                                     "MEASURED_PEAKS.json holds only HBM and bf16 tensor peaks",
-                     "flops_per_launch": flops / args.steps, "traffic": prof_tr},
+                     "flops_per_launch": flops / max(r_prof["iterations"], 1), "traffic": prof_tr,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of this class's launch "
+                                       "in a full mixed Fock build (profiles/traffic.json); the ERI kernels "
+                                       "are compute-bound, traffic far below their roofline"},
         "classes": {f"{k[0]}_{k[1]}": v for k, v in cls.items() if v["ms"] > 0},
         "clocks": clk.summary(),
         "e2e": {"value": e2e_v, "unit": "s/molecule", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},

@@ -110,8 +110,6 @@ __device__ __forceinline__ double warp_sum(double v) {
 
 constexpr int JK_THREADS = 128;
 constexpr int JK_WARPS = JK_THREADS / 32;
-// Upper bound on the primitive quartets one lane evaluates in one task.
-constexpr int JK_LANE_PRIMS = 256;
 
 template <int LA, int LB, int LC, int LD, typename T, bool SACC>
 __global__ void __launch_bounds__(JK_THREADS) k_jk(JKArgs<T> a) {
@@ -328,6 +326,7 @@ struct TaskGenArgs {
   int ncombo;                    // quartet classes (bra pair class, ket pair class)
   int cbra[NCOMBO_MAX], cket[NCOMBO_MAX];
   int all_pairs;                 // every ordered (bra, ket) pair, else ket <= bra in one class
+  int lane_prims[NCOMBO_MAX];    // per combo: primitive quartets per lane and task (bra split)
   int square_w;                  // bound uses the squared density weight (gradient)
   const int* item_combo_start;   // ncombo+1 item offsets
   const int* cls_start;          // NPCLS+1
@@ -383,9 +382,10 @@ __global__ void k_tasks(TaskGenArgs g) {
       const int keep = count_ge(g.Q, s.x, hi, ta);
       int k64 = count_ge(g.Q, s.x, s.x + keep, t64);
       const int k32 = keep - k64;
-      // split the bra primitives so that one lane handles at most
-      // ~JK_LANE_PRIMS primitive quartets per task (bounds the launch tail)
-      const int nch0 = min(kb, (kb * s.z + JK_LANE_PRIMS - 1) / JK_LANE_PRIMS);
+      // split the bra primitives so that one lane handles at most about
+      // lane_prims primitive quartets per task (bounds the launch tail)
+      const int lp = g.lane_prims[k];
+      const int nch0 = min(kb, (kb * s.z + lp - 1) / lp);
       const int cs = (kb + nch0 - 1) / nch0;
       const int nch = (kb + cs - 1) / cs;
       if (FILL) {
@@ -522,8 +522,8 @@ static gbhf_status density_weights(gbhf_ctx* c, TaskLists& st, const double* d_d
 
 // Quartet-class task lists of TL for the combos (cbra[k], cket[k]).
 static gbhf_status build_task_lists(gbhf_ctx* c, TaskLists& TL, int ncombo, const int* cbra, const int* cket,
-                                    bool all_pairs, bool square_w, double thr_all, double thr64, const double* pw,
-                                    const double* sw) {
+                                    const int* lane_prims, bool all_pairs, bool square_w, double thr_all,
+                                    double thr64, const double* pw, const double* sw) {
   PairData& P = c->pairs;
   int* h_ranges = TL.hranges;
   std::vector<int> ics(ncombo + 1, 0);
@@ -555,6 +555,7 @@ static gbhf_status build_task_lists(gbhf_ctx* c, TaskLists& TL, int ncombo, cons
   for (int k = 0; k < NCOMBO_MAX; ++k) {
     g.cbra[k] = k < ncombo ? cbra[k] : 0;
     g.cket[k] = k < ncombo ? cket[k] : 0;
+    g.lane_prims[k] = k < ncombo ? std::max(1, lane_prims[k]) : 1;
   }
   g.all_pairs = all_pairs ? 1 : 0;
   g.square_w = square_w ? 1 : 0;
@@ -600,9 +601,16 @@ static gbhf_status build_task_lists(gbhf_ctx* c, TaskLists& TL, int ncombo, cons
 }
 
 // J/K lists: the six classes with bra class >= ket class, unique quartets.
+// lane_prims bounds the primitive quartets one lane evaluates in one task, per
+// class (ss|ss) (ps|ss) (ps|ps) (pp|ss) (pp|ps) (pp|pp): about the same
+// arithmetic per task, so that the longest task - the tail of a persistent
+// launch - stays short.  A task never splits the ket primitives, so a lane
+// always evaluates at least K_ket of them.
 static gbhf_status build_tasks(gbhf_ctx* c, double thr_all, double thr64, const double* pw = nullptr,
                                const double* sw = nullptr) {
-  return build_task_lists(c, c->tasks, NCOMBO, COMBO_BRA, COMBO_KET, false, false, thr_all, thr64, pw, sw);
+  static const int lane_prims[NCOMBO] = {256, 128, 48, 48, 16, 8};
+  return build_task_lists(c, c->tasks, NCOMBO, COMBO_BRA, COMBO_KET, lane_prims, false, false, thr_all, thr64, pw,
+                          sw);
 }
 
 gbhf_status ensure_shell_arrays(gbhf_ctx* c) {
@@ -637,7 +645,9 @@ gbhf_status build_grad_tasks(gbhf_ctx* c, const double* d_D, double cutoff, doub
   static const int gb[NCOMBO_MAX] = {0, 0, 0, 1, 1, 1, 2, 2, 2};
   static const int gk[NCOMBO_MAX] = {0, 1, 2, 0, 1, 2, 0, 1, 2};
   const double t64 = precision == GBHF_PREC_FP64 ? 0.0 : mixed_cutoff;
-  GBHF_TRY(build_task_lists(c, gt, NCOMBO_MAX, gb, gk, true, true, cutoff, t64, gt.pw.p, gt.sw.p));
+  // (bra class, ket class) of the derivative code: about twice the ERI work per primitive quartet
+  static const int lp[NCOMBO_MAX] = {128, 64, 24, 64, 24, 8, 24, 8, 4};
+  GBHF_TRY(build_task_lists(c, gt, NCOMBO_MAX, gb, gk, lp, true, true, cutoff, t64, gt.pw.p, gt.sw.p));
   return GBHF_OK;
 }
 
