@@ -44,6 +44,10 @@ bool need_basis(gbhf_ctx* c) {
     c->err = "no basis set (call gbhf_set_basis first)";
     return false;
   }
+  if (c->basis.nmol != 1) {
+    c->err = "the context holds the basis of a batch (call gbhf_set_basis first)";
+    return false;
+  }
   return true;
 }
 
@@ -268,7 +272,7 @@ gbhf_status gbhf_eigen_solve(gbhf_ctx* c, int n, const double* a_square, double*
 
 gbhf_status gbhf_sad_density(gbhf_ctx* c, double* density_flat) {
   CTX_CHECK(c);
-  if (!c->basis_dev) return fail(c, GBHF_ERR_BAD_INPUT, "no basis set");
+  if (!need_basis(c)) return GBHF_ERR_BAD_INPUT;
   if (!density_flat) return fail(c, GBHF_ERR_BAD_INPUT, "null output");
   const int n = c->basis.nbf;
   const size_t nn = (size_t)n * n, ntri = (size_t)n * (n + 1) / 2;
@@ -490,11 +494,12 @@ gbhf_status gbhf_profile_reset(gbhf_ctx* c, int enable_events) {
 gbhf_status gbhf_profile_read(gbhf_ctx* c, double* stats, int n_stats) {
   CTX_CHECK(c);
   if (!stats) return fail(c, GBHF_ERR_BAD_INPUT, "null pointer");
-  const double v[15] = {c->prof.jk_ms64,   c->prof.jk_ms32,  c->prof.prim64,        c->prof.prim32,
+  const double v[17] = {c->prof.jk_ms64,   c->prof.jk_ms32,  c->prof.prim64,        c->prof.prim32,
                         c->prof.shellq,    c->prof.fnq,      (double)c->prof.launches, c->prof.dense_ms,
                         c->prof.ph_setup,  c->prof.ph_fock,  c->prof.ph_diis,       c->prof.ph_diag,
-                        c->prof.ph_other,  c->prof.jacobi_sweeps, c->prof.jacobi_calls};
-  for (int i = 0; i < n_stats && i < 15; ++i) stats[i] = v[i];
+                        c->prof.ph_other,  c->prof.jacobi_sweeps, c->prof.jacobi_calls, c->prof.ph_grad,
+                        c->prof.batch_steps};
+  for (int i = 0; i < n_stats && i < 17; ++i) stats[i] = v[i];
   return GBHF_OK;
 }
 

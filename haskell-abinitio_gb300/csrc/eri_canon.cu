@@ -3,6 +3,8 @@
 #include <cmath>
 #include <vector>
 
+#include <algorithm>
+
 #include "gbhf_internal.h"
 #include "gbhf_md.cuh"
 
@@ -58,16 +60,25 @@ __device__ inline void os_table(double gamma, double s00, double pax, double pbx
     }
 }
 
-__global__ void k_onee(bool ref, int nbf, int natoms, const double* __restrict__ xyz, const double* __restrict__ Z,
-                       const int* __restrict__ fn, const double* __restrict__ coef, const double* __restrict__ expo,
-                       const double* __restrict__ grid, const double* __restrict__ tab, double* __restrict__ S,
-                       double* __restrict__ H) {
+// Row i (global function) pairs with the functions j >= i of its molecule;
+// nuclear attraction over that molecule's atoms.  Output: the flat upper
+// triangle of one molecule (moff == nullptr), or both triangles of the
+// molecule's block of stacked square matrices.
+__global__ void k_onee(bool ref, int nbf, const int* __restrict__ fmol, const int* __restrict__ mfo,
+                       const int* __restrict__ mao, const long long* __restrict__ moff, const double* __restrict__ xyz,
+                       const double* __restrict__ Z, const int* __restrict__ fn, const double* __restrict__ coef,
+                       const double* __restrict__ expo, const double* __restrict__ grid,
+                       const double* __restrict__ tab, double* __restrict__ S, double* __restrict__ H) {
   const int i = blockIdx.y;
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= nbf || j < i) return;
+  const int mol = fmol[i];
+  const int f0m = mfo[mol], nm = mfo[mol + 1] - f0m, a0 = mao[mol], a1 = mao[mol + 1];
+  const int il = i - f0m, jl = blockIdx.x * blockDim.x + threadIdx.x;
+  if (jl >= nm || jl < il) return;
+  const int j = f0m + jl;
   const DevFn f = load_fn(fn, i), g = load_fn(fn, j);
   const double *A = xyz + 3 * f.atom, *B = xyz + 3 * g.atom;
-  const long out = flat2_dev(nbf, i, j);
+  const long out = moff ? (long)(moff[mol] + (long long)il * nm + jl) : flat2_dev(nbf, i, j);
+  const long out_t = moff ? (long)(moff[mol] + (long long)jl * nm + il) : out;
   // overlap (sijContracted, IntegralsEvaluation.hs:181-206)
   bool same = false;
   if (ref) {
@@ -104,7 +115,7 @@ __global__ void k_onee(bool ref, int nbf, int natoms, const double* __restrict__
       s_sum += (c1 * c2) * (sx[0] * sx[1] * sx[2]);
       t_sum += c1 * c2 * (tx[0] * sx[1] * sx[2] + sx[0] * tx[1] * sx[2] + sx[0] * sx[1] * tx[2]);
       // nuclear attraction (vijHermite/mcMurchie, IntegralsEvaluation.hs:395-414)
-      for (int cn = 0; cn < natoms; ++cn) {
+      for (int cn = a0; cn < a1; ++cn) {
         const double* Cc = xyz + 3 * cn;
         const double PC[3] = {P[0] - Cc[0], P[1] - Cc[1], P[2] - Cc[2]};
         boys_generic(ref, grid, tab, L, p * (PC[0] * PC[0] + PC[1] * PC[1] + PC[2] * PC[2]), F);
@@ -118,21 +129,38 @@ __global__ void k_onee(bool ref, int nbf, int natoms, const double* __restrict__
         v_sum += (-Z[cn]) * (c1 * c2 * 2.0 * (GBHF_PI / p) * sum);
       }
     }
-  if (S) S[out] = same ? 1.0 : s_sum;
-  if (H) H[out] = t_sum + v_sum;
+  const double sv = same ? 1.0 : s_sum, hv = t_sum + v_sum;
+  if (S) S[out] = sv;
+  if (H) H[out] = hv;
+  if (moff) {
+    if (S) S[out_t] = sv;
+    if (H) H[out_t] = hv;
+  }
 }
 
-gbhf_status onee_matrices(gbhf_ctx* c, bool ref, double* d_S, double* d_H) {
+static gbhf_status onee_launch(gbhf_ctx* c, bool ref, bool stacked, double* d_S, double* d_H) {
   const Basis& b = c->basis;
   if (b.maxL > 2) return fail(c, GBHF_ERR_UNSUPPORTED, "one-electron integrals support s, p, d functions");
   if (ref && !c->have_grid) return fail(c, GBHF_ERR_BAD_INPUT, "reference mode needs gbhf_set_boys_grid");
-  dim3 grid((b.nbf + 63) / 64, b.nbf);
-  k_onee<<<grid, 64, 0, c->stream>>>(ref, b.nbf, b.natoms, c->d_xyz.p, c->d_Z.p, c->d_fn.p, c->d_coef.p,
-                                      c->d_exp.p, c->boys_ref.p, c->boys64.p, d_S, d_H);
+  if (!stacked && b.nmol != 1) return fail(c, GBHF_ERR_BAD_INPUT, "flat one-electron matrices need one molecule");
+  GBHF_TRY(ensure_shell_arrays(c));
+  int max_fn = 0;
+  for (int m = 0; m < b.nmol; ++m) max_fn = std::max(max_fn, b.mol_fn_off[m + 1] - b.mol_fn_off[m]);
+  dim3 grid((max_fn + 63) / 64, b.nbf);
+  const TaskLists& t = c->tasks;
+  k_onee<<<grid, 64, 0, c->stream>>>(ref, b.nbf, t.fmol.p, t.mfo.p, t.mao.p, stacked ? t.moff.p : nullptr,
+                                      c->d_xyz.p, c->d_Z.p, c->d_fn.p, c->d_coef.p, c->d_exp.p, c->boys_ref.p,
+                                      c->boys64.p, d_S, d_H);
   count_launch(c);
   GBHF_CUDA(c, cudaGetLastError());
   return GBHF_OK;
 }
+
+gbhf_status onee_matrices(gbhf_ctx* c, bool ref, double* d_S, double* d_H) {
+  return onee_launch(c, ref, false, d_S, d_H);
+}
+
+gbhf_status onee_stacked(gbhf_ctx* c, double* d_S, double* d_H) { return onee_launch(c, false, true, d_S, d_H); }
 
 // ------------------------------------------------- canonical ERIs ----
 // Key (i<=j | k<=l) with (i,j) <= (k,l) lexicographically <=> flat pair

@@ -124,6 +124,7 @@ struct DBuf {
 
 struct Shell {
   int atom, L, np, ncomp, f0;   // f0: first basis function (components contiguous, x,y,z order)
+  int mol = 0;                  // molecule of the shell (batched SCF); 0 for one molecule
   std::vector<double> expo, coef;
 };
 
@@ -151,6 +152,13 @@ struct Basis {
   int maxL = 0;
   bool shells_ok = false;   // every CGF grouped into a complete s or p shell
   std::string shell_msg;
+  // molecules (batched SCF): atoms [mol_atom_off[m], mol_atom_off[m+1]) and
+  // functions [mol_fn_off[m], mol_fn_off[m+1]) of molecule m; one molecule
+  // otherwise.  No shell pair or quartet spans two molecules.
+  int nmol = 1;
+  std::vector<int> mol_atom_off, mol_fn_off;
+  std::vector<long long> mol_moff;   // offset of molecule m's n_m x n_m block in a stacked matrix
+  long long stacked = 0;             // sum of n_m^2
 };
 
 // Shell-pair data on the device, in the order used by the J/K kernels:
@@ -167,6 +175,11 @@ struct PairData {
   DBuf<int4> seg_info;                       // (start, end, K, data_off) per segment, all classes
   int nseg_total = 0;
   int seg_cls_start[NPCLS + 1] = {0, 0, 0, 0};
+  // molecules: pair -> molecule, and the ket segments of (class, molecule)
+  // [mseg[2*(cls*nmol+m)], mseg[2*(cls*nmol+m)+1])
+  DBuf<int> mol;
+  DBuf<int> mseg;
+  std::vector<int> hmseg;
   // primitive-pair data: bra layout (pair-contiguous) and ket layout
   // (segment-transposed: prim k of pair j at data_off + k*len + (j-start)).
   DBuf<double> bra64, ket64;   // BRA_NFIELD arrays of length nprimpairs each
@@ -189,7 +202,13 @@ struct TaskLists {
   DBuf<int> f0;                        // first basis function per shell
   DBuf<int> nc;                        // components per shell
   DBuf<int> atom;                      // atom of each shell
-  DBuf<double> blk, row, pw, pb, sw;   // density weights (incremental builds)
+  DBuf<int> smol;                      // molecule of each shell
+  DBuf<int> mn;                        // per molecule: functions
+  DBuf<long long> moff;                // per molecule: offset of its block in stacked matrices
+  DBuf<int> fmol;                      // per function: molecule
+  DBuf<int> amol;                      // per atom: molecule
+  DBuf<int> mfo, mao;                  // per molecule: first function, first atom (nmol+1)
+  DBuf<double> row, pw, pb, sw;        // density weights (incremental builds, gradient)
   long f0_gen = -1;                    // basis generation f0 was uploaded for
 };
 
@@ -209,6 +228,7 @@ struct Profile {
   double cls[6][2][4] = {};   // per combo and precision: shell q, fn q, prim q, ms
   // host wall-clock per SCF phase (ms): setup, Fock, DIIS, diagonalisation, other; Jacobi sweeps
   double ph_setup = 0, ph_fock = 0, ph_diis = 0, ph_diag = 0, ph_other = 0, jacobi_sweeps = 0, jacobi_calls = 0;
+  double ph_grad = 0, batch_steps = 0;
 };
 
 }  // namespace gbhf
@@ -235,6 +255,7 @@ struct gbhf_ctx {
   bool pairs_ready = false;
   gbhf::TaskLists tasks;
   gbhf::TaskLists gtasks;        // gradient task lists
+  const int* mol_active = nullptr;   // batched SCF: per molecule 0/1 (device); nullptr = all
   // dense work buffers (n*n doubles)
   gbhf::DBuf<double> w[24];
   gbhf::JacobiWork jac;
@@ -302,6 +323,11 @@ inline double* ws(gbhf_ctx* c, int slot, size_t count) {
   if (!var) return gbhf::fail(ctx, GBHF_ERR_CUDA, "device allocation failed (work buffer)")
 
 // setup.cu
+// Several molecules at once: atom_off / cgf_off (nmol+1 entries) partition the
+// atoms and CGFs; cgf_atom holds global atom indices.
+gbhf_status build_basis_mols(gbhf_ctx* c, int n_atoms, const double* xyz, const double* Z, int n_cgf,
+                             const int* cgf_atom, const int* cgf_lxyz, const int* cgf_nprim, const double* coef,
+                             const double* expo, int nmol, const int* atom_off, const int* cgf_off);
 gbhf_status build_basis(gbhf_ctx* c, int n_atoms, const double* xyz, const double* Z, int n_cgf,
                         const int* cgf_atom, const int* cgf_lxyz, const int* cgf_nprim, const double* coef,
                         const double* expo);
@@ -310,6 +336,7 @@ gbhf_status ensure_pairs(gbhf_ctx* c);
 
 // onee.cu
 gbhf_status onee_matrices(gbhf_ctx* c, bool ref, double* d_S, double* d_H);   // flat (N(N+1)/2), device
+gbhf_status onee_stacked(gbhf_ctx* c, double* d_S, double* d_H);   // square blocks of every molecule (exact mode)
 // eri_canon.cu
 gbhf_status eri_canonical_dev(gbhf_ctx* c, bool ref, double* d_eri);
 gbhf_status fock_canonical_dev(gbhf_ctx* c, const double* d_H, const double* d_D, const double* d_eri, double* d_F);
@@ -347,6 +374,10 @@ gbhf_status diis_error_dev(gbhf_ctx* c, int n, const double* d_F, const double* 
 gbhf_status gauss_elem_dev_call(gbhf_ctx* c, int m, const double* h_a, const double* h_b, double* h_x, bool* ok);
 // scf.cu
 gbhf_status scf_run(gbhf_ctx* c, const gbhf_scf_opts* o, gbhf_result* r);
+// bscf.cu: the SCFs of every molecule of the context's basis (batched);
+// energies / iterations / converged per molecule, grads 3 x total atoms (or nullptr)
+gbhf_status bscf_run(gbhf_ctx* c, const gbhf_scf_opts* o, double* energies, int* iterations, int* converged,
+                     double* grads);
 // sad.cu: superposition-of-atomic-densities guess (n x n square, device)
 gbhf_status sad_density(gbhf_ctx* c, double* d_D);
 // grad.cu: D, W square on the device; gradient (3*natoms) on the device

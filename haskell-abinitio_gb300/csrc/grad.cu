@@ -81,9 +81,11 @@ struct GradArgs {
   const T* ket;
   long long npp;
   const int* shell_f0;
-  const int* shell_atom;
-  const T* D;                // n x n, this precision
-  int n;
+  const int* shell_atom;     // global atom of each shell (grad index)
+  const int* pmol;
+  const int* mn;
+  const long long* moff;
+  const T* D;                // stacked n_m x n_m densities, this precision
   const T* boys;
   double* grad;              // 3 * natoms
 };
@@ -108,7 +110,6 @@ __global__ void __launch_bounds__(GR_THREADS) k_grad_jk(GradArgs<T> a) {
   const int start = a.range[0];
   const int ntask = a.range[1] - start;
   const long long npp = a.npp;
-  const int n = a.n;
   while (true) {
     int t = 0;
     if (lane == 0) t = atomicAdd(a.counter, 1);
@@ -117,6 +118,9 @@ __global__ void __launch_bounds__(GR_THREADS) k_grad_jk(GradArgs<T> a) {
     const int4 task = a.tasks[start + t];
     const int ib = task.x;
     const int jk = task.y + lane;
+    const int mol = a.pmol[ib];
+    const int n = a.mn[mol];
+    const T* __restrict__ Dm = a.D + a.moff[mol];
     const bool active = lane < task.z;
     const int kb0 = task.w & 0xffff, Kb = (task.w >> 16) - kb0, pb0 = a.poff[ib] + kb0;
     for (int idx = lane; idx < BRA_NFIELD * Kb; idx += 32) {
@@ -125,7 +129,7 @@ __global__ void __launch_bounds__(GR_THREADS) k_grad_jk(GradArgs<T> a) {
     }
     const int A = a.pA[ib], B = a.pB[ib];
     const int a0 = a.shell_f0[A], b0 = a.shell_f0[B];
-    if (lane < NAB) sDab[warp][lane] = a.D[(long long)(a0 + lane / NB) * n + b0 + lane % NB];
+    if (lane < NAB) sDab[warp][lane] = Dm[(long long)(a0 + lane / NB) * n + b0 + lane % NB];
     __syncwarp();
     T g[6] = {0, 0, 0, 0, 0, 0};
     T wgt = 0;
@@ -142,11 +146,11 @@ __global__ void __launch_bounds__(GR_THREADS) k_grad_jk(GradArgs<T> a) {
 #pragma unroll
             for (int id = 0; id < ND; ++id) {
               const T dab = sDab[warp][ia * NB + ibb];
-              const T dcd = a.D[(long long)(c0 + ic) * n + d0 + id];
-              const T dac = a.D[(long long)(a0 + ia) * n + c0 + ic];
-              const T dbd = a.D[(long long)(b0 + ibb) * n + d0 + id];
-              const T dad = a.D[(long long)(a0 + ia) * n + d0 + id];
-              const T dbc = a.D[(long long)(b0 + ibb) * n + c0 + ic];
+              const T dcd = Dm[(long long)(c0 + ic) * n + d0 + id];
+              const T dac = Dm[(long long)(a0 + ia) * n + c0 + ic];
+              const T dbd = Dm[(long long)(b0 + ibb) * n + d0 + id];
+              const T dad = Dm[(long long)(a0 + ia) * n + d0 + id];
+              const T dbc = Dm[(long long)(b0 + ibb) * n + c0 + ic];
               gam.set(((ia * NB + ibb) * NC + ic) * ND + id, dab * dcd - T(0.25) * (dac * dbd + dad * dbc));
             }
       const int4 sg = a.seg[a.kseg[jk]];
@@ -217,8 +221,10 @@ static gbhf_status launch_grad_class(gbhf_ctx* c, cudaStream_t strm, int combo, 
   a.npp = (long long)P.nprim_pairs;
   a.shell_f0 = c->tasks.f0.p;
   a.shell_atom = c->tasks.atom.p;
+  a.pmol = P.mol.p;
+  a.mn = c->tasks.mn.p;
+  a.moff = c->tasks.moff.p;
   a.D = D;
-  a.n = c->basis.nbf;
   a.boys = boys;
   a.grad = grad;
   kern<<<grid, GR_THREADS, smem, strm>>>(a);
@@ -248,12 +254,12 @@ static gbhf_status grad_2e(gbhf_ctx* c, const double* d_D, double schwarz, doubl
                            double* d_grad) {
   GBHF_TRY(build_grad_tasks(c, d_D, schwarz, mixed_cutoff, precision));
   TaskLists& gt = c->gtasks;
-  const int n = c->basis.nbf;
+  const size_t nst = (size_t)c->basis.stacked;
   bool any32 = false;
   for (int k = 0; k < NCOMBO_MAX; ++k) any32 |= gt.hranges[4 * k + 3] > gt.hranges[4 * k + 2];
   if (any32) {
-    GBHF_CUDA(c, c->dfloat.alloc((size_t)n * n));
-    GBHF_TRY(to_float(c, (size_t)n * n, d_D, c->dfloat.p));
+    GBHF_CUDA(c, c->dfloat.alloc(nst));
+    GBHF_TRY(to_float(c, nst, d_D, c->dfloat.p));
   }
   GBHF_CUDA(c, cudaMemsetAsync(gt.counters.p, 0, 2 * NCOMBO_MAX * sizeof(int), c->stream));
   GBHF_CUDA(c, cudaEventRecord(c->fork_ev, c->stream));
@@ -291,24 +297,50 @@ static gbhf_status grad_2e(gbhf_ctx* c, const double* d_D, double schwarz, doubl
 constexpr int G1_THREADS = 64;
 constexpr int G1_SMEM_ATOMS = 2048;
 
-__global__ void __launch_bounds__(G1_THREADS) k_grad_1e(int nbf, int natoms, const double* __restrict__ xyz,
-                                                        const double* __restrict__ Z, const int* __restrict__ fn,
-                                                        const double* __restrict__ coef,
-                                                        const double* __restrict__ expo,
-                                                        const double* __restrict__ tab, const double* __restrict__ D,
-                                                        const double* __restrict__ W, double* __restrict__ grad) {
-  extern __shared__ double s_gc[];   // 3 * natoms when natoms <= G1_SMEM_ATOMS
-  const bool use_smem = natoms <= G1_SMEM_ATOMS;
+// Molecule-aware: row i (global function) pairs with the functions j >= i of
+// its molecule; D and W are the stacked n_m x n_m blocks; the operator centres
+// are the molecule's atoms.
+struct Grad1eArgs {
+  const double* xyz;
+  const double* Z;
+  const int* fn;            // per global CGF: atom (global), lx, ly, lz, np, off
+  const double* coef;
+  const double* expo;
+  const double* tab;
+  const int* fmol;          // per global CGF: molecule
+  const int* mfo;           // per molecule: first function (nmol+1)
+  const int* mao;           // per molecule: first atom (nmol+1)
+  const long long* moff;    // per molecule: block offset in D, W
+  const double* D;
+  const double* W;
+  double* grad;             // 3 * total atoms
+  int smem_atoms;           // atoms per molecule that fit the shared accumulator (0: none)
+};
+
+__global__ void __launch_bounds__(G1_THREADS) k_grad_1e(Grad1eArgs g) {
+  extern __shared__ double s_gc[];   // 3 * molecule atoms when they fit
+  const int i = blockIdx.y;
+  const int mol = g.fmol[i];
+  const int f0m = g.mfo[mol], nm = g.mfo[mol + 1] - f0m, a0 = g.mao[mol], a1 = g.mao[mol + 1];
+  const int natoms = a1 - a0;
+  const bool use_smem = natoms <= g.smem_atoms;
   if (use_smem)
     for (int k = threadIdx.x; k < 3 * natoms; k += blockDim.x) s_gc[k] = 0.0;
   __syncthreads();
-  const int i = blockIdx.y;
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j < nbf && j >= i) {
-    const DevFn f = load_fn(fn, i), gfn = load_fn(fn, j);
+  const int il = i - f0m;
+  const int jl = blockIdx.x * blockDim.x + threadIdx.x;   // local column
+  const double* __restrict__ xyz = g.xyz;
+  const double* __restrict__ Z = g.Z;
+  const double* __restrict__ coef = g.coef;
+  const double* __restrict__ expo = g.expo;
+  const double* __restrict__ tab = g.tab;
+  double* __restrict__ grad = g.grad;
+  if (jl < nm && jl >= il) {
+    const int j = f0m + jl;
+    const DevFn f = load_fn(g.fn, i), gfn = load_fn(g.fn, j);
     const double *A = xyz + 3 * f.atom, *B = xyz + 3 * gfn.atom;
     const double mult = (i == j) ? 1.0 : 2.0;
-    const double dab = mult * D[(long)i * nbf + j], wab = mult * W[(long)i * nbf + j];
+    const double dab = mult * g.D[g.moff[mol] + (long)il * nm + jl], wab = mult * g.W[g.moff[mol] + (long)il * nm + jl];
     const int L = f.l[0] + f.l[1] + f.l[2] + gfn.l[0] + gfn.l[1] + gfn.l[2] + 1;
     double ab2 = 0;
     for (int x = 0; x < 3; ++x) ab2 += (A[x] - B[x]) * (A[x] - B[x]);
@@ -379,7 +411,7 @@ __global__ void __launch_bounds__(G1_THREADS) k_grad_1e(int nbf, int natoms, con
           e_axis(E[x], f.l[x] + 1 <= 2 ? f.l[x] + 1 : 2, gfn.l[x] + 1 <= 2 ? gfn.l[x] + 1 : 2, p, P[x] - A[x],
                  P[x] - B[x], exp(-mu * abx * abx));
         }
-        for (int cn = 0; cn < natoms; ++cn) {
+        for (int cn = a0; cn < a1; ++cn) {
           const double* Cc = xyz + 3 * cn;
           const double PC[3] = {P[0] - Cc[0], P[1] - Cc[1], P[2] - Cc[2]};
           boys_generic(false, nullptr, tab, L, p * (PC[0] * PC[0] + PC[1] * PC[1] + PC[2] * PC[2]), F);
@@ -414,7 +446,7 @@ __global__ void __launch_bounds__(G1_THREADS) k_grad_1e(int nbf, int natoms, con
             vA[x] += vpref * dA[x];
             vB[x] += vpref * dB[x];
             const double gc = -vpref * (dA[x] + dB[x]);
-            if (use_smem) atomicAdd(&s_gc[3 * cn + x], gc);
+            if (use_smem) atomicAdd(&s_gc[3 * (cn - a0) + x], gc);
             else atomicAdd(&grad[3 * cn + x], gc);
           }
         }
@@ -427,16 +459,18 @@ __global__ void __launch_bounds__(G1_THREADS) k_grad_1e(int nbf, int natoms, con
   __syncthreads();
   if (use_smem)
     for (int k = threadIdx.x; k < 3 * natoms; k += blockDim.x)
-      if (s_gc[k] != 0.0) atomicAdd(&grad[k], s_gc[k]);
+      if (s_gc[k] != 0.0) atomicAdd(&grad[3 * a0 + k], s_gc[k]);
 }
 
-// Nuclear repulsion gradient, one thread per atom: -sum_L Z_K Z_L (R_K - R_L) / R_KL^3.
-__global__ void k_grad_nuc(int natoms, const double* __restrict__ xyz, const double* __restrict__ Z,
-                           double* __restrict__ grad) {
+// Nuclear repulsion gradient, one thread per atom: -sum_L Z_K Z_L (R_K - R_L) / R_KL^3
+// over the atoms L of the same molecule.
+__global__ void k_grad_nuc(int natoms, const int* __restrict__ amol, const int* __restrict__ mao,
+                           const double* __restrict__ xyz, const double* __restrict__ Z, double* __restrict__ grad) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= natoms) return;
+  const int m = amol[k];
   double g[3] = {0, 0, 0};
-  for (int l = 0; l < natoms; ++l) {
+  for (int l = mao[m]; l < mao[m + 1]; ++l) {
     if (l == k) continue;
     double d[3], r2 = 0;
     for (int x = 0; x < 3; ++x) {
@@ -458,13 +492,34 @@ gbhf_status gradient_dev(gbhf_ctx* c, const double* d_D, const double* d_W, doub
   GBHF_TRY(ensure_boys_tables(c));
   GBHF_TRY(ensure_pairs(c));
   const int n = b.nbf, na = b.natoms;
+  GBHF_TRY(ensure_shell_arrays(c));
   GBHF_CUDA(c, cudaMemsetAsync(d_grad, 0, 3 * na * sizeof(double), c->stream));
-  k_grad_nuc<<<(na + 127) / 128, 128, 0, c->stream>>>(na, c->d_xyz.p, c->d_Z.p, d_grad);
-  const size_t smem1 = na <= G1_SMEM_ATOMS ? 3 * (size_t)na * sizeof(double) : 0;
+  k_grad_nuc<<<(na + 127) / 128, 128, 0, c->stream>>>(na, c->tasks.amol.p, c->tasks.mao.p, c->d_xyz.p, c->d_Z.p,
+                                                      d_grad);
+  int max_atoms = 0, max_fn = 0;
+  for (int m = 0; m < b.nmol; ++m) {
+    max_atoms = std::max(max_atoms, b.mol_atom_off[m + 1] - b.mol_atom_off[m]);
+    max_fn = std::max(max_fn, b.mol_fn_off[m + 1] - b.mol_fn_off[m]);
+  }
+  Grad1eArgs g1;
+  g1.xyz = c->d_xyz.p;
+  g1.Z = c->d_Z.p;
+  g1.fn = c->d_fn.p;
+  g1.coef = c->d_coef.p;
+  g1.expo = c->d_exp.p;
+  g1.tab = c->boys64.p;
+  g1.fmol = c->tasks.fmol.p;
+  g1.mfo = c->tasks.mfo.p;
+  g1.mao = c->tasks.mao.p;
+  g1.moff = c->tasks.moff.p;
+  g1.D = d_D;
+  g1.W = d_W;
+  g1.grad = d_grad;
+  g1.smem_atoms = max_atoms <= G1_SMEM_ATOMS ? max_atoms : 0;
+  const size_t smem1 = 3 * (size_t)g1.smem_atoms * sizeof(double);
   if (smem1 > 48 * 1024)
     GBHF_CUDA(c, cudaFuncSetAttribute(k_grad_1e, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1));
-  k_grad_1e<<<dim3((n + G1_THREADS - 1) / G1_THREADS, n), G1_THREADS, smem1, c->stream>>>(
-      n, na, c->d_xyz.p, c->d_Z.p, c->d_fn.p, c->d_coef.p, c->d_exp.p, c->boys64.p, d_D, d_W, d_grad);
+  k_grad_1e<<<dim3((max_fn + G1_THREADS - 1) / G1_THREADS, n), G1_THREADS, smem1, c->stream>>>(g1);
   count_launch(c, 2);
   GBHF_CUDA(c, cudaGetLastError());
   GBHF_TRY(grad_2e(c, d_D, schwarz, mixed_cutoff, precision, d_grad));

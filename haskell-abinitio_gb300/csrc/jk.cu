@@ -69,10 +69,12 @@ struct JKArgs {
   const T* bra;
   const T* ket;
   long long npp;
-  const int* shell_f0;
-  const T* D;
-  int n;
-  double* G;
+  const int* shell_f0;         // first function of each shell within its molecule
+  const int* pmol;             // molecule of each pair
+  const int* mn;               // functions per molecule
+  const long long* moff;       // offset of each molecule's block in D and G
+  const T* D;                  // stacked n_m x n_m densities
+  double* G;                   // stacked n_m x n_m Fock accumulators
   const T* boys;
   unsigned long long* stats;   // [shell quartets, fn quartets, prim quartets]
 };
@@ -126,7 +128,6 @@ __global__ void __launch_bounds__(JK_THREADS) k_jk(JKArgs<T> a) {
   AccT acc;
   if constexpr (SACC) acc.p = sacc_dyn + threadIdx.x;
   const long long npp = a.npp;
-  const int n = a.n;
   while (true) {
     int t = 0;
     if (lane == 0) t = atomicAdd(a.counter, 1);
@@ -135,6 +136,11 @@ __global__ void __launch_bounds__(JK_THREADS) k_jk(JKArgs<T> a) {
     const int4 task = a.tasks[start + t];
     const int ib = task.x;
     const int jk = task.y + lane;
+    // the molecule's density and Fock blocks (stacked matrices)
+    const int mol = a.pmol[ib];
+    const int n = a.mn[mol];
+    const T* __restrict__ Dm = a.D + a.moff[mol];
+    double* __restrict__ Gm = a.G + a.moff[mol];
     const bool active = lane < task.z;
     // bra primitives [kb0, kb1) of pair ib
     const int kb0 = task.w & 0xffff, Kb = (task.w >> 16) - kb0, pb0 = a.poff[ib] + kb0;
@@ -144,7 +150,7 @@ __global__ void __launch_bounds__(JK_THREADS) k_jk(JKArgs<T> a) {
     }
     const int A = a.pA[ib], B = a.pB[ib];
     const int a0 = a.shell_f0[A], b0 = a.shell_f0[B];
-    if (lane < NAB) sDab[warp][lane] = a.D[(long long)(a0 + lane / NB) * n + b0 + lane % NB];
+    if (lane < NAB) sDab[warp][lane] = Dm[(long long)(a0 + lane / NB) * n + b0 + lane % NB];
     __syncwarp();
     acc.zero();
     int C = 0, Dd = 0, c0 = 0, d0 = 0;
@@ -185,7 +191,7 @@ __global__ void __launch_bounds__(JK_THREADS) k_jk(JKArgs<T> a) {
 #pragma unroll
     for (int ic = 0; ic < NC; ++ic)
 #pragma unroll
-      for (int id = 0; id < ND; ++id) dcd[ic * ND + id] = active ? a.D[(long long)(c0 + ic) * n + d0 + id] : T(0);
+      for (int id = 0; id < ND; ++id) dcd[ic * ND + id] = active ? Dm[(long long)(c0 + ic) * n + d0 + id] : T(0);
     // J_ab (warp reduce over kets)
 #pragma unroll
     for (int ab = 0; ab < NAB; ++ab) {
@@ -193,7 +199,7 @@ __global__ void __launch_bounds__(JK_THREADS) k_jk(JKArgs<T> a) {
 #pragma unroll
       for (int cd = 0; cd < NCD; ++cd) v = fma_t(acc.get(ab * NCD + cd), dcd[cd], v);
       v = warp_sum(T(2) * s * v);   // s depends on the lane's ket: apply before the reduction
-      if (lane == 0) atomicAdd(&a.G[(long long)(a0 + ab / NB) * n + b0 + ab % NB], double(v));
+      if (lane == 0) atomicAdd(&Gm[(long long)(a0 + ab / NB) * n + b0 + ab % NB], double(v));
     }
     if (active) {
       // J_cd
@@ -202,7 +208,7 @@ __global__ void __launch_bounds__(JK_THREADS) k_jk(JKArgs<T> a) {
         T v = 0;
 #pragma unroll
         for (int ab = 0; ab < NAB; ++ab) v = fma_t(acc.get(ab * NCD + cd), sDab[warp][ab], v);
-        atomicAdd(&a.G[(long long)(c0 + cd / ND) * n + d0 + cd % ND], double(T(2) * s * v));
+        atomicAdd(&Gm[(long long)(c0 + cd / ND) * n + d0 + cd % ND], double(T(2) * s * v));
       }
       const T ks = T(-0.5) * s;
       // K_ac -= sum_bd v D_bd ; K_ad -= sum_bc v D_bc
@@ -215,8 +221,8 @@ __global__ void __launch_bounds__(JK_THREADS) k_jk(JKArgs<T> a) {
           for (int ibb = 0; ibb < NB; ++ibb)
 #pragma unroll
             for (int id = 0; id < ND; ++id)
-              v = fma_t(acc.get((ia * NB + ibb) * NCD + ic * ND + id), a.D[(long long)(b0 + ibb) * n + d0 + id], v);
-          atomicAdd(&a.G[(long long)(a0 + ia) * n + c0 + ic], double(ks * v));
+              v = fma_t(acc.get((ia * NB + ibb) * NCD + ic * ND + id), Dm[(long long)(b0 + ibb) * n + d0 + id], v);
+          atomicAdd(&Gm[(long long)(a0 + ia) * n + c0 + ic], double(ks * v));
         }
 #pragma unroll
         for (int id = 0; id < ND; ++id) {
@@ -225,8 +231,8 @@ __global__ void __launch_bounds__(JK_THREADS) k_jk(JKArgs<T> a) {
           for (int ibb = 0; ibb < NB; ++ibb)
 #pragma unroll
             for (int ic = 0; ic < NC; ++ic)
-              v = fma_t(acc.get((ia * NB + ibb) * NCD + ic * ND + id), a.D[(long long)(b0 + ibb) * n + c0 + ic], v);
-          atomicAdd(&a.G[(long long)(a0 + ia) * n + d0 + id], double(ks * v));
+              v = fma_t(acc.get((ia * NB + ibb) * NCD + ic * ND + id), Dm[(long long)(b0 + ibb) * n + c0 + ic], v);
+          atomicAdd(&Gm[(long long)(a0 + ia) * n + d0 + id], double(ks * v));
         }
       }
       // K_bc -= sum_ad v D_ad ; K_bd -= sum_ac v D_ac
@@ -239,8 +245,8 @@ __global__ void __launch_bounds__(JK_THREADS) k_jk(JKArgs<T> a) {
           for (int ia = 0; ia < NA; ++ia)
 #pragma unroll
             for (int id = 0; id < ND; ++id)
-              v = fma_t(acc.get((ia * NB + ibb) * NCD + ic * ND + id), a.D[(long long)(a0 + ia) * n + d0 + id], v);
-          atomicAdd(&a.G[(long long)(b0 + ibb) * n + c0 + ic], double(ks * v));
+              v = fma_t(acc.get((ia * NB + ibb) * NCD + ic * ND + id), Dm[(long long)(a0 + ia) * n + d0 + id], v);
+          atomicAdd(&Gm[(long long)(b0 + ibb) * n + c0 + ic], double(ks * v));
         }
 #pragma unroll
         for (int id = 0; id < ND; ++id) {
@@ -249,8 +255,8 @@ __global__ void __launch_bounds__(JK_THREADS) k_jk(JKArgs<T> a) {
           for (int ia = 0; ia < NA; ++ia)
 #pragma unroll
             for (int ic = 0; ic < NC; ++ic)
-              v = fma_t(acc.get((ia * NB + ibb) * NCD + ic * ND + id), a.D[(long long)(a0 + ia) * n + c0 + ic], v);
-          atomicAdd(&a.G[(long long)(b0 + ibb) * n + d0 + id], double(ks * v));
+              v = fma_t(acc.get((ia * NB + ibb) * NCD + ic * ND + id), Dm[(long long)(a0 + ia) * n + c0 + ic], v);
+          atomicAdd(&Gm[(long long)(b0 + ibb) * n + d0 + id], double(ks * v));
         }
       }
     }
@@ -331,6 +337,10 @@ struct TaskGenArgs {
   const int* item_combo_start;   // ncombo+1 item offsets
   const int* cls_start;          // NPCLS+1
   const int* seg_cls_start;      // NPCLS+1
+  int nmol;
+  const int* pmol;               // molecule of each pair
+  const int* mseg;               // ket segments of (class, molecule)
+  const int* mact;               // per molecule: 1 = build its quartets (nullptr: all)
   const int4* seg;
   const double* Q;
   const int* pK;                 // primitive pairs per shell pair
@@ -363,13 +373,15 @@ __global__ void k_tasks(TaskGenArgs g) {
   while (k + 1 < g.ncombo && it >= g.item_combo_start[k + 1]) ++k;
   const int X = g.cbra[k], Y = g.cket[k];
   const int i = g.cls_start[X] + (it - g.item_combo_start[k]);
-  const double qi = g.Q[i];
+  const double qi = (g.mact && !g.mact[g.pmol[i]]) ? 0.0 : g.Q[i];   // inactive molecule: no tasks
   int n64 = 0, n32 = 0;
   int w64 = FILL ? g.off64[it] : 0, w32 = FILL ? g.off32[it] : 0;
   const double wi = g.pw ? g.pw[i] : 1.0;
   const int kb = g.pK[i];
   if (qi > 0) {
-    for (int sidx = g.seg_cls_start[Y]; sidx < g.seg_cls_start[Y + 1]; ++sidx) {
+    const int m = g.pmol[i];
+    const int s_lo = g.mseg[2 * (Y * g.nmol + m)], s_hi = g.mseg[2 * (Y * g.nmol + m) + 1];
+    for (int sidx = s_lo; sidx < s_hi; ++sidx) {
       const int4 s = g.seg[sidx];
       // bound of (bra|ket) contributions: Q_bra Q_ket max(w_bra, max w over the ket segment)
       double w = g.pw ? fmax(wi, g.sw[sidx]) : 1.0;
@@ -449,37 +461,47 @@ __global__ void k_ranges(int ncombo, const int* item_combo_start, const int* off
   ranges[4 * k + 3] = off32[item_combo_start[k + 1]];
 }
 
-// Density weights for incremental builds: per shell-pair block max |dD|, per
-// shell row max, per pair w = max(block, row A, row B), per ket segment the
-// max block weight of its pairs.
-__global__ void k_block_max(int ns, const int* __restrict__ f0, const int* __restrict__ nc,
-                            const double* __restrict__ D, int n, double* __restrict__ blk) {
-  const int A = blockIdx.y, B = blockIdx.x * blockDim.x + threadIdx.x;
-  if (B >= ns) return;
-  double m = 0;
-  for (int a = 0; a < nc[A]; ++a)
-    for (int b = 0; b < nc[B]; ++b) m = fmax(m, fabs(D[(long)(f0[A] + a) * n + f0[B] + b]));
-  blk[(long)A * ns + B] = m;
-}
-
-__global__ void k_row_max(int ns, const double* __restrict__ blk, double* __restrict__ row) {
-  const int A = blockIdx.x * blockDim.x + threadIdx.x;
-  if (A >= ns) return;
-  double m = 0;
-  for (int B = 0; B < ns; ++B) m = fmax(m, blk[(long)A * ns + B]);
-  row[A] = m;
+// Density weights for incremental builds and the gradient: per shell its row
+// maximum of |D| over its molecule's functions, per pair w = max(block max of
+// the pair, row A, row B) and the block max alone, per ket segment the largest
+// block max of its pairs.
+__global__ void k_shell_rowmax(int ns, const int* __restrict__ f0, const int* __restrict__ nc,
+                               const int* __restrict__ smol, const int* __restrict__ mn,
+                               const long long* __restrict__ moff, const double* __restrict__ D,
+                               double* __restrict__ row) {
+  const int s = blockIdx.x;
+  if (s >= ns) return;
+  const int m = smol[s], n = mn[m];
+  const double* Dm = D + moff[m];
+  double v = 0;
+  for (int a = 0; a < nc[s]; ++a)
+    for (int j = threadIdx.x; j < n; j += blockDim.x) v = fmax(v, fabs(Dm[(long)(f0[s] + a) * n + j]));
+  __shared__ double sh[32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) v = fmax(v, sh[w]);
+    row[s] = v;
+  }
 }
 
 // A quartet (AB|CD) feeds J_AB (dD_CD), J_CD (dD_AB) and K_AC, K_AD, K_BC, K_BD
 // (dD_BD, dD_BC, dD_AD, dD_AC); every exchange block holds a bra shell, so
 // max(pw[bra], pb[ket]) bounds all six density factors.
-__global__ void k_pair_weight(int np, int ns, const int* __restrict__ pA, const int* __restrict__ pB,
-                              const double* __restrict__ blk, const double* __restrict__ row, double* __restrict__ pw,
+__global__ void k_pair_weight(int np, const int* __restrict__ pA, const int* __restrict__ pB,
+                              const int* __restrict__ pmol, const int* __restrict__ f0, const int* __restrict__ nc,
+                              const int* __restrict__ mn, const long long* __restrict__ moff,
+                              const double* __restrict__ D, const double* __restrict__ row, double* __restrict__ pw,
                               double* __restrict__ pb) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= np) return;
-  const int A = pA[p], B = pB[p];
-  const double b = blk[(long)A * ns + B];
+  const int A = pA[p], B = pB[p], m = pmol[p], n = mn[m];
+  const double* Dm = D + moff[m];
+  double b = 0;
+  for (int x = 0; x < nc[A]; ++x)
+    for (int y = 0; y < nc[B]; ++y) b = fmax(b, fabs(Dm[(long)(f0[A] + x) * n + f0[B] + y]));
   pw[p] = fmax(b, fmax(row[A], row[B]));
   pb[p] = b;
 }
@@ -503,19 +525,17 @@ __global__ void k_seg_max(int nseg, const int4* __restrict__ seg, const double* 
 
 static gbhf_status density_weights(gbhf_ctx* c, TaskLists& st, const double* d_dD) {
   PairData& P = c->pairs;
-  const int ns = (int)c->basis.shells.size(), n = c->basis.nbf;
-  GBHF_CUDA(c, st.blk.alloc((size_t)ns * ns));
+  const TaskLists& sh = c->tasks;   // per-shell and per-molecule arrays
+  const int ns = (int)c->basis.shells.size();
   GBHF_CUDA(c, st.row.alloc(ns));
   GBHF_CUDA(c, st.pw.alloc(std::max(P.npairs, 1)));
   GBHF_CUDA(c, st.pb.alloc(std::max(P.npairs, 1)));
   GBHF_CUDA(c, st.sw.alloc(std::max(P.nseg_total, 1)));
-  const TaskLists& sh = c->tasks;   // per-shell arrays
-  k_block_max<<<dim3((ns + 127) / 128, ns), 128, 0, c->stream>>>(ns, sh.f0.p, sh.nc.p, d_dD, n, st.blk.p);
-  k_row_max<<<(ns + 127) / 128, 128, 0, c->stream>>>(ns, st.blk.p, st.row.p);
-  k_pair_weight<<<(P.npairs + 127) / 128, 128, 0, c->stream>>>(P.npairs, ns, P.A.p, P.B.p, st.blk.p, st.row.p,
-                                                               st.pw.p, st.pb.p);
+  k_shell_rowmax<<<ns, 128, 0, c->stream>>>(ns, sh.f0.p, sh.nc.p, sh.smol.p, sh.mn.p, sh.moff.p, d_dD, st.row.p);
+  k_pair_weight<<<(P.npairs + 127) / 128, 128, 0, c->stream>>>(P.npairs, P.A.p, P.B.p, P.mol.p, sh.f0.p, sh.nc.p,
+                                                               sh.mn.p, sh.moff.p, d_dD, st.row.p, st.pw.p, st.pb.p);
   if (P.nseg_total > 0) k_seg_max<<<P.nseg_total, 256, 0, c->stream>>>(P.nseg_total, P.seg_info.p, st.pb.p, st.sw.p);
-  count_launch(c, 4);
+  count_launch(c, 3);
   GBHF_CUDA(c, cudaGetLastError());
   return GBHF_OK;
 }
@@ -565,6 +585,10 @@ static gbhf_status build_task_lists(gbhf_ctx* c, TaskLists& TL, int ncombo, cons
   g.seg = P.seg_info.p;
   g.Q = P.Q.p;
   g.pK = P.K.p;
+  g.nmol = c->basis.nmol;
+  g.pmol = P.mol.p;
+  g.mseg = P.mseg.p;
+  g.mact = c->mol_active;
   g.thr_all = thr_all;
   g.thr64 = thr64;
   g.pw = pw;
@@ -616,19 +640,44 @@ static gbhf_status build_tasks(gbhf_ctx* c, double thr_all, double thr64, const 
 gbhf_status ensure_shell_arrays(gbhf_ctx* c) {
   TaskLists& st = c->tasks;
   if (st.f0_gen == c->basis_gen) return GBHF_OK;
-  const size_t ns = c->basis.shells.size();
-  std::vector<int> f0(ns), nc(ns), at(ns);
+  const Basis& b = c->basis;
+  const size_t ns = b.shells.size();
+  std::vector<int> f0(ns), nc(ns), at(ns), sm(ns);
   for (size_t s = 0; s < ns; ++s) {
-    f0[s] = c->basis.shells[s].f0;
-    nc[s] = c->basis.shells[s].ncomp;
-    at[s] = c->basis.shells[s].atom;
+    f0[s] = b.shells[s].f0 - b.mol_fn_off[b.shells[s].mol];   // first function within its molecule
+    nc[s] = b.shells[s].ncomp;
+    at[s] = b.shells[s].atom;
+    sm[s] = b.shells[s].mol;
+  }
+  std::vector<int> mn(b.nmol), fmol(b.nbf), amol(b.natoms);
+  for (int m = 0; m < b.nmol; ++m) {
+    mn[m] = b.mol_fn_off[m + 1] - b.mol_fn_off[m];
+    for (int i = b.mol_fn_off[m]; i < b.mol_fn_off[m + 1]; ++i) fmol[i] = m;
+    for (int a = b.mol_atom_off[m]; a < b.mol_atom_off[m + 1]; ++a) amol[a] = m;
   }
   GBHF_CUDA(c, st.f0.alloc(ns));
   GBHF_CUDA(c, st.nc.alloc(ns));
   GBHF_CUDA(c, st.atom.alloc(ns));
+  GBHF_CUDA(c, st.smol.alloc(ns));
+  GBHF_CUDA(c, st.mn.alloc(b.nmol));
+  GBHF_CUDA(c, st.moff.alloc(b.nmol + 1));
+  GBHF_CUDA(c, st.fmol.alloc(b.nbf));
+  GBHF_CUDA(c, st.amol.alloc(b.natoms));
+  GBHF_CUDA(c, st.mfo.alloc(b.nmol + 1));
+  GBHF_CUDA(c, st.mao.alloc(b.nmol + 1));
   GBHF_CUDA(c, cudaMemcpyAsync(st.f0.p, f0.data(), ns * sizeof(int), cudaMemcpyHostToDevice, c->stream));
   GBHF_CUDA(c, cudaMemcpyAsync(st.nc.p, nc.data(), ns * sizeof(int), cudaMemcpyHostToDevice, c->stream));
   GBHF_CUDA(c, cudaMemcpyAsync(st.atom.p, at.data(), ns * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  GBHF_CUDA(c, cudaMemcpyAsync(st.smol.p, sm.data(), ns * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  GBHF_CUDA(c, cudaMemcpyAsync(st.mn.p, mn.data(), b.nmol * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  GBHF_CUDA(c, cudaMemcpyAsync(st.moff.p, b.mol_moff.data(), (b.nmol + 1) * sizeof(long long),
+                               cudaMemcpyHostToDevice, c->stream));
+  GBHF_CUDA(c, cudaMemcpyAsync(st.fmol.p, fmol.data(), b.nbf * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  GBHF_CUDA(c, cudaMemcpyAsync(st.amol.p, amol.data(), b.natoms * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  GBHF_CUDA(c, cudaMemcpyAsync(st.mfo.p, b.mol_fn_off.data(), (b.nmol + 1) * sizeof(int), cudaMemcpyHostToDevice,
+                               c->stream));
+  GBHF_CUDA(c, cudaMemcpyAsync(st.mao.p, b.mol_atom_off.data(), (b.nmol + 1) * sizeof(int), cudaMemcpyHostToDevice,
+                               c->stream));
   GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
   st.f0_gen = c->basis_gen;
   return GBHF_OK;
@@ -682,8 +731,10 @@ static gbhf_status launch_class(gbhf_ctx* c, cudaStream_t strm, int combo, int p
   a.ket = ket;
   a.npp = (long long)P.nprim_pairs;
   a.shell_f0 = f0;
+  a.pmol = P.mol.p;
+  a.mn = c->tasks.mn.p;
+  a.moff = c->tasks.moff.p;
   a.D = D;
-  a.n = c->basis.nbf;
   a.G = G;
   a.boys = boys;
   a.stats = c->tasks.stats.p + 3 * (2 * combo + prec);
@@ -721,8 +772,9 @@ gbhf_status jk_build(gbhf_ctx* c, const double* d_Dsq, double* d_G, int precisio
   bool any32 = false;
   for (int k = 0; k < NCOMBO; ++k) any32 |= st.hranges[4 * k + 3] > st.hranges[4 * k + 2];
   if (any32) {
-    GBHF_CUDA(c, c->dfloat.alloc((size_t)n * n));
-    GBHF_TRY(to_float(c, (size_t)n * n, d_Dsq, c->dfloat.p));
+    const size_t nst = (size_t)c->basis.stacked;   // all molecules' blocks
+    GBHF_CUDA(c, c->dfloat.alloc(nst));
+    GBHF_TRY(to_float(c, nst, d_Dsq, c->dfloat.p));
   }
   PairData& P = c->pairs;
   const int* f0 = st.f0.p;

@@ -5,6 +5,7 @@
 #include <vector>
 
 #include "gbhf_internal.h"
+#include "dense.cuh"
 #include "jacobi.cuh"
 
 namespace gbhf {
@@ -15,11 +16,6 @@ namespace gbhf {
 // each warp a 4x4 grid of 8x8 DMMA tiles, k-step 16.
 constexpr int GT = 64, GK = 16;
 
-__device__ __forceinline__ void dmma(double& d0, double& d1, double a, double b) {
-  asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0,%1}, {%2}, {%3}, {%0,%1};\n"
-               : "+d"(d0), "+d"(d1)
-               : "d"(a), "d"(b));
-}
 
 __global__ void __launch_bounds__(128) k_dgemm(bool ta, bool tb, int m, int n, int k, double alpha,
                                                const double* __restrict__ A, int lda, const double* __restrict__ B,
@@ -278,28 +274,6 @@ gbhf_status to_float(gbhf_ctx* c, size_t n, const double* d_x, float* d_y) {
 }
 
 // Block reduction helper (sum or max) into a double.
-__device__ __forceinline__ double block_reduce(double v, bool is_max) {
-  __shared__ double sh[32];
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    double w = __shfl_xor_sync(0xffffffffu, v, o);
-    v = is_max ? fmax(v, w) : v + w;
-  }
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  __syncthreads();
-  if (lane == 0) sh[wid] = v;
-  __syncthreads();
-  const int nw = (blockDim.x + 31) / 32;
-  v = threadIdx.x < nw ? sh[threadIdx.x] : (is_max ? 0.0 : 0.0);
-  if (wid == 0) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      double w = __shfl_xor_sync(0xffffffffu, v, o);
-      v = is_max ? fmax(v, w) : v + w;
-    }
-  }
-  return v;
-}
 
 // out[0] = max|e|, out[1] = 1/2 sum Dnew(H+F) (when H,F given), out[2] = sum (Dnew-Dold)^2,
 // out[3] = sum(D (H + F)) with Dold.  Single block.
@@ -402,34 +376,6 @@ gbhf_status lincomb(gbhf_ctx* c, int n2, int k, const double* const* mats, const
   return GBHF_OK;
 }
 
-// gaussElem (NumericalTools/GaussElimination.hs:42-98), single thread: unpivoted
-// elimination over all pivots, failure when a row of the eliminated matrix has
-// no |entry| > 1e-6 or any entry is NaN/Inf, then back substitution.
-__device__ bool gauss_elem_dev(int m, double* a, double* b, double* x) {
-  for (int k = 0; k < m; ++k) {
-    const double piv = a[k * m + k];
-    for (int i = k + 1; i < m; ++i) {
-      const double alpha = a[i * m + k] / piv;
-      for (int j = m - 1; j >= k; --j) a[i * m + j] = a[i * m + j] - alpha * a[k * m + j];
-      b[i] = b[i] - alpha * b[k];
-    }
-  }
-  for (int i = 0; i < m; ++i) {
-    bool any = false;
-    for (int j = 0; j < m; ++j) {
-      const double v = a[i * m + j];
-      if (isnan(v) || isinf(v)) return false;
-      if (fabs(v) > 1e-6) any = true;
-    }
-    if (!any) return false;
-  }
-  for (int k = m - 1; k >= 0; --k) {
-    double s = 0;
-    for (int j = k + 1; j < m; ++j) s += x[j] * a[k * m + j];
-    x[k] = (b[k] - s) * (1.0 / a[k * m + k]);
-  }
-  return true;
-}
 
 // Note: the reference evaluates alpha = mtx[i][k]/mtx[k][k] from the matrix
 // before the pivot step for every j; updating j from m-1 down to k keeps

@@ -8,6 +8,7 @@
 // RHF of the single atom is run once on the device (stored ERIs, Jacobi
 // eigen-solve) and cached in the context; the molecular guess is the
 // block-diagonal assembly of those atomic densities.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -25,16 +26,21 @@ __global__ void k_sad_scale_cols(int n, const double* __restrict__ C, const doub
   out[(long)i * n + j] = C[(long)i * n + j] * occ[j];
 }
 
+// Row i (global function) of its molecule's block of the stacked densities:
 // D[i][j] = block of atom(i) at (loc(i), loc(j)) when atom(i) == atom(j), else 0.
-__global__ void k_sad_assemble(int n, const int* __restrict__ fatom, const int* __restrict__ floc,
-                               const int* __restrict__ boff, const int* __restrict__ bdim,
-                               const double* __restrict__ blocks, double* __restrict__ D) {
-  const int i = blockIdx.y, j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= n) return;
-  const int a = fatom[i];
+__global__ void k_sad_assemble(const int* __restrict__ fmol, const int* __restrict__ mfo,
+                               const long long* __restrict__ moff, const int* __restrict__ fatom,
+                               const int* __restrict__ floc, const int* __restrict__ boff,
+                               const int* __restrict__ bdim, const double* __restrict__ blocks,
+                               double* __restrict__ D) {
+  const int i = blockIdx.y;
+  const int m = fmol[i], f0 = mfo[m], n = mfo[m + 1] - f0;
+  const int jl = blockIdx.x * blockDim.x + threadIdx.x;
+  if (jl >= n) return;
+  const int j = f0 + jl, a = fatom[i];
   double v = 0.0;
   if (fatom[j] == a) v = blocks[boff[a] + floc[i] * bdim[a] + floc[j]];
-  D[(long)i * n + j] = v;
+  D[moff[m] + (long long)(i - f0) * n + jl] = v;
 }
 
 // Key of atom a: nuclear charge and its functions (Cartesian exponents,
@@ -44,7 +50,9 @@ static std::string atom_key(const Basis& b, int a, std::vector<int>& fns) {
   std::string k;
   auto put = [&](const void* p, size_t s) { k.append(static_cast<const char*>(p), s); };
   put(&b.Z[a], sizeof(double));
-  for (int i = 0; i < b.nbf; ++i) {
+  int m = 0;
+  while (m + 1 < b.nmol && a >= b.mol_atom_off[m + 1]) ++m;
+  for (int i = b.mol_fn_off[m]; i < b.mol_fn_off[m + 1]; ++i) {
     if (b.cgf_atom[i] != a) continue;
     fns.push_back(i);
     put(&b.cgf_lxyz[3 * i], 3 * sizeof(int));
@@ -155,6 +163,7 @@ static gbhf_status atomic_density(gbhf_ctx* c, gbhf_ctx* sub, const Basis& b, in
   return GBHF_OK;
 }
 
+// Stacked blocks of every molecule of the context's basis (one block for one molecule).
 gbhf_status sad_density(gbhf_ctx* c, double* d_D) {
   const Basis& b = c->basis;
   const int n = b.nbf;
@@ -200,7 +209,11 @@ gbhf_status sad_density(gbhf_ctx* c, double* d_D) {
   GBHF_CUDA(c, cudaMemcpyAsync(dbd.p, bdim.data(), b.natoms * sizeof(int), cudaMemcpyHostToDevice, c->stream));
   GBHF_CUDA(c, cudaMemcpyAsync(dbl.p, blocks.data(), blocks.size() * sizeof(double), cudaMemcpyHostToDevice,
                                c->stream));
-  k_sad_assemble<<<dim3((n + 127) / 128, n), 128, 0, c->stream>>>(n, dfa.p, dfl.p, dbo.p, dbd.p, dbl.p, d_D);
+  GBHF_TRY(ensure_shell_arrays(c));
+  int max_fn = 0;
+  for (int m = 0; m < b.nmol; ++m) max_fn = std::max(max_fn, b.mol_fn_off[m + 1] - b.mol_fn_off[m]);
+  k_sad_assemble<<<dim3((max_fn + 127) / 128, n), 128, 0, c->stream>>>(
+      c->tasks.fmol.p, c->tasks.mfo.p, c->tasks.moff.p, dfa.p, dfl.p, dbo.p, dbd.p, dbl.p, d_D);
   count_launch(c);
   GBHF_CUDA(c, cudaGetLastError());
   // the staging buffers are freed on return: finish the copies and the kernel

@@ -83,6 +83,7 @@ struct Hist {
 gbhf_status scf_run(gbhf_ctx* c, const gbhf_scf_opts* o, gbhf_result* r) {
   const Basis& b = c->basis;
   if (!c->basis_dev) return fail(c, GBHF_ERR_BAD_INPUT, "gbhf_scf: no basis set");
+  if (b.nmol != 1) return fail(c, GBHF_ERR_BAD_INPUT, "gbhf_scf: the context holds a batch; call gbhf_set_basis");
   const int n = b.nbf;
   const size_t nn = (size_t)n * n, ntri = (size_t)n * (n + 1) / 2;
   const bool ref = o->mode == GBHF_MODE_REFERENCE;

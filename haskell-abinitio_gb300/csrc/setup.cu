@@ -71,11 +71,36 @@ static void group_shells(Basis& b) {
 
 gbhf_status build_basis(gbhf_ctx* c, int n_atoms, const double* xyz, const double* Z, int n_cgf, const int* cgf_atom,
                         const int* cgf_lxyz, const int* cgf_nprim, const double* coef, const double* expo) {
+  const int aoff[2] = {0, n_atoms}, foff[2] = {0, n_cgf};
+  return build_basis_mols(c, n_atoms, xyz, Z, n_cgf, cgf_atom, cgf_lxyz, cgf_nprim, coef, expo, 1, aoff, foff);
+}
+
+gbhf_status build_basis_mols(gbhf_ctx* c, int n_atoms, const double* xyz, const double* Z, int n_cgf,
+                             const int* cgf_atom, const int* cgf_lxyz, const int* cgf_nprim, const double* coef,
+                             const double* expo, int nmol, const int* atom_off, const int* cgf_off) {
   if (n_atoms <= 0 || n_cgf <= 0 || !xyz || !Z || !cgf_atom || !cgf_lxyz || !cgf_nprim || !coef || !expo)
     return fail(c, GBHF_ERR_BAD_INPUT, "gbhf_set_basis: empty basis or null pointer");
+  if (nmol < 1 || !atom_off || !cgf_off || atom_off[0] != 0 || cgf_off[0] != 0 || atom_off[nmol] != n_atoms ||
+      cgf_off[nmol] != n_cgf)
+    return fail(c, GBHF_ERR_BAD_INPUT, "molecule partition does not cover the atoms and functions");
   Basis b;
   b.natoms = n_atoms;
   b.nbf = n_cgf;
+  b.nmol = nmol;
+  b.mol_atom_off.assign(atom_off, atom_off + nmol + 1);
+  b.mol_fn_off.assign(cgf_off, cgf_off + nmol + 1);
+  b.mol_moff.resize(nmol + 1);
+  b.mol_moff[0] = 0;
+  for (int m = 0; m < nmol; ++m) {
+    const int a0 = atom_off[m], a1 = atom_off[m + 1], f0 = cgf_off[m], f1 = cgf_off[m + 1];
+    if (a1 <= a0 || f1 <= f0)
+      return fail(c, GBHF_ERR_BAD_INPUT, "molecule " + std::to_string(m) + " has no atoms or no functions");
+    for (int i = f0; i < f1; ++i)
+      if (cgf_atom[i] < a0 || cgf_atom[i] >= a1)
+        return fail(c, GBHF_ERR_BAD_INPUT, "a CGF of molecule " + std::to_string(m) + " sits on another molecule's atom");
+    b.mol_moff[m + 1] = b.mol_moff[m] + (long long)(f1 - f0) * (f1 - f0);
+  }
+  b.stacked = b.mol_moff[nmol];
   b.xyz.assign(xyz, xyz + 3 * n_atoms);
   b.Z.assign(Z, Z + n_atoms);
   b.cgf_atom.assign(cgf_atom, cgf_atom + n_cgf);
@@ -104,6 +129,11 @@ gbhf_status build_basis(gbhf_ctx* c, int n_atoms, const double* xyz, const doubl
   for (int k = 0; k < 3 * n_atoms; ++k)
     if (!std::isfinite(xyz[k])) return fail(c, GBHF_ERR_BAD_INPUT, "gbhf_set_basis: non-finite coordinate");
   group_shells(b);
+  for (auto& sh : b.shells) {
+    int m = 0;
+    while (m + 1 < nmol && sh.f0 >= cgf_off[m + 1]) ++m;
+    sh.mol = m;
+  }
   c->basis = std::move(b);
   const Basis& B = c->basis;
   // device copies (function level)
@@ -232,16 +262,21 @@ gbhf_status ensure_pairs(gbhf_ctx* c) {
                 "direct J/K kernels need complete s/p shells: " + (b.shell_msg.empty() ? std::string("d functions present") : b.shell_msg));
   GBHF_TRY(ensure_boys_tables(c));
   const int ns = (int)b.shells.size();
-  // 1. all pairs (la > lb, or la == lb and A >= B)
+  // 1. all pairs (la > lb, or la == lb and A >= B) of shells of one molecule
   std::vector<int> A, B;
-  for (int a = 0; a < ns; ++a)
-    for (int bb = 0; bb < ns; ++bb) {
-      const int la = b.shells[a].L, lb = b.shells[bb].L;
-      if (la > lb || (la == lb && a >= bb)) {
-        A.push_back(a);
-        B.push_back(bb);
+  for (int s0 = 0; s0 < ns;) {
+    int s1 = s0;
+    while (s1 < ns && b.shells[s1].mol == b.shells[s0].mol) ++s1;
+    for (int a = s0; a < s1; ++a)
+      for (int bb = s0; bb < s1; ++bb) {
+        const int la = b.shells[a].L, lb = b.shells[bb].L;
+        if (la > lb || (la == lb && a >= bb)) {
+          A.push_back(a);
+          B.push_back(bb);
+        }
       }
-    }
+    s0 = s1;
+  }
   const int np = (int)A.size();
   // 2. Schwarz bounds on the device, pairs grouped by class (class code, FP64)
   std::vector<double> Q(np);
@@ -285,14 +320,16 @@ gbhf_status ensure_pairs(gbhf_ctx* c) {
     GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
     for (int t = 0; t < np; ++t) Q[ord0[t]] = Q0[t];
   }
-  // 3. order: class, then primitive-pair count descending, then Q descending
+  // 3. order: class, molecule, primitive-pair count descending, Q descending
   std::vector<int> order(np);
   std::iota(order.begin(), order.end(), 0);
   auto K_of = [&](int t) { return b.shells[A[t]].np * b.shells[B[t]].np; };
   auto cls_of = [&](int t) { return pair_class(b.shells[A[t]].L, b.shells[B[t]].L); };
+  auto mol_of = [&](int t) { return b.shells[A[t]].mol; };
   std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
     int cx = cls_of(x), cy = cls_of(y);
     if (cx != cy) return cx < cy;
+    if (mol_of(x) != mol_of(y)) return mol_of(x) < mol_of(y);
     int kx = K_of(x), ky = K_of(y);
     if (kx != ky) return kx > ky;
     if (Q[x] != Q[y]) return Q[x] > Q[y];
@@ -320,7 +357,8 @@ gbhf_status ensure_pairs(gbhf_ctx* c) {
     const int cl = cls_of(o);
     if (P.cls_start[cl] == np) P.cls_start[cl] = t;
     auto& sg = P.segs[cl];
-    if (sg.empty() || sg.back().K != P.hK[t]) sg.push_back({t, t + 1, P.hK[t], 0});
+    if (sg.empty() || sg.back().K != P.hK[t] || mol_of(order[sg.back().start]) != mol_of(o))
+      sg.push_back({t, t + 1, P.hK[t], 0});
     else sg.back().end = t + 1;
   }
   for (int cl = NPCLS - 1; cl >= 0; --cl)
@@ -340,6 +378,20 @@ gbhf_status ensure_pairs(gbhf_ctx* c) {
   }
   P.seg_cls_start[NPCLS] = (int)seginfo.size();
   P.nseg_total = (int)seginfo.size();
+  // segments of each (class, molecule); empty ranges for absent classes
+  const int nmol = b.nmol;
+  P.hmseg.assign(2 * (size_t)NPCLS * nmol, 0);
+  for (int cl = 0; cl < NPCLS; ++cl)
+    for (int m = 0; m < nmol; ++m) P.hmseg[2 * (cl * nmol + m)] = P.hmseg[2 * (cl * nmol + m) + 1] = P.seg_cls_start[cl];
+  for (int cl = 0; cl < NPCLS; ++cl)
+    for (int sidx = P.seg_cls_start[cl]; sidx < P.seg_cls_start[cl + 1]; ++sidx) {
+      const int m = b.shells[P.hA[seginfo[sidx].x]].mol;
+      int* r = &P.hmseg[2 * (cl * nmol + m)];
+      if (r[1] == r[0]) r[0] = sidx;
+      r[1] = sidx + 1;
+    }
+  std::vector<int> pmol(np);
+  for (int t = 0; t < np; ++t) pmol[t] = b.shells[P.hA[t]].mol;
   // 4. primitive-pair data
   const size_t npp = poff;
   std::vector<double> bra((size_t)BRA_NFIELD * npp), ket((size_t)BRA_NFIELD * npp);
@@ -366,6 +418,8 @@ gbhf_status ensure_pairs(gbhf_ctx* c) {
   GBHF_CUDA(c, P.kseg.alloc(np));
   GBHF_CUDA(c, P.Q.alloc(np));
   GBHF_CUDA(c, P.seg_info.alloc(seginfo.size()));
+  GBHF_CUDA(c, P.mol.alloc(np));
+  GBHF_CUDA(c, P.mseg.alloc(P.hmseg.size()));
   GBHF_CUDA(c, P.bra64.alloc(bra.size()));
   GBHF_CUDA(c, P.ket64.alloc(ket.size()));
   GBHF_CUDA(c, P.bra32.alloc(bra.size()));
@@ -380,6 +434,8 @@ gbhf_status ensure_pairs(gbhf_ctx* c) {
   GBHF_CUDA(c, up(P.kseg.p, P.hSeg.data(), np * sizeof(int)));
   GBHF_CUDA(c, up(P.Q.p, P.hQ.data(), np * sizeof(double)));
   GBHF_CUDA(c, up(P.seg_info.p, seginfo.data(), seginfo.size() * sizeof(int4)));
+  GBHF_CUDA(c, up(P.mol.p, pmol.data(), np * sizeof(int)));
+  GBHF_CUDA(c, up(P.mseg.p, P.hmseg.data(), P.hmseg.size() * sizeof(int)));
   GBHF_CUDA(c, up(P.bra64.p, bra.data(), bra.size() * sizeof(double)));
   GBHF_CUDA(c, up(P.ket64.p, ket.data(), ket.size() * sizeof(double)));
   GBHF_CUDA(c, up(P.bra32.p, bra32.data(), bra32.size() * sizeof(float)));

@@ -333,6 +333,8 @@ class Context:
         s = self.L.gbhf_scf_batch(self.h, nm, _i(arrs[0]), _i(arrs[1]), _d(arrs[2]), _d(arrs[3]), _i(arrs[4]),
                                   _i(arrs[5]), _i(arrs[6]), _d(arrs[7]), _d(arrs[8]), C.byref(opts), _d(e), _i(it),
                                   _i(cv), _d(g) if gradients else None)
+        self.n = 0          # the context now holds the batch's basis
+        self._keep = None
         self._check(s)
         grads = [g[3 * ao[k]:3 * ao[k + 1]].reshape(-1, 3) for k in range(nm)] if gradients else None
         return e, it, cv.astype(bool), grads
@@ -354,11 +356,11 @@ class Context:
         self._check(self.L.gbhf_profile_reset(self.h, 1 if events else 0))
 
     def profile_read(self):
-        v = np.zeros(15)
-        self._check(self.L.gbhf_profile_read(self.h, _d(v), 15))
+        v = np.zeros(17)
+        self._check(self.L.gbhf_profile_read(self.h, _d(v), 17))
         keys = ("jk_ms_fp64", "jk_ms_fp32", "prim_quartets_fp64", "prim_quartets_fp32", "shell_quartets",
                 "fn_quartets", "launches", "dense_ms", "ms_setup", "ms_fock", "ms_diis", "ms_diag", "ms_other",
-                "jacobi_sweeps", "jacobi_calls")
+                "jacobi_sweeps", "jacobi_calls", "ms_grad", "batch_steps")
         return dict(zip(keys, v.tolist()))
 
     CLASSES = ("ssss", "psss", "psps", "ppss", "ppps", "pppp")

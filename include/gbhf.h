@@ -230,11 +230,12 @@ gbhf_status gbhf_scf_batch(gbhf_ctx* ctx, int n_mol, const int* atom_off, const 
 
 /* Measurement hooks: device-time of the J/K kernels since the last reset
  * (CUDA events on the context stream), launches issued by the library, and
- * per-kernel-class statistics.  stats[0..14]: J/K milliseconds FP64, FP32,
+ * per-kernel-class statistics.  stats[0..16]: J/K milliseconds FP64, FP32,
  * primitive quartets FP64, FP32, shell quartets, function quartets,
  * total library kernel launches, dense linear-algebra milliseconds, then
  * host wall milliseconds of the SCF phases (setup, Fock, DIIS,
- * diagonalisation, other), Jacobi sweeps and Jacobi calls. */
+ * diagonalisation, other), Jacobi sweeps and Jacobi calls, milliseconds of
+ * the batched gradients, steps of the last batched SCF. */
 gbhf_status gbhf_profile_reset(gbhf_ctx* ctx, int enable_events);
 gbhf_status gbhf_profile_read(gbhf_ctx* ctx, double* stats, int n_stats);
 /* Per ERI class (ss|ss, ps|ss, ps|ps, pp|ss, pp|ps, pp|pp) and precision
