@@ -297,7 +297,8 @@ def run_batch(args, world, rank, local):
     flats = [B.flatten(a) for a in mols]
     mine = replicas.shard([f.n_cgf ** 4 for f in flats], world, rank)
     sub = [flats[i] for i in mine]
-    mixed = _lib.baseline_opts(precision=_lib.PREC_MIXED, incremental=1, final_fp64=0)
+    mixed = _lib.baseline_opts(precision=_lib.PREC_MIXED, incremental=1, final_fp64=0,
+                               mixed_cutoff=args.mixed_cutoff, grad_mixed_cutoff=args.grad_mixed_cutoff)
     ctx.scf_batch(sub[:16], mixed, gradients=True)          # warm-up (tables, SAD atoms)
     barrier(world)
     ctx.profile_reset(events=False)
@@ -306,16 +307,18 @@ def run_batch(args, world, rank, local):
     wall = time.perf_counter() - t0
     prof = ctx.profile_read()
     wall = max_over_ranks(world, wall)
-    # one-at-a-time FP64 on every 8th molecule of this rank, scaled to the shard
+    # one-at-a-time FP64 SCF + gradient on every 8th molecule of this rank, scaled to the shard
     fp64 = _lib.baseline_opts()
-    sample = list(range(0, len(sub), 8))
-    t_single, de = 0.0, []
+    sample = list(range(0, len(sub), 8)) if not args.quick else []
+    t_single, de, dg = 0.0, [], []
     for k in sample:
         t1 = time.perf_counter()
         ctx.set_basis(sub[k])
         r = ctx.scf(fp64, want_matrices=False)
+        g64 = ctx.gradient()
         t_single += time.perf_counter() - t1
         de.append(abs(r["energy"] - e[k]))
+        dg.append(float(np.max(np.abs(g64 - g[k]))))
     single_est = t_single * len(sub) / max(len(sample), 1)
     if rank != 0:
         return
@@ -326,7 +329,9 @@ def run_batch(args, world, rank, local):
             "fp64_one_at_a_time_molecules_per_s": len(sub) / single_est if single_est > 0 else None,
             "speedup_vs_fp64_one_at_a_time": single_est / wall * world if wall > 0 else None,
             "max_abs_delta_e_mixed_vs_fp64_sample": float(max(de)) if de else None,
-            "sample": f"FP64 one-at-a-time timed on {len(sample)} of {len(sub)} molecules and scaled",
+            "max_abs_grad_mixed_vs_fp64_sample": float(max(dg)) if dg else None,
+            "mixed_cutoff": args.mixed_cutoff, "grad_mixed_cutoff": args.grad_mixed_cutoff or args.mixed_cutoff,
+            "sample": f"FP64 one-at-a-time SCF + gradient timed on {len(sample)} of {len(sub)} molecules and scaled",
             "batch_steps": int(prof["batch_steps"]), "gpu_launches": int(prof["launches"]),
             "phases_ms": {k: prof[k] for k in ("ms_setup", "ms_fock", "ms_diis", "ms_diag", "ms_other", "ms_grad")},
             "jk_prim_quartets": prof["prim_quartets_fp64"] + prof["prim_quartets_fp32"],
@@ -452,6 +457,12 @@ def main():
     ap.add_argument("--workload", default="w16", choices=["w16", "batch256", "grad8", "w64", "fock"])
     ap.add_argument("--quick", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--mixed-cutoff", type=float, default=1e-2,
+                    help="batch256: Schwarz-bound cutoff below which ERIs run in FP32 (the workload leaves "
+                         "it free; 1e-2 keeps |dE| vs FP64 near 1e-8 Eh)")
+    ap.add_argument("--grad-mixed-cutoff", type=float, default=1.0,
+                    help="batch256: the same for derivative ERIs (1.0 keeps the gradient within ~1e-6 "
+                         "Eh/bohr of FP64; 0: --mixed-cutoff)")
     args = ap.parse_args()
     world, rank, local = dist_setup()
     if args.impl == "reference":

@@ -859,7 +859,8 @@ gbhf_status bscf_run(gbhf_ctx* c, const gbhf_scf_opts* o, double* energies, int*
     GBHF_TRY(br.gemm(false, false, 0.5, T1, Dg, 0.0, Wm));
     DBuf<double> dgrad;
     GBHF_CUDA(c, dgrad.alloc(3 * (size_t)b.natoms));
-    GBHF_TRY(gradient_dev(c, Dg, Wm, o->schwarz_cutoff > 0 ? o->schwarz_cutoff : 1e-12, 1e-4, o->precision, dgrad.p));
+    GBHF_TRY(gradient_dev(c, Dg, Wm, o->schwarz_cutoff > 0 ? o->schwarz_cutoff : 1e-12,
+                          o->grad_mixed_cutoff > 0 ? o->grad_mixed_cutoff : o->mixed_cutoff, o->precision, dgrad.p));
     GBHF_CUDA(c, cudaMemcpyAsync(grads, dgrad.p, 3 * (size_t)b.natoms * sizeof(double), cudaMemcpyDeviceToHost,
                                  c->stream));
     GBHF_CUDA(c, cudaStreamSynchronize(c->stream));

@@ -42,7 +42,8 @@ class SCFOpts(C.Structure):
                 ("max_iter", C.c_int), ("incremental", C.c_int), ("full_rebuild_every", C.c_int),
                 ("final_fp64", C.c_int), ("ref_stop_rule", C.c_int), ("conv_error", C.c_double),
                 ("conv_energy", C.c_double), ("conv_density", C.c_double), ("diis_start", C.c_double),
-                ("schwarz_cutoff", C.c_double), ("mixed_cutoff", C.c_double), ("charge", C.c_double)]
+                ("schwarz_cutoff", C.c_double), ("mixed_cutoff", C.c_double), ("charge", C.c_double),
+                ("grad_mixed_cutoff", C.c_double)]
 
 
 class SCFResultC(C.Structure):

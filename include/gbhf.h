@@ -82,6 +82,8 @@ typedef struct {
   double schwarz_cutoff; /* contracted Schwarz screening (baseline 1e-12) */
   double mixed_cutoff;   /* FP32 for quartets with bound below this (baseline 1e-4) */
   double charge;         /* total charge; n_occ = floor((sum Z - charge)/2) (HartreeFock.hs:75-76) */
+  double grad_mixed_cutoff; /* gbhf_scf_batch gradients, mixed precision: FP32 derivative integrals for
+                               quartets with bound Q_ab Q_cd max(w)^2 below this (0: mixed_cutoff) */
 } gbhf_scf_opts;
 
 /* Result buffers are caller-owned; any pointer may be NULL.  Sizes:
