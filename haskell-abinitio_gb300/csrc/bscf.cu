@@ -493,20 +493,28 @@ gbhf_status b_density(BatchRun& br, const double* F, const double* X, double* D,
   k_b_purify_init<<<br.egrid(), 256, 0, c->stream>>>(br.desc, br.d_nocc.p, Fp, g, P);
   count_launch(c, 2);
   std::vector<double> hc(4 * (size_t)br.M);
-  bool done = false;
-  for (int it = 0; it < 200 && !done; ++it) {
-    GBHF_TRY(br.gemm(false, false, 1.0, P, P, 0.0, P2));
-    GBHF_TRY(br.gemm(false, false, 1.0, P, P2, 0.0, P3));
-    k_b_purify_coef<<<br.M, 256, 0, c->stream>>>(br.desc, P, P2, P3, coef);
-    k_b_purify_update<<<br.egrid(), 256, 0, c->stream>>>(br.desc, coef, P, P2, P3);
-    count_launch(c, 2);
-    if (it % 4 == 3) {
-      GBHF_CUDA(c, cudaMemcpyAsync(hc.data(), coef, hc.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
-      GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
-      done = true;
-      for (int m = 0; m < br.M; ++m)
-        if (br.active[m] && !(std::fabs(hc[4 * m + 3]) < 1e-11 * std::max(1, br.nocc[m]))) done = false;
+  // four purification steps per CUDA-graph replay, convergence read between replays
+  auto four_steps = [&]() -> gbhf_status {
+    for (int k = 0; k < 4; ++k) {
+      GBHF_TRY(br.gemm(false, false, 1.0, P, P, 0.0, P2));
+      GBHF_TRY(br.gemm(false, false, 1.0, P, P2, 0.0, P3));
+      k_b_purify_coef<<<br.M, 256, 0, c->stream>>>(br.desc, P, P2, P3, coef);
+      k_b_purify_update<<<br.egrid(), 256, 0, c->stream>>>(br.desc, coef, P, P2, P3);
+      count_launch(c, 2);
     }
+    return GBHF_OK;
+  };
+  const std::vector<const void*> key = {(const void*)(size_t)br.M, (const void*)(size_t)br.ntiles,
+                                        (const void*)(size_t)br.nmax, br.desc.n, br.desc.off, br.desc.tstart,
+                                        br.desc.active, P, P2, P3, coef};
+  bool done = false;
+  for (int rep = 0; rep < 50 && !done; ++rep) {
+    GBHF_TRY(graph_run(c, c->g_bpurify, key, four_steps));
+    GBHF_CUDA(c, cudaMemcpyAsync(hc.data(), coef, hc.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
+    done = true;
+    for (int m = 0; m < br.M; ++m)
+      if (br.active[m] && !(std::fabs(hc[4 * m + 3]) < 1e-11 * std::max(1, br.nocc[m]))) done = false;
   }
   for (int m = 0; m < br.M; ++m)
     if (br.active[m] && !(std::fabs(hc[4 * m + 3]) < 1e-6 * std::max(1, br.nocc[m])))

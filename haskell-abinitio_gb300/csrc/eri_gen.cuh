@@ -13,9 +13,10 @@ __device__ __forceinline__ void eri_ketprim_ssss(const T* __restrict__ sb, int n
   const T ekp00_000 = ONE;
   #pragma unroll 1
   for (int kb = 0; kb < nbra; ++kb) {
-    const T p = sb[BRA_P * BRA_STRIDE + kb], invp = sb[BRA_INVP * BRA_STRIDE + kb];
-    const T Px = sb[BRA_PX * BRA_STRIDE + kb], Py = sb[BRA_PY * BRA_STRIDE + kb], Pz = sb[BRA_PZ * BRA_STRIDE + kb];
-    const T Kab = sb[BRA_K * BRA_STRIDE + kb];
+    BraPrim<T> bp;
+    load_bra_prim(sb + kb * BRA_SB, bp);
+    const T p = bp.p, invp = bp.invp, Px = bp.Px, Py = bp.Py, Pz = bp.Pz;
+    const T Kab = bp.K;
     const T X = Px - Qx, Y = Py - Qy, Z = Pz - Qz;
     const T ppq = p + q;
     const T rs = rsqrt_t(ppq);
@@ -47,10 +48,11 @@ __device__ __forceinline__ void eri_ketprim_psss(const T* __restrict__ sb, int n
   const T ekp00_000 = ONE;
   #pragma unroll 1
   for (int kb = 0; kb < nbra; ++kb) {
-    const T p = sb[BRA_P * BRA_STRIDE + kb], invp = sb[BRA_INVP * BRA_STRIDE + kb];
-    const T Px = sb[BRA_PX * BRA_STRIDE + kb], Py = sb[BRA_PY * BRA_STRIDE + kb], Pz = sb[BRA_PZ * BRA_STRIDE + kb];
-    const T PAx = sb[BRA_PAX * BRA_STRIDE + kb], PAy = sb[BRA_PAY * BRA_STRIDE + kb], PAz = sb[BRA_PAZ * BRA_STRIDE + kb];
-    const T Kab = sb[BRA_K * BRA_STRIDE + kb];
+    BraPrim<T> bp;
+    load_bra_prim(sb + kb * BRA_SB, bp);
+    const T p = bp.p, invp = bp.invp, Px = bp.Px, Py = bp.Py, Pz = bp.Pz;
+    const T PAx = bp.PAx, PAy = bp.PAy, PAz = bp.PAz;
+    const T Kab = bp.K;
     const T X = Px - Qx, Y = Py - Qy, Z = Pz - Qz;
     const T ppq = p + q;
     const T rs = rsqrt_t(ppq);
@@ -109,10 +111,11 @@ __device__ __forceinline__ void eri_ketprim_psps(const T* __restrict__ sb, int n
   const T ekp20_001 = -(ekz101);
   #pragma unroll 1
   for (int kb = 0; kb < nbra; ++kb) {
-    const T p = sb[BRA_P * BRA_STRIDE + kb], invp = sb[BRA_INVP * BRA_STRIDE + kb];
-    const T Px = sb[BRA_PX * BRA_STRIDE + kb], Py = sb[BRA_PY * BRA_STRIDE + kb], Pz = sb[BRA_PZ * BRA_STRIDE + kb];
-    const T PAx = sb[BRA_PAX * BRA_STRIDE + kb], PAy = sb[BRA_PAY * BRA_STRIDE + kb], PAz = sb[BRA_PAZ * BRA_STRIDE + kb];
-    const T Kab = sb[BRA_K * BRA_STRIDE + kb];
+    BraPrim<T> bp;
+    load_bra_prim(sb + kb * BRA_SB, bp);
+    const T p = bp.p, invp = bp.invp, Px = bp.Px, Py = bp.Py, Pz = bp.Pz;
+    const T PAx = bp.PAx, PAy = bp.PAy, PAz = bp.PAz;
+    const T Kab = bp.K;
     const T X = Px - Qx, Y = Py - Qy, Z = Pz - Qz;
     const T ppq = p + q;
     const T rs = rsqrt_t(ppq);
@@ -189,11 +192,12 @@ __device__ __forceinline__ void eri_ketprim_ppss(const T* __restrict__ sb, int n
   const T ekp00_000 = ONE;
   #pragma unroll 1
   for (int kb = 0; kb < nbra; ++kb) {
-    const T p = sb[BRA_P * BRA_STRIDE + kb], invp = sb[BRA_INVP * BRA_STRIDE + kb];
-    const T Px = sb[BRA_PX * BRA_STRIDE + kb], Py = sb[BRA_PY * BRA_STRIDE + kb], Pz = sb[BRA_PZ * BRA_STRIDE + kb];
-    const T PAx = sb[BRA_PAX * BRA_STRIDE + kb], PAy = sb[BRA_PAY * BRA_STRIDE + kb], PAz = sb[BRA_PAZ * BRA_STRIDE + kb];
-    const T PBx = sb[BRA_PBX * BRA_STRIDE + kb], PBy = sb[BRA_PBY * BRA_STRIDE + kb], PBz = sb[BRA_PBZ * BRA_STRIDE + kb];
-    const T Kab = sb[BRA_K * BRA_STRIDE + kb];
+    BraPrim<T> bp;
+    load_bra_prim(sb + kb * BRA_SB, bp);
+    const T p = bp.p, invp = bp.invp, Px = bp.Px, Py = bp.Py, Pz = bp.Pz;
+    const T PAx = bp.PAx, PAy = bp.PAy, PAz = bp.PAz;
+    const T PBx = bp.PBx, PBy = bp.PBy, PBz = bp.PBz;
+    const T Kab = bp.K;
     const T X = Px - Qx, Y = Py - Qy, Z = Pz - Qz;
     const T ppq = p + q;
     const T rs = rsqrt_t(ppq);
@@ -290,11 +294,12 @@ __device__ __forceinline__ void eri_ketprim_ppps(const T* __restrict__ sb, int n
   const T ekp20_001 = -(ekz101);
   #pragma unroll 1
   for (int kb = 0; kb < nbra; ++kb) {
-    const T p = sb[BRA_P * BRA_STRIDE + kb], invp = sb[BRA_INVP * BRA_STRIDE + kb];
-    const T Px = sb[BRA_PX * BRA_STRIDE + kb], Py = sb[BRA_PY * BRA_STRIDE + kb], Pz = sb[BRA_PZ * BRA_STRIDE + kb];
-    const T PAx = sb[BRA_PAX * BRA_STRIDE + kb], PAy = sb[BRA_PAY * BRA_STRIDE + kb], PAz = sb[BRA_PAZ * BRA_STRIDE + kb];
-    const T PBx = sb[BRA_PBX * BRA_STRIDE + kb], PBy = sb[BRA_PBY * BRA_STRIDE + kb], PBz = sb[BRA_PBZ * BRA_STRIDE + kb];
-    const T Kab = sb[BRA_K * BRA_STRIDE + kb];
+    BraPrim<T> bp;
+    load_bra_prim(sb + kb * BRA_SB, bp);
+    const T p = bp.p, invp = bp.invp, Px = bp.Px, Py = bp.Py, Pz = bp.Pz;
+    const T PAx = bp.PAx, PAy = bp.PAy, PAz = bp.PAz;
+    const T PBx = bp.PBx, PBy = bp.PBy, PBz = bp.PBz;
+    const T Kab = bp.K;
     const T X = Px - Qx, Y = Py - Qy, Z = Pz - Qz;
     const T ppq = p + q;
     const T rs = rsqrt_t(ppq);
@@ -496,11 +501,12 @@ __device__ __forceinline__ void eri_ketprim_pppp(const T* __restrict__ sb, int n
   const T ekp22_002 = ekz112;
   #pragma unroll 1
   for (int kb = 0; kb < nbra; ++kb) {
-    const T p = sb[BRA_P * BRA_STRIDE + kb], invp = sb[BRA_INVP * BRA_STRIDE + kb];
-    const T Px = sb[BRA_PX * BRA_STRIDE + kb], Py = sb[BRA_PY * BRA_STRIDE + kb], Pz = sb[BRA_PZ * BRA_STRIDE + kb];
-    const T PAx = sb[BRA_PAX * BRA_STRIDE + kb], PAy = sb[BRA_PAY * BRA_STRIDE + kb], PAz = sb[BRA_PAZ * BRA_STRIDE + kb];
-    const T PBx = sb[BRA_PBX * BRA_STRIDE + kb], PBy = sb[BRA_PBY * BRA_STRIDE + kb], PBz = sb[BRA_PBZ * BRA_STRIDE + kb];
-    const T Kab = sb[BRA_K * BRA_STRIDE + kb];
+    BraPrim<T> bp;
+    load_bra_prim(sb + kb * BRA_SB, bp);
+    const T p = bp.p, invp = bp.invp, Px = bp.Px, Py = bp.Py, Pz = bp.Pz;
+    const T PAx = bp.PAx, PAy = bp.PAy, PAz = bp.PAz;
+    const T PBx = bp.PBx, PBy = bp.PBy, PBz = bp.PBz;
+    const T Kab = bp.K;
     const T X = Px - Qx, Y = Py - Qy, Z = Pz - Qz;
     const T ppq = p + q;
     const T rs = rsqrt_t(ppq);

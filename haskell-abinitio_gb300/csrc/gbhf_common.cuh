@@ -30,8 +30,28 @@ constexpr int ncart_c(int L) { return (L + 1) * (L + 2) / 2; }
 // The J/K kernels stage the first BRA_NJK fields; BRA_AEXP (the exponent of
 // the pair's first primitive) is read by the gradient kernels only.
 #define BRA_NJK BRA_AEXP
-#define BRA_STRIDE 40   // >= max primitive pairs per shell pair (6 x 6 = 36)
-#define KMAX_PRIM_PAIRS 36
+#define KMAX_PRIM_PAIRS 36   // primitive pairs per shell pair (6 x 6)
+// A bra primitive pair staged in shared memory: its fields contiguous, padded
+// to 16 values so that every row starts on a 16-byte boundary and is read with
+// vector loads (7 x 16 bytes for double, 4 x 16 bytes for float).
+#define BRA_SB 16
+
+template <typename T>
+struct BraPrim {
+  T p, invp, Px, Py, Pz, PAx, PAy, PAz, PBx, PBy, PBz, K, a;
+};
+__device__ __forceinline__ void load_bra_prim(const double* __restrict__ r, BraPrim<double>& b) {
+  const double2* v = reinterpret_cast<const double2*>(r);
+  const double2 x0 = v[0], x1 = v[1], x2 = v[2], x3 = v[3], x4 = v[4], x5 = v[5], x6 = v[6];
+  b.p = x0.x, b.invp = x0.y, b.Px = x1.x, b.Py = x1.y, b.Pz = x2.x, b.PAx = x2.y, b.PAy = x3.x;
+  b.PAz = x3.y, b.PBx = x4.x, b.PBy = x4.y, b.PBz = x5.x, b.K = x5.y, b.a = x6.x;
+}
+__device__ __forceinline__ void load_bra_prim(const float* __restrict__ r, BraPrim<float>& b) {
+  const float4* v = reinterpret_cast<const float4*>(r);
+  const float4 x0 = v[0], x1 = v[1], x2 = v[2], x3 = v[3];
+  b.p = x0.x, b.invp = x0.y, b.Px = x0.z, b.Py = x0.w, b.Pz = x1.x, b.PAx = x1.y, b.PAy = x1.z;
+  b.PAz = x1.w, b.PBx = x2.x, b.PBy = x2.y, b.PBz = x2.z, b.K = x2.w, b.a = x3.x;
+}
 
 // 1/sqrt(x) in FP64 with few FP64-pipe instructions (that pipe is 1/64 of the
 // FP32 rate on this GPU): x is truncated to single precision by moving its
@@ -85,47 +105,63 @@ template <int L> struct BoysCfg<float, L> {
   static constexpr int NT = BOYS32_NTERM;
 };
 
-// Horner form used by the J/K and gradient kernels: row j holds, for
-// m = 0..BOYSH_LMAX and k = 0..NT-1, G[m*NT + k] = F_(m+k)(T_j) / k!, so that
-// F_m(t) = sum_k G[m*NT+k] (T_j - t)^k costs NT-1 FMAs per m, and in row
-// BOYSH_EXPROW the same expansion of exp(-t), G[k] = exp(-T_j) / k!.  For
-// orders L >= 2 only F_L and exp(-t) are expanded and the lower orders follow
-// by the downward recursion F_m = (2t F_(m+1) + exp(-t)) / (2m + 1), whose
-// terms are all positive.
+// Tables used by the J/K and gradient kernels, one block per order L = 0..BOYSH_LMAX:
+// row j of block L holds G[k] = F_(L+k)(T_j) / k! for k < NT, then E[k] = exp(-T_j) / k!,
+// so that F_L(t) = sum_k G[k] (T_j - t)^k and exp(-t) = sum_k E[k] (T_j - t)^k cost NT-1
+// FMAs each.  The lower orders follow by the downward recursion
+// F_m = (2t F_(m+1) + exp(-t)) / (2m + 1), whose terms are all positive.  Rows are
+// 16-byte aligned and read with vector loads.
 #define BOYSH_LMAX 5
-#define BOYSH_EXPROW (BOYSH_LMAX + 1)
-#define BOYSH64_STRIDE 50   // (BOYSH_LMAX+2) * 7 = 49, padded to 16 bytes
-#define BOYSH32_STRIDE 36   // (BOYSH_LMAX+2) * 5 = 35, padded
+#define BOYSH64_STRIDE 14   // 7 + 7 doubles
+#define BOYSH32_STRIDE 12   // 5 + 5 floats, padded to 16 bytes
 template <typename T> struct BoysHStride;
-template <> struct BoysHStride<double> { static constexpr int S = BOYSH64_STRIDE; };
-template <> struct BoysHStride<float> { static constexpr int S = BOYSH32_STRIDE; };
+template <> struct BoysHStride<double> { static constexpr int S = BOYSH64_STRIDE, NROW = BOYS64_NROW; };
+template <> struct BoysHStride<float> { static constexpr int S = BOYSH32_STRIDE, NROW = BOYS32_NROW; };
+
+// The 2 * NT coefficients of a row (only the first NT when exp is not needed).
+template <int NT, bool EXP>
+__device__ __forceinline__ void boys_row(const double* __restrict__ row, double* c) {
+  const double2* v = reinterpret_cast<const double2*>(row);
+#pragma unroll
+  for (int i = 0; i < (EXP ? 2 * NT : NT + 1) / 2; ++i) {
+    const double2 x = __ldg(v + i);
+    c[2 * i] = x.x;
+    c[2 * i + 1] = x.y;
+  }
+}
+template <int NT, bool EXP>
+__device__ __forceinline__ void boys_row(const float* __restrict__ row, float* c) {
+  const float4* v = reinterpret_cast<const float4*>(row);
+#pragma unroll
+  for (int i = 0; i < (EXP ? 2 * NT + 3 : NT + 3) / 4; ++i) {
+    const float4 x = __ldg(v + i);
+    c[4 * i] = x.x;
+    c[4 * i + 1] = x.y;
+    c[4 * i + 2] = x.z;
+    c[4 * i + 3] = x.w;
+  }
+}
 
 template <typename T, int L>
 __device__ __forceinline__ void boys_eval(T t, const T* __restrict__ tab, T* F) {
   using C = BoysCfg<T, L>;
-  static_assert(L <= BOYSH_LMAX, "Horner Boys table holds m <= BOYSH_LMAX");
+  static_assert(L <= BOYSH_LMAX, "the Boys tables hold orders up to BOYSH_LMAX");
   if (t < T(C::TMAX)) {
     int j;
     const T node = round_node(t * T(1.0 / C::H), j);
     const T dx = node * T(C::H) - t;   // = -(t - T_j)
-    const T* row = tab + j * BoysHStride<T>::S;
-    if constexpr (L <= 1) {
+    const T* row = tab + ((size_t)L * BoysHStride<T>::NROW + j) * BoysHStride<T>::S;
+    constexpr int NT = C::NT;
+    T c[2 * NT + 4];
+    boys_row<NT, (L >= 1)>(row, c);
+    T s = c[NT - 1];
 #pragma unroll
-      for (int m = 0; m <= L; ++m) {
-        T s = __ldg(row + m * C::NT + C::NT - 1);
+    for (int k = NT - 2; k >= 0; --k) s = fma_t(s, dx, c[k]);
+    F[L] = s;
+    if constexpr (L >= 1) {
+      T e = c[2 * NT - 1];
 #pragma unroll
-        for (int k = C::NT - 2; k >= 0; --k) s = fma_t(s, dx, __ldg(row + m * C::NT + k));
-        F[m] = s;
-      }
-    } else {
-      T s = __ldg(row + L * C::NT + C::NT - 1);
-      T e = __ldg(row + BOYSH_EXPROW * C::NT + C::NT - 1);
-#pragma unroll
-      for (int k = C::NT - 2; k >= 0; --k) {
-        s = fma_t(s, dx, __ldg(row + L * C::NT + k));
-        e = fma_t(e, dx, __ldg(row + BOYSH_EXPROW * C::NT + k));
-      }
-      F[L] = s;
+      for (int k = NT - 2; k >= 0; --k) e = fma_t(e, dx, c[NT + k]);
       const T t2 = t + t;
 #pragma unroll
       for (int m = L - 1; m >= 0; --m) F[m] = fma_t(t2, F[m + 1], e) * T(1.0 / (2 * m + 1));

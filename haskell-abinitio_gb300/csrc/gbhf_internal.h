@@ -74,6 +74,23 @@ struct DevPool {
   }
 };
 
+// An instantiated CUDA graph of a fixed launch sequence, rebuilt when the
+// key (sizes and buffer addresses baked into the launches) changes.
+struct GraphCache {
+  cudaGraphExec_t exec = nullptr;
+  std::vector<const void*> key;
+  int launches = 0;   // kernels in one replay
+  GraphCache() = default;
+  GraphCache(const GraphCache&) = delete;
+  GraphCache& operator=(const GraphCache&) = delete;
+  ~GraphCache() { reset(); }
+  void reset() {
+    if (exec) cudaGraphExecDestroy(exec);
+    exec = nullptr;
+    key.clear();
+  }
+};
+
 // Pool used by allocations on this thread: set by every entry point for the
 // context it works on (PoolScope), null outside the library.
 extern thread_local DevPool* tls_pool;
@@ -256,6 +273,7 @@ struct gbhf_ctx {
   gbhf::TaskLists tasks;
   gbhf::TaskLists gtasks;        // gradient task lists
   const int* mol_active = nullptr;   // batched SCF: per molecule 0/1 (device); nullptr = all
+  gbhf::GraphCache g_purify, g_bpurify;   // four purification steps (one molecule, batch)
   // dense work buffers (n*n doubles)
   gbhf::DBuf<double> w[24];
   gbhf::JacobiWork jac;
@@ -310,6 +328,39 @@ gbhf_status cuda_fail(gbhf_ctx* c, cudaError_t e, const char* where);
   } while (0)
 
 inline void count_launch(gbhf_ctx* c, int n = 1) { c->prof.launches += n; }
+
+// Capture `body` (launches on c->stream only, no synchronisation) into the cache
+// unless the key matches the cached graph, then launch the graph once.
+template <typename Body>
+gbhf_status graph_run(gbhf_ctx* c, GraphCache& g, const std::vector<const void*>& key, Body body) {
+  if (!g.exec || g.key != key) {
+    g.reset();
+    const long before = c->prof.launches;
+    cudaError_t e = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return cuda_fail(c, e, "cudaStreamBeginCapture");
+    const gbhf_status s = body();
+    cudaGraph_t graph = nullptr;
+    e = cudaStreamEndCapture(c->stream, &graph);
+    if (s != GBHF_OK) {
+      if (graph) cudaGraphDestroy(graph);
+      return s;
+    }
+    if (e != cudaSuccess) return cuda_fail(c, e, "cudaStreamEndCapture");
+    e = cudaGraphInstantiate(&g.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+      g.exec = nullptr;
+      return cuda_fail(c, e, "cudaGraphInstantiate");
+    }
+    g.key = key;
+    g.launches = (int)(c->prof.launches - before);
+    c->prof.launches = before;
+  }
+  const cudaError_t e = cudaGraphLaunch(g.exec, c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "cudaGraphLaunch");
+  count_launch(c, g.launches);
+  return GBHF_OK;
+}
 
 // Work slot `slot` of the context with at least `count` doubles (nullptr on
 // allocation failure).  Slots 0-9: SCF driver; 10-12: diagonalHF and

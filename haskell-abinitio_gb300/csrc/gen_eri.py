@@ -200,13 +200,14 @@ def gen_class(la, lb, lc, ld):
         ket_terms[(ic, idd)] = lst
     w("  #pragma unroll 1")
     w("  for (int kb = 0; kb < nbra; ++kb) {")
-    w("    const T p = sb[BRA_P * BRA_STRIDE + kb], invp = sb[BRA_INVP * BRA_STRIDE + kb];")
-    w("    const T Px = sb[BRA_PX * BRA_STRIDE + kb], Py = sb[BRA_PY * BRA_STRIDE + kb], Pz = sb[BRA_PZ * BRA_STRIDE + kb];")
+    w("    BraPrim<T> bp;")
+    w("    load_bra_prim(sb + kb * BRA_SB, bp);")
+    w("    const T p = bp.p, invp = bp.invp, Px = bp.Px, Py = bp.Py, Pz = bp.Pz;")
     if la >= 1:
-        w("    const T PAx = sb[BRA_PAX * BRA_STRIDE + kb], PAy = sb[BRA_PAY * BRA_STRIDE + kb], PAz = sb[BRA_PAZ * BRA_STRIDE + kb];")
+        w("    const T PAx = bp.PAx, PAy = bp.PAy, PAz = bp.PAz;")
     if lb >= 1:
-        w("    const T PBx = sb[BRA_PBX * BRA_STRIDE + kb], PBy = sb[BRA_PBY * BRA_STRIDE + kb], PBz = sb[BRA_PBZ * BRA_STRIDE + kb];")
-    w("    const T Kab = sb[BRA_K * BRA_STRIDE + kb];")
+        w("    const T PBx = bp.PBx, PBy = bp.PBy, PBz = bp.PBz;")
+    w("    const T Kab = bp.K;")
     w("    const T X = Px - Qx, Y = Py - Qy, Z = Pz - Qz;")
     w("    const T ppq = p + q;")
     w("    const T rs = rsqrt_t(ppq);")

@@ -100,7 +100,7 @@ template <int LA, int LB, int LC, int LD, typename T, bool SG>
 __global__ void __launch_bounds__(GR_THREADS) k_grad_jk(GradArgs<T> a) {
   constexpr int NA = ncart_c(LA), NB = ncart_c(LB), NC = ncart_c(LC), ND = ncart_c(LD);
   constexpr int NAB = NA * NB, NCD = NC * ND, NOUT = NAB * NCD;
-  __shared__ T sbra[GR_WARPS][BRA_NFIELD * BRA_STRIDE];
+  __shared__ __align__(16) T sbra[GR_WARPS][KMAX_PRIM_PAIRS * BRA_SB];
   __shared__ T sDab[GR_WARPS][NAB];
   extern __shared__ double gsm_dyn[];
   using GamT = typename std::conditional<SG, GamSmem<T, NOUT>, GamReg<T, NOUT>>::type;
@@ -125,7 +125,7 @@ __global__ void __launch_bounds__(GR_THREADS) k_grad_jk(GradArgs<T> a) {
     const int kb0 = task.w & 0xffff, Kb = (task.w >> 16) - kb0, pb0 = a.poff[ib] + kb0;
     for (int idx = lane; idx < BRA_NFIELD * Kb; idx += 32) {
       const int f = idx / Kb, k = idx - f * Kb;
-      sbra[warp][f * BRA_STRIDE + k] = a.bra[(long long)f * npp + pb0 + k];
+      sbra[warp][k * BRA_SB + f] = a.bra[(long long)f * npp + pb0 + k];
     }
     const int A = a.pA[ib], B = a.pB[ib];
     const int a0 = a.shell_f0[A], b0 = a.shell_f0[B];

@@ -117,7 +117,7 @@ template <int LA, int LB, int LC, int LD, typename T, bool SACC>
 __global__ void __launch_bounds__(JK_THREADS) k_jk(JKArgs<T> a) {
   constexpr int NA = ncart_c(LA), NB = ncart_c(LB), NC = ncart_c(LC), ND = ncart_c(LD);
   constexpr int NAB = NA * NB, NCD = NC * ND, NOUT = NAB * NCD;
-  __shared__ T sbra[JK_WARPS][BRA_NJK * BRA_STRIDE];
+  __shared__ __align__(16) T sbra[JK_WARPS][KMAX_PRIM_PAIRS * BRA_SB];
   __shared__ T sDab[JK_WARPS][NAB > 1 ? NAB : 1];
   extern __shared__ double sacc_dyn[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -146,7 +146,7 @@ __global__ void __launch_bounds__(JK_THREADS) k_jk(JKArgs<T> a) {
     const int kb0 = task.w & 0xffff, Kb = (task.w >> 16) - kb0, pb0 = a.poff[ib] + kb0;
     for (int idx = lane; idx < BRA_NJK * Kb; idx += 32) {
       const int f = idx / Kb, k = idx - f * Kb;
-      sbra[warp][f * BRA_STRIDE + k] = a.bra[(long long)f * npp + pb0 + k];
+      sbra[warp][k * BRA_SB + f] = a.bra[(long long)f * npp + pb0 + k];
     }
     const int A = a.pA[ib], B = a.pB[ib];
     const int a0 = a.shell_f0[A], b0 = a.shell_f0[B];
@@ -285,18 +285,18 @@ __global__ void __launch_bounds__(SCHWARZ_THREADS) k_schwarz_cls(int p0, int p1,
                                                                   const double* __restrict__ boys,
                                                                   double* __restrict__ Q) {
   constexpr int NA = ncart_c(LA), NB = ncart_c(LB), NAB = NA * NB;
-  __shared__ double sb[SCHWARZ_THREADS][BRA_NFIELD * BRA_STRIDE];
+  __shared__ __align__(16) double sb[SCHWARZ_THREADS][KMAX_PRIM_PAIRS * BRA_SB];
   const int t = p0 + blockIdx.x * SCHWARZ_THREADS + threadIdx.x;
   if (t >= p1) return;
   const int K = pK[t];
   const long long o = poff[t];
   double* s = sb[threadIdx.x];
   for (int f = 0; f < BRA_NFIELD; ++f)
-    for (int k = 0; k < K; ++k) s[f * BRA_STRIDE + k] = bra[f * npp + o + k];
+    for (int k = 0; k < K; ++k) s[k * BRA_SB + f] = bra[f * npp + o + k];
   RegAcc<double, NAB * NAB> acc;
   acc.zero();
   for (int k = 0; k < K; ++k) {
-    auto g = [&](int f) { return s[f * BRA_STRIDE + k]; };
+    auto g = [&](int f) { return s[k * BRA_SB + f]; };
     ClassFn<LA, LB, LA, LB>::template run<double, RegAcc<double, NAB * NAB>>(
         s, K, g(BRA_P), g(BRA_INVP), g(BRA_PX), g(BRA_PY), g(BRA_PZ), g(BRA_PAX), g(BRA_PAY), g(BRA_PAZ),
         g(BRA_PBX), g(BRA_PBY), g(BRA_PBZ), g(BRA_K), boys, acc);

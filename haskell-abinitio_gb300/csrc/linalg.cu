@@ -807,19 +807,24 @@ gbhf_status purify(gbhf_ctx* c, int n, int ne, const double* d_F, double* d_P, d
   k_purify_init<<<dim3((n + 127) / 128, n), 128, 0, c->stream>>>(n, ne, d_F, g, d_P);
   count_launch(c, 2);
   double err = 1.0;
-  const int max_iter = 200;
-  for (int it = 0; it < max_iter; ++it) {
-    GBHF_TRY(gemm(c, false, false, n, n, n, 1.0, d_P, n, d_P, n, 0.0, P2, n));
-    GBHF_TRY(gemm(c, false, false, n, n, n, 1.0, d_P, n, P2, n, 0.0, P3, n));
-    k_purify_coef<<<1, 1024, 0, c->stream>>>(n, d_P, P2, P3, coef);
-    count_launch(c);
-    const double* mats[3] = {d_P, P2, P3};
-    GBHF_TRY(lincomb(c, (int)nn, 3, mats, coef, d_P));
-    if (it % 4 == 3 || it == max_iter - 1) {
-      GBHF_CUDA(c, cudaMemcpyAsync(&err, coef + 3, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
-      GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
-      if (std::fabs(err) < 1e-11 * std::max(1, ne)) break;
+  // four purification steps per CUDA-graph replay, convergence read between replays
+  auto four_steps = [&]() -> gbhf_status {
+    for (int k = 0; k < 4; ++k) {
+      GBHF_TRY(gemm(c, false, false, n, n, n, 1.0, d_P, n, d_P, n, 0.0, P2, n));
+      GBHF_TRY(gemm(c, false, false, n, n, n, 1.0, d_P, n, P2, n, 0.0, P3, n));
+      k_purify_coef<<<1, 1024, 0, c->stream>>>(n, d_P, P2, P3, coef);
+      count_launch(c);
+      const double* mats[3] = {d_P, P2, P3};
+      GBHF_TRY(lincomb(c, (int)nn, 3, mats, coef, d_P));
     }
+    return GBHF_OK;
+  };
+  const std::vector<const void*> key = {(const void*)(size_t)n, d_P, P2, P3, coef};
+  for (int rep = 0; rep < 50; ++rep) {
+    GBHF_TRY(graph_run(c, c->g_purify, key, four_steps));
+    GBHF_CUDA(c, cudaMemcpyAsync(&err, coef + 3, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (std::fabs(err) < 1e-11 * std::max(1, ne)) break;
   }
   if (err_out) *err_out = err;
   if (!(std::fabs(err) < 1e-6 * std::max(1, ne)))

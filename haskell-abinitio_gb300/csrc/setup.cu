@@ -189,26 +189,28 @@ gbhf_status ensure_boys_tables(gbhf_ctx* c) {
     const float tj = (float)j * BOYS32_H;   // the node the device forms in float
     for (int m = 0; m < BOYS_NCOL; ++m) t32[(size_t)j * BOYS_NCOL + m] = (float)boys_series(m, (double)tj);
   }
-  // Horner tables: G[j][m*NT + k] = F_(m+k)(T_j) / k!
-  std::vector<double> h64((size_t)BOYS64_NROW * BOYSH64_STRIDE, 0.0);
-  std::vector<float> h32((size_t)BOYS32_NROW * BOYSH32_STRIDE, 0.0f);
-  for (int j = 0; j < BOYS64_NROW; ++j) {
-    double inv_fact = 1.0;
-    for (int k = 0; k < BOYS64_NTERM; ++k) {
-      if (k > 0) inv_fact /= k;
-      for (int m = 0; m <= BOYSH_LMAX; ++m)
-        h64[(size_t)j * BOYSH64_STRIDE + m * BOYS64_NTERM + k] = t64[(size_t)j * BOYS_NCOL + m + k] * inv_fact;
-      h64[(size_t)j * BOYSH64_STRIDE + BOYSH_EXPROW * BOYS64_NTERM + k] = std::exp(-j * BOYS64_H) * inv_fact;
+  // Horner tables per order L: row j = [F_(L+k)(T_j)/k!, k < NT][exp(-T_j)/k!, k < NT]
+  std::vector<double> h64((size_t)(BOYSH_LMAX + 1) * BOYS64_NROW * BOYSH64_STRIDE, 0.0);
+  std::vector<float> h32((size_t)(BOYSH_LMAX + 1) * BOYS32_NROW * BOYSH32_STRIDE, 0.0f);
+  for (int L = 0; L <= BOYSH_LMAX; ++L) {
+    for (int j = 0; j < BOYS64_NROW; ++j) {
+      double* row = h64.data() + ((size_t)L * BOYS64_NROW + j) * BOYSH64_STRIDE;
+      double inv_fact = 1.0;
+      for (int k = 0; k < BOYS64_NTERM; ++k) {
+        if (k > 0) inv_fact /= k;
+        row[k] = t64[(size_t)j * BOYS_NCOL + L + k] * inv_fact;
+        row[BOYS64_NTERM + k] = std::exp(-j * BOYS64_H) * inv_fact;
+      }
     }
-  }
-  for (int j = 0; j < BOYS32_NROW; ++j) {
-    const double tj = (double)((float)j * BOYS32_H);
-    double inv_fact = 1.0;
-    for (int k = 0; k < BOYS32_NTERM; ++k) {
-      if (k > 0) inv_fact /= k;
-      for (int m = 0; m <= BOYSH_LMAX; ++m)
-        h32[(size_t)j * BOYSH32_STRIDE + m * BOYS32_NTERM + k] = (float)(boys_series(m + k, tj) * inv_fact);
-      h32[(size_t)j * BOYSH32_STRIDE + BOYSH_EXPROW * BOYS32_NTERM + k] = (float)(std::exp(-tj) * inv_fact);
+    for (int j = 0; j < BOYS32_NROW; ++j) {
+      float* row = h32.data() + ((size_t)L * BOYS32_NROW + j) * BOYSH32_STRIDE;
+      const double tj = (double)((float)j * BOYS32_H);   // the node the device forms in float
+      double inv_fact = 1.0;
+      for (int k = 0; k < BOYS32_NTERM; ++k) {
+        if (k > 0) inv_fact /= k;
+        row[k] = (float)(boys_series(L + k, tj) * inv_fact);
+        row[BOYS32_NTERM + k] = (float)(std::exp(-tj) * inv_fact);
+      }
     }
   }
   GBHF_CUDA(c, c->boys64.alloc(t64.size()));
