@@ -299,7 +299,7 @@ def run_batch(args, world, rank, local):
     flats = [B.flatten(a) for a in mols]
     mine = replicas.shard([f.n_cgf ** 4 for f in flats], world, rank)
     sub = [flats[i] for i in mine]
-    mixed = _lib.baseline_opts(precision=_lib.PREC_MIXED, incremental=1, final_fp64=0,
+    mixed = _lib.baseline_opts(precision=_lib.PREC_MIXED, incremental=1, final_fp64=0, full_rebuild_every=0,
                                mixed_cutoff=args.mixed_cutoff, grad_mixed_cutoff=args.grad_mixed_cutoff)
     ctx.scf_batch(sub[:16], mixed, gradients=True)          # warm-up (tables, SAD atoms)
     barrier(world)

@@ -514,7 +514,7 @@ gbhf_status b_density(BatchRun& br, const double* F, const double* X, double* D,
     GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
     done = true;
     for (int m = 0; m < br.M; ++m)
-      if (br.active[m] && !(std::fabs(hc[4 * m + 3]) < 1e-11 * std::max(1, br.nocc[m]))) done = false;
+      if (br.active[m] && !(std::fabs(hc[4 * m + 3]) < 1e-13 * std::max(1, br.nocc[m]))) done = false;
   }
   for (int m = 0; m < br.M; ++m)
     if (br.active[m] && !(std::fabs(hc[4 * m + 3]) < 1e-6 * std::max(1, br.nocc[m])))
@@ -653,7 +653,6 @@ gbhf_status bscf_run(gbhf_ctx* c, const gbhf_scf_opts* o, double* energies, int*
       if (status != GBHF_OK) break;
       k_b_addsym<<<br.egrid(), 256, 0, c->stream>>>(br.desc, nullptr, Gpp, Gacc);
       since_full = 1;
-      fp64_final_phase = false;
     } else {
       GBHF_TRY(axpby(c, nst, 1.0, D, -1.0, Dref, Dn));   // dD (Dn as scratch)
       status = jk_build(c, Dn, Gpp, precision, o->schwarz_cutoff, o->mixed_cutoff, 1.0, true);
@@ -818,7 +817,10 @@ gbhf_status bscf_run(gbhf_ctx* c, const gbhf_scf_opts* o, double* energies, int*
       const int nm = br.n[m];
       const double rms = std::sqrt(hstats[2 * m + 1] / ((double)nm * nm));
       iters[m] = step + 1;
-      if (have_prev[m] && std::fabs(energy[m] - e_prev[m]) < o->conv_energy && rms < o->conv_density) {
+      const bool handover = o->final_fp64 && precision == GBHF_PREC_MIXED;   // as scf.cu
+      const double ce = handover ? std::max(o->conv_energy, 1e-9) : o->conv_energy;
+      const double cd = handover ? std::max(o->conv_density, 1e-7) : o->conv_density;
+      if (have_prev[m] && std::fabs(energy[m] - e_prev[m]) < ce && rms < cd) {
         conv[m] = 1;
         act[m] = 0;
       }

@@ -271,6 +271,132 @@ def gen_class(la, lb, lc, ld):
     return "\n".join(out), cls
 
 
+def gen_vne(la, lb):
+    """Nuclear-attraction derivatives of one primitive pair of class (la lb) for
+    one nucleus C:  g_A,x += sum_ab w_ab dV^C_ab/dA_x,  g_B,x likewise, with
+    V^C_ab = zpref sum_tuv E^ab_tuv R_tuv(p, P - C) (zpref = -Z_C 2 pi/p c_a c_b
+    exp(-mu AB^2), w_ab the density weights) and the same derivative rule on
+    the Hermite coefficients as the two-electron code.  The operator-centre
+    derivative is -(g_A + g_B)."""
+    ca, cb = CART[la], CART[lb]
+    L = la + lb + 1
+    cls = f"{LNAME[la]}{LNAME[lb]}"
+    bra = {}
+    for ia, a in enumerate(ca):
+        for ib, b in enumerate(cb):
+            ds = {}
+            for side in "AB":
+                for d in range(3):
+                    rng = [a[x] + b[x] + (1 if x == d else 0) for x in range(3)]
+                    ds[(side, d)] = [(t, u, v) for t in range(rng[0] + 1) for u in range(rng[1] + 1)
+                                     for v in range(rng[2] + 1)]
+            bra[(ia, ib)] = (a, b, ds)
+    needed_r = {h for (_, _, ds) in bra.values() for hs in ds.values() for h in hs}
+    r_lines, r_memo, used_n = r_code(L, needed_r)
+    bneed = [set(), set(), set()]
+    for (a, b, _) in bra.values():
+        for x in range(3):
+            i, j = a[x], b[x]
+            for t in range(i + j + 1):
+                bneed[x].add((i, j, t))
+            for t in range(i + j + 2):
+                bneed[x].add((i + 1, j, t))
+                bneed[x].add((i, j + 1, t))
+            if i >= 1:
+                for t in range(i + j):
+                    bneed[x].add((i - 1, j, t))
+            if j >= 1:
+                for t in range(i + j):
+                    bneed[x].add((i, j - 1, t))
+    out = []
+    w = out.append
+    w(f"// ---- nuclear-attraction gradient, pair class ({cls}): one primitive pair, one nucleus")
+    w("template <typename T>")
+    w(f"__device__ __forceinline__ void vne_grad_{cls}(const BraPrim<T>& bp, const T Cx, const T Cy, const T Cz,")
+    w("    const T zpref, const T* __restrict__ dw, const T* __restrict__ boys, T* g) {")
+    w("  const T ONE = T(1);")
+    w("  const T p = bp.p, invp = bp.invp;")
+    w("  const T PAx = bp.PAx, PAy = bp.PAy, PAz = bp.PAz, PBx = bp.PBx, PBy = bp.PBy, PBz = bp.PBz;")
+    w("  const T ta = T(2) * bp.a, tb = T(2) * (p - bp.a);")
+    w("  const T X = bp.Px - Cx, Y = bp.Py - Cy, Z = bp.Pz - Cz;")
+    w("  const T Tb = p * (X * X + Y * Y + Z * Z);")
+    w(f"  T F[{L + 1}];")
+    w(f"  boys_eval<T, {L}>(Tb, boys, F);")
+    w("  const T m2a = T(-2) * p;")
+    w("  T scale = zpref;")
+    for n in range(L + 1):
+        if n in used_n:
+            w(f"  const T R{n}_000 = scale * F[{n}];")
+        if n < L:
+            w("  scale *= m2a;")
+    for ln in r_lines:
+        w("  " + ln)
+    w("  const T hp = T(0.5) * invp;")
+    bmaps = []
+    for x, ax in enumerate("xyz"):
+        lines, memo = e_axis_code(f"eb{ax}", f"PA{ax}", f"PB{ax}", "hp", la + 1, lb + 1, bneed[x])
+        for ln in lines:
+            w("  " + ln)
+        bmaps.append(memo)
+    dnames = {}
+
+    def dfac(side, x, i, j, t):
+        key = (side, x, i, j, t)
+        if key in dnames:
+            return dnames[key]
+        m = bmaps[x]
+        if side == "A":
+            up, dn, k, tw = m.get((i + 1, j, t)), (m.get((i - 1, j, t)) if i >= 1 else None), i, "ta"
+        else:
+            up, dn, k, tw = m.get((i, j + 1, t)), (m.get((i, j - 1, t)) if j >= 1 else None), j, "tb"
+        terms = []
+        if up is not None:
+            terms.append(tw if up == "ONE" else f"{tw} * {up}")
+        if dn is not None:
+            c = "" if k == 1 else f"T({k}) * "
+            terms.append(f"- {c}{'ONE' if dn == 'ONE' else dn}")
+        if not terms:
+            dnames[key] = None
+            return None
+        nm = f"d{side}{'xyz'[x]}{i}{j}_{t}"
+        w(f"  const T {nm} = {terms[0] + (' ' + terms[1] if len(terms) > 1 else '')};")
+        dnames[key] = nm
+        return nm
+
+    for (a, b, ds) in bra.values():
+        for side in "AB":
+            for d in range(3):
+                for tt in ds[(side, d)]:
+                    dfac(side, d, a[d], b[d], tt[d])
+    for (ia, ib), (a, b, ds) in bra.items():
+        iab = ia * len(cb) + ib
+        for si, side in enumerate("AB"):
+            for d in range(3):
+                expr = None
+                for tt in ds[(side, d)]:
+                    facs = []
+                    ok = True
+                    for x in range(3):
+                        f = dfac(side, x, a[x], b[x], tt[x]) if x == d else bmaps[x].get((a[x], b[x], tt[x]))
+                        if f is None:
+                            ok = False
+                            break
+                        if f != "ONE":
+                            facs.append(f)
+                    if not ok:
+                        continue
+                    r = r_memo[(0,) + tt]
+                    coef = " * ".join(facs) if facs else None
+                    if expr is None:
+                        expr = r if coef is None else f"{coef} * {r}"
+                    else:
+                        expr = f"{expr} + {r}" if coef is None else f"fma_t({coef}, {r}, {expr})"
+                if expr is not None:
+                    w(f"  g[{3 * si + d}] = fma_t(dw[{iab}], {expr}, g[{3 * si + d}]);")
+    w("}")
+    return "\n".join(out)
+
+
 def main():
     pcls = [(0, 0), (1, 0), (1, 1)]
     parts = ["// GENERATED by gen_grad.py -- do not edit by hand.", "#pragma once", ""]
@@ -279,6 +405,9 @@ def main():
             code, _ = gen_class(la, lb, lc, ld)
             parts.append(code)
             parts.append("")
+    for (la, lb) in pcls:
+        parts.append(gen_vne(la, lb))
+        parts.append("")
     Path(__file__).with_name("grad_gen.cuh").write_text("\n".join(parts))
 
 

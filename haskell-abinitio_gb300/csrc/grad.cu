@@ -289,13 +289,11 @@ static gbhf_status grad_2e(gbhf_ctx* c, const double* d_D, double schwarz, doubl
 }
 
 // ---------------------------------------------------------- one-electron ----
-// Thread per function pair (a <= b): D-weighted derivatives of T and V (with
-// the operator-centre term) and W-weighted derivatives of S.  Primitive pairs
-// whose weighted prefactor is below 1e-17 are skipped.  The operator-centre
-// terms of the block are summed in shared memory (when 3 * natoms fits) and
-// written with one atomic per atom component.
+// Thread per function pair (a <= b): D-weighted derivatives of T and W-weighted
+// derivatives of S (translational invariance gives d/dB = -d/dA).  Primitive
+// pairs whose weighted prefactor is below 1e-17 are skipped.  The nuclear
+// attraction follows in k_grad_vne.
 constexpr int G1_THREADS = 64;
-constexpr int G1_SMEM_ATOMS = 2048;
 
 // Molecule-aware: row i (global function) pairs with the functions j >= i of
 // its molecule; D and W are the stacked n_m x n_m blocks; the operator centres
@@ -314,26 +312,17 @@ struct Grad1eArgs {
   const double* D;
   const double* W;
   double* grad;             // 3 * total atoms
-  int smem_atoms;           // atoms per molecule that fit the shared accumulator (0: none)
 };
 
 __global__ void __launch_bounds__(G1_THREADS) k_grad_1e(Grad1eArgs g) {
-  extern __shared__ double s_gc[];   // 3 * molecule atoms when they fit
   const int i = blockIdx.y;
   const int mol = g.fmol[i];
-  const int f0m = g.mfo[mol], nm = g.mfo[mol + 1] - f0m, a0 = g.mao[mol], a1 = g.mao[mol + 1];
-  const int natoms = a1 - a0;
-  const bool use_smem = natoms <= g.smem_atoms;
-  if (use_smem)
-    for (int k = threadIdx.x; k < 3 * natoms; k += blockDim.x) s_gc[k] = 0.0;
-  __syncthreads();
+  const int f0m = g.mfo[mol], nm = g.mfo[mol + 1] - f0m;
   const int il = i - f0m;
   const int jl = blockIdx.x * blockDim.x + threadIdx.x;   // local column
   const double* __restrict__ xyz = g.xyz;
-  const double* __restrict__ Z = g.Z;
   const double* __restrict__ coef = g.coef;
   const double* __restrict__ expo = g.expo;
-  const double* __restrict__ tab = g.tab;
   double* __restrict__ grad = g.grad;
   if (jl < nm && jl >= il) {
     const int j = f0m + jl;
@@ -341,13 +330,9 @@ __global__ void __launch_bounds__(G1_THREADS) k_grad_1e(Grad1eArgs g) {
     const double *A = xyz + 3 * f.atom, *B = xyz + 3 * gfn.atom;
     const double mult = (i == j) ? 1.0 : 2.0;
     const double dab = mult * g.D[g.moff[mol] + (long)il * nm + jl], wab = mult * g.W[g.moff[mol] + (long)il * nm + jl];
-    const int L = f.l[0] + f.l[1] + f.l[2] + gfn.l[0] + gfn.l[1] + gfn.l[2] + 1;
     double ab2 = 0;
     for (int x = 0; x < 3; ++x) ab2 += (A[x] - B[x]) * (A[x] - B[x]);
     double gA[3] = {0, 0, 0};   // d/dA of (D T - W S); d/dB = -d/dA
-    double vA[3] = {0, 0, 0}, vB[3] = {0, 0, 0};
-    double F[MD_LMAX + 2];
-    double R[MD_D * MD_D * MD_D];
     for (int p1 = 0; p1 < f.np; ++p1)
       for (int p2 = 0; p2 < gfn.np; ++p2) {
         const double c1 = coef[f.off + p1], a = expo[f.off + p1];
@@ -403,63 +388,156 @@ __global__ void __launch_bounds__(G1_THREADS) k_grad_1e(Grad1eArgs g) {
           }
           gA[dir] += c1 * c2 * (dab * dT - wab * dS);
         }
-        if (fabs(kab) * fabs(dab) * (1.0 + p) * 2.0 * GBHF_PI / p < 1e-17) continue;
-        // nuclear attraction: d/dA and d/dB of V^C, operator centre -(dA + dB)
-        EAx E[3];
-        for (int x = 0; x < 3; ++x) {
-          const double abx = A[x] - B[x];
-          e_axis(E[x], f.l[x] + 1 <= 2 ? f.l[x] + 1 : 2, gfn.l[x] + 1 <= 2 ? gfn.l[x] + 1 : 2, p, P[x] - A[x],
-                 P[x] - B[x], exp(-mu * abx * abx));
-        }
-        for (int cn = a0; cn < a1; ++cn) {
-          const double* Cc = xyz + 3 * cn;
-          const double PC[3] = {P[0] - Cc[0], P[1] - Cc[1], P[2] - Cc[2]};
-          boys_generic(false, nullptr, tab, L, p * (PC[0] * PC[0] + PC[1] * PC[1] + PC[2] * PC[2]), F);
-          hermite_r<MD_LMAX>(L, p, PC[0], PC[1], PC[2], F, R);
-          const double vpref = -Z[cn] * c1 * c2 * 2.0 * (GBHF_PI / p) * dab;
-          double dA[3] = {0, 0, 0}, dB[3] = {0, 0, 0};
-          for (int dir = 0; dir < 3; ++dir) {
-            int hi[3];
-            for (int x = 0; x < 3; ++x) hi[x] = f.l[x] + gfn.l[x] + (x == dir ? 1 : 0);
-            for (int t = 0; t <= hi[0]; ++t)
-              for (int u = 0; u <= hi[1]; ++u)
-                for (int v = 0; v <= hi[2]; ++v) {
-                  const int tt[3] = {t, u, v};
-                  double eA = 1, eB = 1;
-                  for (int x = 0; x < 3; ++x) {
-                    const int li = f.l[x], lj = gfn.l[x];
-                    if (x == dir) {
-                      eA *= 2 * a * E[x].get(li + 1, lj, tt[x]) - li * E[x].get(li - 1, lj, tt[x]);
-                      eB *= 2 * b * E[x].get(li, lj + 1, tt[x]) - lj * E[x].get(li, lj - 1, tt[x]);
-                    } else {
-                      const double e = E[x].get(li, lj, tt[x]);
-                      eA *= e;
-                      eB *= e;
-                    }
-                  }
-                  const double r = R[(t * MD_D + u) * MD_D + v];
-                  dA[dir] += eA * r;
-                  dB[dir] += eB * r;
-                }
-          }
-          for (int x = 0; x < 3; ++x) {
-            vA[x] += vpref * dA[x];
-            vB[x] += vpref * dB[x];
-            const double gc = -vpref * (dA[x] + dB[x]);
-            if (use_smem) atomicAdd(&s_gc[3 * (cn - a0) + x], gc);
-            else atomicAdd(&grad[3 * cn + x], gc);
-          }
-        }
       }
     for (int x = 0; x < 3; ++x) {
-      atomicAdd(&grad[3 * f.atom + x], gA[x] + vA[x]);
-      atomicAdd(&grad[3 * gfn.atom + x], -gA[x] + vB[x]);
+      atomicAdd(&grad[3 * f.atom + x], gA[x]);
+      atomicAdd(&grad[3 * gfn.atom + x], -gA[x]);
     }
   }
-  __syncthreads();
-  if (use_smem)
-    for (int k = threadIdx.x; k < 3 * natoms; k += blockDim.x)
-      if (s_gc[k] != 0.0) atomicAdd(&grad[3 * a0 + k], s_gc[k]);
+}
+
+// Nuclear-attraction terms: warp per shell pair of class (LA, LB), lanes over the
+// molecule's nuclei; generated per-primitive-pair code (grad_gen.cuh).  The pair
+// covers (a, b) and (b, a) when A != B (weight 2).  Bra-centre sums are reduced
+// over the warp; each lane adds the operator-centre term -(dA + dB) of its nucleus.
+template <int LA, int LB>
+struct VneFn;
+template <>
+struct VneFn<0, 0> {
+  static __device__ __forceinline__ void run(const BraPrim<double>& bp, double x, double y, double z, double zp,
+                                             const double* dw, const double* boys, double* g) {
+    vne_grad_ss<double>(bp, x, y, z, zp, dw, boys, g);
+  }
+};
+template <>
+struct VneFn<1, 0> {
+  static __device__ __forceinline__ void run(const BraPrim<double>& bp, double x, double y, double z, double zp,
+                                             const double* dw, const double* boys, double* g) {
+    vne_grad_ps<double>(bp, x, y, z, zp, dw, boys, g);
+  }
+};
+template <>
+struct VneFn<1, 1> {
+  static __device__ __forceinline__ void run(const BraPrim<double>& bp, double x, double y, double z, double zp,
+                                             const double* dw, const double* boys, double* g) {
+    vne_grad_pp<double>(bp, x, y, z, zp, dw, boys, g);
+  }
+};
+
+struct VneArgs {
+  int p0, p1;               // pairs of this class
+  const int *pA, *pB, *pK, *poff, *pmol;
+  const double* bra;        // pair-contiguous primitive-pair fields
+  long long npp;
+  const int* shell_f0;      // within the molecule
+  const int* shell_atom;
+  const int* mn;
+  const long long* moff;
+  const int* mao;           // first atom of each molecule (nmol + 1)
+  const double* xyz;
+  const double* Z;
+  const double* D;          // stacked
+  const double* boys;       // FP64 Horner tables
+  double kvf;               // 2 pi / sqrt(2 pi^2.5): K' of the pair data -> 2 pi/p c c exp(-mu AB^2)
+  double* grad;
+};
+
+template <int LA, int LB>
+__global__ void __launch_bounds__(128) k_grad_vne(VneArgs a) {
+  constexpr int NA = ncart_c(LA), NB = ncart_c(LB);
+  const int lane = threadIdx.x & 31;
+  const int pr = a.p0 + blockIdx.x * 4 + (threadIdx.x >> 5);
+  if (pr >= a.p1) return;
+  const int A = a.pA[pr], B = a.pB[pr], mol = a.pmol[pr], n = a.mn[mol];
+  const double* Dm = a.D + a.moff[mol];
+  const int fa = a.shell_f0[A], fb = a.shell_f0[B];
+  const double mult = A == B ? 1.0 : 2.0;
+  double dw[NA * NB];
+  double dmax = 0;
+#pragma unroll
+  for (int ia = 0; ia < NA; ++ia)
+#pragma unroll
+    for (int ib = 0; ib < NB; ++ib) {
+      dw[ia * NB + ib] = mult * Dm[(long)(fa + ia) * n + fb + ib];
+      dmax = fmax(dmax, fabs(dw[ia * NB + ib]));
+    }
+  double gAB[6] = {0, 0, 0, 0, 0, 0};
+  const int K = a.pK[pr];
+  const long long po = a.poff[pr];
+  const int c0 = a.mao[mol], c1 = a.mao[mol + 1];
+  for (int cb = c0; cb < c1; cb += 32) {
+    const int cn = cb + lane;
+    if (cn < c1) {
+      const double Cx = a.xyz[3 * cn], Cy = a.xyz[3 * cn + 1], Cz = a.xyz[3 * cn + 2], Zc = a.Z[cn];
+      double gC[3] = {0, 0, 0};
+      for (int k = 0; k < K; ++k) {
+        BraPrim<double> bp;
+        const long long idx = po + k;
+        bp.p = a.bra[BRA_P * a.npp + idx];
+        bp.invp = a.bra[BRA_INVP * a.npp + idx];
+        bp.Px = a.bra[BRA_PX * a.npp + idx];
+        bp.Py = a.bra[BRA_PY * a.npp + idx];
+        bp.Pz = a.bra[BRA_PZ * a.npp + idx];
+        bp.PAx = a.bra[BRA_PAX * a.npp + idx];
+        bp.PAy = a.bra[BRA_PAY * a.npp + idx];
+        bp.PAz = a.bra[BRA_PAZ * a.npp + idx];
+        bp.PBx = a.bra[BRA_PBX * a.npp + idx];
+        bp.PBy = a.bra[BRA_PBY * a.npp + idx];
+        bp.PBz = a.bra[BRA_PBZ * a.npp + idx];
+        bp.K = a.bra[BRA_K * a.npp + idx];
+        bp.a = a.bra[BRA_AEXP * a.npp + idx];
+        const double zpref = -Zc * bp.K * a.kvf;
+        if (fabs(zpref) * dmax * (1.0 + bp.p) < 1e-17) continue;
+        double g6[6] = {0, 0, 0, 0, 0, 0};
+        VneFn<LA, LB>::run(bp, Cx, Cy, Cz, zpref, dw, a.boys, g6);
+#pragma unroll
+        for (int x = 0; x < 3; ++x) {
+          gAB[x] += g6[x];
+          gAB[3 + x] += g6[3 + x];
+          gC[x] -= g6[x] + g6[3 + x];
+        }
+      }
+#pragma unroll
+      for (int x = 0; x < 3; ++x)
+        if (gC[x] != 0.0) atomicAdd(&a.grad[3 * cn + x], gC[x]);
+    }
+  }
+#pragma unroll
+  for (int x = 0; x < 6; ++x) {
+    const double v = warp_sum_d(gAB[x]);
+    if (lane == 0 && v != 0.0) atomicAdd(&a.grad[3 * a.shell_atom[x < 3 ? A : B] + x % 3], v);
+  }
+}
+
+template <int LA, int LB>
+static gbhf_status launch_vne(gbhf_ctx* c, int cls, const double* d_D, double* d_grad) {
+  PairData& P = c->pairs;
+  VneArgs a;
+  a.p0 = P.cls_start[cls];
+  a.p1 = P.cls_start[cls + 1];
+  if (a.p1 <= a.p0) return GBHF_OK;
+  a.pA = P.A.p;
+  a.pB = P.B.p;
+  a.pK = P.K.p;
+  a.poff = P.poff.p;
+  a.pmol = P.mol.p;
+  a.bra = P.bra64.p;
+  a.npp = (long long)P.nprim_pairs;
+  a.shell_f0 = c->tasks.f0.p;
+  a.shell_atom = c->tasks.atom.p;
+  a.mn = c->tasks.mn.p;
+  a.moff = c->tasks.moff.p;
+  a.mao = c->tasks.mao.p;
+  a.xyz = c->d_xyz.p;
+  a.Z = c->d_Z.p;
+  a.D = d_D;
+  a.boys = c->boysh64.p;
+  a.kvf = 2.0 * GBHF_PI / std::sqrt(TWO_PI_2P5);
+  a.grad = d_grad;
+  k_grad_vne<LA, LB><<<(a.p1 - a.p0 + 3) / 4, 128, 0, c->stream>>>(a);
+  count_launch(c);
+  GBHF_CUDA(c, cudaGetLastError());
+  return GBHF_OK;
 }
 
 // Nuclear repulsion gradient, one thread per atom: -sum_L Z_K Z_L (R_K - R_L) / R_KL^3
@@ -496,11 +574,8 @@ gbhf_status gradient_dev(gbhf_ctx* c, const double* d_D, const double* d_W, doub
   GBHF_CUDA(c, cudaMemsetAsync(d_grad, 0, 3 * na * sizeof(double), c->stream));
   k_grad_nuc<<<(na + 127) / 128, 128, 0, c->stream>>>(na, c->tasks.amol.p, c->tasks.mao.p, c->d_xyz.p, c->d_Z.p,
                                                       d_grad);
-  int max_atoms = 0, max_fn = 0;
-  for (int m = 0; m < b.nmol; ++m) {
-    max_atoms = std::max(max_atoms, b.mol_atom_off[m + 1] - b.mol_atom_off[m]);
-    max_fn = std::max(max_fn, b.mol_fn_off[m + 1] - b.mol_fn_off[m]);
-  }
+  int max_fn = 0;
+  for (int m = 0; m < b.nmol; ++m) max_fn = std::max(max_fn, b.mol_fn_off[m + 1] - b.mol_fn_off[m]);
   Grad1eArgs g1;
   g1.xyz = c->d_xyz.p;
   g1.Z = c->d_Z.p;
@@ -515,13 +590,12 @@ gbhf_status gradient_dev(gbhf_ctx* c, const double* d_D, const double* d_W, doub
   g1.D = d_D;
   g1.W = d_W;
   g1.grad = d_grad;
-  g1.smem_atoms = max_atoms <= G1_SMEM_ATOMS ? max_atoms : 0;
-  const size_t smem1 = 3 * (size_t)g1.smem_atoms * sizeof(double);
-  if (smem1 > 48 * 1024)
-    GBHF_CUDA(c, cudaFuncSetAttribute(k_grad_1e, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1));
-  k_grad_1e<<<dim3((max_fn + G1_THREADS - 1) / G1_THREADS, n), G1_THREADS, smem1, c->stream>>>(g1);
+  k_grad_1e<<<dim3((max_fn + G1_THREADS - 1) / G1_THREADS, n), G1_THREADS, 0, c->stream>>>(g1);
   count_launch(c, 2);
   GBHF_CUDA(c, cudaGetLastError());
+  GBHF_TRY((launch_vne<0, 0>(c, 0, d_D, d_grad)));
+  GBHF_TRY((launch_vne<1, 0>(c, 1, d_D, d_grad)));
+  GBHF_TRY((launch_vne<1, 1>(c, 2, d_D, d_grad)));
   GBHF_TRY(grad_2e(c, d_D, schwarz, mixed_cutoff, precision, d_grad));
   GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
   return GBHF_OK;

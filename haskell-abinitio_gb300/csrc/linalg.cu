@@ -824,7 +824,7 @@ gbhf_status purify(gbhf_ctx* c, int n, int ne, const double* d_F, double* d_P, d
     GBHF_TRY(graph_run(c, c->g_purify, key, four_steps));
     GBHF_CUDA(c, cudaMemcpyAsync(&err, coef + 3, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
-    if (std::fabs(err) < 1e-11 * std::max(1, ne)) break;
+    if (std::fabs(err) < 1e-13 * std::max(1, ne)) break;   // E[D] is first order in the idempotency error
   }
   if (err_out) *err_out = err;
   if (!(std::fabs(err) < 1e-6 * std::max(1, ne)))

@@ -5,6 +5,8 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <vector>
 
 #include "gbhf_internal.h"
@@ -200,9 +202,16 @@ gbhf_status scf_run(gbhf_ctx* c, const gbhf_scf_opts* o, gbhf_result* r) {
   bool diis_on = false;
   double e_prev = 0, energy = 0;
   bool have_prev = false, converged = false;
+  // final_fp64: after converging in mixed precision, continue with full FP64
+  // builds until converged again.  Incremental builds carry a noise floor near
+  // 1e-11 Eh (each screened-out contribution of a build is below the absolute
+  // cutoff but new ones are dropped every step), so the final phase never uses them.
   bool fp64_final_phase = false;
   int precision = o->precision;
   int step = 0, since_full = 1 << 30;
+  // GBHF_SCF_TRACE=1: one line per step on stderr (energy, changes, DIIS size)
+  const char* tr_env = std::getenv("GBHF_SCF_TRACE");
+  const bool trace = tr_env && tr_env[0] == '1';
   double fock_builds = 0;
   const double* last_fuse = F;
   double hstats[4];
@@ -225,7 +234,6 @@ gbhf_status scf_run(gbhf_ctx* c, const gbhf_scf_opts* o, gbhf_result* r) {
         GBHF_TRY(jk_build(c, D, Gpp, precision, o->schwarz_cutoff, o->mixed_cutoff, 1.0));
         GBHF_TRY(add_sym(c, n, nullptr, Gpp, Gacc));
         since_full = 1;
-        fp64_final_phase = false;
       } else {
         GBHF_TRY(axpby(c, nn, 1.0, D, -1.0, Dref, Dnew));   // dD (Dnew as scratch)
         double w = 0;
@@ -343,7 +351,16 @@ gbhf_status scf_run(gbhf_ctx* c, const gbhf_scf_opts* o, gbhf_result* r) {
       GBHF_TRY(reduce_stats(c, n, nullptr, H, F, Dnew, D, hstats));
       energy = hstats[3] + enuc;   // E[D] with F = F(D)
       const double rms = std::sqrt(hstats[2] / (double)nn);
-      converged = have_prev && std::fabs(energy - e_prev) < o->conv_energy && rms < o->conv_density;
+      // with final_fp64 the mixed phase hands over at 1e-9 Eh / 1e-7 (the FP64 full
+      // builds that follow reach the requested thresholds in a few steps)
+      const bool handover = o->final_fp64 && precision == GBHF_PREC_MIXED;
+      const double ce = handover ? std::max(o->conv_energy, 1e-9) : o->conv_energy;
+      const double cd = handover ? std::max(o->conv_density, 1e-7) : o->conv_density;
+      converged = have_prev && std::fabs(energy - e_prev) < ce && rms < cd;
+      if (trace)
+        std::fprintf(stderr, "gbhf scf %3d  E %.12f  dE %+.3e  rms(dD) %.3e  max|e| %.3e  diis %d  %s%s\n", step,
+                     energy, have_prev ? energy - e_prev : 0.0, rms, maxe, diis_on ? (int)stored.size() : 0,
+                     precision == GBHF_PREC_FP64 ? "fp64" : "mixed", fp64_final_phase ? " final" : "");
     }
     c->prof.ph_other += ms_since(t_phase);
     e_prev = energy;

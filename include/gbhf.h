@@ -72,7 +72,8 @@ typedef struct {
   int max_iter;          /* reference: 30 */
   int incremental;       /* 1: rebuild only G(D_n - D_(n-1)) between full builds */
   int full_rebuild_every;/* incremental mode: full rebuild period (0 = never) */
-  int final_fp64;        /* mixed mode: finish with FP64 builds once converged in mixed precision */
+  int final_fp64;        /* mixed mode: once converged in mixed precision, continue with full FP64
+                            builds until converged again */
   int ref_stop_rule;     /* 1: stop when step>0 and max|e| < conv_error, E from F_DIIS and the new D
                                 (HartreeFock.hs:112-114); 0: stop on |dE| and RMS(dD) */
   double conv_error;     /* reference: 1e-7 */
