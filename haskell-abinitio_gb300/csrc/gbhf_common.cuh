@@ -70,6 +70,18 @@ __device__ __forceinline__ double rsqrt_d(double x) {
   return fma(y * e, fma(0.375, e, 0.5), y);
 }
 
+// float -> double without the conversion instruction (which runs on the FP64
+// pipe): the exponent is rebiased and the mantissa shifted with integer ops.
+// Zeros and float denormals (|x| < 1.2e-38) give 0; the FP32 kernels never
+// produce Inf or NaN from finite data.
+__device__ __forceinline__ double widen(double x) { return x; }
+__device__ __forceinline__ double widen(float x) {
+  const int b = __float_as_int(x);
+  if ((b & 0x7f800000) == 0) return 0.0;
+  const int hi = (b & (int)0x80000000) | ((((b >> 23) & 0xff) + 896) << 20) | ((b >> 3) & 0xfffff);
+  return __hiloint2double(hi, (int)((unsigned)b << 29));
+}
+
 template <typename T> __device__ __forceinline__ T rsqrt_t(T x);
 template <> __device__ __forceinline__ double rsqrt_t<double>(double x) { return rsqrt_d(x); }
 template <> __device__ __forceinline__ float rsqrt_t<float>(float x) { return rsqrtf(x); }
@@ -112,13 +124,14 @@ template <int L> struct BoysCfg<float, L> {
 // F_m = (2t F_(m+1) + exp(-t)) / (2m + 1), whose terms are all positive.  Rows are
 // 16-byte aligned and read with vector loads.
 #define BOYSH_LMAX 5
-#define BOYSH64_STRIDE 14   // 7 + 7 doubles
+#define BOYSH64_STRIDE 16   // 7 + 7 doubles, the node T_j, padding
 #define BOYSH32_STRIDE 12   // 5 + 5 floats, padded to 16 bytes
 template <typename T> struct BoysHStride;
 template <> struct BoysHStride<double> { static constexpr int S = BOYSH64_STRIDE, NROW = BOYS64_NROW; };
 template <> struct BoysHStride<float> { static constexpr int S = BOYSH32_STRIDE, NROW = BOYS32_NROW; };
 
-// The 2 * NT coefficients of a row (only the first NT when exp is not needed).
+// The 2 * NT coefficients of a row (only the first NT when exp is not needed);
+// FP64 rows also carry their node T_j in c[2 * NT].
 template <int NT, bool EXP>
 __device__ __forceinline__ void boys_row(const double* __restrict__ row, double* c) {
   const double2* v = reinterpret_cast<const double2*>(row);
@@ -128,6 +141,8 @@ __device__ __forceinline__ void boys_row(const double* __restrict__ row, double*
     c[2 * i] = x.x;
     c[2 * i + 1] = x.y;
   }
+  const double2 x = __ldg(v + NT);   // node (and padding)
+  c[2 * NT] = x.x;
 }
 template <int NT, bool EXP>
 __device__ __forceinline__ void boys_row(const float* __restrict__ row, float* c) {
@@ -146,14 +161,30 @@ template <typename T, int L>
 __device__ __forceinline__ void boys_eval(T t, const T* __restrict__ tab, T* F) {
   using C = BoysCfg<T, L>;
   static_assert(L <= BOYSH_LMAX, "the Boys tables hold orders up to BOYSH_LMAX");
-  if (t < T(C::TMAX)) {
-    int j;
-    const T node = round_node(t * T(1.0 / C::H), j);
-    const T dx = node * T(C::H) - t;   // = -(t - T_j)
+  // Node index and range test in FP32 for FP64 arguments (t truncated to float by
+  // moving its exponent and mantissa bits; |t - T_j| stays within 0.0251), so the
+  // FP64 pipe only does dx = T_j - t.
+  bool in_table;
+  int j;
+  T node;
+  if constexpr (sizeof(T) == 8) {
+    const int hi = __double2hiint(t);
+    const float tf = hi < 0x38100000 ? 0.0f : __int_as_float((hi - 0x38000000) << 3);
+    in_table = tf < float(C::TMAX);
+    round_node(tf * float(1.0 / C::H), j);
+    node = T(0);
+  } else {
+    in_table = t < T(C::TMAX);
+    node = round_node(t * T(1.0 / C::H), j);
+  }
+  if (in_table) {
     const T* row = tab + ((size_t)L * BoysHStride<T>::NROW + j) * BoysHStride<T>::S;
     constexpr int NT = C::NT;
     T c[2 * NT + 4];
     boys_row<NT, (L >= 1)>(row, c);
+    T dx;   // = -(t - T_j)
+    if constexpr (sizeof(T) == 8) dx = c[2 * NT] - t;
+    else dx = node * T(C::H) - t;
     T s = c[NT - 1];
 #pragma unroll
     for (int k = NT - 2; k >= 0; --k) s = fma_t(s, dx, c[k]);

@@ -180,8 +180,10 @@ __global__ void __launch_bounds__(GR_THREADS) k_grad_jk(GradArgs<T> a) {
     }
 #pragma unroll
     for (int x = 0; x < 6; ++x) {
-      const double v = warp_sum_d(double(wgt * g[x]));
-      if (lane == 0) atomicAdd(&a.grad[3 * a.shell_atom[x < 3 ? A : B] + x % 3], v);
+      T v = wgt * g[x];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      if (lane == 0) atomicAdd(&a.grad[3 * a.shell_atom[x < 3 ? A : B] + x % 3], widen(v));
     }
     __syncwarp();
   }

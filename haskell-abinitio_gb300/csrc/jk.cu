@@ -199,7 +199,7 @@ __global__ void __launch_bounds__(JK_THREADS) k_jk(JKArgs<T> a) {
 #pragma unroll
       for (int cd = 0; cd < NCD; ++cd) v = fma_t(acc.get(ab * NCD + cd), dcd[cd], v);
       v = warp_sum(T(2) * s * v);   // s depends on the lane's ket: apply before the reduction
-      if (lane == 0) atomicAdd(&Gm[(long long)(a0 + ab / NB) * n + b0 + ab % NB], double(v));
+      if (lane == 0) atomicAdd(&Gm[(long long)(a0 + ab / NB) * n + b0 + ab % NB], widen(v));
     }
     if (active) {
       // J_cd
@@ -208,7 +208,7 @@ __global__ void __launch_bounds__(JK_THREADS) k_jk(JKArgs<T> a) {
         T v = 0;
 #pragma unroll
         for (int ab = 0; ab < NAB; ++ab) v = fma_t(acc.get(ab * NCD + cd), sDab[warp][ab], v);
-        atomicAdd(&Gm[(long long)(c0 + cd / ND) * n + d0 + cd % ND], double(T(2) * s * v));
+        atomicAdd(&Gm[(long long)(c0 + cd / ND) * n + d0 + cd % ND], widen(T(2) * s * v));
       }
       const T ks = T(-0.5) * s;
       // K_ac -= sum_bd v D_bd ; K_ad -= sum_bc v D_bc
@@ -222,7 +222,7 @@ __global__ void __launch_bounds__(JK_THREADS) k_jk(JKArgs<T> a) {
 #pragma unroll
             for (int id = 0; id < ND; ++id)
               v = fma_t(acc.get((ia * NB + ibb) * NCD + ic * ND + id), Dm[(long long)(b0 + ibb) * n + d0 + id], v);
-          atomicAdd(&Gm[(long long)(a0 + ia) * n + c0 + ic], double(ks * v));
+          atomicAdd(&Gm[(long long)(a0 + ia) * n + c0 + ic], widen(ks * v));
         }
 #pragma unroll
         for (int id = 0; id < ND; ++id) {
@@ -232,7 +232,7 @@ __global__ void __launch_bounds__(JK_THREADS) k_jk(JKArgs<T> a) {
 #pragma unroll
             for (int ic = 0; ic < NC; ++ic)
               v = fma_t(acc.get((ia * NB + ibb) * NCD + ic * ND + id), Dm[(long long)(b0 + ibb) * n + c0 + ic], v);
-          atomicAdd(&Gm[(long long)(a0 + ia) * n + d0 + id], double(ks * v));
+          atomicAdd(&Gm[(long long)(a0 + ia) * n + d0 + id], widen(ks * v));
         }
       }
       // K_bc -= sum_ad v D_ad ; K_bd -= sum_ac v D_ac
@@ -246,7 +246,7 @@ __global__ void __launch_bounds__(JK_THREADS) k_jk(JKArgs<T> a) {
 #pragma unroll
             for (int id = 0; id < ND; ++id)
               v = fma_t(acc.get((ia * NB + ibb) * NCD + ic * ND + id), Dm[(long long)(a0 + ia) * n + d0 + id], v);
-          atomicAdd(&Gm[(long long)(b0 + ibb) * n + c0 + ic], double(ks * v));
+          atomicAdd(&Gm[(long long)(b0 + ibb) * n + c0 + ic], widen(ks * v));
         }
 #pragma unroll
         for (int id = 0; id < ND; ++id) {
@@ -256,7 +256,7 @@ __global__ void __launch_bounds__(JK_THREADS) k_jk(JKArgs<T> a) {
 #pragma unroll
             for (int ic = 0; ic < NC; ++ic)
               v = fma_t(acc.get((ia * NB + ibb) * NCD + ic * ND + id), Dm[(long long)(a0 + ia) * n + c0 + ic], v);
-          atomicAdd(&Gm[(long long)(b0 + ibb) * n + d0 + id], double(ks * v));
+          atomicAdd(&Gm[(long long)(b0 + ibb) * n + d0 + id], widen(ks * v));
         }
       }
     }

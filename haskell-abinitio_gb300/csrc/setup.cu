@@ -201,6 +201,7 @@ gbhf_status ensure_boys_tables(gbhf_ctx* c) {
         row[k] = t64[(size_t)j * BOYS_NCOL + L + k] * inv_fact;
         row[BOYS64_NTERM + k] = std::exp(-j * BOYS64_H) * inv_fact;
       }
+      row[2 * BOYS64_NTERM] = j * BOYS64_H;   // the node itself
     }
     for (int j = 0; j < BOYS32_NROW; ++j) {
       float* row = h32.data() + ((size_t)L * BOYS32_NROW + j) * BOYSH32_STRIDE;
