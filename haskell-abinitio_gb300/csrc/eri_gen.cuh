@@ -3,7 +3,7 @@
 
 // ---- class (ss|ss): 1x1 integrals, L = 0
 template <typename T, typename Acc>
-__device__ __forceinline__ void eri_ketprim_ssss(const T* __restrict__ sb, int nbra,
+__device__ __forceinline__ void eri_ketprim_ssss(const T* __restrict__ sb, int nbra, int bstep,
     const T q, const T invq, const T Qx, const T Qy, const T Qz,
     const T QCx, const T QCy, const T QCz, const T QDx, const T QDy, const T QDz,
     const T Kcd, const T* __restrict__ boys, Acc& acc) {
@@ -14,7 +14,7 @@ __device__ __forceinline__ void eri_ketprim_ssss(const T* __restrict__ sb, int n
   #pragma unroll 1
   for (int kb = 0; kb < nbra; ++kb) {
     BraPrim<T> bp;
-    load_bra_prim(sb + kb * BRA_SB, bp);
+    load_bra_prim(sb + kb * bstep, bp);
     const T p = bp.p, invp = bp.invp, Px = bp.Px, Py = bp.Py, Pz = bp.Pz;
     const T Kab = bp.K;
     const T X = Px - Qx, Y = Py - Qy, Z = Pz - Qz;
@@ -38,7 +38,7 @@ __device__ __forceinline__ void eri_ketprim_ssss(const T* __restrict__ sb, int n
 
 // ---- class (ps|ss): 3x1 integrals, L = 1
 template <typename T, typename Acc>
-__device__ __forceinline__ void eri_ketprim_psss(const T* __restrict__ sb, int nbra,
+__device__ __forceinline__ void eri_ketprim_psss(const T* __restrict__ sb, int nbra, int bstep,
     const T q, const T invq, const T Qx, const T Qy, const T Qz,
     const T QCx, const T QCy, const T QCz, const T QDx, const T QDy, const T QDz,
     const T Kcd, const T* __restrict__ boys, Acc& acc) {
@@ -49,7 +49,7 @@ __device__ __forceinline__ void eri_ketprim_psss(const T* __restrict__ sb, int n
   #pragma unroll 1
   for (int kb = 0; kb < nbra; ++kb) {
     BraPrim<T> bp;
-    load_bra_prim(sb + kb * BRA_SB, bp);
+    load_bra_prim(sb + kb * bstep, bp);
     const T p = bp.p, invp = bp.invp, Px = bp.Px, Py = bp.Py, Pz = bp.Pz;
     const T PAx = bp.PAx, PAy = bp.PAy, PAz = bp.PAz;
     const T Kab = bp.K;
@@ -90,7 +90,7 @@ __device__ __forceinline__ void eri_ketprim_psss(const T* __restrict__ sb, int n
 
 // ---- class (ps|ps): 3x3 integrals, L = 2
 template <typename T, typename Acc>
-__device__ __forceinline__ void eri_ketprim_psps(const T* __restrict__ sb, int nbra,
+__device__ __forceinline__ void eri_ketprim_psps(const T* __restrict__ sb, int nbra, int bstep,
     const T q, const T invq, const T Qx, const T Qy, const T Qz,
     const T QCx, const T QCy, const T QCz, const T QDx, const T QDy, const T QDz,
     const T Kcd, const T* __restrict__ boys, Acc& acc) {
@@ -112,7 +112,7 @@ __device__ __forceinline__ void eri_ketprim_psps(const T* __restrict__ sb, int n
   #pragma unroll 1
   for (int kb = 0; kb < nbra; ++kb) {
     BraPrim<T> bp;
-    load_bra_prim(sb + kb * BRA_SB, bp);
+    load_bra_prim(sb + kb * bstep, bp);
     const T p = bp.p, invp = bp.invp, Px = bp.Px, Py = bp.Py, Pz = bp.Pz;
     const T PAx = bp.PAx, PAy = bp.PAy, PAz = bp.PAz;
     const T Kab = bp.K;
@@ -182,7 +182,7 @@ __device__ __forceinline__ void eri_ketprim_psps(const T* __restrict__ sb, int n
 
 // ---- class (pp|ss): 9x1 integrals, L = 2
 template <typename T, typename Acc>
-__device__ __forceinline__ void eri_ketprim_ppss(const T* __restrict__ sb, int nbra,
+__device__ __forceinline__ void eri_ketprim_ppss(const T* __restrict__ sb, int nbra, int bstep,
     const T q, const T invq, const T Qx, const T Qy, const T Qz,
     const T QCx, const T QCy, const T QCz, const T QDx, const T QDy, const T QDz,
     const T Kcd, const T* __restrict__ boys, Acc& acc) {
@@ -193,7 +193,7 @@ __device__ __forceinline__ void eri_ketprim_ppss(const T* __restrict__ sb, int n
   #pragma unroll 1
   for (int kb = 0; kb < nbra; ++kb) {
     BraPrim<T> bp;
-    load_bra_prim(sb + kb * BRA_SB, bp);
+    load_bra_prim(sb + kb * bstep, bp);
     const T p = bp.p, invp = bp.invp, Px = bp.Px, Py = bp.Py, Pz = bp.Pz;
     const T PAx = bp.PAx, PAy = bp.PAy, PAz = bp.PAz;
     const T PBx = bp.PBx, PBy = bp.PBy, PBz = bp.PBz;
@@ -273,7 +273,7 @@ __device__ __forceinline__ void eri_ketprim_ppss(const T* __restrict__ sb, int n
 
 // ---- class (pp|ps): 9x3 integrals, L = 3
 template <typename T, typename Acc>
-__device__ __forceinline__ void eri_ketprim_ppps(const T* __restrict__ sb, int nbra,
+__device__ __forceinline__ void eri_ketprim_ppps(const T* __restrict__ sb, int nbra, int bstep,
     const T q, const T invq, const T Qx, const T Qy, const T Qz,
     const T QCx, const T QCy, const T QCz, const T QDx, const T QDy, const T QDz,
     const T Kcd, const T* __restrict__ boys, Acc& acc) {
@@ -295,7 +295,7 @@ __device__ __forceinline__ void eri_ketprim_ppps(const T* __restrict__ sb, int n
   #pragma unroll 1
   for (int kb = 0; kb < nbra; ++kb) {
     BraPrim<T> bp;
-    load_bra_prim(sb + kb * BRA_SB, bp);
+    load_bra_prim(sb + kb * bstep, bp);
     const T p = bp.p, invp = bp.invp, Px = bp.Px, Py = bp.Py, Pz = bp.Pz;
     const T PAx = bp.PAx, PAy = bp.PAy, PAz = bp.PAz;
     const T PBx = bp.PBx, PBy = bp.PBy, PBz = bp.PBz;
@@ -438,7 +438,7 @@ __device__ __forceinline__ void eri_ketprim_ppps(const T* __restrict__ sb, int n
 
 // ---- class (pp|pp): 9x9 integrals, L = 4
 template <typename T, typename Acc>
-__device__ __forceinline__ void eri_ketprim_pppp(const T* __restrict__ sb, int nbra,
+__device__ __forceinline__ void eri_ketprim_pppp(const T* __restrict__ sb, int nbra, int bstep,
     const T q, const T invq, const T Qx, const T Qy, const T Qz,
     const T QCx, const T QCy, const T QCz, const T QDx, const T QDy, const T QDz,
     const T Kcd, const T* __restrict__ boys, Acc& acc) {
@@ -502,7 +502,7 @@ __device__ __forceinline__ void eri_ketprim_pppp(const T* __restrict__ sb, int n
   #pragma unroll 1
   for (int kb = 0; kb < nbra; ++kb) {
     BraPrim<T> bp;
-    load_bra_prim(sb + kb * BRA_SB, bp);
+    load_bra_prim(sb + kb * bstep, bp);
     const T p = bp.p, invp = bp.invp, Px = bp.Px, Py = bp.Py, Pz = bp.Pz;
     const T PAx = bp.PAx, PAy = bp.PAy, PAz = bp.PAz;
     const T PBx = bp.PBx, PBy = bp.PBy, PBz = bp.PBz;

@@ -86,10 +86,11 @@ struct ClassFn;
   template <>                                                                                            \
   struct ClassFn<la, lb, lc, ld> {                                                                       \
     template <typename T, typename Acc>                                                                  \
-    static __device__ __forceinline__ void run(const T* sb, int nbra, T q, T invq, T Qx, T Qy, T Qz, T QCx, \
-                                               T QCy, T QCz, T QDx, T QDy, T QDz, T Kcd, const T* boys,   \
-                                               Acc& acc) {                                               \
-      eri_ketprim_##name<T, Acc>(sb, nbra, q, invq, Qx, Qy, Qz, QCx, QCy, QCz, QDx, QDy, QDz, Kcd, boys, acc); \
+    static __device__ __forceinline__ void run(const T* sb, int nbra, int bstep, T q, T invq, T Qx, T Qy, T Qz,  \
+                                               T QCx, T QCy, T QCz, T QDx, T QDy, T QDz, T Kcd,           \
+                                               const T* boys, Acc& acc) {                                 \
+      eri_ketprim_##name<T, Acc>(sb, nbra, bstep, q, invq, Qx, Qy, Qz, QCx, QCy, QCz, QDx, QDy, QDz, Kcd, boys, \
+                                 acc);                                                                   \
     }                                                                                                    \
   };
 GBHF_CLASS_FN(0, 0, 0, 0, ssss)
@@ -135,15 +136,34 @@ __global__ void __launch_bounds__(JK_THREADS) k_jk(JKArgs<T> a) {
     if (t >= ntask) break;
     const int4 task = a.tasks[start + t];
     const int ib = task.x;
-    const int jk = task.y + lane;
+    // lanes beyond the task's kets split the primitive quartets: kets sit on the
+    // low lg bits of the lane (nk <= 2^lg), the rest of the lane is the slice;
+    // the nsl slices form an nsb x (nsl / nsb) grid over bra and ket primitives
+    const int nk = task.z;
+    const int lg = 32 - __clz(max(nk, 1) - 1);   // ceil(log2(nk)), 0 for one ket
+    const int nsl = 32 >> lg;
+    const int slice = lane >> lg;
+    const int jk = task.y + (lane & ((1 << lg) - 1));
+    const int kb0 = task.w & 0xffff, Kb = (task.w >> 16) - kb0, pb0 = a.poff[ib] + kb0;
+    const int K = a.seg[a.kseg[task.y]].z;   // ket primitive pairs, shared by the task's kets
+    int lb = 0;
+    for (int l = 0, best = 1 << 30; (1 << l) <= nsl; ++l) {   // fewest primitive quartets per lane
+      const int cost = ((Kb + (1 << l) - 1) >> l) * ((K + (nsl >> l) - 1) / (nsl >> l));
+      if (cost <= best) {
+        best = cost;
+        lb = l;
+      }
+    }
+    const int nsb = 1 << lb, nsk = nsl >> lb;
+    const int sb = slice & (nsb - 1), sk = slice >> lb;
     // the molecule's density and Fock blocks (stacked matrices)
     const int mol = a.pmol[ib];
     const int n = a.mn[mol];
     const T* __restrict__ Dm = a.D + a.moff[mol];
     double* __restrict__ Gm = a.G + a.moff[mol];
-    const bool active = lane < task.z;
+    const bool active = (lane & ((1 << lg) - 1)) < nk;   // computes
+    const bool lead = active && slice == 0;               // scatters
     // bra primitives [kb0, kb1) of pair ib
-    const int kb0 = task.w & 0xffff, Kb = (task.w >> 16) - kb0, pb0 = a.poff[ib] + kb0;
     for (int idx = lane; idx < BRA_NJK * Kb; idx += 32) {
       const int f = idx / Kb, k = idx - f * Kb;
       sbra[warp][k * BRA_SB + f] = a.bra[(long long)f * npp + pb0 + k];
@@ -160,9 +180,10 @@ __global__ void __launch_bounds__(JK_THREADS) k_jk(JKArgs<T> a) {
       c0 = a.shell_f0[C];
       d0 = a.shell_f0[Dd];
       const int4 sg = a.seg[a.kseg[jk]];
-      const int K = sg.z, len = sg.y - sg.x;
+      const int len = sg.y - sg.x;
       const long long base = (long long)sg.w + (jk - sg.x);
-      for (int kc = 0; kc < K; ++kc) {
+      const int nbl = sb < Kb ? (Kb - sb + nsb - 1) / nsb : 0;   // this lane's bra primitives
+      for (int kc = sk; kc < K; kc += nsk) {
         const long long idx = base + (long long)kc * len;
         const T q = a.ket[BRA_P * npp + idx];
         const T invq = a.ket[BRA_INVP * npp + idx];
@@ -179,11 +200,16 @@ __global__ void __launch_bounds__(JK_THREADS) k_jk(JKArgs<T> a) {
           QDz = a.ket[BRA_PBZ * npp + idx];
         }
         const T Kcd = a.ket[BRA_K * npp + idx];
-        ClassFn<LA, LB, LC, LD>::template run<T, AccT>(sbra[warp], Kb, q, invq, Qx, Qy, Qz, QCx, QCy, QCz, QDx,
-                                                       QDy, QDz, Kcd, a.boys, acc);
+        ClassFn<LA, LB, LC, LD>::template run<T, AccT>(sbra[warp] + sb * BRA_SB, nbl, nsb * BRA_SB, q, invq,
+                                                       Qx, Qy, Qz, QCx, QCy, QCz, QDx, QDy, QDz, Kcd, a.boys, acc);
       }
-      cnt_q += kb0 == 0;
-      cnt_p += (unsigned long long)Kb * K;
+      cnt_q += lead && kb0 == 0;
+      cnt_p += (unsigned long long)nbl * (sk < K ? (K - sk + nsk - 1) / nsk : 0);
+    }
+    // warp-uniform: sum the slices (every lane ends with the total of its ket)
+    for (int o = 1 << lg; o < 32; o <<= 1) {
+#pragma unroll
+      for (int i = 0; i < NOUT; ++i) acc[i] += __shfl_xor_sync(0xffffffffu, acc.get(i), o);
     }
     // ---- scatter into G'' (FP64 atomics)
     const T s = (A == B ? T(0.5) : T(1)) * (C == Dd ? T(0.5) : T(1)) * (ib == jk ? T(0.5) : T(1));
@@ -191,7 +217,7 @@ __global__ void __launch_bounds__(JK_THREADS) k_jk(JKArgs<T> a) {
 #pragma unroll
     for (int ic = 0; ic < NC; ++ic)
 #pragma unroll
-      for (int id = 0; id < ND; ++id) dcd[ic * ND + id] = active ? Dm[(long long)(c0 + ic) * n + d0 + id] : T(0);
+      for (int id = 0; id < ND; ++id) dcd[ic * ND + id] = lead ? Dm[(long long)(c0 + ic) * n + d0 + id] : T(0);
     // J_ab (warp reduce over kets)
 #pragma unroll
     for (int ab = 0; ab < NAB; ++ab) {
@@ -201,7 +227,7 @@ __global__ void __launch_bounds__(JK_THREADS) k_jk(JKArgs<T> a) {
       v = warp_sum(T(2) * s * v);   // s depends on the lane's ket: apply before the reduction
       if (lane == 0) atomicAdd(&Gm[(long long)(a0 + ab / NB) * n + b0 + ab % NB], widen(v));
     }
-    if (active) {
+    if (lead) {
       // J_cd
 #pragma unroll
       for (int cd = 0; cd < NCD; ++cd) {
@@ -298,7 +324,7 @@ __global__ void __launch_bounds__(SCHWARZ_THREADS) k_schwarz_cls(int p0, int p1,
   for (int k = 0; k < K; ++k) {
     auto g = [&](int f) { return s[k * BRA_SB + f]; };
     ClassFn<LA, LB, LA, LB>::template run<double, RegAcc<double, NAB * NAB>>(
-        s, K, g(BRA_P), g(BRA_INVP), g(BRA_PX), g(BRA_PY), g(BRA_PZ), g(BRA_PAX), g(BRA_PAY), g(BRA_PAZ),
+        s, K, BRA_SB, g(BRA_P), g(BRA_INVP), g(BRA_PX), g(BRA_PY), g(BRA_PZ), g(BRA_PAX), g(BRA_PAY), g(BRA_PAZ),
         g(BRA_PBX), g(BRA_PBY), g(BRA_PBZ), g(BRA_K), boys, acc);
   }
   double mx = 0;
