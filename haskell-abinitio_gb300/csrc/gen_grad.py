@@ -92,7 +92,7 @@ def gen_class(la, lb, lc, ld):
     w = out.append
     w(f"// ---- gradient class ({cls[0]}{cls[1]}|{cls[2]}{cls[3]}): bra-centre derivatives, L + 1 = {L}")
     w("template <typename T, typename G>")
-    w(f"__device__ __forceinline__ void grad_ketprim_{cls}(const T* __restrict__ sb, int nbra,")
+    w(f"__device__ __forceinline__ void grad_ketprim_{cls}(const T* __restrict__ sb, int nbra, int bstep,")
     w("    const T q, const T invq, const T Qx, const T Qy, const T Qz,")
     w("    const T QCx, const T QCy, const T QCz, const T QDx, const T QDy, const T QDz,")
     w("    const T Kcd, const T* __restrict__ boys, const G& gam, T* g) {")
@@ -130,7 +130,7 @@ def gen_class(la, lb, lc, ld):
     w("  #pragma unroll 1")
     w("  for (int kb = 0; kb < nbra; ++kb) {")
     w("    BraPrim<T> bp;")
-    w("    load_bra_prim(sb + kb * BRA_SB, bp);")
+    w("    load_bra_prim(sb + kb * bstep, bp);")
     w("    const T p = bp.p, invp = bp.invp, Px = bp.Px, Py = bp.Py, Pz = bp.Pz;")
     w("    const T PAx = bp.PAx, PAy = bp.PAy, PAz = bp.PAz;")
     w("    const T PBx = bp.PBx, PBy = bp.PBy, PBz = bp.PBz;")

@@ -54,10 +54,11 @@ struct GradFn;
   template <>                                                                                                  \
   struct GradFn<la, lb, lc, ld> {                                                                              \
     template <typename T, typename G>                                                                          \
-    static __device__ __forceinline__ void run(const T* sb, int nbra, T q, T invq, T Qx, T Qy, T Qz, T QCx,    \
-                                               T QCy, T QCz, T QDx, T QDy, T QDz, T Kcd, const T* boys,         \
+    static __device__ __forceinline__ void run(const T* sb, int nbra, int bstep, T q, T invq, T Qx, T Qy, T Qz, \
+                                               T QCx, T QCy, T QCz, T QDx, T QDy, T QDz, T Kcd, const T* boys,  \
                                                const G& gam, T* g) {                                           \
-      grad_ketprim_##name<T, G>(sb, nbra, q, invq, Qx, Qy, Qz, QCx, QCy, QCz, QDx, QDy, QDz, Kcd, boys, gam, g); \
+      grad_ketprim_##name<T, G>(sb, nbra, bstep, q, invq, Qx, Qy, Qz, QCx, QCy, QCz, QDx, QDy, QDz, Kcd, boys, \
+                                gam, g);                                                                       \
     }                                                                                                          \
   };
 GBHF_GRAD_FN(0, 0, 0, 0, ssss)
@@ -117,12 +118,30 @@ __global__ void __launch_bounds__(GR_THREADS) k_grad_jk(GradArgs<T> a) {
     if (t >= ntask) break;
     const int4 task = a.tasks[start + t];
     const int ib = task.x;
-    const int jk = task.y + lane;
+    // lanes beyond the task's kets split the primitive quartets (as in k_jk):
+    // ket on the low lg bits of the lane, an nsb x nsk grid of bra and ket
+    // primitive slices on the rest; the closing warp sum adds the slices
+    const int nk = task.z;
+    const int lg = 32 - __clz(max(nk, 1) - 1);
+    const int nsl = 32 >> lg;
+    const int slice = lane >> lg;
+    const int jk = task.y + (lane & ((1 << lg) - 1));
     const int mol = a.pmol[ib];
     const int n = a.mn[mol];
     const T* __restrict__ Dm = a.D + a.moff[mol];
-    const bool active = lane < task.z;
+    const bool active = (lane & ((1 << lg) - 1)) < nk;
     const int kb0 = task.w & 0xffff, Kb = (task.w >> 16) - kb0, pb0 = a.poff[ib] + kb0;
+    const int K = a.seg[a.kseg[task.y]].z;
+    int lb = 0;
+    for (int l = 0, best = 1 << 30; (1 << l) <= nsl; ++l) {
+      const int cost = ((Kb + (1 << l) - 1) >> l) * ((K + (nsl >> l) - 1) / (nsl >> l));
+      if (cost <= best) {
+        best = cost;
+        lb = l;
+      }
+    }
+    const int nsb = 1 << lb, nsk = nsl >> lb;
+    const int sb = slice & (nsb - 1), sk = slice >> lb;
     for (int idx = lane; idx < BRA_NFIELD * Kb; idx += 32) {
       const int f = idx / Kb, k = idx - f * Kb;
       sbra[warp][k * BRA_SB + f] = a.bra[(long long)f * npp + pb0 + k];
@@ -154,9 +173,10 @@ __global__ void __launch_bounds__(GR_THREADS) k_grad_jk(GradArgs<T> a) {
               gam.set(((ia * NB + ibb) * NC + ic) * ND + id, dab * dcd - T(0.25) * (dac * dbd + dad * dbc));
             }
       const int4 sg = a.seg[a.kseg[jk]];
-      const int K = sg.z, len = sg.y - sg.x;
+      const int len = sg.y - sg.x;
       const long long base = (long long)sg.w + (jk - sg.x);
-      for (int kc = 0; kc < K; ++kc) {
+      const int nbl = sb < Kb ? (Kb - sb + nsb - 1) / nsb : 0;
+      for (int kc = sk; kc < K; kc += nsk) {
         const long long idx = base + (long long)kc * len;
         const T q = a.ket[BRA_P * npp + idx];
         const T invq = a.ket[BRA_INVP * npp + idx];
@@ -173,8 +193,8 @@ __global__ void __launch_bounds__(GR_THREADS) k_grad_jk(GradArgs<T> a) {
           QDz = a.ket[BRA_PBZ * npp + idx];
         }
         const T Kcd = a.ket[BRA_K * npp + idx];
-        GradFn<LA, LB, LC, LD>::run(sbra[warp], Kb, q, invq, Qx, Qy, Qz, QCx, QCy, QCz, QDx, QDy, QDz, Kcd, a.boys,
-                                    gam, g);
+        GradFn<LA, LB, LC, LD>::run(sbra[warp] + sb * BRA_SB, nbl, nsb * BRA_SB, q, invq, Qx, Qy, Qz, QCx, QCy,
+                                    QCz, QDx, QDy, QDz, Kcd, a.boys, gam, g);
       }
       wgt = (A == B ? T(1) : T(2)) * (C == Dd ? T(1) : T(2));
     }
