@@ -186,6 +186,7 @@ __device__ __forceinline__ void sort_key(long& i, long& j, long& k, long& l) {
   }
 }
 
+template <int LM>
 __global__ void k_eri_canonical(bool ref, int nbf, const int* __restrict__ pair_i, const int* __restrict__ pair_j,
                                 long npair, const long* __restrict__ off, const double* __restrict__ xyz,
                                 const int* __restrict__ fn, const double* __restrict__ coef,
@@ -196,7 +197,7 @@ __global__ void k_eri_canonical(bool ref, int nbf, const int* __restrict__ pair_
   if (Q >= npair || Q < P) return;
   const long i = pair_i[P], j = pair_j[P], k = pair_i[Q], l = pair_j[Q];
   eri[canon_pos(off, nbf, i, j, k, l)] =
-      eri_fn_generic(ref, xyz, fn, coef, expo, grid, tab, (int)i, (int)j, (int)k, (int)l);
+      eri_fn_generic<LM>(ref, xyz, fn, coef, expo, grid, tab, (int)i, (int)j, (int)k, (int)l);
 }
 
 static void canonical_offsets(long n, std::vector<long>& off) {
@@ -237,16 +238,22 @@ static gbhf_status canon_aux(gbhf_ctx* c, CanonAux& aux) {
 
 gbhf_status eri_canonical_dev(gbhf_ctx* c, bool ref, double* d_eri) {
   const Basis& b = c->basis;
-  if (b.maxL > 1) return fail(c, GBHF_ERR_UNSUPPORTED, "canonical ERIs support s and p functions");
+  if (b.maxL > 2) return fail(c, GBHF_ERR_UNSUPPORTED, "canonical ERIs support s, p and d functions");
   if (ref && !c->have_grid) return fail(c, GBHF_ERR_BAD_INPUT, "reference mode needs gbhf_set_boys_grid");
   CanonAux aux;
   GBHF_TRY(canon_aux(c, aux));
   const long np = (long)b.nbf * (b.nbf + 1) / 2;
   if (np > 65535) return fail(c, GBHF_ERR_UNSUPPORTED, "canonical ERI array too large");
   dim3 grid((unsigned)((np + 127) / 128), (unsigned)np);
-  k_eri_canonical<<<grid, 128, 0, c->stream>>>(ref, b.nbf, aux.pi.p, aux.pj.p, np, aux.off.p, c->d_xyz.p,
-                                                c->d_fn.p, c->d_coef.p, c->d_exp.p, c->boys_ref.p, c->boys64.p,
-                                                d_eri);
+  // per-thread Hermite cubes sized for the largest total angular momentum: s/p quartets L <= 4, d L <= 8
+  if (b.maxL <= 1)
+    k_eri_canonical<MD_LMAX><<<grid, 128, 0, c->stream>>>(ref, b.nbf, aux.pi.p, aux.pj.p, np, aux.off.p, c->d_xyz.p,
+                                                          c->d_fn.p, c->d_coef.p, c->d_exp.p, c->boys_ref.p,
+                                                          c->boys64.p, d_eri);
+  else
+    k_eri_canonical<8><<<grid, 128, 0, c->stream>>>(ref, b.nbf, aux.pi.p, aux.pj.p, np, aux.off.p, c->d_xyz.p,
+                                                    c->d_fn.p, c->d_coef.p, c->d_exp.p, c->boys_ref.p, c->boys64.p,
+                                                    d_eri);
   count_launch(c);
   GBHF_CUDA(c, cudaGetLastError());
   GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -291,48 +298,6 @@ gbhf_status fock_canonical_dev(gbhf_ctx* c, const double* d_H, const double* d_D
   return GBHF_OK;
 }
 
-// ------------------------------------------------- Schwarz bounds ----
-// Q_AB = sqrt(max_{a in A, b in B} (ab|ab)), exact numerics.
-__global__ void k_schwarz(int npairs, const int* __restrict__ pa, const int* __restrict__ pb,
-                          const int* __restrict__ shell_f0, const int* __restrict__ shell_nc,
-                          const double* __restrict__ xyz, const int* __restrict__ fn,
-                          const double* __restrict__ coef, const double* __restrict__ expo,
-                          const double* __restrict__ tab, double* __restrict__ Q) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= npairs) return;
-  const int A = pa[t], B = pb[t];
-  double mx = 0;
-  for (int a = 0; a < shell_nc[A]; ++a)
-    for (int b = 0; b < shell_nc[B]; ++b) {
-      const int fa = shell_f0[A] + a, fb = shell_f0[B] + b;
-      const double v = eri_fn_generic(false, xyz, fn, coef, expo, nullptr, tab, fa, fb, fa, fb);
-      mx = fmax(mx, fabs(v));
-    }
-  Q[t] = sqrt(mx);
-}
-
-gbhf_status schwarz_pairs_dev(gbhf_ctx* c, const int* d_A, const int* d_B, int npairs, double* d_Q) {
-  const Basis& b = c->basis;
-  const int ns = (int)b.shells.size();
-  std::vector<int> f0(ns), nc(ns);
-  for (int s = 0; s < ns; ++s) {
-    f0[s] = b.shells[s].f0;
-    nc[s] = b.shells[s].ncomp;
-  }
-  DBuf<int> df0, dnc;
-  GBHF_CUDA(c, df0.alloc(ns));
-  GBHF_CUDA(c, dnc.alloc(ns));
-  GBHF_CUDA(c, cudaMemcpyAsync(df0.p, f0.data(), ns * sizeof(int), cudaMemcpyHostToDevice, c->stream));
-  GBHF_CUDA(c, cudaMemcpyAsync(dnc.p, nc.data(), ns * sizeof(int), cudaMemcpyHostToDevice, c->stream));
-  if (npairs > 0) {
-    k_schwarz<<<(npairs + 63) / 64, 64, 0, c->stream>>>(npairs, d_A, d_B, df0.p, dnc.p, c->d_xyz.p, c->d_fn.p,
-                                                       c->d_coef.p, c->d_exp.p, c->boys64.p, d_Q);
-    count_launch(c);
-    GBHF_CUDA(c, cudaGetLastError());
-  }
-  GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
-  return GBHF_OK;
-}
 
 }  // namespace gbhf
 

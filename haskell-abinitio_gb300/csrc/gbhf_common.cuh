@@ -8,15 +8,18 @@
 
 // Boys tables: F_m(T_j) on a uniform grid, row j holds m = 0 .. BOYS_NCOL-1.
 #define BOYS_NCOL 16
-// FP64: spacing 0.05 up to 38, 7-term Taylor about the nearest node.
+// FP64: spacing 0.05 up to 60, 7-term Taylor about the nearest node.  Beyond
+// TMAX the asymptotic form drops a term of relative size
+// exp(-T) T^(m-1/2) / Gamma(m+1/2): below 1e-16 for m <= 9 at T = 60.
 #define BOYS64_H 0.05
-#define BOYS64_TMAX 38.0
-#define BOYS64_NROW 762
+#define BOYS64_TMAX 60.0
+#define BOYS64_NROW 1202
 #define BOYS64_NTERM 7
-// FP32: spacing 0.1 up to 20, 5-term Taylor about the nearest node.
+// FP32: spacing 0.1 up to 36, 5-term Taylor about the nearest node (the
+// asymptotic term above is below 4e-8 for m <= 9 at T = 36).
 #define BOYS32_H 0.1f
-#define BOYS32_TMAX 20.0f
-#define BOYS32_NROW 202
+#define BOYS32_TMAX 36.0f
+#define BOYS32_NROW 362
 #define BOYS32_NTERM 5
 
 // Bra primitive-pair fields (shared-memory staging and global SoA layout).
@@ -105,8 +108,7 @@ template <> __device__ __forceinline__ double fma_t<double>(double a, double b, 
 template <> __device__ __forceinline__ float fma_t<float>(float a, float b, float c) { return fmaf(a, b, c); }
 
 // F_0..F_L(T) from the table by Taylor expansion about the nearest node;
-// asymptotic form F_0 = sqrt(pi/T)/2, F_m = F_(m-1) (2m-1)/(2T) beyond TMAX
-// (the neglected exp(-T) term is below 4e-17 there for FP64, 2e-9 for FP32).
+// asymptotic form F_0 = sqrt(pi/T)/2, F_m = F_(m-1) (2m-1)/(2T) beyond TMAX.
 template <typename T, int L> struct BoysCfg;
 template <int L> struct BoysCfg<double, L> {
   static constexpr double H = BOYS64_H, TMAX = BOYS64_TMAX;
@@ -123,7 +125,7 @@ template <int L> struct BoysCfg<float, L> {
 // FMAs each.  The lower orders follow by the downward recursion
 // F_m = (2t F_(m+1) + exp(-t)) / (2m + 1), whose terms are all positive.  Rows are
 // 16-byte aligned and read with vector loads.
-#define BOYSH_LMAX 5
+#define BOYSH_LMAX 9   // (dd|dd) gradient: L = 9
 #define BOYSH64_STRIDE 16   // 7 + 7 doubles, the node T_j, padding
 #define BOYSH32_STRIDE 12   // 5 + 5 floats, padded to 16 bytes
 template <typename T> struct BoysHStride;

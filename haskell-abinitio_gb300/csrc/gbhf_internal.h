@@ -140,18 +140,28 @@ struct DBuf {
 };
 
 struct Shell {
-  int atom, L, np, ncomp, f0;   // f0: first basis function (components contiguous, x,y,z order)
+  int atom, L, np, ncomp, f0;   // f0: first basis function (components contiguous: x,y,z; xx,xy,xz,yy,yz,zz)
   int mol = 0;                  // molecule of the shell (batched SCF); 0 for one molecule
-  std::vector<double> expo, coef;
+  std::vector<double> expo, coef;   // coef: the first component's contraction coefficients
+  double scale[6] = {1, 1, 1, 1, 1, 1};   // component c's coefficients = scale[c] * coef (d shells)
 };
 
-// Number of shell-pair classes with L <= 1: (s,s), (p,s), (p,p).
-constexpr int NPCLS = 3;
-// Quartet combos (bra class >= ket class).
-constexpr int NCOMBO = 6;
-constexpr int NCOMBO_MAX = 9;   // all (bra class, ket class) combinations (gradient lists)
-constexpr int COMBO_BRA[NCOMBO] = {0, 1, 1, 2, 2, 2};
-constexpr int COMBO_KET[NCOMBO] = {0, 0, 1, 0, 1, 2};
+// Shell-pair classes (la >= lb): 0 (s,s), 1 (p,s), 2 (p,p), 3 (d,s), 4 (d,p), 5 (d,d).
+constexpr int NPCLS = 6;
+__host__ __device__ constexpr int pair_class_of(int la, int lb) { return la * (la + 1) / 2 + lb; }
+// J/K quartet combos (bra class >= ket class): the six s/p classes first, then
+// the fifteen with a d pair (warp-per-quartet kernels).
+constexpr int NCOMBO = 21;
+constexpr int NCOMBO_SP = 6;
+constexpr int COMBO_BRA[NCOMBO] = {0, 1, 1, 2, 2, 2, 3, 3, 3, 3, 4, 4, 4, 4, 4, 5, 5, 5, 5, 5, 5};
+constexpr int COMBO_KET[NCOMBO] = {0, 0, 1, 0, 1, 2, 0, 1, 2, 3, 0, 1, 2, 3, 4, 0, 1, 2, 3, 4, 5};
+// Gradient combos: every ordered (bra class, ket class); the nine s/p ones first.
+constexpr int NCOMBO_MAX = 36;
+constexpr int NGCOMBO_SP = 9;
+constexpr int GRAD_COMBO_BRA[NCOMBO_MAX] = {0, 0, 0, 1, 1, 1, 2, 2, 2, 0, 0, 0, 1, 1, 1, 2, 2, 2,
+                                            3, 3, 3, 3, 3, 3, 4, 4, 4, 4, 4, 4, 5, 5, 5, 5, 5, 5};
+constexpr int GRAD_COMBO_KET[NCOMBO_MAX] = {0, 1, 2, 0, 1, 2, 0, 1, 2, 3, 4, 5, 3, 4, 5, 3, 4, 5,
+                                            0, 1, 2, 3, 4, 5, 0, 1, 2, 3, 4, 5, 0, 1, 2, 3, 4, 5};
 
 struct Segment {
   int start, end, K;   // global pair indices [start, end), primitive pairs per pair
@@ -183,7 +193,7 @@ struct Basis {
 // primitive-pair count (segments), inside a segment by Schwarz bound descending.
 struct PairData {
   int npairs = 0;
-  int cls_start[NPCLS + 1] = {0, 0, 0, 0};
+  int cls_start[NPCLS + 1] = {};
   std::vector<Segment> segs[NPCLS];
   std::vector<int> hA, hB, hK, hPoff, hSeg;  // host copies
   std::vector<double> hQ;
@@ -191,7 +201,7 @@ struct PairData {
   DBuf<double> Q;
   DBuf<int4> seg_info;                       // (start, end, K, data_off) per segment, all classes
   int nseg_total = 0;
-  int seg_cls_start[NPCLS + 1] = {0, 0, 0, 0};
+  int seg_cls_start[NPCLS + 1] = {};
   // molecules: pair -> molecule, and the ket segments of (class, molecule)
   // [mseg[2*(cls*nmol+m)], mseg[2*(cls*nmol+m)+1])
   DBuf<int> mol;
@@ -217,6 +227,7 @@ struct TaskLists {
   int ncombo = 0;
   int hranges[4 * NCOMBO_MAX] = {0};   // host copy of ranges
   DBuf<int> f0;                        // first basis function per shell
+  DBuf<double> sscale;                 // per shell: 6 component scales (d shells; 1 otherwise)
   DBuf<int> nc;                        // components per shell
   DBuf<int> atom;                      // atom of each shell
   DBuf<int> smol;                      // molecule of each shell
@@ -242,7 +253,7 @@ struct Profile {
   double jk_ms64 = 0, jk_ms32 = 0, dense_ms = 0;
   double prim64 = 0, prim32 = 0, shellq = 0, fnq = 0;
   long long launches = 0;
-  double cls[6][2][4] = {};   // per combo and precision: shell q, fn q, prim q, ms
+  double cls[NCOMBO][2][4] = {};   // per combo and precision: shell q, fn q, prim q, ms
   // host wall-clock per SCF phase (ms): setup, Fock, DIIS, diagonalisation, other; Jacobi sweeps
   double ph_setup = 0, ph_fock = 0, ph_diis = 0, ph_diag = 0, ph_other = 0, jacobi_sweeps = 0, jacobi_calls = 0;
   double ph_grad = 0, batch_steps = 0;
@@ -292,7 +303,7 @@ struct gbhf_ctx {
   gbhf::DBuf<double> small;
   gbhf::Profile prof;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
-  cudaEvent_t evc[13] = {};      // per-class J/K launch boundaries (profiling)
+  cudaEvent_t evc[2 * gbhf::NCOMBO + 1] = {};   // per-class J/K launch boundaries (profiling)
   cudaEvent_t evu[8] = {};       // user slots (gbhf_event_record)
   // side streams of the J/K build: the class kernels of one build run
   // concurrently so that the tail of one persistent launch overlaps the next
@@ -393,7 +404,6 @@ gbhf_status eri_canonical_dev(gbhf_ctx* c, bool ref, double* d_eri);
 gbhf_status fock_canonical_dev(gbhf_ctx* c, const double* d_H, const double* d_D, const double* d_eri, double* d_F);
 gbhf_status boys_dev(gbhf_ctx* c, bool ref, int mmax, int n, const double* d_x, double* d_out);
 gbhf_status boys_ref_grid_dev(gbhf_ctx* c, double* d_grid);
-gbhf_status schwarz_pairs_dev(gbhf_ctx* c, const int* d_A, const int* d_B, int npairs, double* d_Q);
 // jk.cu
 // G_acc (n*n) += sym(G''(D)), D square n*n.  w = screening weight.
 // local_weights: screen and choose precision with per-pair |D| weights (D is a
@@ -406,6 +416,16 @@ gbhf_status jk_build(gbhf_ctx* c, const double* d_Dsq, double* d_G, int precisio
 // bra-layout primitive data at d_poff), FP64 class code.
 gbhf_status schwarz_classes_dev(gbhf_ctx* c, const int* cls_start, const int* d_K, const int* d_poff,
                                 const double* d_bra, long long npp, double* d_Q);
+// jkd.cu / gradd.cu: the classes with a d pair (warp per shell quartet).
+// Schwarz bounds of classes 3..5 (dA, dB: shells of each pair, same order).
+gbhf_status schwarz_dclasses_dev(gbhf_ctx* c, const int* cls_start, const int* dA, const int* dB, const int* d_K,
+                                 const int* d_poff, const double* d_bra, long long npp, double* d_Q);
+// J/K launch of combo 6..20 (COMBO_BRA/COMBO_KET), precision 0 = FP64, 1 = FP32.
+gbhf_status launch_jk_dclass(gbhf_ctx* c, cudaStream_t strm, int combo, int prec, const double* D64,
+                             const float* D32, double* G, int ntask);
+// Gradient launch of combo 9..35 (GRAD_COMBO_BRA/GRAD_COMBO_KET).
+gbhf_status launch_grad_dclass(gbhf_ctx* c, cudaStream_t strm, int combo, int prec, const double* D64,
+                               const float* D32, double* grad, int ntask);
 // linalg.cu
 gbhf_status gemm(gbhf_ctx* c, bool ta, bool tb, int m, int n, int k, double alpha, const double* A, int lda,
                  const double* B, int ldb, double beta, double* C, int ldc);

@@ -7,7 +7,7 @@
 
 namespace gbhf {
 
-constexpr int MD_LMAX = 4;          // total angular momentum handled here (s,p quartets; d one-electron)
+constexpr int MD_LMAX = 4;          // default total angular momentum (s,p quartets; d one-electron)
 constexpr int MD_D = MD_LMAX + 1;
 
 struct DevFn {   // one contracted Gaussian
@@ -180,6 +180,7 @@ __device__ inline double two_terms_eri(const double* A, const int* la, double ca
 // One contracted ERI (ab|cd) over CGFs (contracted4Centers,
 // Integrals/IntegralsEvaluation.hs:294-306); ref enables the per-primitive
 // screening of schwarz (:308-315) and reference Boys.
+template <int LM = MD_LMAX>
 __device__ inline double eri_fn_generic(bool ref, const double* __restrict__ xyz, const int* __restrict__ fn,
                                         const double* __restrict__ coef, const double* __restrict__ expo,
                                         const double* __restrict__ grid, const double* __restrict__ tab, int i,
@@ -193,9 +194,10 @@ __device__ inline double eri_fn_generic(bool ref, const double* __restrict__ xyz
     lcd[x] = f[2].l[x] + f[3].l[x];
     L += lab[x] + lcd[x];
   }
+  constexpr int D = LM + 1;
   double sum = 0;
-  double F[MD_LMAX + 1];
-  double R[MD_D * MD_D * MD_D];
+  double F[LM + 1];
+  double R[D * D * D];
   EAx E1[3], E2[3];
   for (int p1 = 0; p1 < f[0].np; ++p1) {
     const double c1 = coef[f[0].off + p1], e1 = expo[f[0].off + p1];
@@ -227,7 +229,7 @@ __device__ inline double eri_fn_generic(bool ref, const double* __restrict__ xyz
           }
           const double alpha = p * q / (p + q);
           boys_generic(ref, grid, tab, L, alpha * (PQ[0] * PQ[0] + PQ[1] * PQ[1] + PQ[2] * PQ[2]), F);
-          hermite_r<MD_LMAX>(L, alpha, PQ[0], PQ[1], PQ[2], F, R);
+          hermite_r<LM>(L, alpha, PQ[0], PQ[1], PQ[2], F, R);
           double total = 0;
           for (int t = 0; t <= lab[0]; ++t)
             for (int u = 0; u <= lab[1]; ++u)
@@ -240,7 +242,7 @@ __device__ inline double eri_fn_generic(bool ref, const double* __restrict__ xyz
                     for (int phi = 0; phi <= lcd[2]; ++phi) {
                       double ek = E2[0].get(f[2].l[0], f[3].l[0], tau) * E2[1].get(f[2].l[1], f[3].l[1], nu2) *
                                   E2[2].get(f[2].l[2], f[3].l[2], phi);
-                      double r = R[((t + tau) * MD_D + (u + nu2)) * MD_D + (v + phi)];
+                      double r = R[((t + tau) * D + (u + nu2)) * D + (v + phi)];
                       inner += ((tau + nu2 + phi) & 1) ? -ek * r : ek * r;
                     }
                 total += eb * inner;

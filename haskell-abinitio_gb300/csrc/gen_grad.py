@@ -405,7 +405,7 @@ def main():
             code, _ = gen_class(la, lb, lc, ld)
             parts.append(code)
             parts.append("")
-    for (la, lb) in pcls:
+    for (la, lb) in pcls + [(2, 0), (2, 1), (2, 2)]:
         parts.append(gen_vne(la, lb))
         parts.append("")
     Path(__file__).with_name("grad_gen.cuh").write_text("\n".join(parts))

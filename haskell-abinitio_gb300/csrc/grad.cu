@@ -288,7 +288,9 @@ static gbhf_status grad_2e(gbhf_ctx* c, const double* d_D, double schwarz, doubl
   for (int i = 0; i < gbhf_ctx::NSIDE; ++i) GBHF_CUDA(c, cudaStreamWaitEvent(c->side[i], c->fork_ev, 0));
   PairData& P = c->pairs;
   int nl = 0;
-  static const int order[NCOMBO_MAX] = {8, 7, 5, 6, 4, 2, 3, 1, 0};   // heaviest first
+  // heaviest first: the d combinations, then the s/p ones
+  static const int order[NCOMBO_MAX] = {35, 34, 29, 33, 28, 23, 32, 27, 22, 17, 31, 26, 21, 16, 11, 30, 25, 20,
+                                        15, 14, 10, 24, 19, 13, 9, 18, 12, 8, 7, 5, 6, 4, 2, 3, 1, 0};
   for (int prec = 0; prec < 2; ++prec) {
     if (prec == 1 && !any32) break;
     for (int oi = 0; oi < NCOMBO_MAX; ++oi) {
@@ -296,7 +298,9 @@ static gbhf_status grad_2e(gbhf_ctx* c, const double* d_D, double schwarz, doubl
       const int nt = gt.hranges[4 * k + 2 * prec + 1] - gt.hranges[4 * k + 2 * prec];
       if (nt <= 0) continue;
       cudaStream_t strm = c->side[nl++ % gbhf_ctx::NSIDE];
-      if (prec == 0)
+      if (k >= NGCOMBO_SP)
+        GBHF_TRY(launch_grad_dclass(c, strm, k, prec, d_D, c->dfloat.p, d_grad, nt));
+      else if (prec == 0)
         GBHF_TRY(launch_grad_combo<double>(c, strm, k, 0, d_D, P.bra64.p, P.ket64.p, c->boysh64.p, d_grad, nt));
       else
         GBHF_TRY(launch_grad_combo<float>(c, strm, k, 1, c->dfloat.p, P.bra32.p, P.ket32.p, c->boysh32.p, d_grad,
@@ -364,7 +368,7 @@ __global__ void __launch_bounds__(G1_THREADS) k_grad_1e(Grad1eArgs g) {
         if (fabs(kab) * (1.0 + p) * (fabs(dab) * (1.0 + p) + fabs(wab)) * (GBHF_PI / p) * sqrt(GBHF_PI / p) < 1e-17)
           continue;
         const double cte = sqrt(GBHF_PI / p);
-        double P[3], s[3][3][5];
+        double P[3], s[3][4][5];   // up to l_a + 1 <= 3 on A, l_b + 2 <= 4 on B
         for (int x = 0; x < 3; ++x) {
           P[x] = (a * A[x] + b * B[x]) / p;
           const double abx = A[x] - B[x];
@@ -445,6 +449,27 @@ struct VneFn<1, 1> {
     vne_grad_pp<double>(bp, x, y, z, zp, dw, boys, g);
   }
 };
+template <>
+struct VneFn<2, 0> {
+  static __device__ __forceinline__ void run(const BraPrim<double>& bp, double x, double y, double z, double zp,
+                                             const double* dw, const double* boys, double* g) {
+    vne_grad_ds<double>(bp, x, y, z, zp, dw, boys, g);
+  }
+};
+template <>
+struct VneFn<2, 1> {
+  static __device__ __forceinline__ void run(const BraPrim<double>& bp, double x, double y, double z, double zp,
+                                             const double* dw, const double* boys, double* g) {
+    vne_grad_dp<double>(bp, x, y, z, zp, dw, boys, g);
+  }
+};
+template <>
+struct VneFn<2, 2> {
+  static __device__ __forceinline__ void run(const BraPrim<double>& bp, double x, double y, double z, double zp,
+                                             const double* dw, const double* boys, double* g) {
+    vne_grad_dd<double>(bp, x, y, z, zp, dw, boys, g);
+  }
+};
 
 struct VneArgs {
   int p0, p1;               // pairs of this class
@@ -453,6 +478,7 @@ struct VneArgs {
   long long npp;
   const int* shell_f0;      // within the molecule
   const int* shell_atom;
+  const double* sscale;     // per shell 6 component scales (d shells)
   const int* mn;
   const long long* moff;
   const int* mao;           // first atom of each molecule (nmol + 1)
@@ -480,7 +506,7 @@ __global__ void __launch_bounds__(128) k_grad_vne(VneArgs a) {
   for (int ia = 0; ia < NA; ++ia)
 #pragma unroll
     for (int ib = 0; ib < NB; ++ib) {
-      dw[ia * NB + ib] = mult * Dm[(long)(fa + ia) * n + fb + ib];
+      dw[ia * NB + ib] = mult * Dm[(long)(fa + ia) * n + fb + ib] * a.sscale[6 * A + ia] * a.sscale[6 * B + ib];
       dmax = fmax(dmax, fabs(dw[ia * NB + ib]));
     }
   double gAB[6] = {0, 0, 0, 0, 0, 0};
@@ -547,6 +573,7 @@ static gbhf_status launch_vne(gbhf_ctx* c, int cls, const double* d_D, double* d
   a.npp = (long long)P.nprim_pairs;
   a.shell_f0 = c->tasks.f0.p;
   a.shell_atom = c->tasks.atom.p;
+  a.sscale = c->tasks.sscale.p;
   a.mn = c->tasks.mn.p;
   a.moff = c->tasks.moff.p;
   a.mao = c->tasks.mao.p;
@@ -587,8 +614,8 @@ __global__ void k_grad_nuc(int natoms, const int* __restrict__ amol, const int* 
 gbhf_status gradient_dev(gbhf_ctx* c, const double* d_D, const double* d_W, double schwarz, double mixed_cutoff,
                          int precision, double* d_grad) {
   const Basis& b = c->basis;
-  if (!b.shells_ok || b.maxL > 1)
-    return fail(c, GBHF_ERR_UNSUPPORTED, "gradient kernels need complete s/p shells");
+  if (!b.shells_ok || b.maxL > 2)
+    return fail(c, GBHF_ERR_UNSUPPORTED, "gradient kernels need complete s, p and d shells");
   GBHF_TRY(ensure_boys_tables(c));
   GBHF_TRY(ensure_pairs(c));
   const int n = b.nbf, na = b.natoms;
@@ -618,6 +645,9 @@ gbhf_status gradient_dev(gbhf_ctx* c, const double* d_D, const double* d_W, doub
   GBHF_TRY((launch_vne<0, 0>(c, 0, d_D, d_grad)));
   GBHF_TRY((launch_vne<1, 0>(c, 1, d_D, d_grad)));
   GBHF_TRY((launch_vne<1, 1>(c, 2, d_D, d_grad)));
+  GBHF_TRY((launch_vne<2, 0>(c, 3, d_D, d_grad)));
+  GBHF_TRY((launch_vne<2, 1>(c, 4, d_D, d_grad)));
+  GBHF_TRY((launch_vne<2, 2>(c, 5, d_D, d_grad)));
   GBHF_TRY(grad_2e(c, d_D, schwarz, mixed_cutoff, precision, d_grad));
   GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
   return GBHF_OK;

@@ -335,7 +335,7 @@ __global__ void __launch_bounds__(SCHWARZ_THREADS) k_schwarz_cls(int p0, int p1,
 
 gbhf_status schwarz_classes_dev(gbhf_ctx* c, const int* cls_start, const int* d_K, const int* d_poff,
                                 const double* d_bra, long long npp, double* d_Q) {
-  for (int cl = 0; cl < NPCLS; ++cl) {
+  for (int cl = 0; cl < 3; ++cl) {   // s/p classes; jkd.cu has the d classes
     const int p0 = cls_start[cl], p1 = cls_start[cl + 1];
     if (p1 <= p0) continue;
     const int blocks = (p1 - p0 + SCHWARZ_THREADS - 1) / SCHWARZ_THREADS;
@@ -642,7 +642,7 @@ static gbhf_status build_task_lists(gbhf_ctx* c, TaskLists& TL, int ncombo, cons
     k_tasks<true><<<(ni + 127) / 128, 128, 0, c->stream>>>(g);
     count_launch(c);
   }
-  k_ranges<<<1, 32, 0, c->stream>>>(ncombo, d_ics.p, off64, off32, TL.ranges.p);
+  k_ranges<<<1, 64, 0, c->stream>>>(ncombo, d_ics.p, off64, off32, TL.ranges.p);
   count_launch(c);
   GBHF_CUDA(c, cudaGetLastError());
   GBHF_CUDA(c, cudaMemcpyAsync(h_ranges, TL.ranges.p, 4 * ncombo * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
@@ -650,15 +650,17 @@ static gbhf_status build_task_lists(gbhf_ctx* c, TaskLists& TL, int ncombo, cons
   return GBHF_OK;
 }
 
-// J/K lists: the six classes with bra class >= ket class, unique quartets.
+// J/K lists: the classes with bra class >= ket class, unique quartets.
 // lane_prims bounds the primitive quartets one lane evaluates in one task, per
 // class (ss|ss) (ps|ss) (ps|ps) (pp|ss) (pp|ps) (pp|pp): about the same
 // arithmetic per task, so that the longest task - the tail of a persistent
 // launch - stays short.  A task never splits the ket primitives, so a lane
-// always evaluates at least K_ket of them.
+// always evaluates at least K_ket of them.  For the d classes (a warp per
+// quartet) it bounds the primitive quartets of one quartet in one task.
 static gbhf_status build_tasks(gbhf_ctx* c, double thr_all, double thr64, const double* pw = nullptr,
                                const double* sw = nullptr) {
-  static const int lane_prims[NCOMBO] = {256, 128, 48, 48, 16, 8};
+  static const int lane_prims[NCOMBO] = {256, 128, 48, 48, 16, 8, 36, 36, 36, 36, 36, 36, 36, 36, 36, 36, 36, 36,
+                                         36, 36, 36};
   return build_task_lists(c, c->tasks, NCOMBO, COMBO_BRA, COMBO_KET, lane_prims, false, false, thr_all, thr64, pw,
                           sw);
 }
@@ -669,11 +671,13 @@ gbhf_status ensure_shell_arrays(gbhf_ctx* c) {
   const Basis& b = c->basis;
   const size_t ns = b.shells.size();
   std::vector<int> f0(ns), nc(ns), at(ns), sm(ns);
+  std::vector<double> sc(6 * std::max<size_t>(ns, 1), 1.0);
   for (size_t s = 0; s < ns; ++s) {
     f0[s] = b.shells[s].f0 - b.mol_fn_off[b.shells[s].mol];   // first function within its molecule
     nc[s] = b.shells[s].ncomp;
     at[s] = b.shells[s].atom;
     sm[s] = b.shells[s].mol;
+    for (int k = 0; k < 6; ++k) sc[6 * s + k] = b.shells[s].scale[k];
   }
   std::vector<int> mn(b.nmol), fmol(b.nbf), amol(b.natoms);
   for (int m = 0; m < b.nmol; ++m) {
@@ -682,6 +686,7 @@ gbhf_status ensure_shell_arrays(gbhf_ctx* c) {
     for (int a = b.mol_atom_off[m]; a < b.mol_atom_off[m + 1]; ++a) amol[a] = m;
   }
   GBHF_CUDA(c, st.f0.alloc(ns));
+  GBHF_CUDA(c, st.sscale.alloc(sc.size()));
   GBHF_CUDA(c, st.nc.alloc(ns));
   GBHF_CUDA(c, st.atom.alloc(ns));
   GBHF_CUDA(c, st.smol.alloc(ns));
@@ -692,6 +697,8 @@ gbhf_status ensure_shell_arrays(gbhf_ctx* c) {
   GBHF_CUDA(c, st.mfo.alloc(b.nmol + 1));
   GBHF_CUDA(c, st.mao.alloc(b.nmol + 1));
   GBHF_CUDA(c, cudaMemcpyAsync(st.f0.p, f0.data(), ns * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  GBHF_CUDA(c, cudaMemcpyAsync(st.sscale.p, sc.data(), sc.size() * sizeof(double), cudaMemcpyHostToDevice,
+                               c->stream));
   GBHF_CUDA(c, cudaMemcpyAsync(st.nc.p, nc.data(), ns * sizeof(int), cudaMemcpyHostToDevice, c->stream));
   GBHF_CUDA(c, cudaMemcpyAsync(st.atom.p, at.data(), ns * sizeof(int), cudaMemcpyHostToDevice, c->stream));
   GBHF_CUDA(c, cudaMemcpyAsync(st.smol.p, sm.data(), ns * sizeof(int), cudaMemcpyHostToDevice, c->stream));
@@ -709,20 +716,22 @@ gbhf_status ensure_shell_arrays(gbhf_ctx* c) {
   return GBHF_OK;
 }
 
-// Gradient lists: all nine (bra class, ket class) combinations, every ordered
-// pair of shell pairs, bound Q_bra Q_ket max(w_bra, w_ket)^2 with the pair
-// weights of D (|Gamma_abcd| <= that squared weight).
+// Gradient lists: every (bra class, ket class) combination, every ordered pair
+// of shell pairs, bound Q_bra Q_ket max(w_bra, w_ket)^2 with the pair weights
+// of D (|Gamma_abcd| <= that squared weight).
 gbhf_status build_grad_tasks(gbhf_ctx* c, const double* d_D, double cutoff, double mixed_cutoff, int precision) {
   GBHF_TRY(ensure_pairs(c));
   GBHF_TRY(ensure_shell_arrays(c));
   TaskLists& gt = c->gtasks;
   GBHF_TRY(density_weights(c, gt, d_D));
-  static const int gb[NCOMBO_MAX] = {0, 0, 0, 1, 1, 1, 2, 2, 2};
-  static const int gk[NCOMBO_MAX] = {0, 1, 2, 0, 1, 2, 0, 1, 2};
   const double t64 = precision == GBHF_PREC_FP64 ? 0.0 : mixed_cutoff;
-  // (bra class, ket class) of the derivative code: about twice the ERI work per primitive quartet
-  static const int lp[NCOMBO_MAX] = {128, 64, 24, 64, 24, 8, 24, 8, 4};
-  GBHF_TRY(build_task_lists(c, gt, NCOMBO_MAX, gb, gk, lp, true, true, cutoff, t64, gt.pw.p, gt.sw.p));
+  // (bra class, ket class) of the derivative code: about twice the ERI work per primitive quartet;
+  // the d combinations (warp per quartet) bound the primitive quartets of one quartet per task
+  int lp[NCOMBO_MAX];
+  static const int lp_sp[NGCOMBO_SP] = {128, 64, 24, 64, 24, 8, 24, 8, 4};
+  for (int k = 0; k < NCOMBO_MAX; ++k) lp[k] = k < NGCOMBO_SP ? lp_sp[k] : 36;
+  GBHF_TRY(build_task_lists(c, gt, NCOMBO_MAX, GRAD_COMBO_BRA, GRAD_COMBO_KET, lp, true, true, cutoff, t64, gt.pw.p,
+                            gt.sw.p));
   return GBHF_OK;
 }
 
@@ -815,9 +824,9 @@ gbhf_status jk_build(gbhf_ctx* c, const double* d_Dsq, double* d_G, int precisio
   // persistent grid that fills the GPU, and the next one takes over SMs as the
   // tail of the previous one drains.  With profiling events they run in order
   // on the context stream so that each launch is timed alone.
-  static const int order[NCOMBO] = {5, 4, 3, 2, 1, 0};
+  static const int order[NCOMBO] = {20, 19, 18, 17, 16, 15, 14, 13, 12, 11, 10, 9, 8, 7, 6, 5, 4, 3, 2, 1, 0};
   int ne = 0, nl = 0;
-  int ev_combo[12], ev_prec[12];
+  int ev_combo[2 * NCOMBO], ev_prec[2 * NCOMBO];
   if (ev) GBHF_CUDA(c, cudaEventRecord(c->evc[ne], c->stream));
   else {
     GBHF_CUDA(c, cudaEventRecord(c->fork_ev, c->stream));
@@ -833,7 +842,9 @@ gbhf_status jk_build(gbhf_ctx* c, const double* d_Dsq, double* d_G, int precisio
       gbhf_status s = GBHF_OK;
       cudaStream_t strm = ev ? c->stream : c->side[nl % gbhf_ctx::NSIDE];
       ++nl;
-      if (prec == 0) {
+      if (k >= NCOMBO_SP) {
+        s = launch_jk_dclass(c, strm, k, prec, D64, D32, d_G, nt[k][prec]);
+      } else if (prec == 0) {
         switch (k) {
           case 5: s = launch_class<1, 1, 1, 1, double, true>(c, strm, 5, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boysh64.p, f0, nt[5][0]); break;
           case 4: s = launch_class<1, 1, 1, 0, double, false>(c, strm, 4, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boysh64.p, f0, nt[4][0]); break;

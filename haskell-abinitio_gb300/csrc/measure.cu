@@ -32,7 +32,7 @@ extern "C" {
 
 gbhf_status gbhf_profile_classes(gbhf_ctx* c, double* out) {
   if (!c || !out) return GBHF_ERR_BAD_INPUT;
-  for (int k = 0; k < 6; ++k)
+  for (int k = 0; k < gbhf::NCOMBO; ++k)
     for (int p = 0; p < 2; ++p)
       for (int q = 0; q < 4; ++q) out[(k * 2 + p) * 4 + q] = c->prof.cls[k][p][q];
   return GBHF_OK;

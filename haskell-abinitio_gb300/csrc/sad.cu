@@ -101,7 +101,7 @@ static gbhf_status atomic_density(gbhf_ctx* c, gbhf_ctx* sub, const Basis& b, in
   const double origin[3] = {0, 0, 0};
   const double Z = b.Z[a];
   GBHF_TRY(build_basis(sub, 1, origin, &Z, nf, atom0.data(), lxyz.data(), nprim.data(), coef.data(), expo.data()));
-  if (sub->basis.maxL > 1) return fail(c, GBHF_ERR_UNSUPPORTED, "SAD guess: atomic basis with d functions");
+  if (sub->basis.maxL > 2) return fail(c, GBHF_ERR_UNSUPPORTED, "SAD guess: atomic basis above d functions");
   GBHF_TRY(ensure_boys_tables(sub));
   const int n = nf;
   const size_t nn = (size_t)n * n, ntri = (size_t)n * (n + 1) / 2;

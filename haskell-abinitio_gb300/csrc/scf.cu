@@ -145,7 +145,7 @@ gbhf_status scf_run(gbhf_ctx* c, const gbhf_scf_opts* o, gbhf_result* r) {
   const long long neri = P * (P + 1) / 2;
   const bool need_eri = ref || o->guess == GBHF_GUESS_HARRIS;
   if (need_eri) {
-    if (b.maxL > 1) return fail(c, GBHF_ERR_UNSUPPORTED, "stored ERIs support s and p functions");
+    if (b.maxL > 2) return fail(c, GBHF_ERR_UNSUPPORTED, "stored ERIs support s, p and d functions");
     if (neri > (1ll << 31)) return fail(c, GBHF_ERR_UNSUPPORTED, "stored canonical ERIs too large for this basis");
     GBHF_CUDA(c, eri.alloc((size_t)neri));
     GBHF_TRY(eri_canonical_dev(c, ref, eri.p));

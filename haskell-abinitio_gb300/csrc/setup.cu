@@ -23,15 +23,20 @@ gbhf_status cuda_fail(gbhf_ctx* c, cudaError_t e, const char* where) {
 static int ncart(int L) { return (L + 1) * (L + 2) / 2; }
 
 // Group CGFs into shells: consecutive CGFs on one atom with the same total
-// angular momentum and identical exponents, in the Cartesian order x, y, z
-// (the order createCGF emits, BasisSet/FetchBasis.hs:50-59).
+// angular momentum and identical exponents, in the Cartesian order x, y, z and
+// xx, xy, xz, yy, yz, zz (the order createCGF emits, BasisSet/FetchBasis.hs:50-59).
+// The components of a d shell differ in their primitive normalisation
+// (normCoeff, BasisSet/NormalizeBasis.hs:37-59: a factor 1/sqrt(prod (2l_k-1)!!)),
+// so their coefficients need only be proportional: the shell keeps the first
+// component's coefficients and the ratio of every component as its scale.
 static void group_shells(Basis& b) {
   b.shells.clear();
   b.shells_ok = true;
   b.maxL = 0;
   const int n = b.nbf;
   int i = 0;
-  static const int px[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+  static const int cart[10][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}, {2, 0, 0},
+                                  {1, 1, 0}, {1, 0, 1}, {0, 2, 0}, {0, 1, 1}, {0, 0, 2}};
   while (i < n) {
     const int* l = &b.cgf_lxyz[3 * i];
     const int L = l[0] + l[1] + l[2];
@@ -44,21 +49,28 @@ static void group_shells(Basis& b) {
     s.f0 = i;
     s.expo.assign(b.prim_exp.begin() + b.cgf_off[i], b.prim_exp.begin() + b.cgf_off[i] + s.np);
     s.coef.assign(b.prim_coef.begin() + b.cgf_off[i], b.prim_coef.begin() + b.cgf_off[i] + s.np);
-    bool ok = L <= 1;
-    int take = (L <= 1) ? s.ncomp : 1;
+    bool ok = L <= 2;
+    int take = ok ? s.ncomp : 1;
     if (i + take > n) ok = false;
+    const int c0 = L == 0 ? 0 : (L == 1 ? 1 : 4);   // first row of this L in cart
     for (int c = 0; ok && c < take; ++c) {
       const int j = i + c;
       const int* lj = &b.cgf_lxyz[3 * j];
       if (b.cgf_atom[j] != s.atom || b.cgf_nprim[j] != s.np) ok = false;
-      if (ok && L == 1 && !(lj[0] == px[c][0] && lj[1] == px[c][1] && lj[2] == px[c][2])) ok = false;
-      for (int k = 0; ok && k < s.np; ++k)
-        if (b.prim_exp[b.cgf_off[j] + k] != s.expo[k] || b.prim_coef[b.cgf_off[j] + k] != s.coef[k]) ok = false;
+      if (ok && !(lj[0] == cart[c0 + c][0] && lj[1] == cart[c0 + c][1] && lj[2] == cart[c0 + c][2])) ok = false;
+      const double r = (ok && s.coef[0] != 0.0) ? b.prim_coef[b.cgf_off[j]] / s.coef[0] : 1.0;
+      for (int k = 0; ok && k < s.np; ++k) {
+        const double cj = b.prim_coef[b.cgf_off[j] + k];
+        if (b.prim_exp[b.cgf_off[j] + k] != s.expo[k]) ok = false;
+        if (L <= 1 ? cj != s.coef[k] : std::fabs(cj - r * s.coef[k]) > 1e-13 * std::fabs(cj)) ok = false;
+      }
+      if (ok) s.scale[c] = r;
     }
     if (!ok) {
       if (b.shells_ok) {
         b.shell_msg = "basis function " + std::to_string(i) +
-                      " does not start a complete s or p shell (components x,y,z, shared primitives)";
+                      " does not start a complete s, p or d shell (Cartesian components in order, shared"
+                      " exponents, proportional coefficients)";
       }
       b.shells_ok = false;
       s.ncomp = 1;
@@ -226,7 +238,7 @@ gbhf_status ensure_boys_tables(gbhf_ctx* c) {
   return GBHF_OK;
 }
 
-static int pair_class(int la, int lb) { return la == 0 ? 0 : (lb == 0 ? 1 : 2); }
+static int pair_class(int la, int lb) { return pair_class_of(la, lb); }
 
 // Fields of every primitive pair of shells (A, B), out[k*BRA_NFIELD + field],
 // k = ia*np_B + ib.  K' = sqrt(2 pi^(5/2)) c_a c_b exp(-mu |AB|^2) / p, so the
@@ -260,10 +272,12 @@ gbhf_status ensure_pairs(gbhf_ctx* c) {
   if (c->pairs_ready) return GBHF_OK;
   const Basis& b = c->basis;
   if (!c->basis_dev) return fail(c, GBHF_ERR_BAD_INPUT, "no basis set");
-  if (!b.shells_ok || b.maxL > 1)
+  if (!b.shells_ok || b.maxL > 2)
     return fail(c, GBHF_ERR_UNSUPPORTED,
-                "direct J/K kernels need complete s/p shells: " + (b.shell_msg.empty() ? std::string("d functions present") : b.shell_msg));
+                "direct J/K kernels need complete s, p and d shells: " +
+                    (b.shell_msg.empty() ? std::string("functions above d present") : b.shell_msg));
   GBHF_TRY(ensure_boys_tables(c));
+  GBHF_TRY(ensure_shell_arrays(c));   // component scales for the d-class Schwarz bounds
   const int ns = (int)b.shells.size();
   // 1. all pairs (la > lb, or la == lb and A >= B) of shells of one molecule
   std::vector<int> A, B;
@@ -308,16 +322,26 @@ gbhf_status ensure_pairs(gbhf_ctx* c) {
       for (int k = 0; k < K0[t]; ++k)
         for (int fl = 0; fl < BRA_NFIELD; ++fl) bra0[(size_t)fl * npp0 + off0[t] + k] = f[k * BRA_NFIELD + fl];
     }
-    DBuf<int> dK, doff;
+    std::vector<int> A0(np), B0(np);
+    for (int t = 0; t < np; ++t) {
+      A0[t] = A[ord0[t]];
+      B0[t] = B[ord0[t]];
+    }
+    DBuf<int> dK, doff, dA0, dB0;
     DBuf<double> dQ, dbra;
     GBHF_CUDA(c, dK.alloc(np));
     GBHF_CUDA(c, doff.alloc(np));
+    GBHF_CUDA(c, dA0.alloc(np));
+    GBHF_CUDA(c, dB0.alloc(np));
     GBHF_CUDA(c, dQ.alloc(np));
     GBHF_CUDA(c, dbra.alloc(bra0.size()));
     GBHF_CUDA(c, cudaMemcpyAsync(dK.p, K0.data(), np * sizeof(int), cudaMemcpyHostToDevice, c->stream));
     GBHF_CUDA(c, cudaMemcpyAsync(doff.p, off0.data(), np * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    GBHF_CUDA(c, cudaMemcpyAsync(dA0.p, A0.data(), np * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    GBHF_CUDA(c, cudaMemcpyAsync(dB0.p, B0.data(), np * sizeof(int), cudaMemcpyHostToDevice, c->stream));
     GBHF_CUDA(c, cudaMemcpyAsync(dbra.p, bra0.data(), bra0.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
     GBHF_TRY(schwarz_classes_dev(c, cs0, dK.p, doff.p, dbra.p, (long long)npp0, dQ.p));
+    GBHF_TRY(schwarz_dclasses_dev(c, cs0, dA0.p, dB0.p, dK.p, doff.p, dbra.p, (long long)npp0, dQ.p));
     std::vector<double> Q0(np);
     GBHF_CUDA(c, cudaMemcpyAsync(Q0.data(), dQ.p, np * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     GBHF_CUDA(c, cudaStreamSynchronize(c->stream));

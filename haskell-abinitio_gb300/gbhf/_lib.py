@@ -364,11 +364,12 @@ class Context:
                 "jacobi_sweeps", "jacobi_calls", "ms_grad", "batch_steps")
         return dict(zip(keys, v.tolist()))
 
-    CLASSES = ("ssss", "psss", "psps", "ppss", "ppps", "pppp")
+    CLASSES = ("ssss", "psss", "psps", "ppss", "ppps", "pppp", "dsss", "dsps", "dspp", "dsds", "dpss", "dpps",
+               "dppp", "dpds", "dpdp", "ddss", "ddps", "ddpp", "ddds", "dddp", "dddd")
 
     def profile_classes(self):
         """{(class, 'fp64'|'fp32'): dict(shell_quartets, fn_quartets, prim_quartets, ms)}"""
-        v = np.zeros(48)
+        v = np.zeros(8 * len(self.CLASSES))
         self._check(self.L.gbhf_profile_classes(self.h, _d(v)))
         out = {}
         for k, name in enumerate(self.CLASSES):

@@ -16,7 +16,11 @@ compare work, not implementation details.
 from math import comb
 
 CLASSES = {"ssss": (0, 0, 0, 0), "psss": (1, 0, 0, 0), "psps": (1, 0, 1, 0),
-           "ppss": (1, 1, 0, 0), "ppps": (1, 1, 1, 0), "pppp": (1, 1, 1, 1)}
+           "ppss": (1, 1, 0, 0), "ppps": (1, 1, 1, 0), "pppp": (1, 1, 1, 1),
+           "dsss": (2, 0, 0, 0), "dsps": (2, 0, 1, 0), "dspp": (2, 0, 1, 1), "dsds": (2, 0, 2, 0),
+           "dpss": (2, 1, 0, 0), "dpps": (2, 1, 1, 0), "dppp": (2, 1, 1, 1), "dpds": (2, 1, 2, 0),
+           "dpdp": (2, 1, 2, 1), "ddss": (2, 2, 0, 0), "ddps": (2, 2, 1, 0), "ddpp": (2, 2, 1, 1),
+           "ddds": (2, 2, 2, 0), "dddp": (2, 2, 2, 1), "dddd": (2, 2, 2, 2)}
 
 
 def ncart(l):

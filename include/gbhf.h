@@ -38,7 +38,7 @@ typedef enum {
   GBHF_ERR_CUDA = 4,           /* a CUDA runtime call failed */
   GBHF_ERR_DEVICE_TIMEOUT = 5, /* a bounded device loop gave up (Jacobi sweeps, grid barrier) */
   GBHF_ERR_NO_DEVICE = 6,      /* no usable GPU */
-  GBHF_ERR_UNSUPPORTED = 7,    /* input outside what the kernels implement (e.g. d shells in direct J/K) */
+  GBHF_ERR_UNSUPPORTED = 7,    /* input outside what the kernels implement (e.g. f functions, incomplete shells) */
   GBHF_ERR_INDEX = 8           /* the reference's bounds-checked lookup would fail (Harris guess, HartreeFock.hs:143-146) */
 } gbhf_status;
 
@@ -241,10 +241,13 @@ gbhf_status gbhf_scf_batch(gbhf_ctx* ctx, int n_mol, const int* atom_off, const 
  * the batched gradients, steps of the last batched SCF. */
 gbhf_status gbhf_profile_reset(gbhf_ctx* ctx, int enable_events);
 gbhf_status gbhf_profile_read(gbhf_ctx* ctx, double* stats, int n_stats);
-/* Per ERI class (ss|ss, ps|ss, ps|ps, pp|ss, pp|ps, pp|pp) and precision
- * (FP64, FP32) since the last reset: out[(class*2+prec)*4 + k], k = shell
- * quartets, function quartets, primitive quartets, kernel milliseconds. */
-gbhf_status gbhf_profile_classes(gbhf_ctx* ctx, double* out48);
+/* Per ERI class and precision (FP64, FP32) since the last reset:
+ * out[(class*2+prec)*4 + k], k = shell quartets, function quartets, primitive
+ * quartets, kernel milliseconds; 21 classes (168 values): (ss|ss) (ps|ss)
+ * (ps|ps) (pp|ss) (pp|ps) (pp|pp), then (ds|ss) (ds|ps) (ds|pp) (ds|ds)
+ * (dp|ss) (dp|ps) (dp|pp) (dp|ds) (dp|dp) (dd|ss) (dd|ps) (dd|pp) (dd|ds)
+ * (dd|dp) (dd|dd). */
+gbhf_status gbhf_profile_classes(gbhf_ctx* ctx, double* out168);
 /* CUDA events on the context stream (slots 0..7) and the time between two. */
 gbhf_status gbhf_event_record(gbhf_ctx* ctx, int slot);
 gbhf_status gbhf_event_elapsed(gbhf_ctx* ctx, int slot_start, int slot_end, double* ms);

@@ -70,11 +70,33 @@ def test_canonical_eris_dimer(ctx):
         np.testing.assert_allclose(ctx.eri_canonical(mode), ob.eri_canonical(ref), rtol=0, atol=1e-13)
 
 
-def test_unsupported_and_bad_input(ctx):
+def _drop_cgf(fb, i):
+    """The flat basis without CGF i (its primitives removed too)."""
+    off = np.concatenate([[0], np.cumsum(fb.cgf_nprim)])
+    keep = np.ones(len(fb.prim_exp), bool)
+    keep[off[i]:off[i + 1]] = False
+    fb.prim_exp, fb.prim_coef = fb.prim_exp[keep], fb.prim_coef[keep]
+    for k in ("cgf_atom", "cgf_lxyz", "cgf_nprim"):
+        setattr(fb, k, np.delete(getattr(fb, k), i, axis=0))
+    fb.n_cgf -= 1
+    return fb
+
+
+def test_canonical_eris_with_d_shells(ctx):
     fb = B.flatten(M.water_atoms("6-31g*", "text"))
     ctx.set_basis(fb)
+    got = ctx.eri_canonical(_lib.MODE_EXACT)
+    np.testing.assert_allclose(got, O.OracleBasis(fb).eri_canonical(False), rtol=0, atol=1e-12)
+
+
+def test_unsupported_and_bad_input(ctx):
+    # O 2p without its y component: fine for per-function integrals, not for the
+    # shell-based direct J/K build
+    fb = _drop_cgf(B.flatten(M.water_atoms("sto-3g", "text")), 3)
+    ctx.set_basis(fb)
+    d = np.zeros(fb.n_cgf * (fb.n_cgf + 1) // 2)
     with pytest.raises(_lib.GBHFError) as e:
-        ctx.eri_canonical(_lib.MODE_EXACT)
+        ctx.fock(d, d, _lib.MODE_EXACT)
     assert e.value.name == "GBHF_ERR_UNSUPPORTED"
     with pytest.raises(_lib.GBHFError) as e:
         ctx.boys(_lib.MODE_EXACT, 3, [-1.0])

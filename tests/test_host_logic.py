@@ -73,7 +73,9 @@ def test_workload_sizes():
 
 
 def test_flop_model_table():
-    assert F_ALG == {"ssss": 33, "psss": 98, "psps": 291, "ppss": 323, "ppps": 1004, "pppp": 3847}
+    sp = {k: F_ALG[k] for k in ("ssss", "psss", "psps", "ppss", "ppps", "pppp")}
+    assert sp == {"ssss": 33, "psss": 98, "psps": 291, "ppss": 323, "ppps": 1004, "pppp": 3847}
+    assert len(F_ALG) == 21 and F_ALG["dddd"] > F_ALG["dddp"] > F_ALG["pppp"]
 
 
 def test_shard_balanced_and_complete():
