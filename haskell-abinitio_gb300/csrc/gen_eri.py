@@ -293,6 +293,9 @@ def main():
         for (lc, ld) in [(0, 0), (1, 0), (1, 1)]:
             if (la, lb) >= (lc, ld):
                 classes.append((la, lb, lc, ld))
+    # the d classes with few components per quartet (the larger ones use the
+    # warp-per-quartet kernels of jkd.cu)
+    classes += [(2, 0, 0, 0), (2, 0, 1, 0), (2, 0, 1, 1), (2, 0, 2, 0), (2, 1, 0, 0), (2, 1, 1, 0), (2, 2, 0, 0)]
     parts = ["// GENERATED by gen_eri.py -- do not edit by hand.",
              "#pragma once", ""]
     for c in classes:

@@ -148,7 +148,7 @@ __global__ void __launch_bounds__(GR_THREADS) k_grad_jk(GradArgs<T> a) {
     }
     const int A = a.pA[ib], B = a.pB[ib];
     const int a0 = a.shell_f0[A], b0 = a.shell_f0[B];
-    if (lane < NAB) sDab[warp][lane] = Dm[(long long)(a0 + lane / NB) * n + b0 + lane % NB];
+    for (int i = lane; i < NAB; i += 32) sDab[warp][i] = Dm[(long long)(a0 + i / NB) * n + b0 + i % NB];
     __syncwarp();
     T g[6] = {0, 0, 0, 0, 0, 0};
     T wgt = 0;

@@ -77,6 +77,7 @@ struct JKArgs {
   double* G;                   // stacked n_m x n_m Fock accumulators
   const T* boys;
   unsigned long long* stats;   // [shell quartets, fn quartets, prim quartets]
+  const double* sscale;        // per shell 6 component scales (d shells)
 };
 
 template <int LA, int LB, int LC, int LD>
@@ -99,6 +100,13 @@ GBHF_CLASS_FN(1, 0, 1, 0, psps)
 GBHF_CLASS_FN(1, 1, 0, 0, ppss)
 GBHF_CLASS_FN(1, 1, 1, 0, ppps)
 GBHF_CLASS_FN(1, 1, 1, 1, pppp)
+GBHF_CLASS_FN(2, 0, 0, 0, dsss)
+GBHF_CLASS_FN(2, 0, 1, 0, dsps)
+GBHF_CLASS_FN(2, 0, 1, 1, dspp)
+GBHF_CLASS_FN(2, 0, 2, 0, dsds)
+GBHF_CLASS_FN(2, 1, 0, 0, dpss)
+GBHF_CLASS_FN(2, 1, 1, 0, dpps)
+GBHF_CLASS_FN(2, 2, 0, 0, ddss)
 
 __device__ __forceinline__ float warp_sum(float v) {
 #pragma unroll
@@ -170,7 +178,7 @@ __global__ void __launch_bounds__(JK_THREADS) k_jk(JKArgs<T> a) {
     }
     const int A = a.pA[ib], B = a.pB[ib];
     const int a0 = a.shell_f0[A], b0 = a.shell_f0[B];
-    if (lane < NAB) sDab[warp][lane] = Dm[(long long)(a0 + lane / NB) * n + b0 + lane % NB];
+    for (int i = lane; i < NAB; i += 32) sDab[warp][i] = Dm[(long long)(a0 + i / NB) * n + b0 + i % NB];
     __syncwarp();
     acc.zero();
     int C = 0, Dd = 0, c0 = 0, d0 = 0;
@@ -210,6 +218,21 @@ __global__ void __launch_bounds__(JK_THREADS) k_jk(JKArgs<T> a) {
     for (int o = 1 << lg; o < 32; o <<= 1) {
 #pragma unroll
       for (int i = 0; i < NOUT; ++i) acc[i] += __shfl_xor_sync(0xffffffffu, acc.get(i), o);
+    }
+    if constexpr (LA == 2 || LB == 2 || LC == 2 || LD == 2) {
+      // d shells: the generated code used the first component's coefficients
+      if (active) {
+#pragma unroll
+        for (int e = 0; e < NOUT; ++e) {
+          const int ab = e / NCD, cd = e - ab * NCD;
+          T f = T(1);
+          if (LA == 2) f *= T(a.sscale[6 * A + ab / NB]);
+          if (LB == 2) f *= T(a.sscale[6 * B + ab % NB]);
+          if (LC == 2) f *= T(a.sscale[6 * C + cd / ND]);
+          if (LD == 2) f *= T(a.sscale[6 * Dd + cd % ND]);
+          acc[e] = acc.get(e) * f;
+        }
+      }
     }
     // ---- scatter into G'' (FP64 atomics)
     const T s = (A == B ? T(0.5) : T(1)) * (C == Dd ? T(0.5) : T(1)) * (ib == jk ? T(0.5) : T(1));
@@ -659,7 +682,7 @@ static gbhf_status build_task_lists(gbhf_ctx* c, TaskLists& TL, int ncombo, cons
 // quartet) it bounds the primitive quartets of one quartet in one task.
 static gbhf_status build_tasks(gbhf_ctx* c, double thr_all, double thr64, const double* pw = nullptr,
                                const double* sw = nullptr) {
-  static const int lane_prims[NCOMBO] = {256, 128, 48, 48, 16, 8, 36, 36, 36, 36, 36, 36, 36, 36, 36, 36, 36, 36,
+  static const int lane_prims[NCOMBO] = {256, 128, 48, 48, 16, 8, 48, 16, 8, 8, 16, 8, 36, 36, 36, 16, 36, 36,
                                          36, 36, 36};
   return build_task_lists(c, c->tasks, NCOMBO, COMBO_BRA, COMBO_KET, lane_prims, false, false, thr_all, thr64, pw,
                           sw);
@@ -773,11 +796,16 @@ static gbhf_status launch_class(gbhf_ctx* c, cudaStream_t strm, int combo, int p
   a.G = G;
   a.boys = boys;
   a.stats = c->tasks.stats.p + 3 * (2 * combo + prec);
+  a.sscale = c->tasks.sscale.p;
   kern<<<grid, JK_THREADS, smem, strm>>>(a);
   count_launch(c);
   GBHF_CUDA(c, cudaGetLastError());
   return GBHF_OK;
 }
+
+// d combos evaluated by the generated lane-per-ket code (few components per
+// quartet); the others go to the warp-per-quartet kernels of jkd.cu.
+static bool gen_dclass(int k) { return (k >= 6 && k <= 11) || k == 15; }
 
 gbhf_status jk_build(gbhf_ctx* c, const double* d_Dsq, double* d_G, int precision, double schwarz,
                      double mixed_cutoff, double weight, bool local_weights) {
@@ -842,10 +870,17 @@ gbhf_status jk_build(gbhf_ctx* c, const double* d_Dsq, double* d_G, int precisio
       gbhf_status s = GBHF_OK;
       cudaStream_t strm = ev ? c->stream : c->side[nl % gbhf_ctx::NSIDE];
       ++nl;
-      if (k >= NCOMBO_SP) {
+      if (k >= NCOMBO_SP && !gen_dclass(k)) {
         s = launch_jk_dclass(c, strm, k, prec, D64, D32, d_G, nt[k][prec]);
       } else if (prec == 0) {
         switch (k) {
+          case 6: s = launch_class<2, 0, 0, 0, double, false>(c, strm, 6, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boysh64.p, f0, nt[6][0]); break;
+          case 7: s = launch_class<2, 0, 1, 0, double, false>(c, strm, 7, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boysh64.p, f0, nt[7][0]); break;
+          case 8: s = launch_class<2, 0, 1, 1, double, true>(c, strm, 8, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boysh64.p, f0, nt[8][0]); break;
+          case 9: s = launch_class<2, 0, 2, 0, double, true>(c, strm, 9, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boysh64.p, f0, nt[9][0]); break;
+          case 10: s = launch_class<2, 1, 0, 0, double, false>(c, strm, 10, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boysh64.p, f0, nt[10][0]); break;
+          case 11: s = launch_class<2, 1, 1, 0, double, true>(c, strm, 11, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boysh64.p, f0, nt[11][0]); break;
+          case 15: s = launch_class<2, 2, 0, 0, double, true>(c, strm, 15, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boysh64.p, f0, nt[15][0]); break;
           case 5: s = launch_class<1, 1, 1, 1, double, true>(c, strm, 5, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boysh64.p, f0, nt[5][0]); break;
           case 4: s = launch_class<1, 1, 1, 0, double, false>(c, strm, 4, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boysh64.p, f0, nt[4][0]); break;
           case 3: s = launch_class<1, 1, 0, 0, double, false>(c, strm, 3, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boysh64.p, f0, nt[3][0]); break;
@@ -855,6 +890,13 @@ gbhf_status jk_build(gbhf_ctx* c, const double* d_Dsq, double* d_G, int precisio
         }
       } else {
         switch (k) {
+          case 6: s = launch_class<2, 0, 0, 0, float, false>(c, strm, 6, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boysh32.p, f0, nt[6][1]); break;
+          case 7: s = launch_class<2, 0, 1, 0, float, false>(c, strm, 7, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boysh32.p, f0, nt[7][1]); break;
+          case 8: s = launch_class<2, 0, 1, 1, float, false>(c, strm, 8, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boysh32.p, f0, nt[8][1]); break;
+          case 9: s = launch_class<2, 0, 2, 0, float, false>(c, strm, 9, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boysh32.p, f0, nt[9][1]); break;
+          case 10: s = launch_class<2, 1, 0, 0, float, false>(c, strm, 10, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boysh32.p, f0, nt[10][1]); break;
+          case 11: s = launch_class<2, 1, 1, 0, float, false>(c, strm, 11, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boysh32.p, f0, nt[11][1]); break;
+          case 15: s = launch_class<2, 2, 0, 0, float, false>(c, strm, 15, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boysh32.p, f0, nt[15][1]); break;
           case 5: s = launch_class<1, 1, 1, 1, float, false>(c, strm, 5, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boysh32.p, f0, nt[5][1]); break;
           case 4: s = launch_class<1, 1, 1, 0, float, false>(c, strm, 4, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boysh32.p, f0, nt[4][1]); break;
           case 3: s = launch_class<1, 1, 0, 0, float, false>(c, strm, 3, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boysh32.p, f0, nt[3][1]); break;
