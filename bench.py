@@ -391,14 +391,20 @@ def run_gradient(args, world, rank, local):
     print(json.dumps(line), flush=True)
 
 
-def run_large(args, world, rank, local):
-    """(H2O)64 RHF/6-31G (832 functions): mixed direct SCF with incremental
-    builds, then the analytic gradient; the plain FP64 GPU SCF beside it."""
+def run_large(args, world, rank, local, cluster="w64", basis="6-31g"):
+    """A cluster SCF with its gradient: mixed direct SCF with incremental builds,
+    then the analytic gradient; the plain FP64 GPU SCF beside it.  w64:
+    (H2O)64 RHF/6-31G (832 functions); w16d: (H2O)16 RHF/6-31G* (304 functions,
+    the d-shell classes)."""
     from gbhf import _lib, basis as B, molecules as M
     from gbhf.flops_model import F_ALG
     ctx = _lib.Context(local)
-    fb = B.flatten(M.cluster_atoms("w64", "6-31g"))
+    fb = B.flatten(M.cluster_atoms(cluster, basis))
     ctx.set_basis(fb)
+    if args.workload == "w16d":   # first launches of the d-class kernels load their code
+        ctx.scf(_lib.baseline_opts(precision=_lib.PREC_MIXED, incremental=1), want_matrices=False)
+        ctx.gradient(precision=_lib.PREC_MIXED)
+        ctx.set_basis(fb)
     ctx.profile_reset(events=True)
     ctx.event_record(0)
     rmx = ctx.scf(_lib.baseline_opts(precision=_lib.PREC_MIXED, incremental=1), want_matrices=False)
@@ -412,7 +418,7 @@ def run_large(args, world, rank, local):
     g64 = ctx.gradient()
     ctx.event_record(5)
     tg64 = ctx.event_elapsed(2, 5)
-    out = {"workload": "w64", "n_basis": fb.n_cgf, "mixed_scf_s": tmx / 1e3, "gradient_mixed_s": tg / 1e3,
+    out = {"workload": args.workload, "basis": basis, "n_basis": fb.n_cgf, "mixed_scf_s": tmx / 1e3, "gradient_mixed_s": tg / 1e3,
            "gradient_fp64_s": tg64 / 1e3, "max_abs_grad_mixed_vs_fp64": float(abs(gmx - g64).max()),
            "energy_mixed": rmx["energy"], "iterations": rmx["iterations"],
            "eri_quartets_per_s": prof["fn_quartets"] / (tmx / 1e3),
@@ -456,7 +462,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gbhf", choices=["gbhf", "reference"])
-    ap.add_argument("--workload", default="w16", choices=["w16", "batch256", "grad8", "w64", "fock"])
+    ap.add_argument("--workload", default="w16", choices=["w16", "batch256", "grad8", "w64", "w16d", "fock"])
     ap.add_argument("--quick", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--mixed-cutoff", type=float, default=1e-2,
@@ -475,6 +481,8 @@ def main():
         run_gradient(args, world, rank, local)
     elif args.workload == "w64":
         run_large(args, world, rank, local)
+    elif args.workload == "w16d":
+        run_large(args, world, rank, local, "w16", "6-31g*")
     elif args.workload == "fock":
         run_fock_case(args, world, rank, local)
     else:

@@ -423,7 +423,10 @@ gbhf_status schwarz_dclasses_dev(gbhf_ctx* c, const int* cls_start, const int* d
 // J/K launch of combo 6..20 (COMBO_BRA/COMBO_KET), precision 0 = FP64, 1 = FP32.
 gbhf_status launch_jk_dclass(gbhf_ctx* c, cudaStream_t strm, int combo, int prec, const double* D64,
                              const float* D32, double* G, int ntask);
-// Gradient launch of combo 9..35 (GRAD_COMBO_BRA/GRAD_COMBO_KET).
+// Gradient combos on the generated lane-per-ket kernels (grad.cu); the rest
+// go to launch_grad_dclass.
+bool grad_gen_combo(int k);
+// Gradient launch of a combo 9..35 (GRAD_COMBO_BRA/GRAD_COMBO_KET) without generated code.
 gbhf_status launch_grad_dclass(gbhf_ctx* c, cudaStream_t strm, int combo, int prec, const double* D64,
                                const float* D32, double* grad, int ntask);
 // linalg.cu

@@ -397,6 +397,10 @@ def gen_vne(la, lb):
     return "\n".join(out)
 
 
+# (the FP64 code of the larger ones spills registers heavily)
+GEN_D_CLASSES = [(0, 0, 2, 0), (0, 0, 2, 1), (1, 0, 2, 0), (2, 0, 0, 0), (2, 0, 1, 0)]
+
+
 def main():
     pcls = [(0, 0), (1, 0), (1, 1)]
     parts = ["// GENERATED by gen_grad.py -- do not edit by hand.", "#pragma once", ""]
@@ -405,6 +409,12 @@ def main():
             code, _ = gen_class(la, lb, lc, ld)
             parts.append(code)
             parts.append("")
+    # (bra class, ket class) combinations with a d pair and few components per
+    # quartet; the larger ones use the warp-per-quartet kernels of gradd.cu
+    for c in GEN_D_CLASSES:
+        code, _ = gen_class(*c)
+        parts.append(code)
+        parts.append("")
     for (la, lb) in pcls + [(2, 0), (2, 1), (2, 2)]:
         parts.append(gen_vne(la, lb))
         parts.append("")

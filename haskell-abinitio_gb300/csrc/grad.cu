@@ -61,6 +61,11 @@ struct GradFn;
                                 gam, g);                                                                       \
     }                                                                                                          \
   };
+GBHF_GRAD_FN(0, 0, 2, 0, ssds)
+GBHF_GRAD_FN(0, 0, 2, 1, ssdp)
+GBHF_GRAD_FN(1, 0, 2, 0, psds)
+GBHF_GRAD_FN(2, 0, 0, 0, dsss)
+GBHF_GRAD_FN(2, 0, 1, 0, dsps)
 GBHF_GRAD_FN(0, 0, 0, 0, ssss)
 GBHF_GRAD_FN(0, 0, 1, 0, ssps)
 GBHF_GRAD_FN(0, 0, 1, 1, sspp)
@@ -89,6 +94,7 @@ struct GradArgs {
   const T* D;                // stacked n_m x n_m densities, this precision
   const T* boys;
   double* grad;              // 3 * natoms
+  const double* sscale;      // per shell 6 component scales (d shells)
 };
 
 __device__ __forceinline__ double warp_sum_d(double v) {
@@ -170,7 +176,14 @@ __global__ void __launch_bounds__(GR_THREADS) k_grad_jk(GradArgs<T> a) {
               const T dbd = Dm[(long long)(b0 + ibb) * n + d0 + id];
               const T dad = Dm[(long long)(a0 + ia) * n + d0 + id];
               const T dbc = Dm[(long long)(b0 + ibb) * n + c0 + ic];
-              gam.set(((ia * NB + ibb) * NC + ic) * ND + id, dab * dcd - T(0.25) * (dac * dbd + dad * dbc));
+              T gv = dab * dcd - T(0.25) * (dac * dbd + dad * dbc);
+              if constexpr (LA == 2 || LB == 2 || LC == 2 || LD == 2) {   // d components: scaled functions
+                if (LA == 2) gv *= T(a.sscale[6 * A + ia]);
+                if (LB == 2) gv *= T(a.sscale[6 * B + ibb]);
+                if (LC == 2) gv *= T(a.sscale[6 * C + ic]);
+                if (LD == 2) gv *= T(a.sscale[6 * Dd + id]);
+              }
+              gam.set(((ia * NB + ibb) * NC + ic) * ND + id, gv);
             }
       const int4 sg = a.seg[a.kseg[jk]];
       const int len = sg.y - sg.x;
@@ -249,6 +262,7 @@ static gbhf_status launch_grad_class(gbhf_ctx* c, cudaStream_t strm, int combo, 
   a.D = D;
   a.boys = boys;
   a.grad = grad;
+  a.sscale = c->tasks.sscale.p;
   kern<<<grid, GR_THREADS, smem, strm>>>(a);
   count_launch(c);
   GBHF_CUDA(c, cudaGetLastError());
@@ -267,8 +281,21 @@ static gbhf_status launch_grad_combo(gbhf_ctx* c, cudaStream_t strm, int k, int 
     case 5: return launch_grad_class<1, 0, 1, 1, T>(c, strm, k, prec, D, bra, ket, boys, grad, nt);
     case 6: return launch_grad_class<1, 1, 0, 0, T>(c, strm, k, prec, D, bra, ket, boys, grad, nt);
     case 7: return launch_grad_class<1, 1, 1, 0, T>(c, strm, k, prec, D, bra, ket, boys, grad, nt);
-    default: return launch_grad_class<1, 1, 1, 1, T>(c, strm, k, prec, D, bra, ket, boys, grad, nt);
+    case 8: return launch_grad_class<1, 1, 1, 1, T>(c, strm, k, prec, D, bra, ket, boys, grad, nt);
+    // combinations with a d pair on generated code (GRAD_COMBO_BRA / GRAD_COMBO_KET)
+    case 9: return launch_grad_class<0, 0, 2, 0, T>(c, strm, k, prec, D, bra, ket, boys, grad, nt);
+    case 10: return launch_grad_class<0, 0, 2, 1, T>(c, strm, k, prec, D, bra, ket, boys, grad, nt);
+    case 12: return launch_grad_class<1, 0, 2, 0, T>(c, strm, k, prec, D, bra, ket, boys, grad, nt);
+    case 18: return launch_grad_class<2, 0, 0, 0, T>(c, strm, k, prec, D, bra, ket, boys, grad, nt);
+    case 19: return launch_grad_class<2, 0, 1, 0, T>(c, strm, k, prec, D, bra, ket, boys, grad, nt);
+    default: return fail(c, GBHF_ERR_UNSUPPORTED, "no generated gradient kernel for combo " + std::to_string(k));
   }
+}
+
+// Gradient combinations with a d pair evaluated by the generated lane-per-ket
+// code; the others go to the warp-per-quartet kernels of gradd.cu.
+bool grad_gen_combo(int k) {
+  return k < NGCOMBO_SP || k == 9 || k == 10 || k == 12 || k == 18 || k == 19;
 }
 
 // Two-electron gradient of D (n x n, device) into d_grad (accumulated).
@@ -298,7 +325,7 @@ static gbhf_status grad_2e(gbhf_ctx* c, const double* d_D, double schwarz, doubl
       const int nt = gt.hranges[4 * k + 2 * prec + 1] - gt.hranges[4 * k + 2 * prec];
       if (nt <= 0) continue;
       cudaStream_t strm = c->side[nl++ % gbhf_ctx::NSIDE];
-      if (k >= NGCOMBO_SP)
+      if (!grad_gen_combo(k))
         GBHF_TRY(launch_grad_dclass(c, strm, k, prec, d_D, c->dfloat.p, d_grad, nt));
       else if (prec == 0)
         GBHF_TRY(launch_grad_combo<double>(c, strm, k, 0, d_D, P.bra64.p, P.ket64.p, c->boysh64.p, d_grad, nt));

@@ -382,6 +382,7 @@ struct TaskGenArgs {
   int cbra[NCOMBO_MAX], cket[NCOMBO_MAX];
   int all_pairs;                 // every ordered (bra, ket) pair, else ket <= bra in one class
   int lane_prims[NCOMBO_MAX];    // per combo: primitive quartets per lane and task (bra split)
+  int task_kets[NCOMBO_MAX];     // per combo: kets per task (32: a lane per ket; fewer: a warp per quartet)
   int square_w;                  // bound uses the squared density weight (gradient)
   const int* item_combo_start;   // ncombo+1 item offsets
   const int* cls_start;          // NPCLS+1
@@ -445,19 +446,19 @@ __global__ void k_tasks(TaskGenArgs g) {
       const int k32 = keep - k64;
       // split the bra primitives so that one lane handles at most about
       // lane_prims primitive quartets per task (bounds the launch tail)
-      const int lp = g.lane_prims[k];
+      const int lp = g.lane_prims[k], tk = g.task_kets[k];
       const int nch0 = min(kb, (kb * s.z + lp - 1) / lp);
       const int cs = (kb + nch0 - 1) / nch0;
       const int nch = (kb + cs - 1) / cs;
       if (FILL) {
         for (int ch = 0; ch < nch; ++ch) {
           const int w = (ch * cs) | (min(kb, (ch + 1) * cs) << 16);
-          for (int o = 0; o < k64; o += 32) g.tasks64[w64++] = make_int4(i, s.x + o, min(32, k64 - o), w);
-          for (int o = 0; o < k32; o += 32) g.tasks32[w32++] = make_int4(i, s.x + k64 + o, min(32, k32 - o), w);
+          for (int o = 0; o < k64; o += tk) g.tasks64[w64++] = make_int4(i, s.x + o, min(tk, k64 - o), w);
+          for (int o = 0; o < k32; o += tk) g.tasks32[w32++] = make_int4(i, s.x + k64 + o, min(tk, k32 - o), w);
         }
       } else {
-        n64 += nch * ((k64 + 31) / 32);
-        n32 += nch * ((k32 + 31) / 32);
+        n64 += nch * ((k64 + tk - 1) / tk);
+        n32 += nch * ((k32 + tk - 1) / tk);
       }
     }
   }
@@ -591,8 +592,8 @@ static gbhf_status density_weights(gbhf_ctx* c, TaskLists& st, const double* d_d
 
 // Quartet-class task lists of TL for the combos (cbra[k], cket[k]).
 static gbhf_status build_task_lists(gbhf_ctx* c, TaskLists& TL, int ncombo, const int* cbra, const int* cket,
-                                    const int* lane_prims, bool all_pairs, bool square_w, double thr_all,
-                                    double thr64, const double* pw, const double* sw) {
+                                    const int* lane_prims, const int* task_kets, bool all_pairs, bool square_w,
+                                    double thr_all, double thr64, const double* pw, const double* sw) {
   PairData& P = c->pairs;
   int* h_ranges = TL.hranges;
   std::vector<int> ics(ncombo + 1, 0);
@@ -625,6 +626,7 @@ static gbhf_status build_task_lists(gbhf_ctx* c, TaskLists& TL, int ncombo, cons
     g.cbra[k] = k < ncombo ? cbra[k] : 0;
     g.cket[k] = k < ncombo ? cket[k] : 0;
     g.lane_prims[k] = k < ncombo ? std::max(1, lane_prims[k]) : 1;
+    g.task_kets[k] = k < ncombo ? std::min(32, std::max(1, task_kets[k])) : 32;
   }
   g.all_pairs = all_pairs ? 1 : 0;
   g.square_w = square_w ? 1 : 0;
@@ -684,8 +686,11 @@ static gbhf_status build_tasks(gbhf_ctx* c, double thr_all, double thr64, const 
                                const double* sw = nullptr) {
   static const int lane_prims[NCOMBO] = {256, 128, 48, 48, 16, 8, 48, 16, 8, 8, 16, 8, 36, 36, 36, 16, 36, 36,
                                          36, 36, 36};
-  return build_task_lists(c, c->tasks, NCOMBO, COMBO_BRA, COMBO_KET, lane_prims, false, false, thr_all, thr64, pw,
-                          sw);
+  // one quartet per task for the warp-per-quartet classes: a launch then spreads
+  // its quartets over every resident warp
+  static const int task_kets[NCOMBO] = {32, 32, 32, 32, 32, 32, 32, 32, 32, 32, 32, 32, 1, 1, 1, 32, 1, 1, 1, 1, 1};
+  return build_task_lists(c, c->tasks, NCOMBO, COMBO_BRA, COMBO_KET, lane_prims, task_kets, false, false, thr_all,
+                          thr64, pw, sw);
 }
 
 gbhf_status ensure_shell_arrays(gbhf_ctx* c) {
@@ -750,11 +755,14 @@ gbhf_status build_grad_tasks(gbhf_ctx* c, const double* d_D, double cutoff, doub
   const double t64 = precision == GBHF_PREC_FP64 ? 0.0 : mixed_cutoff;
   // (bra class, ket class) of the derivative code: about twice the ERI work per primitive quartet;
   // the d combinations (warp per quartet) bound the primitive quartets of one quartet per task
-  int lp[NCOMBO_MAX];
+  int lp[NCOMBO_MAX], tk[NCOMBO_MAX];
   static const int lp_sp[NGCOMBO_SP] = {128, 64, 24, 64, 24, 8, 24, 8, 4};
-  for (int k = 0; k < NCOMBO_MAX; ++k) lp[k] = k < NGCOMBO_SP ? lp_sp[k] : 36;
-  GBHF_TRY(build_task_lists(c, gt, NCOMBO_MAX, GRAD_COMBO_BRA, GRAD_COMBO_KET, lp, true, true, cutoff, t64, gt.pw.p,
-                            gt.sw.p));
+  for (int k = 0; k < NCOMBO_MAX; ++k) {
+    lp[k] = k < NGCOMBO_SP ? lp_sp[k] : (grad_gen_combo(k) ? 8 : 36);
+    tk[k] = grad_gen_combo(k) ? 32 : 1;
+  }
+  GBHF_TRY(build_task_lists(c, gt, NCOMBO_MAX, GRAD_COMBO_BRA, GRAD_COMBO_KET, lp, tk, true, true, cutoff, t64,
+                            gt.pw.p, gt.sw.p));
   return GBHF_OK;
 }
 
