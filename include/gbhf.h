@@ -118,7 +118,10 @@ int gbhf_version(void);
  * n_cgf contracted Gaussians, CGF k on atom cgf_atom[k] with Cartesian
  * exponents cgf_lxyz[3k..3k+2] and cgf_nprim[k] primitives whose
  * (coefficient, exponent) follow in prim_coef/prim_exp (coefficients already
- * carry normCoeff, NormalizeBasis.hs:52-59). */
+ * carry normCoeff, NormalizeBasis.hs:52-59).  s, p and d functions; the direct
+ * J/K and gradient kernels group them into shells (components in createCGF
+ * order x,y,z and xx,xy,xz,yy,yz,zz, shared exponents, proportional
+ * coefficients) and return GBHF_ERR_UNSUPPORTED for CGFs that form no shell. */
 gbhf_status gbhf_set_basis(gbhf_ctx* ctx, int n_atoms, const double* xyz_bohr, const double* charges,
                            int n_cgf, const int* cgf_atom, const int* cgf_lxyz, const int* cgf_nprim,
                            const double* prim_coef, const double* prim_exp);
