@@ -491,6 +491,27 @@ gbhf_status gbhf_profile_reset(gbhf_ctx* c, int enable_events) {
   return GBHF_OK;
 }
 
+gbhf_status gbhf_set_guess_density(gbhf_ctx* c, const double* density_flat) {
+  CTX_CHECK(c);
+  if (!need_basis(c)) return GBHF_ERR_BAD_INPUT;
+  if (!density_flat) return fail(c, GBHF_ERR_BAD_INPUT, "null density");
+  const size_t n = (size_t)c->basis.nbf;
+  GBHF_TRY(upload(c, c->guess_D, density_flat, n * (n + 1) / 2));
+  c->guess_gen = c->basis_gen;
+  GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
+  return GBHF_OK;
+}
+
+gbhf_status gbhf_scf_trace(gbhf_ctx* c, double* out, int max_records, int* n_records) {
+  CTX_CHECK(c);
+  if (!n_records || (max_records > 0 && !out)) return fail(c, GBHF_ERR_BAD_INPUT, "null pointer");
+  const int nrec = (int)(c->scf_trace.size() / GBHF_SCF_TRACE_FIELDS);
+  *n_records = nrec;
+  const int m = std::min(nrec, std::max(max_records, 0));
+  std::copy(c->scf_trace.begin(), c->scf_trace.begin() + (size_t)m * GBHF_SCF_TRACE_FIELDS, out);
+  return GBHF_OK;
+}
+
 gbhf_status gbhf_profile_read(gbhf_ctx* c, double* stats, int n_stats) {
   CTX_CHECK(c);
   if (!stats) return fail(c, GBHF_ERR_BAD_INPUT, "null pointer");

@@ -53,15 +53,19 @@ constexpr int BT = 32, BKK = 16;
 
 // C_m = alpha op(A_m) op(B_m) + beta C_m for every active molecule; one 32 x 32
 // tile of one molecule's C per CTA (4 warps of 16 x 16, 2 x 2 DMMA tiles each).
-// C must not alias A or B.
-__global__ void __launch_bounds__(128) k_bgemm(BDesc d, int ta, int tb, double alpha, const double* __restrict__ A,
-                                               const double* __restrict__ B, double beta, double* __restrict__ C) {
+// C must not alias A or B.  sym (C_m symmetric, beta = 0): tiles below the
+// diagonal return at once and each tile above it is stored at its mirror too.
+__global__ void __launch_bounds__(128) k_bgemm(BDesc d, int ta, int tb, int sym, double alpha,
+                                               const double* __restrict__ A, const double* __restrict__ B,
+                                               double beta, double* __restrict__ C) {
   const int m = bd_mol(d.tstart, d.M, blockIdx.x);
   if (!d.active[m]) return;
   const int n = d.n[m];
   const long long o = d.off[m];
   const int nt = (n + BT - 1) / BT, t = blockIdx.x - d.tstart[m];
-  const int row0 = (t / nt) * BT, col0 = (t % nt) * BT;
+  const int rt = t / nt, ct = t % nt;
+  if (sym && rt > ct) return;
+  const int row0 = rt * BT, col0 = ct * BT;
   const double* Am = A + o;
   const double* Bm = B + o;
   double* Cm = C + o;
@@ -125,6 +129,7 @@ __global__ void __launch_bounds__(128) k_bgemm(BDesc d, int ta, int tb, double a
         if (r < n && cc < n) {
           double* p = Cm + (long)r * n + cc;
           *p = alpha * acc[i][j][h] + (beta == 0.0 ? 0.0 : beta * *p);
+          if (sym && rt < ct) Cm[(long)cc * n + r] = alpha * acc[i][j][h];
         }
       }
 }
@@ -253,9 +258,12 @@ __global__ void k_b_maxdev_identity(BDesc d, const double* __restrict__ T, doubl
   if (threadIdx.x == 0) out[m] = v;
 }
 
-// traces of P, P^2, P^3 -> next purification polynomial, coef[4m] = (a, b, c, tr(P - P^2))
+// traces of P, P^2, P^3 -> next purification polynomial, coef[4m] = (a, b, c, tr(P - P^2));
+// a molecule whose idempotency error is below tol * nocc leaves the purification
+// (its flag in d.active, a copy of the batch's flags, is cleared)
 __global__ void k_b_purify_coef(BDesc d, const double* __restrict__ P, const double* __restrict__ P2,
-                                const double* __restrict__ P3, double* __restrict__ coef) {
+                                const double* __restrict__ P3, double* __restrict__ coef,
+                                const int* __restrict__ nocc, double tol, int* __restrict__ pact) {
   const int m = blockIdx.x;
   if (!d.active[m]) return;
   const int n = d.n[m];
@@ -290,6 +298,7 @@ __global__ void k_b_purify_coef(BDesc d, const double* __restrict__ P, const dou
     coef[4 * m + 1] = b;
     coef[4 * m + 2] = c;
     coef[4 * m + 3] = den;
+    if (fabs(den) < tol * (double)max(1, nocc[m])) pact[m] = 0;   // P meets the tolerance: no further update
   }
 }
 
@@ -388,7 +397,7 @@ struct BatchRun {
   size_t nst = 0;
   std::vector<int> n, tstart, nocc, active;
   std::vector<long long> off;
-  DBuf<int> d_n, d_tstart, d_active, d_nocc;
+  DBuf<int> d_n, d_tstart, d_active, d_nocc, d_pact;
   DBuf<long long> d_off;
   BDesc desc{};
 
@@ -435,8 +444,11 @@ struct BatchRun {
     return GBHF_OK;
   }
   dim3 egrid() const { return dim3((unsigned)((nmax * nmax + 255) / 256), (unsigned)M); }
-  gbhf_status gemm(bool ta, bool tb, double alpha, const double* A, const double* B, double beta, double* C) {
-    k_bgemm<<<ntiles, 128, 0, c->stream>>>(desc, ta, tb, alpha, A, B, beta, C);
+  // sym: every C_m is symmetric (beta must be 0); dsc: other per-molecule active flags
+  gbhf_status gemm(bool ta, bool tb, double alpha, const double* A, const double* B, double beta, double* C,
+                   bool sym = false, const BDesc* dsc = nullptr) {
+    k_bgemm<<<ntiles, 128, 0, c->stream>>>(dsc ? *dsc : desc, ta, tb, sym && beta == 0.0 ? 1 : 0, alpha, A, B, beta,
+                                           C);
     count_launch(c);
     GBHF_CUDA(c, cudaGetLastError());
     return GBHF_OK;
@@ -488,25 +500,31 @@ gbhf_status b_density(BatchRun& br, const double* F, const double* X, double* D,
                       double* P2, double* P3, double* g, double* coef) {
   gbhf_ctx* c = br.c;
   GBHF_TRY(br.gemm(true, false, 1.0, X, F, 0.0, T1));
-  GBHF_TRY(br.gemm(false, false, 1.0, T1, X, 0.0, Fp));
+  GBHF_TRY(br.gemm(false, false, 1.0, T1, X, 0.0, Fp, true));
   k_b_gershgorin<<<br.M, 256, 0, c->stream>>>(br.desc, Fp, g);
   k_b_purify_init<<<br.egrid(), 256, 0, c->stream>>>(br.desc, br.d_nocc.p, Fp, g, P);
   count_launch(c, 2);
   std::vector<double> hc(4 * (size_t)br.M);
+  // molecules still purifying: a copy of the active flags that k_b_purify_coef clears
+  GBHF_CUDA(c, br.d_pact.alloc(br.M));
+  GBHF_CUDA(c, cudaMemcpyAsync(br.d_pact.p, br.d_active.p, br.M * sizeof(int), cudaMemcpyDeviceToDevice, c->stream));
+  BDesc pd = br.desc;
+  pd.active = br.d_pact.p;
+  const double tol = 1e-13;
   // four purification steps per CUDA-graph replay, convergence read between replays
   auto four_steps = [&]() -> gbhf_status {
     for (int k = 0; k < 4; ++k) {
-      GBHF_TRY(br.gemm(false, false, 1.0, P, P, 0.0, P2));
-      GBHF_TRY(br.gemm(false, false, 1.0, P, P2, 0.0, P3));
-      k_b_purify_coef<<<br.M, 256, 0, c->stream>>>(br.desc, P, P2, P3, coef);
-      k_b_purify_update<<<br.egrid(), 256, 0, c->stream>>>(br.desc, coef, P, P2, P3);
+      GBHF_TRY(br.gemm(false, false, 1.0, P, P, 0.0, P2, true, &pd));
+      GBHF_TRY(br.gemm(false, false, 1.0, P, P2, 0.0, P3, true, &pd));
+      k_b_purify_coef<<<br.M, 256, 0, c->stream>>>(pd, P, P2, P3, coef, br.d_nocc.p, tol, br.d_pact.p);
+      k_b_purify_update<<<br.egrid(), 256, 0, c->stream>>>(pd, coef, P, P2, P3);
       count_launch(c, 2);
     }
     return GBHF_OK;
   };
   const std::vector<const void*> key = {(const void*)(size_t)br.M, (const void*)(size_t)br.ntiles,
                                         (const void*)(size_t)br.nmax, br.desc.n, br.desc.off, br.desc.tstart,
-                                        br.desc.active, P, P2, P3, coef};
+                                        br.d_pact.p, br.d_nocc.p, P, P2, P3, coef};
   bool done = false;
   for (int rep = 0; rep < 50 && !done; ++rep) {
     GBHF_TRY(graph_run(c, c->g_bpurify, key, four_steps));
@@ -514,13 +532,13 @@ gbhf_status b_density(BatchRun& br, const double* F, const double* X, double* D,
     GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
     done = true;
     for (int m = 0; m < br.M; ++m)
-      if (br.active[m] && !(std::fabs(hc[4 * m + 3]) < 1e-13 * std::max(1, br.nocc[m]))) done = false;
+      if (br.active[m] && !(std::fabs(hc[4 * m + 3]) < tol * std::max(1, br.nocc[m]))) done = false;
   }
   for (int m = 0; m < br.M; ++m)
     if (br.active[m] && !(std::fabs(hc[4 * m + 3]) < 1e-6 * std::max(1, br.nocc[m])))
       return fail(c, GBHF_ERR_NOT_CONVERGED, "density purification did not converge for molecule " + std::to_string(m));
   GBHF_TRY(br.gemm(false, false, 2.0, X, P, 0.0, T1));
-  GBHF_TRY(br.gemm(false, true, 1.0, T1, X, 0.0, D));
+  GBHF_TRY(br.gemm(false, true, 1.0, T1, X, 0.0, D, true));
   return GBHF_OK;
 }
 
@@ -866,7 +884,7 @@ gbhf_status bscf_run(gbhf_ctx* c, const gbhf_scf_opts* o, double* energies, int*
     GBHF_TRY(br.set_active(all));
     GBHF_TRY(b_density(br, Ffin, X, Dg, T1, Fp, P, P2, P3, d_g, d_coef));
     GBHF_TRY(br.gemm(false, false, 1.0, Dg, Ffin, 0.0, T1));
-    GBHF_TRY(br.gemm(false, false, 0.5, T1, Dg, 0.0, Wm));
+    GBHF_TRY(br.gemm(false, false, 0.5, T1, Dg, 0.0, Wm, true));
     DBuf<double> dgrad;
     GBHF_CUDA(c, dgrad.alloc(3 * (size_t)b.natoms));
     GBHF_TRY(gradient_dev(c, Dg, Wm, o->schwarz_cutoff > 0 ? o->schwarz_cutoff : 1e-12,

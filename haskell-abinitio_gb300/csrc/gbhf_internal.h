@@ -290,6 +290,9 @@ struct gbhf_ctx {
   gbhf::JacobiWork jac;
   // state of the last SCF (for the gradient): density, Fock matrix, occupation
   gbhf::DBuf<double> last_D, last_F;
+  gbhf::DBuf<double> guess_D;        // gbhf_set_guess_density (flat), valid for basis generation guess_gen
+  long guess_gen = -1;
+  std::vector<double> scf_trace;     // per-step records of the last SCF (GBHF_SCF_TRACE_FIELDS each)
   int last_nocc = -1;
   long last_gen = -1;
   // worker contexts of gbhf_scf_batch (owned; destroyed with this context)
@@ -430,8 +433,9 @@ bool grad_gen_combo(int k);
 gbhf_status launch_grad_dclass(gbhf_ctx* c, cudaStream_t strm, int combo, int prec, const double* D64,
                                const float* D32, double* grad, int ntask);
 // linalg.cu
+// sym: C (square) is known to be symmetric; only its upper tiles are computed and mirrored.
 gbhf_status gemm(gbhf_ctx* c, bool ta, bool tb, int m, int n, int k, double alpha, const double* A, int lda,
-                 const double* B, int ldb, double beta, double* C, int ldc);
+                 const double* B, int ldb, double beta, double* C, int ldc, bool sym = false);
 gbhf_status eigh(gbhf_ctx* c, int n, const double* d_A, double* d_evals, double* d_evecs, const double* d_V0);
 gbhf_status flat_to_square(gbhf_ctx* c, int n, const double* d_flat, double* d_sq);
 gbhf_status square_to_flat(gbhf_ctx* c, int n, const double* d_sq, double* d_flat);

@@ -94,13 +94,16 @@ __global__ void __launch_bounds__(128) k_dgemm(bool ta, bool tb, int m, int n, i
 // Small-matrix variant: 32x32 C tile per CTA (4 warps of 16x16 = 2x2 DMMA
 // tiles), K split over gridDim.z slices whose partial products are added
 // with FP64 atomics into C (pre-scaled by beta), so that N ~ 200 matrices
-// still occupy every SM.
+// still occupy every SM.  sym (square C known to be symmetric, e.g. P P or
+// X^T F X): only the tiles on and above the diagonal are computed, each
+// added to its mirror position as well.
 constexpr int ST = 32, SK = 16;
 
-__global__ void __launch_bounds__(128) k_dgemm_split(bool ta, bool tb, int m, int n, int k, int kslice,
+__global__ void __launch_bounds__(128) k_dgemm_split(bool ta, bool tb, bool sym, int m, int n, int k, int kslice,
                                                      double alpha, const double* __restrict__ A, int lda,
                                                      const double* __restrict__ B, int ldb, double* __restrict__ C,
                                                      int ldc) {
+  if (sym && blockIdx.y > blockIdx.x) return;   // mirrored from tile (x, y)
   __shared__ double As[ST][SK + 1];
   __shared__ double Bs[SK][ST + 2];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -160,7 +163,10 @@ __global__ void __launch_bounds__(128) k_dgemm_split(bool ta, bool tb, int m, in
       for (int h = 0; h < 2; ++h) {
         const int r = row0 + wr + i * 8 + (lane >> 2);
         const int cc = col0 + wc + j * 8 + 2 * (lane & 3) + h;
-        if (r < m && cc < n) atomicAdd(C + (long)r * ldc + cc, alpha * acc[i][j][h]);
+        if (r < m && cc < n) {
+          atomicAdd(C + (long)r * ldc + cc, alpha * acc[i][j][h]);
+          if (sym && blockIdx.y < blockIdx.x) atomicAdd(C + (long)cc * ldc + r, alpha * acc[i][j][h]);
+        }
       }
 }
 
@@ -172,8 +178,9 @@ __global__ void k_scale_matrix(int m, int n, double beta, double* __restrict__ C
 }
 
 gbhf_status gemm(gbhf_ctx* c, bool ta, bool tb, int m, int n, int k, double alpha, const double* A, int lda,
-                 const double* B, int ldb, double beta, double* C, int ldc) {
+                 const double* B, int ldb, double beta, double* C, int ldc, bool sym) {
   if (m <= 0 || n <= 0) return GBHF_OK;
+  sym = sym && m == n;
   const long tiles64 = (long)((n + GT - 1) / GT) * ((m + GT - 1) / GT);
   if (tiles64 >= 2L * c->nsm) {
     dim3 grid((n + GT - 1) / GT, (m + GT - 1) / GT);
@@ -182,7 +189,8 @@ gbhf_status gemm(gbhf_ctx* c, bool ta, bool tb, int m, int n, int k, double alph
     GBHF_CUDA(c, cudaGetLastError());
     return GBHF_OK;
   }
-  const int tiles = ((n + ST - 1) / ST) * ((m + ST - 1) / ST);
+  const int nt = (n + ST - 1) / ST;
+  const int tiles = sym ? nt * (nt + 1) / 2 : nt * ((m + ST - 1) / ST);
   int splits = std::max(1, (2 * c->nsm + tiles - 1) / tiles);
   splits = std::min(splits, std::max(1, (k + 4 * SK - 1) / (4 * SK)));   // at least 4 k-steps per slice
   int kslice = (k + splits - 1) / splits;
@@ -190,7 +198,7 @@ gbhf_status gemm(gbhf_ctx* c, bool ta, bool tb, int m, int n, int k, double alph
   splits = std::max(1, (k + kslice - 1) / kslice);
   k_scale_matrix<<<dim3((n + 127) / 128, m), 128, 0, c->stream>>>(m, n, beta, C, ldc);
   k_dgemm_split<<<dim3((n + ST - 1) / ST, (m + ST - 1) / ST, splits), 128, 0, c->stream>>>(
-      ta, tb, m, n, k, kslice, alpha, A, lda, B, ldb, C, ldc);
+      ta, tb, sym, m, n, k, kslice, alpha, A, lda, B, ldb, C, ldc);
   count_launch(c, 2);
   GBHF_CUDA(c, cudaGetLastError());
   return GBHF_OK;
@@ -810,8 +818,8 @@ gbhf_status purify(gbhf_ctx* c, int n, int ne, const double* d_F, double* d_P, d
   // four purification steps per CUDA-graph replay, convergence read between replays
   auto four_steps = [&]() -> gbhf_status {
     for (int k = 0; k < 4; ++k) {
-      GBHF_TRY(gemm(c, false, false, n, n, n, 1.0, d_P, n, d_P, n, 0.0, P2, n));
-      GBHF_TRY(gemm(c, false, false, n, n, n, 1.0, d_P, n, P2, n, 0.0, P3, n));
+      GBHF_TRY(gemm(c, false, false, n, n, n, 1.0, d_P, n, d_P, n, 0.0, P2, n, true));
+      GBHF_TRY(gemm(c, false, false, n, n, n, 1.0, d_P, n, P2, n, 0.0, P3, n, true));
       k_purify_coef<<<1, 1024, 0, c->stream>>>(n, d_P, P2, P3, coef);
       count_launch(c);
       const double* mats[3] = {d_P, P2, P3};
@@ -841,7 +849,7 @@ gbhf_status density_purified_dev(gbhf_ctx* c, int n, const double* d_Fsq, const 
   GBHF_WS(c, Fp, 11, nn);
   GBHF_WS(c, P, 12, nn);
   GBHF_TRY(gemm(c, true, false, n, n, n, 1.0, d_X, n, d_Fsq, n, 0.0, T1, n));
-  GBHF_TRY(gemm(c, false, false, n, n, n, 1.0, T1, n, d_X, n, 0.0, Fp, n));
+  GBHF_TRY(gemm(c, false, false, n, n, n, 1.0, T1, n, d_X, n, 0.0, Fp, n, true));
   if (nocc <= 0) {
     GBHF_CUDA(c, cudaMemsetAsync(d_Dsq, 0, nn * sizeof(double), c->stream));
     return GBHF_OK;
@@ -849,7 +857,7 @@ gbhf_status density_purified_dev(gbhf_ctx* c, int n, const double* d_Fsq, const 
   double err = 0;
   GBHF_TRY(purify(c, n, nocc, Fp, P, &err));
   GBHF_TRY(gemm(c, false, false, n, n, n, 2.0, d_X, n, P, n, 0.0, T1, n));
-  GBHF_TRY(gemm(c, false, true, n, n, n, 1.0, T1, n, d_X, n, 0.0, d_Dsq, n));
+  GBHF_TRY(gemm(c, false, true, n, n, n, 1.0, T1, n, d_X, n, 0.0, d_Dsq, n, true));
   return GBHF_OK;
 }
 
@@ -956,7 +964,7 @@ gbhf_status diagonal_hf_dev(gbhf_ctx* c, int n, const double* d_Fsq, const doubl
   GBHF_WS(c, Fp, 11, nn);
   GBHF_WS(c, Cp, 12, nn);
   GBHF_TRY(gemm(c, true, false, n, n, n, 1.0, d_X, n, d_Fsq, n, 0.0, T1, n));
-  GBHF_TRY(gemm(c, false, false, n, n, n, 1.0, T1, n, d_X, n, 0.0, Fp, n));
+  GBHF_TRY(gemm(c, false, false, n, n, n, 1.0, T1, n, d_X, n, 0.0, Fp, n, true));
   GBHF_TRY(eigh(c, n, Fp, d_eps, Cp, d_Cp));
   if (d_Cp) GBHF_CUDA(c, cudaMemcpyAsync(d_Cp, Cp, nn * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
   GBHF_TRY(gemm(c, false, false, n, n, n, 1.0, d_X, n, Cp, n, 0.0, d_C, n));

@@ -187,6 +187,10 @@ gbhf_status scf_run(gbhf_ctx* c, const gbhf_scf_opts* o, gbhf_result* r) {
     GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
   } else if (o->guess == GBHF_GUESS_SAD) {
     GBHF_TRY(sad_density(c, D));
+  } else if (o->guess == GBHF_GUESS_DENSITY) {
+    if (!c->guess_D.p || c->guess_gen != c->basis_gen)
+      return fail(c, GBHF_ERR_BAD_INPUT, "GBHF_GUESS_DENSITY: no density set for this basis (gbhf_set_guess_density)");
+    GBHF_TRY(flat_to_square(c, n, c->guess_D.p, D));
   } else {
     GBHF_TRY(new_density(H, D));
   }
@@ -218,8 +222,10 @@ gbhf_status scf_run(gbhf_ctx* c, const gbhf_scf_opts* o, gbhf_result* r) {
   const double prim64_0 = c->prof.prim64, prim32_0 = c->prof.prim32, shq0 = c->prof.shellq, fnq0 = c->prof.fnq;
   GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
   c->prof.ph_setup += ms_since(t_phase);
+  c->scf_trace.clear();
   for (step = 0; step < o->max_iter; ++step) {
     t_phase = clk::now();
+    const auto t_step = t_phase;
     // ---- Fock matrix of the current density
     if (ref) {
       GBHF_TRY(square_to_flat(c, n, D, fD));
@@ -343,14 +349,16 @@ gbhf_status scf_run(gbhf_ctx* c, const gbhf_scf_opts* o, gbhf_result* r) {
     c->prof.ph_diag += ms_since(t_phase);
     t_phase = clk::now();
     // ---- energies and convergence
+    double rms = 0;
     if (o->ref_stop_rule) {
       GBHF_TRY(reduce_stats(c, n, nullptr, H, Fuse, Dnew, D, hstats));
       energy = hstats[1] + enuc;   // variationalE with F_DIIS and the new density
+      rms = std::sqrt(hstats[2] / (double)nn);
       converged = step != 0 && maxe < o->conv_error;
     } else {
       GBHF_TRY(reduce_stats(c, n, nullptr, H, F, Dnew, D, hstats));
       energy = hstats[3] + enuc;   // E[D] with F = F(D)
-      const double rms = std::sqrt(hstats[2] / (double)nn);
+      rms = std::sqrt(hstats[2] / (double)nn);
       // with final_fp64 the mixed phase hands over at 1e-9 Eh / 1e-7 (the FP64 full
       // builds that follow reach the requested thresholds in a few steps)
       const bool handover = o->final_fp64 && precision == GBHF_PREC_MIXED;
@@ -363,6 +371,12 @@ gbhf_status scf_run(gbhf_ctx* c, const gbhf_scf_opts* o, gbhf_result* r) {
                      precision == GBHF_PREC_FP64 ? "fp64" : "mixed", fp64_final_phase ? " final" : "");
     }
     c->prof.ph_other += ms_since(t_phase);
+    {
+      const double rec[GBHF_SCF_TRACE_FIELDS] = {
+          (double)step, energy, have_prev ? energy - e_prev : 0.0, rms, maxe, diis_on ? (double)stored.size() : 0.0,
+          fp64_final_phase ? 2.0 : (precision == GBHF_PREC_MIXED ? 1.0 : 0.0), ms_since(t_step)};
+      c->scf_trace.insert(c->scf_trace.end(), rec, rec + GBHF_SCF_TRACE_FIELDS);
+    }
     e_prev = energy;
     have_prev = true;
     GBHF_CUDA(c, cudaMemcpyAsync(D, Dnew, nn * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));

@@ -19,7 +19,7 @@ STATUS = {0: "GBHF_OK", 1: "GBHF_ERR_BAD_INPUT", 2: "GBHF_ERR_NOT_CONVERGED", 3:
           8: "GBHF_ERR_INDEX"}
 MODE_REFERENCE, MODE_EXACT = 0, 1
 PREC_FP64, PREC_MIXED = 0, 1
-GUESS_HARRIS, GUESS_CORE, GUESS_SAD = 0, 1, 2
+GUESS_HARRIS, GUESS_CORE, GUESS_SAD, GUESS_DENSITY = 0, 1, 2, 3
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
@@ -86,6 +86,8 @@ def load():
         "gbhf_eigen_solve_noalloc": (st, [C.c_int, _vp, _vp, _vp, _vp]),
         "gbhf_diagonal_hf": (st, [_vp, C.c_int, _dp, _dp, C.c_int, _dp, _dp, _dp]),
         "gbhf_sad_density": (st, [_vp, _dp]),
+        "gbhf_set_guess_density": (st, [_vp, _dp]),
+        "gbhf_scf_trace": (st, [_vp, _dp, C.c_int, _ip]),
         "gbhf_diis_error": (st, [_vp, C.c_int, _dp, _dp, _dp, _dp, _dp]),
         "gbhf_diis_extrapolate": (st, [_vp, C.c_int, C.c_int, _dp, _dp, _dp, _ip]),
         "gbhf_gauss_elem": (st, [_vp, C.c_int, _dp, _dp, _dp]),
@@ -263,6 +265,25 @@ class Context:
         d = np.zeros(self.n * (self.n + 1) // 2)
         self._check(self.L.gbhf_sad_density(self.h, _d(d)))
         return d
+
+    def set_guess_density(self, d_flat):
+        """Starting density (flat upper triangle) for an SCF with GUESS_DENSITY (restart)."""
+        d = _f64(d_flat)
+        if d.size != self.n * (self.n + 1) // 2:
+            raise ValueError("density size does not match the basis")
+        self._check(self.L.gbhf_set_guess_density(self.h, _d(d)))
+
+    TRACE_KEYS = ("step", "energy", "delta_e", "rms_delta_d", "max_diis_error", "diis_vectors", "phase", "ms")
+
+    def scf_trace(self):
+        """Per-step records of the last SCF: list of dicts (TRACE_KEYS; phase 0 FP64,
+        1 mixed, 2 FP64 after a mixed phase)."""
+        nrec = C.c_int(0)
+        self._check(self.L.gbhf_scf_trace(self.h, None, 0, C.byref(nrec)))
+        out = np.zeros(max(nrec.value, 1) * len(self.TRACE_KEYS))
+        self._check(self.L.gbhf_scf_trace(self.h, _d(out), nrec.value, C.byref(nrec)))
+        recs = out[:nrec.value * len(self.TRACE_KEYS)].reshape(-1, len(self.TRACE_KEYS))
+        return [dict(zip(self.TRACE_KEYS, r.tolist())) for r in recs]
 
     def diis_error(self, f_flat, s_flat, d_flat, x_square):
         x = _f64(x_square)

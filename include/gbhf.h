@@ -59,8 +59,9 @@ typedef enum {
 /* GBHF_GUESS_SAD (superposition of atomic densities: block-diagonal densities of
  * spherically averaged free atoms) has no counterpart in the reference, which
  * offers the Harris functional and the core Hamiltonian
- * (HartreeFock/HartreeFock.hs:128-149). */
-typedef enum { GBHF_GUESS_HARRIS = 0, GBHF_GUESS_CORE = 1, GBHF_GUESS_SAD = 2 } gbhf_guess;
+ * (HartreeFock/HartreeFock.hs:128-149).  GBHF_GUESS_DENSITY restarts from the
+ * density given to gbhf_set_guess_density (a checkpoint of an earlier SCF). */
+typedef enum { GBHF_GUESS_HARRIS = 0, GBHF_GUESS_CORE = 1, GBHF_GUESS_SAD = 2, GBHF_GUESS_DENSITY = 3 } gbhf_guess;
 
 /* SCF options.  gbhf_scf_opts_reference() fills the reference's constants
  * (HartreeFock.hs:78,81,87,113; DIIS.hs:58). */
@@ -186,6 +187,19 @@ gbhf_status gbhf_eigen_solve_noalloc(int n, const double* d_a, double* d_evals, 
  * are harrisFunctional and the core Hamiltonian, HartreeFock/HartreeFock.hs:
  * 128-149); it is the starting density of gbhf_scf with GBHF_GUESS_SAD. */
 gbhf_status gbhf_sad_density(gbhf_ctx* ctx, double* density_flat);
+
+/* Checkpoint / restart and structured logging of the SCF (the reference prints
+ * `show` dumps of its matrices every step, HartreeFock.hs:116-117, and has no
+ * restart).  gbhf_set_guess_density stores a starting density (flat upper
+ * triangle of the current basis, e.g. density_flat of an earlier gbhf_scf) for
+ * the next gbhf_scf with guess = GBHF_GUESS_DENSITY; a new basis clears it.
+ * gbhf_scf_trace copies the per-step records of the last gbhf_scf,
+ * GBHF_SCF_TRACE_FIELDS doubles each: step, energy, energy change, RMS density
+ * change, max |DIIS error|, stored DIIS vectors, phase (0 FP64, 1 mixed, 2 the
+ * FP64 phase after a mixed one), milliseconds of the step; *n_records = steps. */
+#define GBHF_SCF_TRACE_FIELDS 8
+gbhf_status gbhf_set_guess_density(gbhf_ctx* ctx, const double* density_flat);
+gbhf_status gbhf_scf_trace(gbhf_ctx* ctx, double* out, int max_records, int* n_records);
 
 /* diagonalHF (HartreeFock/HartreeFock.hs:263-273): X^T F X, eigen-solve,
  * C = X C', density P = 2 C_occ C_occ^T (calcDensity, :195-208). */

@@ -126,3 +126,30 @@ def test_sad_guess_converges_where_core_guess_does_not(ctx):
     o = O.scf(fb, O.SCFOptions.baseline(guess="sad"))
     assert r["converged"] and abs(r["energy"] - o.energy) < 1e-8
     assert r["iterations"] <= 15
+
+
+def test_restart_from_checkpoint_density_and_step_records(ctx):
+    """GBHF_GUESS_DENSITY restarts from a stored density: from the converged
+    density of an earlier run the SCF stops after two steps at the same energy.
+    The per-step records describe each run (energies, phases)."""
+    fb = B.flatten(M.cluster_atoms("batch256", "6-31g", index=7))
+    ctx.set_basis(fb)
+    r = ctx.scf(_lib.baseline_opts(guess=_lib.GUESS_SAD))
+    tr = ctx.scf_trace()
+    assert len(tr) == r["iterations"]
+    assert [t["step"] for t in tr] == list(range(len(tr)))
+    assert abs(tr[-1]["energy"] - r["energy"]) < 1e-12
+    assert all(t["phase"] == 0 for t in tr) and all(t["ms"] > 0 for t in tr)
+    assert tr[-1]["rms_delta_d"] < 1e-8 and abs(tr[-1]["delta_e"]) < 1e-10
+    ctx.set_guess_density(r["density"])
+    r2 = ctx.scf(_lib.baseline_opts(guess=_lib.GUESS_DENSITY))
+    assert r2["iterations"] <= 2 and abs(r2["energy"] - r["energy"]) < 1e-9
+    # mixed precision with the FP64 final phase: phases 1 then 2 in the records
+    ctx.scf(_lib.baseline_opts(precision=_lib.PREC_MIXED, incremental=1, final_fp64=1), want_matrices=False)
+    ph = [t["phase"] for t in ctx.scf_trace()]
+    assert ph[0] == 1 and ph[-1] == 2 and sorted(ph) == ph
+    # a new basis drops the stored density
+    ctx.set_basis(B.flatten(M.water_atoms("sto-3g", "text")))
+    with pytest.raises(_lib.GBHFError) as e:
+        ctx.scf(_lib.baseline_opts(guess=_lib.GUESS_DENSITY))
+    assert e.value.name == "GBHF_ERR_BAD_INPUT"
