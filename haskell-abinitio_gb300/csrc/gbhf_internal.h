@@ -302,6 +302,7 @@ struct gbhf_ctx {
   gbhf_ctx* sad_ctx = nullptr;
   gbhf::DBuf<float> dfloat;
   gbhf::DBuf<int> dev_status;
+  int purify_grid = 0;              // co-resident blocks of the fused purification kernel
   gbhf::DBuf<unsigned> barrier;
   gbhf::DBuf<double> small;
   gbhf::Profile prof;

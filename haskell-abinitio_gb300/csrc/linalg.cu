@@ -99,16 +99,21 @@ __global__ void __launch_bounds__(128) k_dgemm(bool ta, bool tb, int m, int n, i
 // added to its mirror position as well.
 constexpr int ST = 32, SK = 16;
 
-__global__ void __launch_bounds__(128) k_dgemm_split(bool ta, bool tb, bool sym, int m, int n, int k, int kslice,
-                                                     double alpha, const double* __restrict__ A, int lda,
-                                                     const double* __restrict__ B, int ldb, double* __restrict__ C,
-                                                     int ldc) {
-  if (sym && blockIdx.y > blockIdx.x) return;   // mirrored from tile (x, y)
-  __shared__ double As[ST][SK + 1];
-  __shared__ double Bs[SK][ST + 2];
+struct SplitSmem {
+  double As[ST][SK + 1];
+  double Bs[SK][ST + 2];
+};
+
+// One 32 x 32 tile (row tile rt, column tile ct) of C += alpha op(A) op(B) over
+// k in [k0, k1), added with FP64 atomics; sym: also added at the mirror tile
+// (rt < ct); trace (nullable): the tile's diagonal entries summed into *trace.
+// Called by every thread of a 128-thread block.
+__device__ __forceinline__ void dgemm_tile(bool ta, bool tb, bool sym, int m, int n, int rt, int ct, int k0, int k1,
+                                           double alpha, const double* __restrict__ A, int lda,
+                                           const double* __restrict__ B, int ldb, double* __restrict__ C, int ldc,
+                                           double* trace, SplitSmem& sm) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int row0 = blockIdx.y * ST, col0 = blockIdx.x * ST;
-  const int k0 = blockIdx.z * kslice, k1 = min(k, k0 + kslice);
+  const int row0 = rt * ST, col0 = ct * ST;
   const int wr = (warp >> 1) * 16, wc = (warp & 1) * 16;
   double acc[2][2][2] = {};
   for (int kk = k0; kk < k1; kk += SK) {
@@ -124,7 +129,7 @@ __global__ void __launch_bounds__(128) k_dgemm_split(bool ta, bool tb, bool sym,
       const int gr = row0 + r, gk = kk + cc;
       double v = 0.0;
       if (gr < m && gk < k1) v = ta ? A[(long)gk * lda + gr] : A[(long)gr * lda + gk];
-      As[r][cc] = v;
+      sm.As[r][cc] = v;
     }
     for (int idx = tid; idx < SK * ST; idx += 128) {
       int r, cc;
@@ -138,16 +143,16 @@ __global__ void __launch_bounds__(128) k_dgemm_split(bool ta, bool tb, bool sym,
       const int gk = kk + r, gc = col0 + cc;
       double v = 0.0;
       if (gk < k1 && gc < n) v = tb ? B[(long)gc * ldb + gk] : B[(long)gk * ldb + gc];
-      Bs[r][cc] = v;
+      sm.Bs[r][cc] = v;
     }
     __syncthreads();
 #pragma unroll
     for (int k4 = 0; k4 < SK; k4 += 4) {
       double af[2], bf[2];
 #pragma unroll
-      for (int i = 0; i < 2; ++i) af[i] = As[wr + i * 8 + (lane >> 2)][k4 + (lane & 3)];
+      for (int i = 0; i < 2; ++i) af[i] = sm.As[wr + i * 8 + (lane >> 2)][k4 + (lane & 3)];
 #pragma unroll
-      for (int j = 0; j < 2; ++j) bf[j] = Bs[k4 + (lane & 3)][wc + j * 8 + (lane >> 2)];
+      for (int j = 0; j < 2; ++j) bf[j] = sm.Bs[k4 + (lane & 3)][wc + j * 8 + (lane >> 2)];
 #pragma unroll
       for (int i = 0; i < 2; ++i)
 #pragma unroll
@@ -164,10 +169,22 @@ __global__ void __launch_bounds__(128) k_dgemm_split(bool ta, bool tb, bool sym,
         const int r = row0 + wr + i * 8 + (lane >> 2);
         const int cc = col0 + wc + j * 8 + 2 * (lane & 3) + h;
         if (r < m && cc < n) {
-          atomicAdd(C + (long)r * ldc + cc, alpha * acc[i][j][h]);
-          if (sym && blockIdx.y < blockIdx.x) atomicAdd(C + (long)cc * ldc + r, alpha * acc[i][j][h]);
+          const double v = alpha * acc[i][j][h];
+          atomicAdd(C + (long)r * ldc + cc, v);
+          if (sym && rt < ct) atomicAdd(C + (long)cc * ldc + r, v);
+          if (trace && r == cc) atomicAdd(trace, v);
         }
       }
+}
+
+__global__ void __launch_bounds__(128) k_dgemm_split(bool ta, bool tb, bool sym, int m, int n, int k, int kslice,
+                                                     double alpha, const double* __restrict__ A, int lda,
+                                                     const double* __restrict__ B, int ldb, double* __restrict__ C,
+                                                     int ldc) {
+  if (sym && blockIdx.y > blockIdx.x) return;   // mirrored from tile (x, y)
+  __shared__ SplitSmem sm;
+  const int k0 = blockIdx.z * kslice, k1 = min(k, k0 + kslice);
+  dgemm_tile(ta, tb, sym, m, n, blockIdx.y, blockIdx.x, k0, k1, alpha, A, lda, B, ldb, C, ldc, nullptr, sm);
 }
 
 __global__ void k_scale_matrix(int m, int n, double beta, double* __restrict__ C, int ldc) {
@@ -798,6 +815,114 @@ __global__ void k_purify_coef(int n, const double* __restrict__ P, const double*
   }
 }
 
+// The whole purification in one cooperative launch: per step the symmetric
+// products P2 = P P and P3 = P P2 are shared out as (upper tile, k slice) items
+// with atomic accumulation, their traces summed in the tile epilogues; then
+// every block derives the step's coefficients from the same three traces (so
+// all blocks take the same decision to stop) and updates its share of P while
+// clearing P2 and P3 for the next step.  Three bounded grid barriers per step.
+// Trace slots tr[3 * parity + {0, 1, 2}] (tr P, tr P2, tr P3) alternate between
+// steps; P2, P3 and tr must be zero at launch.
+struct PurifyArgs {
+  int n, ne, nt, ks, kslice, max_steps;
+  double tol;
+  double *P, *P2, *P3, *tr, *out;   // out: [0] last tr(P - P^2), [1] steps
+  unsigned* bar;
+  int* status;
+};
+
+__global__ void __launch_bounds__(128) k_purify_fused(PurifyArgs a) {
+  __shared__ SplitSmem sm;
+  __shared__ double s_red[4];
+  const int n = a.n;
+  const long nn = (long)n * n;
+  const int ntile = a.nt * (a.nt + 1) / 2, items = ntile * a.ks;
+  const long gt = blockIdx.x * (long)blockDim.x + threadIdx.x, gs = (long)gridDim.x * blockDim.x;
+  unsigned* cnt = a.bar;
+  unsigned* gen = a.bar + 1;
+  auto block_sum_add = [&](double v, double* dst) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      const double t = s_red[0] + s_red[1] + s_red[2] + s_red[3];
+      if (t != 0.0) atomicAdd(dst, t);
+    }
+    __syncthreads();
+  };
+  // upper-triangle tile index -> (row tile, column tile)
+  auto tile_of = [&](int t, int& rt, int& ct) {
+    rt = 0;
+    while (t >= a.nt - rt) {
+      t -= a.nt - rt;
+      ++rt;
+    }
+    ct = rt + t;
+  };
+  {
+    double v = 0;
+    for (long i = gt; i < n; i += gs) v += a.P[i * n + i];
+    block_sum_add(v, a.tr);
+  }
+  if (!grid_barrier(cnt, gen, a.status)) return;
+  int step = 0;
+  for (; step < a.max_steps; ++step) {
+    double* trp = a.tr + 3 * (step & 1);
+    double* trq = a.tr + 3 * ((step + 1) & 1);
+    if (gt == 0) {   // the other parity: read last in the previous step's coefficients
+      trq[0] = 0.0;
+      trq[1] = 0.0;
+      trq[2] = 0.0;
+    }
+    for (int it = blockIdx.x; it < items; it += gridDim.x) {
+      int rt, ct;
+      tile_of(it / a.ks, rt, ct);
+      const int k0 = (it % a.ks) * a.kslice, k1 = min(n, k0 + a.kslice);
+      dgemm_tile(false, false, true, n, n, rt, ct, k0, k1, 1.0, a.P, n, a.P, n, a.P2, n, trp + 1, sm);
+    }
+    if (!grid_barrier(cnt, gen, a.status)) return;
+    for (int it = blockIdx.x; it < items; it += gridDim.x) {
+      int rt, ct;
+      tile_of(it / a.ks, rt, ct);
+      const int k0 = (it % a.ks) * a.kslice, k1 = min(n, k0 + a.kslice);
+      dgemm_tile(false, false, true, n, n, rt, ct, k0, k1, 1.0, a.P, n, a.P2, n, a.P3, n, trp + 2, sm);
+    }
+    if (!grid_barrier(cnt, gen, a.status)) return;
+    const double t1 = *((volatile double*)trp), t2 = *((volatile double*)(trp + 1)),
+                 t3 = *((volatile double*)(trp + 2));
+    const double den = t1 - t2, num = t2 - t3;
+    if (gt == 0) {
+      a.out[0] = den;
+      a.out[1] = step + 1;
+    }
+    if (fabs(den) < a.tol * max(1, a.ne)) break;   // the same decision in every block
+    double ca = 1, cb = 0, cd = 0;
+    if (fabs(den) > 1e-300) {
+      const double cc = num / den;
+      if (cc >= 0.5) {
+        ca = 0;
+        cb = (1 + cc) / cc;
+        cd = -1 / cc;
+      } else {
+        ca = (1 - 2 * cc) / (1 - cc);
+        cb = (1 + cc) / (1 - cc);
+        cd = -1 / (1 - cc);
+      }
+    }
+    double dsum = 0;
+    for (long e = gt; e < nn; e += gs) {
+      const double v = ca * a.P[e] + cb * a.P2[e] + cd * a.P3[e];
+      a.P[e] = v;
+      a.P2[e] = 0.0;
+      a.P3[e] = 0.0;
+      if (e / n == e % n) dsum += v;
+    }
+    block_sum_add(dsum, trq);
+    if (!grid_barrier(cnt, gen, a.status)) return;
+  }
+}
+
 // Canonical purification (Palser & Manolopoulos, Phys. Rev. B 58, 12704 (1998)):
 // the spectral projector onto the ne lowest eigenvectors of the symmetric F,
 // by trace-conserving cubic polynomials of P, two GEMMs per step.  Returns the
@@ -805,35 +930,56 @@ __global__ void k_purify_coef(int n, const double* __restrict__ P, const double*
 gbhf_status purify(gbhf_ctx* c, int n, int ne, const double* d_F, double* d_P, double* err_out) {
   const size_t nn = (size_t)n * n;
   GBHF_WS(c, P2, 23, nn);
-  double* P3 = c->jac.t1.p;
   GBHF_CUDA(c, c->jac.t1.alloc(nn));
-  P3 = c->jac.t1.p;
+  double* P3 = c->jac.t1.p;
   GBHF_CUDA(c, c->small.alloc(64));
   double* g = c->small.p + 32;
-  double* coef = c->small.p + 40;
+  double* tr = c->small.p + 40;   // 6 trace slots
+  double* out = c->small.p + 48;
+  GBHF_CUDA(c, c->jac.bar.alloc(2));
+  GBHF_CUDA(c, c->dev_status.alloc(1));
   k_gershgorin<<<1, 1024, 0, c->stream>>>(n, d_F, g);
   k_purify_init<<<dim3((n + 127) / 128, n), 128, 0, c->stream>>>(n, ne, d_F, g, d_P);
   count_launch(c, 2);
-  double err = 1.0;
-  // four purification steps per CUDA-graph replay, convergence read between replays
-  auto four_steps = [&]() -> gbhf_status {
-    for (int k = 0; k < 4; ++k) {
-      GBHF_TRY(gemm(c, false, false, n, n, n, 1.0, d_P, n, d_P, n, 0.0, P2, n, true));
-      GBHF_TRY(gemm(c, false, false, n, n, n, 1.0, d_P, n, P2, n, 0.0, P3, n, true));
-      k_purify_coef<<<1, 1024, 0, c->stream>>>(n, d_P, P2, P3, coef);
-      count_launch(c);
-      const double* mats[3] = {d_P, P2, P3};
-      GBHF_TRY(lincomb(c, (int)nn, 3, mats, coef, d_P));
-    }
-    return GBHF_OK;
-  };
-  const std::vector<const void*> key = {(const void*)(size_t)n, d_P, P2, P3, coef};
-  for (int rep = 0; rep < 50; ++rep) {
-    GBHF_TRY(graph_run(c, c->g_purify, key, four_steps));
-    GBHF_CUDA(c, cudaMemcpyAsync(&err, coef + 3, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
-    GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
-    if (std::fabs(err) < 1e-13 * std::max(1, ne)) break;   // E[D] is first order in the idempotency error
+  GBHF_CUDA(c, cudaMemsetAsync(P2, 0, nn * sizeof(double), c->stream));
+  GBHF_CUDA(c, cudaMemsetAsync(P3, 0, nn * sizeof(double), c->stream));
+  GBHF_CUDA(c, cudaMemsetAsync(tr, 0, 16 * sizeof(double), c->stream));
+  GBHF_CUDA(c, cudaMemsetAsync(c->jac.bar.p, 0, 2 * sizeof(unsigned), c->stream));
+  GBHF_CUDA(c, cudaMemsetAsync(c->dev_status.p, 0, sizeof(int), c->stream));
+  PurifyArgs a;
+  a.n = n;
+  a.ne = ne;
+  a.nt = (n + ST - 1) / ST;
+  const int ntile = a.nt * (a.nt + 1) / 2;
+  // k slices: about one item per SM, at least two k-steps per slice
+  int ks = std::max(1, std::min((c->nsm + ntile - 1) / ntile, (n + 2 * SK - 1) / (2 * SK)));
+  a.kslice = ((n + ks - 1) / ks + SK - 1) / SK * SK;
+  a.ks = (n + a.kslice - 1) / a.kslice;
+  a.max_steps = 200;
+  a.tol = 1e-13;   // E[D] is first order in the idempotency error
+  a.P = d_P;
+  a.P2 = P2;
+  a.P3 = P3;
+  a.tr = tr;
+  a.out = out;
+  a.bar = c->jac.bar.p;
+  a.status = c->dev_status.p;
+  if (c->purify_grid == 0) {
+    int per_sm = 0;
+    GBHF_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_purify_fused, 128, 0));
+    c->purify_grid = std::max(1, c->nsm * std::max(per_sm, 1));
   }
+  const int grid = std::max(1, std::min(c->purify_grid, ntile * a.ks));
+  void* args[] = {&a};
+  GBHF_CUDA(c, cudaLaunchCooperativeKernel((void*)k_purify_fused, dim3(grid), dim3(128), args, 0, c->stream));
+  count_launch(c);
+  double hout[2] = {1.0, 0.0};
+  int st = 0;
+  GBHF_CUDA(c, cudaMemcpyAsync(hout, out, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  GBHF_CUDA(c, cudaMemcpyAsync(&st, c->dev_status.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (st & GBHF_DEV_ERR_TIMEOUT) return fail(c, GBHF_ERR_DEVICE_TIMEOUT, "purification grid barrier timed out");
+  const double err = hout[0];
   if (err_out) *err_out = err;
   if (!(std::fabs(err) < 1e-6 * std::max(1, ne)))
     return fail(c, GBHF_ERR_NOT_CONVERGED, "density purification did not converge");
