@@ -26,8 +26,9 @@ import struct
 import sys
 from pathlib import Path
 
-ELEMENTS = ("H", "He", "C", "N", "O")
-BASES = {"sto-3g": "sto-3g", "6-31g": "6-31g", "6-31g*": "6-31gs"}
+ELEMENTS = ("H", "He", "Li", "Be", "B", "C", "N", "O", "F", "Ne")
+BASES = {"sto-3g": "sto-3g", "3-21g": "3-21g", "6-31g": "6-31g", "6-31g*": "6-31gs", "6-31g**": "6-31gss",
+         "6-31++g*": "6-31mmgs"}
 TAGS = {0: "S", 1: "SP", 2: "P", 3: "D"}
 
 

@@ -135,3 +135,42 @@ def batch_workload(variant="text"):
 
 if __name__ == "__main__":
     print(write_cluster_file())
+
+
+def _small_geometries():
+    """Small molecules over the elements of the basis data (H-Ne), bohr;
+    approximate experimental bond lengths, charge of the molecule."""
+    s3 = math.sqrt(3.0)
+    r_nh, a_nh = 1.913, math.radians(106.7)
+    # NH3: N on the axis, the three H on a cone (H-N-H angle a_nh)
+    hx = r_nh * math.sqrt(2 * (1 - math.cos(a_nh)) / 3)
+    hz = -math.sqrt(r_nh ** 2 - hx ** 2)
+    nh3 = [("N", (0.0, 0.0, 0.0))] + [("H", (hx * math.cos(t), hx * math.sin(t), hz))
+                                      for t in (0.0, 2 * math.pi / 3, 4 * math.pi / 3)]
+    r_ch = 2.052 / s3
+    ch4 = [("C", (0.0, 0.0, 0.0)), ("H", (r_ch, r_ch, r_ch)), ("H", (-r_ch, -r_ch, r_ch)),
+           ("H", (-r_ch, r_ch, -r_ch)), ("H", (r_ch, -r_ch, -r_ch))]
+    r_bh = 2.25
+    bh3 = [("B", (0.0, 0.0, 0.0))] + [("H", (r_bh * math.cos(t), r_bh * math.sin(t), 0.0))
+                                      for t in (0.0, 2 * math.pi / 3, 4 * math.pi / 3)]
+    return {
+        "CO": ([("C", (0.0, 0.0, 0.0)), ("O", (0.0, 0.0, 2.132))], 0.0),
+        "HF": ([("F", (0.0, 0.0, 0.0)), ("H", (0.0, 0.0, 1.733))], 0.0),
+        "NH3": (nh3, 0.0),
+        "CH4": (ch4, 0.0),
+        "BH3": (bh3, 0.0),
+        "LiH": ([("Li", (0.0, 0.0, 0.0)), ("H", (0.0, 0.0, 3.015))], 0.0),
+        "BeH2": ([("Be", (0.0, 0.0, 0.0)), ("H", (0.0, 0.0, 2.54)), ("H", (0.0, 0.0, -2.54))], 0.0),
+        "Ne": ([("Ne", (0.0, 0.0, 0.0))], 0.0),
+        "HHe+": ([("H", (0.0, 0.0, 0.0)), ("He", (0.0, 0.0, 1.4632))], 1.0),
+    }
+
+
+def small_molecule(name, basis="sto-3g", variant="text"):
+    """(atoms, charge) of one of the small test molecules (``_small_geometries``)."""
+    geo, charge = _small_geometries()[name]
+    labels = [l for l, _ in geo]
+    return make_atoms(labels, [xyz for _, xyz in geo], basis, variant), charge
+
+
+SMALL_MOLECULES = ("CO", "HF", "NH3", "CH4", "BH3", "LiH", "BeH2", "Ne", "HHe+")
