@@ -438,6 +438,13 @@ gbhf_status gbhf_scf(gbhf_ctx* c, const gbhf_scf_opts* opts, gbhf_result* result
   return scf_run(c, opts, result);
 }
 
+gbhf_status gbhf_scf_uhf(gbhf_ctx* c, const gbhf_scf_opts* opts, int multiplicity, gbhf_uhf_result* result) {
+  CTX_CHECK(c);
+  if (!opts) return fail(c, GBHF_ERR_BAD_INPUT, "null options");
+  if (!need_basis(c)) return GBHF_ERR_BAD_INPUT;
+  return uhf_run(c, opts, multiplicity, result);
+}
+
 gbhf_status gbhf_gradient(gbhf_ctx* c, int precision, double schwarz_cutoff, const double* d_flat,
                           const double* w_flat, double* grad) {
   CTX_CHECK(c);

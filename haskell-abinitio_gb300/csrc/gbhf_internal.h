@@ -414,8 +414,9 @@ gbhf_status boys_ref_grid_dev(gbhf_ctx* c, double* d_grid);
 // density change); otherwise a uniform weight `weight`.
 gbhf_status ensure_shell_arrays(gbhf_ctx* c);
 gbhf_status build_grad_tasks(gbhf_ctx* c, const double* d_D, double cutoff, double mixed_cutoff, int precision);
+// with_j = false: exchange only, G = -K(D)/2 (the open-shell spin-density term).
 gbhf_status jk_build(gbhf_ctx* c, const double* d_Dsq, double* d_G, int precision, double schwarz,
-                     double mixed_cutoff, double weight, bool local_weights = false);
+                     double mixed_cutoff, double weight, bool local_weights = false, bool with_j = true);
 // Q of every pair in [cls_start[cl], cls_start[cl+1]) (pairs grouped by class,
 // bra-layout primitive data at d_poff), FP64 class code.
 gbhf_status schwarz_classes_dev(gbhf_ctx* c, const int* cls_start, const int* d_K, const int* d_poff,
@@ -426,7 +427,7 @@ gbhf_status schwarz_dclasses_dev(gbhf_ctx* c, const int* cls_start, const int* d
                                  const int* d_poff, const double* d_bra, long long npp, double* d_Q);
 // J/K launch of combo 6..20 (COMBO_BRA/COMBO_KET), precision 0 = FP64, 1 = FP32.
 gbhf_status launch_jk_dclass(gbhf_ctx* c, cudaStream_t strm, int combo, int prec, const double* D64,
-                             const float* D32, double* G, int ntask);
+                             const float* D32, double* G, int ntask, int with_j);
 // Gradient combos on the generated lane-per-ket kernels (grad.cu); the rest
 // go to launch_grad_dclass.
 bool grad_gen_combo(int k);
@@ -453,6 +454,7 @@ gbhf_status diis_error_dev(gbhf_ctx* c, int n, const double* d_F, const double* 
 gbhf_status gauss_elem_dev_call(gbhf_ctx* c, int m, const double* h_a, const double* h_b, double* h_x, bool* ok);
 // scf.cu
 gbhf_status scf_run(gbhf_ctx* c, const gbhf_scf_opts* o, gbhf_result* r);
+gbhf_status uhf_run(gbhf_ctx* c, const gbhf_scf_opts* o, int multiplicity, gbhf_uhf_result* r);   // uhf.cu
 // bscf.cu: the SCFs of every molecule of the context's basis (batched);
 // energies / iterations / converged per molecule, grads 3 x total atoms (or nullptr)
 gbhf_status bscf_run(gbhf_ctx* c, const gbhf_scf_opts* o, double* energies, int* iterations, int* converged,

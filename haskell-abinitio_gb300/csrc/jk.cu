@@ -78,6 +78,7 @@ struct JKArgs {
   const T* boys;
   unsigned long long* stats;   // [shell quartets, fn quartets, prim quartets]
   const double* sscale;        // per shell 6 component scales (d shells)
+  int with_j;                  // 0: exchange only (the open-shell spin-density build)
 };
 
 template <int LA, int LB, int LC, int LD>
@@ -242,22 +243,26 @@ __global__ void __launch_bounds__(JK_THREADS) k_jk(JKArgs<T> a) {
 #pragma unroll
       for (int id = 0; id < ND; ++id) dcd[ic * ND + id] = lead ? Dm[(long long)(c0 + ic) * n + d0 + id] : T(0);
     // J_ab (warp reduce over kets)
+    if (a.with_j) {
 #pragma unroll
-    for (int ab = 0; ab < NAB; ++ab) {
-      T v = 0;
+      for (int ab = 0; ab < NAB; ++ab) {
+        T v = 0;
 #pragma unroll
-      for (int cd = 0; cd < NCD; ++cd) v = fma_t(acc.get(ab * NCD + cd), dcd[cd], v);
-      v = warp_sum(T(2) * s * v);   // s depends on the lane's ket: apply before the reduction
-      if (lane == 0) atomicAdd(&Gm[(long long)(a0 + ab / NB) * n + b0 + ab % NB], widen(v));
+        for (int cd = 0; cd < NCD; ++cd) v = fma_t(acc.get(ab * NCD + cd), dcd[cd], v);
+        v = warp_sum(T(2) * s * v);   // s depends on the lane's ket: apply before the reduction
+        if (lane == 0) atomicAdd(&Gm[(long long)(a0 + ab / NB) * n + b0 + ab % NB], widen(v));
+      }
     }
     if (lead) {
       // J_cd
+      if (a.with_j) {
 #pragma unroll
-      for (int cd = 0; cd < NCD; ++cd) {
-        T v = 0;
+        for (int cd = 0; cd < NCD; ++cd) {
+          T v = 0;
 #pragma unroll
-        for (int ab = 0; ab < NAB; ++ab) v = fma_t(acc.get(ab * NCD + cd), sDab[warp][ab], v);
-        atomicAdd(&Gm[(long long)(c0 + cd / ND) * n + d0 + cd % ND], widen(T(2) * s * v));
+          for (int ab = 0; ab < NAB; ++ab) v = fma_t(acc.get(ab * NCD + cd), sDab[warp][ab], v);
+          atomicAdd(&Gm[(long long)(c0 + cd / ND) * n + d0 + cd % ND], widen(T(2) * s * v));
+        }
       }
       const T ks = T(-0.5) * s;
       // K_ac -= sum_bd v D_bd ; K_ad -= sum_bc v D_bc
@@ -768,7 +773,7 @@ gbhf_status build_grad_tasks(gbhf_ctx* c, const double* d_D, double cutoff, doub
 
 template <int LA, int LB, int LC, int LD, typename T, bool SACC>
 static gbhf_status launch_class(gbhf_ctx* c, cudaStream_t strm, int combo, int prec, const T* D, double* G,
-                                const T* bra, const T* ket, const T* boys, const int* f0, int ntask) {
+                                const T* bra, const T* ket, const T* boys, const int* f0, int ntask, int with_j) {
   if (ntask <= 0) return GBHF_OK;
   constexpr int NOUT = ncart_c(LA) * ncart_c(LB) * ncart_c(LC) * ncart_c(LD);
   const size_t smem = SACC ? (size_t)NOUT * JK_THREADS * sizeof(double) : 0;
@@ -805,6 +810,7 @@ static gbhf_status launch_class(gbhf_ctx* c, cudaStream_t strm, int combo, int p
   a.boys = boys;
   a.stats = c->tasks.stats.p + 3 * (2 * combo + prec);
   a.sscale = c->tasks.sscale.p;
+  a.with_j = with_j;
   kern<<<grid, JK_THREADS, smem, strm>>>(a);
   count_launch(c);
   GBHF_CUDA(c, cudaGetLastError());
@@ -816,7 +822,8 @@ static gbhf_status launch_class(gbhf_ctx* c, cudaStream_t strm, int combo, int p
 static bool gen_dclass(int k) { return (k >= 6 && k <= 11) || k == 15; }
 
 gbhf_status jk_build(gbhf_ctx* c, const double* d_Dsq, double* d_G, int precision, double schwarz,
-                     double mixed_cutoff, double weight, bool local_weights) {
+                     double mixed_cutoff, double weight, bool local_weights, bool with_j) {
+  const int wj = with_j ? 1 : 0;
   GBHF_TRY(ensure_pairs(c));
   const int n = c->basis.nbf;
   TaskLists& st = c->tasks;
@@ -879,38 +886,38 @@ gbhf_status jk_build(gbhf_ctx* c, const double* d_Dsq, double* d_G, int precisio
       cudaStream_t strm = ev ? c->stream : c->side[nl % gbhf_ctx::NSIDE];
       ++nl;
       if (k >= NCOMBO_SP && !gen_dclass(k)) {
-        s = launch_jk_dclass(c, strm, k, prec, D64, D32, d_G, nt[k][prec]);
+        s = launch_jk_dclass(c, strm, k, prec, D64, D32, d_G, nt[k][prec], wj);
       } else if (prec == 0) {
         switch (k) {
-          case 6: s = launch_class<2, 0, 0, 0, double, false>(c, strm, 6, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boysh64.p, f0, nt[6][0]); break;
-          case 7: s = launch_class<2, 0, 1, 0, double, false>(c, strm, 7, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boysh64.p, f0, nt[7][0]); break;
-          case 8: s = launch_class<2, 0, 1, 1, double, true>(c, strm, 8, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boysh64.p, f0, nt[8][0]); break;
-          case 9: s = launch_class<2, 0, 2, 0, double, true>(c, strm, 9, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boysh64.p, f0, nt[9][0]); break;
-          case 10: s = launch_class<2, 1, 0, 0, double, false>(c, strm, 10, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boysh64.p, f0, nt[10][0]); break;
-          case 11: s = launch_class<2, 1, 1, 0, double, true>(c, strm, 11, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boysh64.p, f0, nt[11][0]); break;
-          case 15: s = launch_class<2, 2, 0, 0, double, true>(c, strm, 15, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boysh64.p, f0, nt[15][0]); break;
-          case 5: s = launch_class<1, 1, 1, 1, double, true>(c, strm, 5, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boysh64.p, f0, nt[5][0]); break;
-          case 4: s = launch_class<1, 1, 1, 0, double, false>(c, strm, 4, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boysh64.p, f0, nt[4][0]); break;
-          case 3: s = launch_class<1, 1, 0, 0, double, false>(c, strm, 3, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boysh64.p, f0, nt[3][0]); break;
-          case 2: s = launch_class<1, 0, 1, 0, double, false>(c, strm, 2, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boysh64.p, f0, nt[2][0]); break;
-          case 1: s = launch_class<1, 0, 0, 0, double, false>(c, strm, 1, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boysh64.p, f0, nt[1][0]); break;
-          default: s = launch_class<0, 0, 0, 0, double, false>(c, strm, 0, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boysh64.p, f0, nt[0][0]); break;
+          case 6: s = launch_class<2, 0, 0, 0, double, false>(c, strm, 6, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boysh64.p, f0, nt[6][0], wj); break;
+          case 7: s = launch_class<2, 0, 1, 0, double, false>(c, strm, 7, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boysh64.p, f0, nt[7][0], wj); break;
+          case 8: s = launch_class<2, 0, 1, 1, double, true>(c, strm, 8, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boysh64.p, f0, nt[8][0], wj); break;
+          case 9: s = launch_class<2, 0, 2, 0, double, true>(c, strm, 9, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boysh64.p, f0, nt[9][0], wj); break;
+          case 10: s = launch_class<2, 1, 0, 0, double, false>(c, strm, 10, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boysh64.p, f0, nt[10][0], wj); break;
+          case 11: s = launch_class<2, 1, 1, 0, double, true>(c, strm, 11, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boysh64.p, f0, nt[11][0], wj); break;
+          case 15: s = launch_class<2, 2, 0, 0, double, true>(c, strm, 15, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boysh64.p, f0, nt[15][0], wj); break;
+          case 5: s = launch_class<1, 1, 1, 1, double, true>(c, strm, 5, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boysh64.p, f0, nt[5][0], wj); break;
+          case 4: s = launch_class<1, 1, 1, 0, double, false>(c, strm, 4, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boysh64.p, f0, nt[4][0], wj); break;
+          case 3: s = launch_class<1, 1, 0, 0, double, false>(c, strm, 3, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boysh64.p, f0, nt[3][0], wj); break;
+          case 2: s = launch_class<1, 0, 1, 0, double, false>(c, strm, 2, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boysh64.p, f0, nt[2][0], wj); break;
+          case 1: s = launch_class<1, 0, 0, 0, double, false>(c, strm, 1, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boysh64.p, f0, nt[1][0], wj); break;
+          default: s = launch_class<0, 0, 0, 0, double, false>(c, strm, 0, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boysh64.p, f0, nt[0][0], wj); break;
         }
       } else {
         switch (k) {
-          case 6: s = launch_class<2, 0, 0, 0, float, false>(c, strm, 6, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boysh32.p, f0, nt[6][1]); break;
-          case 7: s = launch_class<2, 0, 1, 0, float, false>(c, strm, 7, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boysh32.p, f0, nt[7][1]); break;
-          case 8: s = launch_class<2, 0, 1, 1, float, false>(c, strm, 8, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boysh32.p, f0, nt[8][1]); break;
-          case 9: s = launch_class<2, 0, 2, 0, float, false>(c, strm, 9, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boysh32.p, f0, nt[9][1]); break;
-          case 10: s = launch_class<2, 1, 0, 0, float, false>(c, strm, 10, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boysh32.p, f0, nt[10][1]); break;
-          case 11: s = launch_class<2, 1, 1, 0, float, false>(c, strm, 11, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boysh32.p, f0, nt[11][1]); break;
-          case 15: s = launch_class<2, 2, 0, 0, float, false>(c, strm, 15, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boysh32.p, f0, nt[15][1]); break;
-          case 5: s = launch_class<1, 1, 1, 1, float, false>(c, strm, 5, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boysh32.p, f0, nt[5][1]); break;
-          case 4: s = launch_class<1, 1, 1, 0, float, false>(c, strm, 4, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boysh32.p, f0, nt[4][1]); break;
-          case 3: s = launch_class<1, 1, 0, 0, float, false>(c, strm, 3, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boysh32.p, f0, nt[3][1]); break;
-          case 2: s = launch_class<1, 0, 1, 0, float, false>(c, strm, 2, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boysh32.p, f0, nt[2][1]); break;
-          case 1: s = launch_class<1, 0, 0, 0, float, false>(c, strm, 1, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boysh32.p, f0, nt[1][1]); break;
-          default: s = launch_class<0, 0, 0, 0, float, false>(c, strm, 0, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boysh32.p, f0, nt[0][1]); break;
+          case 6: s = launch_class<2, 0, 0, 0, float, false>(c, strm, 6, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boysh32.p, f0, nt[6][1], wj); break;
+          case 7: s = launch_class<2, 0, 1, 0, float, false>(c, strm, 7, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boysh32.p, f0, nt[7][1], wj); break;
+          case 8: s = launch_class<2, 0, 1, 1, float, false>(c, strm, 8, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boysh32.p, f0, nt[8][1], wj); break;
+          case 9: s = launch_class<2, 0, 2, 0, float, false>(c, strm, 9, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boysh32.p, f0, nt[9][1], wj); break;
+          case 10: s = launch_class<2, 1, 0, 0, float, false>(c, strm, 10, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boysh32.p, f0, nt[10][1], wj); break;
+          case 11: s = launch_class<2, 1, 1, 0, float, false>(c, strm, 11, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boysh32.p, f0, nt[11][1], wj); break;
+          case 15: s = launch_class<2, 2, 0, 0, float, false>(c, strm, 15, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boysh32.p, f0, nt[15][1], wj); break;
+          case 5: s = launch_class<1, 1, 1, 1, float, false>(c, strm, 5, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boysh32.p, f0, nt[5][1], wj); break;
+          case 4: s = launch_class<1, 1, 1, 0, float, false>(c, strm, 4, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boysh32.p, f0, nt[4][1], wj); break;
+          case 3: s = launch_class<1, 1, 0, 0, float, false>(c, strm, 3, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boysh32.p, f0, nt[3][1], wj); break;
+          case 2: s = launch_class<1, 0, 1, 0, float, false>(c, strm, 2, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boysh32.p, f0, nt[2][1], wj); break;
+          case 1: s = launch_class<1, 0, 0, 0, float, false>(c, strm, 1, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boysh32.p, f0, nt[1][1], wj); break;
+          default: s = launch_class<0, 0, 0, 0, float, false>(c, strm, 0, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boysh32.p, f0, nt[0][1], wj); break;
         }
       }
       if (s != GBHF_OK) return s;

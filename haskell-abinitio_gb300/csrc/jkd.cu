@@ -39,6 +39,7 @@ struct JKDArgs {
   double* G;
   const T* boys;
   unsigned long long* stats;
+  int with_j;             // 0: exchange only
 };
 
 template <int LA, int LB, int LC, int LD, typename T>
@@ -111,7 +112,7 @@ __global__ void __launch_bounds__(JKD_THREADS) k_jkd(JKDArgs<T> a) {
         }
       }
       __syncwarp();
-      for (int ab = lane; ab < C::NAB; ab += 32) {   // J_ab += 2 sum_cd v D_cd
+      for (int ab = lane; a.with_j && ab < C::NAB; ab += 32) {   // J_ab += 2 sum_cd v D_cd
         const int ia = ab / C::NB, ibb = ab - ia * C::NB;
         T v = T(0);
         for (int cd = 0; cd < C::NCD; ++cd) {
@@ -120,7 +121,7 @@ __global__ void __launch_bounds__(JKD_THREADS) k_jkd(JKDArgs<T> a) {
         }
         atomicAdd(&Gm[(long long)(a0 + ia) * n + b0 + ibb], widen(T(2) * v));
       }
-      for (int cd = lane; cd < C::NCD; cd += 32) {   // J_cd += 2 sum_ab v D_ab
+      for (int cd = lane; a.with_j && cd < C::NCD; cd += 32) {   // J_cd += 2 sum_ab v D_ab
         const int ic = cd / C::ND, id = cd - ic * C::ND;
         T v = T(0);
         for (int ab = 0; ab < C::NAB; ++ab) {
@@ -173,7 +174,7 @@ __global__ void __launch_bounds__(JKD_THREADS) k_jkd(JKDArgs<T> a) {
 
 template <int LA, int LB, int LC, int LD, typename T>
 static gbhf_status launch_jkd_t(gbhf_ctx* c, cudaStream_t strm, int combo, int prec, const T* D, double* G,
-                                const T* bra, const T* ket, const T* boys, int ntask) {
+                                const T* bra, const T* ket, const T* boys, int ntask, int with_j) {
   if (ntask <= 0) return GBHF_OK;
   using C = MDCfg<LA, LB, LC, LD, 0>;
   const size_t smem = TUV_BYTES + (size_t)JKD_WARPS * C::WS * sizeof(T);
@@ -209,6 +210,7 @@ static gbhf_status launch_jkd_t(gbhf_ctx* c, cudaStream_t strm, int combo, int p
   a.G = G;
   a.boys = boys;
   a.stats = c->tasks.stats.p + 3 * (2 * combo + prec);
+  a.with_j = with_j;
   kern<<<grid, JKD_THREADS, smem, strm>>>(a);
   count_launch(c);
   GBHF_CUDA(c, cudaGetLastError());
@@ -217,9 +219,9 @@ static gbhf_status launch_jkd_t(gbhf_ctx* c, cudaStream_t strm, int combo, int p
 
 template <typename T>
 static gbhf_status launch_jkd_combo(gbhf_ctx* c, cudaStream_t strm, int k, int prec, const T* D, double* G,
-                                    const T* bra, const T* ket, const T* boys, int nt) {
+                                    const T* bra, const T* ket, const T* boys, int nt, int wj) {
 #define GBHF_JKD(K, la, lb, lc, ld) \
-  case K: return launch_jkd_t<la, lb, lc, ld, T>(c, strm, k, prec, D, G, bra, ket, boys, nt);
+  case K: return launch_jkd_t<la, lb, lc, ld, T>(c, strm, k, prec, D, G, bra, ket, boys, nt, wj);
   switch (k) {   // COMBO_BRA / COMBO_KET 6..20; class 3 = ds, 4 = dp, 5 = dd
     GBHF_JKD(6, 2, 0, 0, 0)
     GBHF_JKD(7, 2, 0, 1, 0)
@@ -242,10 +244,11 @@ static gbhf_status launch_jkd_combo(gbhf_ctx* c, cudaStream_t strm, int k, int p
 }
 
 gbhf_status launch_jk_dclass(gbhf_ctx* c, cudaStream_t strm, int combo, int prec, const double* D64,
-                             const float* D32, double* G, int ntask) {
+                             const float* D32, double* G, int ntask, int with_j) {
   PairData& P = c->pairs;
-  if (prec == 0) return launch_jkd_combo<double>(c, strm, combo, 0, D64, G, P.bra64.p, P.ket64.p, c->boysh64.p, ntask);
-  return launch_jkd_combo<float>(c, strm, combo, 1, D32, G, P.bra32.p, P.ket32.p, c->boysh32.p, ntask);
+  if (prec == 0)
+    return launch_jkd_combo<double>(c, strm, combo, 0, D64, G, P.bra64.p, P.ket64.p, c->boysh64.p, ntask, with_j);
+  return launch_jkd_combo<float>(c, strm, combo, 1, D32, G, P.bra32.p, P.ket32.p, c->boysh32.p, ntask, with_j);
 }
 
 // --------------------------------------------------------- Schwarz bounds ----

@@ -46,6 +46,12 @@ class SCFOpts(C.Structure):
                 ("grad_mixed_cutoff", C.c_double)]
 
 
+class UHFResultC(C.Structure):
+    _fields_ = [("energy", C.c_double), ("iterations", C.c_int), ("converged", C.c_int), ("n_alpha", C.c_int),
+                ("n_beta", C.c_int), ("s2", C.c_double), ("density_alpha_flat", _dp), ("density_beta_flat", _dp),
+                ("orb_energies_alpha", _dp), ("orb_energies_beta", _dp)]
+
+
 class SCFResultC(C.Structure):
     _fields_ = [("energy", C.c_double), ("iterations", C.c_int), ("converged", C.c_int),
                 ("n_occupied", C.c_int), ("nuclear_repulsion", C.c_double), ("fock_flat", _dp),
@@ -87,6 +93,7 @@ def load():
         "gbhf_diagonal_hf": (st, [_vp, C.c_int, _dp, _dp, C.c_int, _dp, _dp, _dp]),
         "gbhf_sad_density": (st, [_vp, _dp]),
         "gbhf_set_guess_density": (st, [_vp, _dp]),
+        "gbhf_scf_uhf": (st, [_vp, C.POINTER(SCFOpts), C.c_int, C.POINTER(UHFResultC)]),
         "gbhf_scf_trace": (st, [_vp, _dp, C.c_int, _ip]),
         "gbhf_diis_error": (st, [_vp, C.c_int, _dp, _dp, _dp, _dp, _dp]),
         "gbhf_diis_extrapolate": (st, [_vp, C.c_int, C.c_int, _dp, _dp, _dp, _ip]),
@@ -265,6 +272,25 @@ class Context:
         d = np.zeros(self.n * (self.n + 1) // 2)
         self._check(self.L.gbhf_sad_density(self.h, _d(d)))
         return d
+
+    def scf_uhf(self, multiplicity, opts=None, want_matrices=True):
+        """Unrestricted SCF of the current basis for ``multiplicity`` (2S+1)."""
+        opts = opts or baseline_opts()
+        res = UHFResultC()
+        keep = []
+        if want_matrices:
+            da, db = np.zeros(self.ntri), np.zeros(self.ntri)
+            ea, eb = np.zeros(self.n), np.zeros(self.n)
+            res.density_alpha_flat, res.density_beta_flat = _d(da), _d(db)
+            res.orb_energies_alpha, res.orb_energies_beta = _d(ea), _d(eb)
+            keep = [da, db, ea, eb]
+        self._check(self.L.gbhf_scf_uhf(self.h, C.byref(opts), int(multiplicity), C.byref(res)))
+        out = dict(energy=res.energy, iterations=res.iterations, converged=bool(res.converged),
+                   n_alpha=res.n_alpha, n_beta=res.n_beta, s2=res.s2)
+        if want_matrices:
+            out.update(density_alpha=keep[0], density_beta=keep[1], orb_energies_alpha=keep[2],
+                       orb_energies_beta=keep[3])
+        return out
 
     def set_guess_density(self, d_flat):
         """Starting density (flat upper triangle) for an SCF with GUESS_DENSITY (restart)."""

@@ -174,3 +174,29 @@ def small_molecule(name, basis="sto-3g", variant="text"):
 
 
 SMALL_MOLECULES = ("CO", "HF", "NH3", "CH4", "BH3", "LiH", "BeH2", "Ne", "HHe+")
+
+
+def _open_shell_geometries():
+    """Open-shell test systems: (atoms (label, bohr), charge, multiplicity)."""
+    def bent(center, r, angle_deg):
+        t = math.radians(angle_deg) / 2
+        return [(center, (0.0, 0.0, 0.0)), ("H", (0.0, r * math.sin(t), r * math.cos(t))),
+                ("H", (0.0, -r * math.sin(t), r * math.cos(t)))]
+    return {
+        "H": ([("H", (0.0, 0.0, 0.0))], 0.0, 2),
+        "Li": ([("Li", (0.0, 0.0, 0.0))], 0.0, 2),
+        "OH": ([("O", (0.0, 0.0, 0.0)), ("H", (0.0, 0.0, 1.834))], 0.0, 2),
+        "NH2": (bent("N", 1.936, 103.0), 0.0, 2),
+        "CH2": (bent("C", 2.04, 134.0), 0.0, 3),
+        "O2": ([("O", (0.0, 0.0, 0.0)), ("O", (0.0, 0.0, 2.282))], 0.0, 3),
+        "H2O+": ([("O", tuple(WATER_BOHR[0])), ("H", tuple(WATER_BOHR[1])), ("H", tuple(WATER_BOHR[2]))], 1.0, 2),
+    }
+
+
+def open_shell_molecule(name, basis="sto-3g", variant="text"):
+    """(atoms, charge, multiplicity) of an open-shell test system."""
+    geo, charge, mult = _open_shell_geometries()[name]
+    return make_atoms([l for l, _ in geo], [x for _, x in geo], basis, variant), charge, mult
+
+
+OPEN_SHELL = ("H", "Li", "OH", "NH2", "CH2", "O2", "H2O+")

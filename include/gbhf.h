@@ -198,6 +198,25 @@ gbhf_status gbhf_sad_density(gbhf_ctx* ctx, double* density_flat);
  * change, max |DIIS error|, stored DIIS vectors, phase (0 FP64, 1 mixed, 2 the
  * FP64 phase after a mixed one), milliseconds of the step; *n_records = steps. */
 #define GBHF_SCF_TRACE_FIELDS 8
+
+/* Open-shell (unrestricted) SCF for multiplicity 2S+1: the reference parses a
+ * multiplicity (--multi, Main.hs:55; OptsCheck.hs:31) but always runs the
+ * closed-shell scfHF.  n_alpha - n_beta = multiplicity - 1 electrons of the
+ * molecule (charge from opts); exact mode (direct J/K), FP64 or mixed builds,
+ * core or SAD start; DIIS on both spins with one set of coefficients.  s2 is
+ * <S^2> of the UHF determinant.  Output arrays may be NULL. */
+typedef struct {
+  double energy;
+  int iterations;
+  int converged;
+  int n_alpha, n_beta;
+  double s2;
+  double* density_alpha_flat;   /* N(N+1)/2: D_a = C_a,occ C_a,occ^T */
+  double* density_beta_flat;
+  double* orb_energies_alpha;   /* N */
+  double* orb_energies_beta;
+} gbhf_uhf_result;
+gbhf_status gbhf_scf_uhf(gbhf_ctx* ctx, const gbhf_scf_opts* opts, int multiplicity, gbhf_uhf_result* result);
 gbhf_status gbhf_set_guess_density(gbhf_ctx* ctx, const double* density_flat);
 gbhf_status gbhf_scf_trace(gbhf_ctx* ctx, double* out, int max_records, int* n_records);
 

@@ -599,3 +599,94 @@ def scf(fb, opts: Optional[SCFOptions] = None, grid=None):
             e_prev = etot
         density = new_density
     raise SCFNotConverged("SCF maxium steps exceeded")
+
+
+# ------------------------------------------------------------ open shell ----
+
+def eri_tensor(ob, n):
+    """Full (ab|cd) tensor from the oracle's contracted ERIs (exact numerics), small n."""
+    t = np.zeros((n, n, n, n))
+    for i in range(n):
+        for j in range(i + 1):
+            for k in range(n):
+                for l in range(k + 1):
+                    if k * (k + 1) // 2 + l > i * (i + 1) // 2 + j:
+                        continue
+                    v = ob.eri(i, j, k, l, ref_compat=False)
+                    for (a, b, c, d) in ((i, j, k, l), (j, i, k, l), (i, j, l, k), (j, i, l, k),
+                                         (k, l, i, j), (l, k, i, j), (k, l, j, i), (l, k, j, i)):
+                        t[a, b, c, d] = v
+    return t
+
+
+@dataclass
+class UHFResult:
+    energy: float
+    density_alpha: np.ndarray   # square
+    density_beta: np.ndarray
+    n_alpha: int
+    n_beta: int
+    s2: float
+    iterations: int
+
+
+def uhf(fb, multiplicity, charge=0.0, max_iter=200, conv_energy=1e-12, conv_density=1e-10, diis_size=6):
+    """Unrestricted HF with a core-Hamiltonian start and DIIS over both spins
+    (the reference has no open-shell SCF; this is the textbook UHF of Pople and
+    Nesbet, F_a = H + J(D_a + D_b) - K(D_a)), in numpy on the full ERI tensor."""
+    ob = OracleBasis(fb)
+    n = fb.n_cgf
+    S = tri_to_square(ob.overlap(False))
+    H = tri_to_square(ob.hcore(False))
+    w, U = np.linalg.eigh(S)
+    X = (U / np.sqrt(w)) @ U.T
+    nel = int(round(float(fb.charge.sum()) - charge))
+    na = (nel + multiplicity - 1) // 2
+    nb = nel - na
+    eri = eri_tensor(ob, n)
+    e_nn = nuclear_rep(fb.xyz, fb.charge)
+
+    def dens(F, nocc):
+        e, V = np.linalg.eigh(X.T @ F @ X)
+        C = X @ V
+        return C[:, :nocc] @ C[:, :nocc].T
+
+    Da, Db = dens(H, na), dens(H, nb)
+    hist = []
+    e_prev = None
+    for it in range(max_iter):
+        J = np.einsum("abcd,cd->ab", eri, Da + Db)
+        Fa = H + J - np.einsum("acbd,cd->ab", eri, Da)
+        Fb = H + J - np.einsum("acbd,cd->ab", eri, Db)
+        energy = 0.5 * (np.sum((Da + Db) * H) + np.sum(Da * Fa) + np.sum(Db * Fb)) + e_nn
+        ea = X.T @ (Fa @ Da @ S - S @ Da @ Fa) @ X
+        eb = X.T @ (Fb @ Db @ S - S @ Db @ Fb) @ X
+        hist.insert(0, (ea, eb, Fa, Fb))
+        del hist[diis_size:]
+        fa, fb_ = Fa, Fb
+        while it > 0 and len(hist) >= 2:
+            k = len(hist)
+            B = -np.ones((k + 1, k + 1))
+            B[k, k] = 0
+            for i in range(k):
+                for j in range(k):
+                    B[i, j] = np.sum(hist[i][0] * hist[j][0]) + np.sum(hist[i][1] * hist[j][1])
+            rhs = np.zeros(k + 1)
+            rhs[k] = -1
+            try:
+                x = np.linalg.solve(B, rhs)[:k]
+            except np.linalg.LinAlgError:
+                hist.pop()
+                continue
+            fa = sum(x[i] * hist[i][2] for i in range(k))
+            fb_ = sum(x[i] * hist[i][3] for i in range(k))
+            break
+        Na, Nb = dens(fa, na), dens(fb_, nb)
+        rms = math.sqrt((np.sum((Na - Da) ** 2) + np.sum((Nb - Db) ** 2)) / (2.0 * n * n))
+        if e_prev is not None and abs(energy - e_prev) < conv_energy and rms < conv_density:
+            sz = 0.5 * (na - nb)
+            s2 = sz * (sz + 1) + nb - np.sum((S @ Na @ S) * Nb)
+            return UHFResult(energy, Na, Nb, na, nb, float(s2), it + 1)
+        e_prev = energy
+        Da, Db = Na, Nb
+    raise SCFNotConverged("UHF did not converge")
