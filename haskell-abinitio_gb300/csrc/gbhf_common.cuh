@@ -104,6 +104,10 @@ __device__ __forceinline__ float round_node(float x, int& j) {
 }
 
 template <typename T> __device__ __forceinline__ T fma_t(T a, T b, T c);
+__device__ __forceinline__ double fabs_t(double x) { return fabs(x); }
+__device__ __forceinline__ float fabs_t(float x) { return fabsf(x); }
+__device__ __forceinline__ double fmax_t(double a, double b) { return fmax(a, b); }
+__device__ __forceinline__ float fmax_t(float a, float b) { return fmaxf(a, b); }
 template <> __device__ __forceinline__ double fma_t<double>(double a, double b, double c) { return fma(a, b, c); }
 template <> __device__ __forceinline__ float fma_t<float>(float a, float b, float c) { return fmaf(a, b, c); }
 

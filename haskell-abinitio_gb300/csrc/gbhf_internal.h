@@ -224,6 +224,7 @@ struct TaskLists {
   int nitems = 0;
   std::vector<int> combo_item_start;   // host: first item of each combo
   double thr_all = -1, thr64 = -1;     // thresholds the current lists were built for
+  double thr_exact = 0;                // per-quartet density screening cutoff of the current build
   int ncombo = 0;
   int hranges[4 * NCOMBO_MAX] = {0};   // host copy of ranges
   DBuf<int> f0;                        // first basis function per shell

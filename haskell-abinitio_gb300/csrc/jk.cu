@@ -79,6 +79,8 @@ struct JKArgs {
   unsigned long long* stats;   // [shell quartets, fn quartets, prim quartets]
   const double* sscale;        // per shell 6 component scales (d shells)
   int with_j;                  // 0: exchange only (the open-shell spin-density build)
+  const double* Q;             // Schwarz bound of each pair
+  double thr;                  // drop a quartet when Q_ab Q_cd max|D| over its six density blocks is below
 };
 
 template <int LA, int LB, int LC, int LD>
@@ -183,11 +185,38 @@ __global__ void __launch_bounds__(JK_THREADS) k_jk(JKArgs<T> a) {
     __syncwarp();
     acc.zero();
     int C = 0, Dd = 0, c0 = 0, d0 = 0;
+    bool keep = false;
     if (active) {
       C = a.pA[jk];
       Dd = a.pB[jk];
       c0 = a.shell_f0[C];
       d0 = a.shell_f0[Dd];
+      // exact screening of this quartet: the six density blocks it touches
+      // (J: D_ab, D_cd; K: D_ac, D_ad, D_bc, D_bd), tighter than the task lists'
+      // per-pair weights (a superposition of atomic densities has zero blocks
+      // between atoms, so most quartets of the first build drop here)
+      T dmx = T(0);
+#pragma unroll
+      for (int i = 0; i < NAB; ++i) dmx = fmax_t(dmx, fabs_t(sDab[warp][i]));
+#pragma unroll
+      for (int ic = 0; ic < NC; ++ic) {
+#pragma unroll
+        for (int id = 0; id < ND; ++id) dmx = fmax_t(dmx, fabs_t(Dm[(long long)(c0 + ic) * n + d0 + id]));
+#pragma unroll
+        for (int ia = 0; ia < NA; ++ia) dmx = fmax_t(dmx, fabs_t(Dm[(long long)(a0 + ia) * n + c0 + ic]));
+#pragma unroll
+        for (int ibb = 0; ibb < NB; ++ibb) dmx = fmax_t(dmx, fabs_t(Dm[(long long)(b0 + ibb) * n + c0 + ic]));
+      }
+#pragma unroll
+      for (int id = 0; id < ND; ++id) {
+#pragma unroll
+        for (int ia = 0; ia < NA; ++ia) dmx = fmax_t(dmx, fabs_t(Dm[(long long)(a0 + ia) * n + d0 + id]));
+#pragma unroll
+        for (int ibb = 0; ibb < NB; ++ibb) dmx = fmax_t(dmx, fabs_t(Dm[(long long)(b0 + ibb) * n + d0 + id]));
+      }
+      keep = a.Q[ib] * a.Q[jk] * (double)dmx >= a.thr;
+    }
+    if (keep) {
       const int4 sg = a.seg[a.kseg[jk]];
       const int len = sg.y - sg.x;
       const long long base = (long long)sg.w + (jk - sg.x);
@@ -215,6 +244,7 @@ __global__ void __launch_bounds__(JK_THREADS) k_jk(JKArgs<T> a) {
       cnt_q += lead && kb0 == 0;
       cnt_p += (unsigned long long)nbl * (sk < K ? (K - sk + nsk - 1) / nsk : 0);
     }
+    const bool lead_k = lead && keep;   // scatters
     // warp-uniform: sum the slices (every lane ends with the total of its ket)
     for (int o = 1 << lg; o < 32; o <<= 1) {
 #pragma unroll
@@ -222,7 +252,7 @@ __global__ void __launch_bounds__(JK_THREADS) k_jk(JKArgs<T> a) {
     }
     if constexpr (LA == 2 || LB == 2 || LC == 2 || LD == 2) {
       // d shells: the generated code used the first component's coefficients
-      if (active) {
+      if (keep) {
 #pragma unroll
         for (int e = 0; e < NOUT; ++e) {
           const int ab = e / NCD, cd = e - ab * NCD;
@@ -241,7 +271,7 @@ __global__ void __launch_bounds__(JK_THREADS) k_jk(JKArgs<T> a) {
 #pragma unroll
     for (int ic = 0; ic < NC; ++ic)
 #pragma unroll
-      for (int id = 0; id < ND; ++id) dcd[ic * ND + id] = lead ? Dm[(long long)(c0 + ic) * n + d0 + id] : T(0);
+      for (int id = 0; id < ND; ++id) dcd[ic * ND + id] = lead_k ? Dm[(long long)(c0 + ic) * n + d0 + id] : T(0);
     // J_ab (warp reduce over kets)
     if (a.with_j) {
 #pragma unroll
@@ -253,7 +283,7 @@ __global__ void __launch_bounds__(JK_THREADS) k_jk(JKArgs<T> a) {
         if (lane == 0) atomicAdd(&Gm[(long long)(a0 + ab / NB) * n + b0 + ab % NB], widen(v));
       }
     }
-    if (lead) {
+    if (lead_k) {
       // J_cd
       if (a.with_j) {
 #pragma unroll
@@ -811,6 +841,8 @@ static gbhf_status launch_class(gbhf_ctx* c, cudaStream_t strm, int combo, int p
   a.stats = c->tasks.stats.p + 3 * (2 * combo + prec);
   a.sscale = c->tasks.sscale.p;
   a.with_j = with_j;
+  a.Q = P.Q.p;
+  a.thr = c->tasks.thr_exact;
   kern<<<grid, JK_THREADS, smem, strm>>>(a);
   count_launch(c);
   GBHF_CUDA(c, cudaGetLastError());
@@ -824,6 +856,7 @@ static bool gen_dclass(int k) { return (k >= 6 && k <= 11) || k == 15; }
 gbhf_status jk_build(gbhf_ctx* c, const double* d_Dsq, double* d_G, int precision, double schwarz,
                      double mixed_cutoff, double weight, bool local_weights, bool with_j) {
   const int wj = with_j ? 1 : 0;
+  c->tasks.thr_exact = schwarz;   // per-quartet test in the kernels, on the density passed here
   GBHF_TRY(ensure_pairs(c));
   const int n = c->basis.nbf;
   TaskLists& st = c->tasks;

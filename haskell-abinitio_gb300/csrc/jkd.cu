@@ -40,6 +40,8 @@ struct JKDArgs {
   const T* boys;
   unsigned long long* stats;
   int with_j;             // 0: exchange only
+  const double* Q;        // Schwarz bound of each pair
+  double thr;             // per-quartet screening on the six density blocks (as k_jk)
 };
 
 template <int LA, int LB, int LC, int LD, typename T>
@@ -79,6 +81,28 @@ __global__ void __launch_bounds__(JKD_THREADS) k_jkd(JKDArgs<T> a) {
       const int jk = task.y + q;
       const int Cs = a.pA[jk], Ds = a.pB[jk];
       const int c0 = a.shell_f0[Cs], d0 = a.shell_f0[Ds];
+      {   // exact screening on the six density blocks of the quartet (as k_jk)
+        double dmx = 0.0;
+        constexpr int NB6 = C::NAB + C::NCD + (C::NA + C::NB) * (C::NC + C::ND);
+        for (int e = lane; e < NB6; e += 32) {
+          int r, q2;
+          if (e < C::NAB) {
+            r = a0 + e / C::NB;
+            q2 = b0 + e % C::NB;
+          } else if (e < C::NAB + C::NCD) {
+            r = c0 + (e - C::NAB) / C::ND;
+            q2 = d0 + (e - C::NAB) % C::ND;
+          } else {
+            const int f = e - C::NAB - C::NCD, rr = f / (C::NC + C::ND), cc = f % (C::NC + C::ND);
+            r = rr < C::NA ? a0 + rr : b0 + (rr - C::NA);
+            q2 = cc < C::NC ? c0 + cc : d0 + (cc - C::NC);
+          }
+          dmx = fmax(dmx, fabs((double)Dm[(long long)r * n + q2]));
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) dmx = fmax(dmx, __shfl_xor_sync(0xffffffffu, dmx, o));
+        if (a.Q[ib] * a.Q[jk] * dmx < a.thr) continue;   // warp-uniform
+      }
       const int4 sg = a.seg[a.kseg[jk]];
       const int K = sg.z, len = sg.y - sg.x;
       const long long base = (long long)sg.w + (jk - sg.x);
@@ -211,6 +235,8 @@ static gbhf_status launch_jkd_t(gbhf_ctx* c, cudaStream_t strm, int combo, int p
   a.boys = boys;
   a.stats = c->tasks.stats.p + 3 * (2 * combo + prec);
   a.with_j = with_j;
+  a.Q = P.Q.p;
+  a.thr = c->tasks.thr_exact;
   kern<<<grid, JKD_THREADS, smem, strm>>>(a);
   count_launch(c);
   GBHF_CUDA(c, cudaGetLastError());

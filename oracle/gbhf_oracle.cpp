@@ -848,9 +848,12 @@ void orc_fock_canonical(int n, const double* H, const double* D, const double* e
 }
 
 // Direct shell-based J/K Fock build (exact numerics).  Skips shell quartets
-// with Q_AB*Q_CD < schwarz.  stats[0] = computed shell quartets,
+// with Q_AB*Q_CD < schwarz and, with density_screen, those whose bound times
+// the largest |D| over the six density blocks the quartet touches (AB, CD, AC,
+// AD, BC, BD) is below schwarz.  stats[0] = computed shell quartets,
 // stats[1] = computed primitive quartets, stats[2] = skipped shell quartets.
-void orc_fock_direct(void* h, const double* H, const double* D, double schwarz, double* F, long long* stats) {
+void orc_fock_direct(void* h, const double* H, const double* D, double schwarz, int density_screen, double* F,
+                     long long* stats) {
   Basis* b = (Basis*)h;
   const int n = b->nf();
   std::vector<ShellPair> pairs = make_shell_pairs(*b);
@@ -875,6 +878,23 @@ void orc_fock_direct(void* h, const double* H, const double* D, double schwarz, 
         }
         const Shell &C = b->shells[Q.A], &Dd = b->shells[Q.B];
         const int na = A.ncomp, nb = B.ncomp, nc = C.ncomp, nd = Dd.ncomp;
+        if (density_screen) {
+          double dm = 0;
+          auto blk = [&](const Shell& X, const Shell& Y) {
+            for (int x = 0; x < X.ncomp; ++x)
+              for (int y = 0; y < Y.ncomp; ++y) dm = std::max(dm, std::fabs(Dsq[(size_t)X.fidx[x] * n + Y.fidx[y]]));
+          };
+          blk(A, B);
+          blk(C, Dd);
+          blk(A, C);
+          blk(A, Dd);
+          blk(B, C);
+          blk(B, Dd);
+          if (P.Q * Q.Q * dm < schwarz) {
+            ++nskip;
+            continue;
+          }
+        }
         buf.resize((size_t)na * nb * nc * nd);
         eri_shell_quartet(*b, A, B, C, Dd, buf.data());
         ++nq;

@@ -97,7 +97,7 @@ def lib():
         L.orc_eri.restype = C.c_double
         L.orc_eri.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]
         L.orc_fock_canonical.argtypes = [C.c_int, _dp, _dp, _dp, _dp]
-        L.orc_fock_direct.argtypes = [C.c_void_p, _dp, _dp, C.c_double, _dp, C.POINTER(C.c_longlong)]
+        L.orc_fock_direct.argtypes = [C.c_void_p, _dp, _dp, C.c_double, C.c_int, _dp, C.POINTER(C.c_longlong)]
         L.orc_shell_pair_bounds.argtypes = [C.c_void_p, _dp]
         L.orc_num_threads.restype = C.c_int
         _lib = L
@@ -202,11 +202,14 @@ class OracleBasis:
     def eri(self, i, j, k, l, ref_compat=True):
         return lib().orc_eri(self.h, int(ref_compat), i, j, k, l)
 
-    def fock_direct(self, H, D, schwarz=1e-12):
+    def fock_direct(self, H, D, schwarz=1e-12, density_screen=True):
+        """H + G(D) by shell quartets; drops Q_AB Q_CD < schwarz and (density_screen)
+        Q_AB Q_CD max|D| over the quartet's six density blocks < schwarz, as the device build."""
         F = np.zeros(self.ntri)
         st = np.zeros(3, dtype=np.int64)
         lib().orc_fock_direct(self.h, _p(np.ascontiguousarray(H)), _p(np.ascontiguousarray(D)),
-                              float(schwarz), _p(F), st.ctypes.data_as(C.POINTER(C.c_longlong)))
+                              float(schwarz), int(bool(density_screen)), _p(F),
+                              st.ctypes.data_as(C.POINTER(C.c_longlong)))
         return F, st
 
     def shell_pair_bounds(self):
