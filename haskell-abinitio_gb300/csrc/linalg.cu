@@ -980,6 +980,8 @@ gbhf_status purify(gbhf_ctx* c, int n, int ne, const double* d_F, double* d_P, d
   GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
   if (st & GBHF_DEV_ERR_TIMEOUT) return fail(c, GBHF_ERR_DEVICE_TIMEOUT, "purification grid barrier timed out");
   const double err = hout[0];
+  c->prof.purify_steps += hout[1];
+  c->prof.purify_calls += 1;
   if (err_out) *err_out = err;
   if (!(std::fabs(err) < 1e-6 * std::max(1, ne)))
     return fail(c, GBHF_ERR_NOT_CONVERGED, "density purification did not converge");
