@@ -335,7 +335,8 @@ def run_batch(args, world, rank, local):
             "mixed_cutoff": args.mixed_cutoff, "grad_mixed_cutoff": args.grad_mixed_cutoff or args.mixed_cutoff,
             "sample": f"FP64 one-at-a-time SCF + gradient timed on {len(sample)} of {len(sub)} molecules and scaled",
             "batch_steps": int(prof["batch_steps"]), "gpu_launches": int(prof["launches"]),
-            "phases_ms": {k: prof[k] for k in ("ms_setup", "ms_fock", "ms_diis", "ms_diag", "ms_other", "ms_grad")},
+            "phases_ms": {k: prof[k] for k in ("ms_pairs", "ms_setup", "ms_fock", "ms_diis", "ms_diag", "ms_other",
+                                               "ms_grad")},
             "jk_prim_quartets": prof["prim_quartets_fp64"] + prof["prim_quartets_fp32"],
             "data": "synthetic (256 seeded water conformers)", "dtype": "f32+f64", "higher_is_better": True}
     print(json.dumps(line), flush=True)

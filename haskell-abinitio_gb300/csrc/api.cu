@@ -522,12 +522,12 @@ gbhf_status gbhf_scf_trace(gbhf_ctx* c, double* out, int max_records, int* n_rec
 gbhf_status gbhf_profile_read(gbhf_ctx* c, double* stats, int n_stats) {
   CTX_CHECK(c);
   if (!stats) return fail(c, GBHF_ERR_BAD_INPUT, "null pointer");
-  const double v[19] = {c->prof.jk_ms64,   c->prof.jk_ms32,  c->prof.prim64,        c->prof.prim32,
+  const double v[20] = {c->prof.jk_ms64,   c->prof.jk_ms32,  c->prof.prim64,        c->prof.prim32,
                         c->prof.shellq,    c->prof.fnq,      (double)c->prof.launches, c->prof.dense_ms,
                         c->prof.ph_setup,  c->prof.ph_fock,  c->prof.ph_diis,       c->prof.ph_diag,
                         c->prof.ph_other,  c->prof.jacobi_sweeps, c->prof.jacobi_calls, c->prof.ph_grad,
-                        c->prof.batch_steps, c->prof.purify_steps, c->prof.purify_calls};
-  for (int i = 0; i < n_stats && i < 19; ++i) stats[i] = v[i];
+                        c->prof.batch_steps, c->prof.purify_steps, c->prof.purify_calls, c->prof.ph_pairs};
+  for (int i = 0; i < n_stats && i < 20; ++i) stats[i] = v[i];
   return GBHF_OK;
 }
 

@@ -257,7 +257,7 @@ struct Profile {
   double cls[NCOMBO][2][4] = {};   // per combo and precision: shell q, fn q, prim q, ms
   // host wall-clock per SCF phase (ms): setup, Fock, DIIS, diagonalisation, other; Jacobi sweeps
   double ph_setup = 0, ph_fock = 0, ph_diis = 0, ph_diag = 0, ph_other = 0, jacobi_sweeps = 0, jacobi_calls = 0;
-  double ph_grad = 0, batch_steps = 0, purify_steps = 0, purify_calls = 0;
+  double ph_grad = 0, batch_steps = 0, purify_steps = 0, purify_calls = 0, ph_pairs = 0;
 };
 
 }  // namespace gbhf

@@ -1,5 +1,6 @@
 // Basis upload, Boys tables and shell-pair data for the direct J/K build.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <numeric>
@@ -240,36 +241,80 @@ gbhf_status ensure_boys_tables(gbhf_ctx* c) {
 
 static int pair_class(int la, int lb) { return pair_class_of(la, lb); }
 
-// Fields of every primitive pair of shells (A, B), out[k*BRA_NFIELD + field],
-// k = ia*np_B + ib.  K' = sqrt(2 pi^(5/2)) c_a c_b exp(-mu |AB|^2) / p, so the
-// product of a bra and a ket K' times 1/sqrt(p+q) is the whole ERI prefactor.
-static void pair_prims(const Basis& b, int A, int B, double* out) {
-  const Shell &sa = b.shells[A], &sb = b.shells[B];
-  const double* RA = &b.xyz[3 * sa.atom];
-  const double* RB = &b.xyz[3 * sb.atom];
+// Fields of primitive pair k = ia*np_B + ib of shells (A, B).
+// K' = sqrt(2 pi^(5/2)) c_a c_b exp(-mu |AB|^2) / p, so the product of a bra
+// and a ket K' times 1/sqrt(p+q) is the whole ERI prefactor.  sh: per shell
+// (atom, primitives, offset of its first CGF's primitives in coef/expo).
+__device__ __forceinline__ void pair_prim_fields(const int4* __restrict__ sh, const double* __restrict__ xyz,
+                                                 const double* __restrict__ coef, const double* __restrict__ expo,
+                                                 int A, int B, int k, double* f) {
+  const int4 sa = sh[A], sb = sh[B];
+  const int ia = k / sb.y, ib = k - ia * sb.y;
+  const double* RA = xyz + 3 * sa.x;
+  const double* RB = xyz + 3 * sb.x;
   double r2 = 0;
   for (int x = 0; x < 3; ++x) r2 += (RA[x] - RB[x]) * (RA[x] - RB[x]);
-  int k = 0;
-  for (int ia = 0; ia < sa.np; ++ia)
-    for (int ib = 0; ib < sb.np; ++ib, ++k) {
-      const double ea = sa.expo[ia], eb = sb.expo[ib];
-      const double p = ea + eb, mu = ea * eb / p;
-      double* f = out + (size_t)k * BRA_NFIELD;
-      f[BRA_P] = p;
-      f[BRA_INVP] = 1.0 / p;
-      for (int x = 0; x < 3; ++x) {
-        const double Px = (ea * RA[x] + eb * RB[x]) / p;
-        f[BRA_PX + x] = Px;
-        f[BRA_PAX + x] = Px - RA[x];
-        f[BRA_PBX + x] = Px - RB[x];
-      }
-      f[BRA_K] = std::sqrt(TWO_PI_2P5) * sa.coef[ia] * sb.coef[ib] * std::exp(-mu * r2) / p;
-      f[BRA_AEXP] = ea;
+  const double ea = expo[sa.z + ia], eb = expo[sb.z + ib];
+  const double p = ea + eb, mu = ea * eb / p;
+  f[BRA_P] = p;
+  f[BRA_INVP] = 1.0 / p;
+  for (int x = 0; x < 3; ++x) {
+    const double Px = (ea * RA[x] + eb * RB[x]) / p;
+    f[BRA_PX + x] = Px;
+    f[BRA_PAX + x] = Px - RA[x];
+    f[BRA_PBX + x] = Px - RB[x];
+  }
+  f[BRA_K] = sqrt(TWO_PI_2P5) * coef[sa.z + ia] * coef[sb.z + ib] * exp(-mu * r2) / p;
+  f[BRA_AEXP] = ea;
+}
+
+// Pair-contiguous FP64 fields of pairs (pA, pB) at poff (the Schwarz pass).
+__global__ void k_pair_fields(int np, const int* __restrict__ pA, const int* __restrict__ pB,
+                              const int* __restrict__ poff, const int4* __restrict__ sh,
+                              const double* __restrict__ xyz, const double* __restrict__ coef,
+                              const double* __restrict__ expo, long long npp, double* __restrict__ out) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= np) return;
+  const int A = pA[t], B = pB[t];
+  const int K = sh[A].y * sh[B].y;
+  double f[BRA_NFIELD];
+  for (int k = 0; k < K; ++k) {
+    pair_prim_fields(sh, xyz, coef, expo, A, B, k, f);
+    for (int fl = 0; fl < BRA_NFIELD; ++fl) out[(long long)fl * npp + poff[t] + k] = f[fl];
+  }
+}
+
+// Final layouts of the sorted pairs: bra (pair-contiguous) and ket
+// (segment-transposed: primitive k of pair t at data_off + k*len + (t - start)),
+// FP64 and FP32.
+__global__ void k_pair_layouts(int np, const int* __restrict__ pA, const int* __restrict__ pB,
+                               const int* __restrict__ poff, const int* __restrict__ kseg,
+                               const int4* __restrict__ seg, const int4* __restrict__ sh,
+                               const double* __restrict__ xyz, const double* __restrict__ coef,
+                               const double* __restrict__ expo, long long npp, double* __restrict__ bra64,
+                               double* __restrict__ ket64, float* __restrict__ bra32, float* __restrict__ ket32) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= np) return;
+  const int A = pA[t], B = pB[t];
+  const int K = sh[A].y * sh[B].y;
+  const int4 sg = seg[kseg[t]];
+  const long long len = sg.y - sg.x;
+  double f[BRA_NFIELD];
+  for (int k = 0; k < K; ++k) {
+    pair_prim_fields(sh, xyz, coef, expo, A, B, k, f);
+    const long long bi = (long long)poff[t] + k, ki = (long long)sg.w + k * len + (t - sg.x);
+    for (int fl = 0; fl < BRA_NFIELD; ++fl) {
+      bra64[(long long)fl * npp + bi] = f[fl];
+      ket64[(long long)fl * npp + ki] = f[fl];
+      bra32[(long long)fl * npp + bi] = (float)f[fl];
+      ket32[(long long)fl * npp + ki] = (float)f[fl];
     }
+  }
 }
 
 gbhf_status ensure_pairs(gbhf_ctx* c) {
   if (c->pairs_ready) return GBHF_OK;
+  const auto t_pairs = std::chrono::steady_clock::now();
   const Basis& b = c->basis;
   if (!c->basis_dev) return fail(c, GBHF_ERR_BAD_INPUT, "no basis set");
   if (!b.shells_ok || b.maxL > 2)
@@ -279,8 +324,18 @@ gbhf_status ensure_pairs(gbhf_ctx* c) {
   GBHF_TRY(ensure_boys_tables(c));
   GBHF_TRY(ensure_shell_arrays(c));   // component scales for the d-class Schwarz bounds
   const int ns = (int)b.shells.size();
-  // 1. all pairs (la > lb, or la == lb and A >= B) of shells of one molecule
-  std::vector<int> A, B;
+  // shell table for the device: atom, primitives, first primitive of the shell's first CGF
+  std::vector<int4> shv(ns);
+  for (int s2 = 0; s2 < ns; ++s2) {
+    const Shell& sh = b.shells[s2];
+    shv[s2] = make_int4(sh.atom, sh.np, b.cgf_off[sh.f0], 0);
+  }
+  DBuf<int4> dsh;
+  GBHF_CUDA(c, dsh.alloc(std::max(ns, 1)));
+  GBHF_CUDA(c, cudaMemcpyAsync(dsh.p, shv.data(), ns * sizeof(int4), cudaMemcpyHostToDevice, c->stream));
+  // 1. all pairs (la > lb, or la == lb and A >= B) of shells of one molecule,
+  //    grouped by class as they are generated (counting sort)
+  std::vector<int> A, B, cls;
   for (int s0 = 0; s0 < ns;) {
     int s1 = s0;
     while (s1 < ns && b.shells[s1].mol == b.shells[s0].mol) ++s1;
@@ -290,56 +345,51 @@ gbhf_status ensure_pairs(gbhf_ctx* c) {
         if (la > lb || (la == lb && a >= bb)) {
           A.push_back(a);
           B.push_back(bb);
+          cls.push_back(pair_class(la, lb));
         }
       }
     s0 = s1;
   }
   const int np = (int)A.size();
+  std::vector<int> ord0(np);
+  int cs0[NPCLS + 1] = {};
+  {
+    std::vector<int> cnt(NPCLS + 1, 0);
+    for (int t = 0; t < np; ++t) ++cnt[cls[t] + 1];
+    for (int cl = 0; cl < NPCLS; ++cl) cnt[cl + 1] += cnt[cl];
+    for (int cl = 0; cl <= NPCLS; ++cl) cs0[cl] = cnt[cl];
+    for (int t = 0; t < np; ++t) ord0[cnt[cls[t]]++] = t;
+  }
   // 2. Schwarz bounds on the device, pairs grouped by class (class code, FP64)
   std::vector<double> Q(np);
   {
-    std::vector<int> ord0(np);
-    std::iota(ord0.begin(), ord0.end(), 0);
-    std::stable_sort(ord0.begin(), ord0.end(), [&](int x, int y) {
-      return pair_class(b.shells[A[x]].L, b.shells[B[x]].L) < pair_class(b.shells[A[y]].L, b.shells[B[y]].L);
-    });
-    int cs0[NPCLS + 1];
-    for (int cl = 0; cl <= NPCLS; ++cl) cs0[cl] = np;
-    std::vector<int> K0(np), off0(np);
+    std::vector<int> A0(np), B0(np), K0(np), off0(np);
     size_t npp0 = 0;
-    for (int t = np - 1; t >= 0; --t)
-      cs0[pair_class(b.shells[A[ord0[t]]].L, b.shells[B[ord0[t]]].L)] = t;
-    for (int cl = NPCLS - 1; cl >= 0; --cl)
-      if (cs0[cl] == np) cs0[cl] = cs0[cl + 1];
-    for (int t = 0; t < np; ++t) {
-      K0[t] = b.shells[A[ord0[t]]].np * b.shells[B[ord0[t]]].np;
-      off0[t] = (int)npp0;
-      npp0 += K0[t];
-    }
-    std::vector<double> bra0((size_t)BRA_NFIELD * npp0), f(BRA_NFIELD * KMAX_PRIM_PAIRS);
-    for (int t = 0; t < np; ++t) {
-      pair_prims(b, A[ord0[t]], B[ord0[t]], f.data());
-      for (int k = 0; k < K0[t]; ++k)
-        for (int fl = 0; fl < BRA_NFIELD; ++fl) bra0[(size_t)fl * npp0 + off0[t] + k] = f[k * BRA_NFIELD + fl];
-    }
-    std::vector<int> A0(np), B0(np);
     for (int t = 0; t < np; ++t) {
       A0[t] = A[ord0[t]];
       B0[t] = B[ord0[t]];
+      K0[t] = b.shells[A0[t]].np * b.shells[B0[t]].np;
+      off0[t] = (int)npp0;
+      npp0 += K0[t];
     }
     DBuf<int> dK, doff, dA0, dB0;
     DBuf<double> dQ, dbra;
-    GBHF_CUDA(c, dK.alloc(np));
-    GBHF_CUDA(c, doff.alloc(np));
-    GBHF_CUDA(c, dA0.alloc(np));
-    GBHF_CUDA(c, dB0.alloc(np));
-    GBHF_CUDA(c, dQ.alloc(np));
-    GBHF_CUDA(c, dbra.alloc(bra0.size()));
+    GBHF_CUDA(c, dK.alloc(std::max(np, 1)));
+    GBHF_CUDA(c, doff.alloc(std::max(np, 1)));
+    GBHF_CUDA(c, dA0.alloc(std::max(np, 1)));
+    GBHF_CUDA(c, dB0.alloc(std::max(np, 1)));
+    GBHF_CUDA(c, dQ.alloc(std::max(np, 1)));
+    GBHF_CUDA(c, dbra.alloc(std::max<size_t>((size_t)BRA_NFIELD * npp0, 1)));
     GBHF_CUDA(c, cudaMemcpyAsync(dK.p, K0.data(), np * sizeof(int), cudaMemcpyHostToDevice, c->stream));
     GBHF_CUDA(c, cudaMemcpyAsync(doff.p, off0.data(), np * sizeof(int), cudaMemcpyHostToDevice, c->stream));
     GBHF_CUDA(c, cudaMemcpyAsync(dA0.p, A0.data(), np * sizeof(int), cudaMemcpyHostToDevice, c->stream));
     GBHF_CUDA(c, cudaMemcpyAsync(dB0.p, B0.data(), np * sizeof(int), cudaMemcpyHostToDevice, c->stream));
-    GBHF_CUDA(c, cudaMemcpyAsync(dbra.p, bra0.data(), bra0.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    if (np > 0) {
+      k_pair_fields<<<(np + 127) / 128, 128, 0, c->stream>>>(np, dA0.p, dB0.p, doff.p, dsh.p, c->d_xyz.p,
+                                                             c->d_coef.p, c->d_exp.p, (long long)npp0, dbra.p);
+      count_launch(c);
+      GBHF_CUDA(c, cudaGetLastError());
+    }
     GBHF_TRY(schwarz_classes_dev(c, cs0, dK.p, doff.p, dbra.p, (long long)npp0, dQ.p));
     GBHF_TRY(schwarz_dclasses_dev(c, cs0, dA0.p, dB0.p, dK.p, doff.p, dbra.p, (long long)npp0, dQ.p));
     std::vector<double> Q0(np);
@@ -348,17 +398,16 @@ gbhf_status ensure_pairs(gbhf_ctx* c) {
     for (int t = 0; t < np; ++t) Q[ord0[t]] = Q0[t];
   }
   // 3. order: class, molecule, primitive-pair count descending, Q descending
-  std::vector<int> order(np);
+  std::vector<int> order(np), Kp(np), molp(np);
+  for (int t = 0; t < np; ++t) {
+    Kp[t] = b.shells[A[t]].np * b.shells[B[t]].np;
+    molp[t] = b.shells[A[t]].mol;
+  }
   std::iota(order.begin(), order.end(), 0);
-  auto K_of = [&](int t) { return b.shells[A[t]].np * b.shells[B[t]].np; };
-  auto cls_of = [&](int t) { return pair_class(b.shells[A[t]].L, b.shells[B[t]].L); };
-  auto mol_of = [&](int t) { return b.shells[A[t]].mol; };
-  std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
-    int cx = cls_of(x), cy = cls_of(y);
-    if (cx != cy) return cx < cy;
-    if (mol_of(x) != mol_of(y)) return mol_of(x) < mol_of(y);
-    int kx = K_of(x), ky = K_of(y);
-    if (kx != ky) return kx > ky;
+  std::sort(order.begin(), order.end(), [&](int x, int y) {
+    if (cls[x] != cls[y]) return cls[x] < cls[y];
+    if (molp[x] != molp[y]) return molp[x] < molp[y];
+    if (Kp[x] != Kp[y]) return Kp[x] > Kp[y];
     if (Q[x] != Q[y]) return Q[x] > Q[y];
     return x < y;
   });
@@ -377,14 +426,14 @@ gbhf_status ensure_pairs(gbhf_ctx* c) {
     const int o = order[t];
     P.hA[t] = A[o];
     P.hB[t] = B[o];
-    P.hK[t] = K_of(o);
+    P.hK[t] = Kp[o];
     P.hQ[t] = Q[o];
     P.hPoff[t] = (int)poff;
     poff += P.hK[t];
-    const int cl = cls_of(o);
+    const int cl = cls[o];
     if (P.cls_start[cl] == np) P.cls_start[cl] = t;
     auto& sg = P.segs[cl];
-    if (sg.empty() || sg.back().K != P.hK[t] || mol_of(order[sg.back().start]) != mol_of(o))
+    if (sg.empty() || sg.back().K != P.hK[t] || molp[order[sg.back().start]] != molp[o])
       sg.push_back({t, t + 1, P.hK[t], 0});
     else sg.back().end = t + 1;
   }
@@ -396,11 +445,11 @@ gbhf_status ensure_pairs(gbhf_ctx* c) {
   size_t koff = 0;
   for (int cl = 0; cl < NPCLS; ++cl) {
     P.seg_cls_start[cl] = (int)seginfo.size();
-    for (auto& s : P.segs[cl]) {
-      s.data_off = (int)koff;
-      koff += (size_t)(s.end - s.start) * s.K;
-      for (int t = s.start; t < s.end; ++t) P.hSeg[t] = (int)seginfo.size();
-      seginfo.push_back(make_int4(s.start, s.end, s.K, s.data_off));
+    for (auto& sgm : P.segs[cl]) {
+      sgm.data_off = (int)koff;
+      koff += (size_t)(sgm.end - sgm.start) * sgm.K;
+      for (int t = sgm.start; t < sgm.end; ++t) P.hSeg[t] = (int)seginfo.size();
+      seginfo.push_back(make_int4(sgm.start, sgm.end, sgm.K, sgm.data_off));
     }
   }
   P.seg_cls_start[NPCLS] = (int)seginfo.size();
@@ -419,38 +468,22 @@ gbhf_status ensure_pairs(gbhf_ctx* c) {
     }
   std::vector<int> pmol(np);
   for (int t = 0; t < np; ++t) pmol[t] = b.shells[P.hA[t]].mol;
-  // 4. primitive-pair data
+  // 4. primitive-pair data, built on the device in both layouts and precisions
   const size_t npp = poff;
-  std::vector<double> bra((size_t)BRA_NFIELD * npp), ket((size_t)BRA_NFIELD * npp);
-  std::vector<double> fbuf(BRA_NFIELD * KMAX_PRIM_PAIRS);
-  for (int t = 0; t < np; ++t) {
-    pair_prims(b, P.hA[t], P.hB[t], fbuf.data());
-    const int4 sg = seginfo[P.hSeg[t]];
-    const int seglen = sg.y - sg.x;
-    for (int k = 0; k < P.hK[t]; ++k) {
-      const double* f = fbuf.data() + (size_t)k * BRA_NFIELD;
-      const size_t bidx = (size_t)P.hPoff[t] + k;
-      const size_t kidx = (size_t)sg.w + (size_t)k * seglen + (t - sg.x);
-      for (int fl = 0; fl < BRA_NFIELD; ++fl) {
-        bra[(size_t)fl * npp + bidx] = f[fl];
-        ket[(size_t)fl * npp + kidx] = f[fl];
-      }
-    }
-  }
-  std::vector<float> bra32(bra.begin(), bra.end()), ket32(ket.begin(), ket.end());
-  GBHF_CUDA(c, P.A.alloc(np));
-  GBHF_CUDA(c, P.B.alloc(np));
-  GBHF_CUDA(c, P.K.alloc(np));
-  GBHF_CUDA(c, P.poff.alloc(np));
-  GBHF_CUDA(c, P.kseg.alloc(np));
-  GBHF_CUDA(c, P.Q.alloc(np));
-  GBHF_CUDA(c, P.seg_info.alloc(seginfo.size()));
-  GBHF_CUDA(c, P.mol.alloc(np));
-  GBHF_CUDA(c, P.mseg.alloc(P.hmseg.size()));
-  GBHF_CUDA(c, P.bra64.alloc(bra.size()));
-  GBHF_CUDA(c, P.ket64.alloc(ket.size()));
-  GBHF_CUDA(c, P.bra32.alloc(bra.size()));
-  GBHF_CUDA(c, P.ket32.alloc(ket.size()));
+  const size_t nf = std::max<size_t>((size_t)BRA_NFIELD * npp, 1);
+  GBHF_CUDA(c, P.A.alloc(std::max(np, 1)));
+  GBHF_CUDA(c, P.B.alloc(std::max(np, 1)));
+  GBHF_CUDA(c, P.K.alloc(std::max(np, 1)));
+  GBHF_CUDA(c, P.poff.alloc(std::max(np, 1)));
+  GBHF_CUDA(c, P.kseg.alloc(std::max(np, 1)));
+  GBHF_CUDA(c, P.Q.alloc(std::max(np, 1)));
+  GBHF_CUDA(c, P.seg_info.alloc(std::max<size_t>(seginfo.size(), 1)));
+  GBHF_CUDA(c, P.mol.alloc(std::max(np, 1)));
+  GBHF_CUDA(c, P.mseg.alloc(std::max<size_t>(P.hmseg.size(), 1)));
+  GBHF_CUDA(c, P.bra64.alloc(nf));
+  GBHF_CUDA(c, P.ket64.alloc(nf));
+  GBHF_CUDA(c, P.bra32.alloc(nf));
+  GBHF_CUDA(c, P.ket32.alloc(nf));
   auto up = [&](void* d, const void* h, size_t bytes) {
     return cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, c->stream);
   };
@@ -463,12 +496,16 @@ gbhf_status ensure_pairs(gbhf_ctx* c) {
   GBHF_CUDA(c, up(P.seg_info.p, seginfo.data(), seginfo.size() * sizeof(int4)));
   GBHF_CUDA(c, up(P.mol.p, pmol.data(), np * sizeof(int)));
   GBHF_CUDA(c, up(P.mseg.p, P.hmseg.data(), P.hmseg.size() * sizeof(int)));
-  GBHF_CUDA(c, up(P.bra64.p, bra.data(), bra.size() * sizeof(double)));
-  GBHF_CUDA(c, up(P.ket64.p, ket.data(), ket.size() * sizeof(double)));
-  GBHF_CUDA(c, up(P.bra32.p, bra32.data(), bra32.size() * sizeof(float)));
-  GBHF_CUDA(c, up(P.ket32.p, ket32.data(), ket32.size() * sizeof(float)));
+  if (np > 0) {
+    k_pair_layouts<<<(np + 127) / 128, 128, 0, c->stream>>>(np, P.A.p, P.B.p, P.poff.p, P.kseg.p, P.seg_info.p, dsh.p,
+                                                            c->d_xyz.p, c->d_coef.p, c->d_exp.p, (long long)npp,
+                                                            P.bra64.p, P.ket64.p, P.bra32.p, P.ket32.p);
+    count_launch(c);
+    GBHF_CUDA(c, cudaGetLastError());
+  }
   GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
   c->pairs_ready = true;
+  c->prof.ph_pairs += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_pairs).count();
   return GBHF_OK;
 }
 

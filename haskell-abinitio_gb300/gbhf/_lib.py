@@ -404,11 +404,11 @@ class Context:
         self._check(self.L.gbhf_profile_reset(self.h, 1 if events else 0))
 
     def profile_read(self):
-        v = np.zeros(19)
-        self._check(self.L.gbhf_profile_read(self.h, _d(v), 19))
+        v = np.zeros(20)
+        self._check(self.L.gbhf_profile_read(self.h, _d(v), 20))
         keys = ("jk_ms_fp64", "jk_ms_fp32", "prim_quartets_fp64", "prim_quartets_fp32", "shell_quartets",
                 "fn_quartets", "launches", "dense_ms", "ms_setup", "ms_fock", "ms_diis", "ms_diag", "ms_other",
-                "jacobi_sweeps", "jacobi_calls", "ms_grad", "batch_steps", "purify_steps", "purify_calls")
+                "jacobi_sweeps", "jacobi_calls", "ms_grad", "batch_steps", "purify_steps", "purify_calls", "ms_pairs")
         return dict(zip(keys, v.tolist()))
 
     CLASSES = ("ssss", "psss", "psps", "ppss", "ppps", "pppp", "dsss", "dsps", "dspp", "dsds", "dpss", "dpps",

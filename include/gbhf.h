@@ -269,13 +269,14 @@ gbhf_status gbhf_scf_batch(gbhf_ctx* ctx, int n_mol, const int* atom_off, const 
 
 /* Measurement hooks: device-time of the J/K kernels since the last reset
  * (CUDA events on the context stream), launches issued by the library, and
- * per-kernel-class statistics.  stats[0..18]: J/K milliseconds FP64, FP32,
+ * per-kernel-class statistics.  stats[0..19]: J/K milliseconds FP64, FP32,
  * primitive quartets FP64, FP32, shell quartets, function quartets,
  * total library kernel launches, dense linear-algebra milliseconds, then
  * host wall milliseconds of the SCF phases (setup, Fock, DIIS,
  * diagonalisation, other), Jacobi sweeps and Jacobi calls, milliseconds of
  * the batched gradients, steps of the last batched SCF, purification steps
- * and calls (single-molecule density builds). */
+ * and calls (single-molecule density builds), host milliseconds of the
+ * shell-pair setup. */
 gbhf_status gbhf_profile_reset(gbhf_ctx* ctx, int enable_events);
 gbhf_status gbhf_profile_read(gbhf_ctx* ctx, double* stats, int n_stats);
 /* Per ERI class and precision (FP64, FP32) since the last reset:
