@@ -174,6 +174,22 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+def autotune_jk(ctx, fb, args):
+    """Tune the J/K task budgets on the workload's basis (SAD density, mixed
+    precision) before the warm-up; returns a summary for the JSON line."""
+    from gbhf import _lib
+    if args.no_autotune:
+        return {"enabled": False}
+    ctx.set_basis(fb)
+    t0 = time.perf_counter()
+    ms0, ms1 = ctx.autotune(0, _lib.PREC_MIXED, 1e-12, 1e-4)
+    dt = time.perf_counter() - t0
+    tab = ctx.task_budgets(0)
+    changed = {name: [int(x) for x in tab[k]] for k, name in enumerate(ctx.CLASSES) if ms1[k] < ms0[k]}
+    return {"enabled": True, "tuning_s": dt, "jk_ms_default": float(ms0.sum()), "jk_ms_tuned": float(ms1.sum()),
+            "changed_budgets": changed}
+
+
 def run_gbhf(args, world, rank, local):
     import numpy as np
     from gbhf import _lib, basis as B, molecules as M
@@ -191,6 +207,7 @@ def run_gbhf(args, world, rank, local):
         ctx.event_record(1)
         return r, ctx.event_elapsed(0, 1)
 
+    tune = autotune_jk(ctx, fb, args)
     for _ in range(max(args.warmup, 3)):
         step(mixed)
     # plain FP64 GPU SCF, once (reported beside the headline)
@@ -262,6 +279,7 @@ def run_gbhf(args, world, rank, local):
                                                                   "ms_other")},
         "jacobi_sweeps_per_call": prof["jacobi_sweeps"] / max(prof["jacobi_calls"], 1),
         "gpu_launches": int(prof["launches"]),
+        "autotune": tune,
         "roofline": {"kernel": f"k_jk<{cname}, {prec}>", "bound": f"{prec} CUDA-core pipe", "achieved": achieved,
                      "timing": "CUDA events around each launch of this class in one profiling SCF run after "
                                "the timed steps (class launches serialised on one stream)",
@@ -302,6 +320,15 @@ def run_batch(args, world, rank, local):
     mixed = _lib.baseline_opts(precision=_lib.PREC_MIXED, incremental=1, final_fp64=0, full_rebuild_every=0,
                                mixed_cutoff=args.mixed_cutoff, grad_mixed_cutoff=args.grad_mixed_cutoff)
     ctx.scf_batch(sub[:16], mixed, gradients=True)          # warm-up (tables, SAD atoms)
+    tune = {"enabled": not args.no_autotune}
+    if not args.no_autotune:
+        # tune the J/K and gradient budgets on the whole batch once (untimed)
+        mixed.autotune = 1
+        t0 = time.perf_counter()
+        ctx.scf_batch(sub, mixed, gradients=True)
+        tune["tuning_run_s"] = time.perf_counter() - t0
+        tune["jk_budgets"] = ctx.task_budgets(0).tolist()
+        tune["grad_budgets"] = ctx.task_budgets(1).tolist()
     barrier(world)
     ctx.profile_reset(events=False)
     t0 = time.perf_counter()
@@ -334,7 +361,7 @@ def run_batch(args, world, rank, local):
             "max_abs_grad_mixed_vs_fp64_sample": float(max(dg)) if dg else None,
             "mixed_cutoff": args.mixed_cutoff, "grad_mixed_cutoff": args.grad_mixed_cutoff or args.mixed_cutoff,
             "sample": f"FP64 one-at-a-time SCF + gradient timed on {len(sample)} of {len(sub)} molecules and scaled",
-            "batch_steps": int(prof["batch_steps"]), "gpu_launches": int(prof["launches"]),
+            "batch_steps": int(prof["batch_steps"]), "gpu_launches": int(prof["launches"]), "autotune": tune,
             "phases_ms": {k: prof[k] for k in ("ms_pairs", "ms_setup", "ms_fock", "ms_diis", "ms_diag", "ms_other",
                                                "ms_grad")},
             "jk_prim_quartets": prof["prim_quartets_fp64"] + prof["prim_quartets_fp32"],
@@ -466,6 +493,7 @@ def main():
     ap.add_argument("--workload", default="w16", choices=["w16", "batch256", "grad8", "w64", "w16d", "fock"])
     ap.add_argument("--quick", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default task budgets")
     ap.add_argument("--mixed-cutoff", type=float, default=1e-2,
                     help="batch256: Schwarz-bound cutoff below which ERIs run in FP32 (the workload leaves "
                          "it free; 1e-2 keeps |dE| vs FP64 near 1e-8 Eh)")

@@ -79,6 +79,9 @@ gbhf_status gbhf_create(gbhf_ctx** out, int device) {
   for (auto& e : c->ev) cudaEventCreate(&e);
   for (auto& e : c->evc) cudaEventCreate(&e);
   for (auto& e : c->evu) cudaEventCreate(&e);
+  for (auto& e : c->evg) cudaEventCreate(&e);
+  default_budgets(c, 0);
+  default_budgets(c, 1);
   for (int i = 0; i < gbhf_ctx::NSIDE; ++i) {
     if (cudaStreamCreateWithFlags(&c->side[i], cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->join_ev[i], cudaEventDisableTiming) != cudaSuccess) {
@@ -103,6 +106,8 @@ gbhf_status gbhf_destroy(gbhf_ctx* c) {
   for (auto& e : c->evc)
     if (e) cudaEventDestroy(e);
   for (auto& e : c->evu)
+    if (e) cudaEventDestroy(e);
+  for (auto& e : c->evg)
     if (e) cudaEventDestroy(e);
   for (int i = 0; i < gbhf_ctx::NSIDE; ++i) {
     if (c->side[i]) {
@@ -489,6 +494,72 @@ gbhf_status gbhf_gradient(gbhf_ctx* c, int precision, double schwarz_cutoff, con
   // Q_ab Q_cd max(w)^2 is below 1e-4, the SCF's mixed cutoff
   GBHF_TRY(gradient_dev(c, D, W, schwarz_cutoff, 1e-4, precision, g.p));
   return download(c, grad, g.p, 3 * (size_t)na * sizeof(double));
+}
+
+static int budget_classes(int which) { return which == 0 ? NCOMBO : which == 1 ? NCOMBO_MAX : 0; }
+
+gbhf_status gbhf_get_task_budgets(gbhf_ctx* c, int which, int* budgets, int n) {
+  CTX_CHECK(c);
+  const int nc = budget_classes(which);
+  if (nc == 0 || !budgets || n < 2 * nc) return fail(c, GBHF_ERR_BAD_INPUT, "bad arguments");
+  const int* lp = which == 0 ? c->jk_lp : c->gr_lp;
+  const int* tk = which == 0 ? c->jk_tk : c->gr_tk;
+  for (int k = 0; k < nc; ++k) {
+    budgets[2 * k] = lp[k];
+    budgets[2 * k + 1] = tk[k];
+  }
+  return GBHF_OK;
+}
+
+gbhf_status gbhf_set_task_budgets(gbhf_ctx* c, int which, const int* budgets, int n) {
+  CTX_CHECK(c);
+  const int nc = budget_classes(which);
+  if (nc == 0 || n < 2 * nc) return fail(c, GBHF_ERR_BAD_INPUT, "bad arguments");
+  if (!budgets) {   // back to the defaults
+    default_budgets(c, which);
+    c->tuned[which] = false;
+  } else {
+    for (int k = 0; k < nc; ++k)
+      if (budgets[2 * k] < 1 || budgets[2 * k] > 65535 || budgets[2 * k + 1] < 1 || budgets[2 * k + 1] > 32)
+        return fail(c, GBHF_ERR_BAD_INPUT, "budgets: primitive quartets per lane 1..65535, kets per task 1..32");
+    int* lp = which == 0 ? c->jk_lp : c->gr_lp;
+    int* tk = which == 0 ? c->jk_tk : c->gr_tk;
+    for (int k = 0; k < nc; ++k) {
+      lp[k] = budgets[2 * k];
+      tk[k] = budgets[2 * k + 1];
+    }
+    c->tuned[which] = true;
+  }
+  if (which == 0) c->tasks.thr_all = -1;   // cached lists follow the old budgets
+  return GBHF_OK;
+}
+
+gbhf_status gbhf_autotune(gbhf_ctx* c, int which, int precision, double schwarz_cutoff, double mixed_cutoff,
+                          const double* density_flat, int repeats, double* class_ms) {
+  CTX_CHECK(c);
+  if (budget_classes(which) == 0) return fail(c, GBHF_ERR_BAD_INPUT, "which must be 0 (J/K) or 1 (gradient)");
+  if (precision != GBHF_PREC_FP64 && precision != GBHF_PREC_MIXED)
+    return fail(c, GBHF_ERR_BAD_INPUT, "precision must be GBHF_PREC_FP64 or GBHF_PREC_MIXED");
+  if (!(schwarz_cutoff >= 0) || !(mixed_cutoff >= 0) || repeats < 1)
+    return fail(c, GBHF_ERR_BAD_INPUT, "cutoffs must be >= 0 and repeats >= 1");
+  if (!need_basis(c)) return GBHF_ERR_BAD_INPUT;
+  const Basis& b = c->basis;
+  if (!b.shells_ok || b.maxL > 2) return fail(c, GBHF_ERR_UNSUPPORTED, "direct builds need complete s, p, d shells");
+  GBHF_TRY(ensure_boys_tables(c));
+  GBHF_TRY(ensure_pairs(c));
+  GBHF_TRY(ensure_shell_arrays(c));
+  const int n = b.nbf;
+  const size_t nn = (size_t)n * n, ntri = (size_t)n * (n + 1) / 2;
+  GBHF_WS(c, D, 15, nn);
+  if (density_flat) {
+    GBHF_WS(c, t, 16, ntri);
+    GBHF_CUDA(c, cudaMemcpyAsync(t, density_flat, ntri * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    GBHF_TRY(flat_to_square(c, n, t, D));
+  } else {
+    GBHF_TRY(sad_density(c, D));
+  }
+  const double mc = precision == GBHF_PREC_FP64 ? 0.0 : mixed_cutoff;
+  return autotune_dev(c, which, D, precision, schwarz_cutoff, mc, repeats, class_ms);
 }
 
 gbhf_status gbhf_profile_reset(gbhf_ctx* c, int enable_events) {

@@ -635,6 +635,10 @@ gbhf_status bscf_run(gbhf_ctx* c, const gbhf_scf_opts* o, double* energies, int*
   }
   GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
   c->prof.ph_setup += ms_since(t_phase);
+  if (o->autotune && !c->tuned[0]) {   // J/K budgets on this basis and starting density
+    GBHF_TRY(autotune_dev(c, 0, D, o->precision, o->schwarz_cutoff,
+                          o->precision == GBHF_PREC_FP64 ? 0.0 : o->mixed_cutoff, 2, nullptr));
+  }
   std::vector<MolDiis> diis(M);
   for (auto& md : diis)
     for (int s = 0; s <= maxstore; ++s) md.free_slots.push_back(s);
@@ -887,8 +891,10 @@ gbhf_status bscf_run(gbhf_ctx* c, const gbhf_scf_opts* o, double* energies, int*
     GBHF_TRY(br.gemm(false, false, 0.5, T1, Dg, 0.0, Wm, true));
     DBuf<double> dgrad;
     GBHF_CUDA(c, dgrad.alloc(3 * (size_t)b.natoms));
-    GBHF_TRY(gradient_dev(c, Dg, Wm, o->schwarz_cutoff > 0 ? o->schwarz_cutoff : 1e-12,
-                          o->grad_mixed_cutoff > 0 ? o->grad_mixed_cutoff : o->mixed_cutoff, o->precision, dgrad.p));
+    const double gs = o->schwarz_cutoff > 0 ? o->schwarz_cutoff : 1e-12;
+    const double gm = o->grad_mixed_cutoff > 0 ? o->grad_mixed_cutoff : o->mixed_cutoff;
+    if (o->autotune && !c->tuned[1]) GBHF_TRY(autotune_dev(c, 1, Dg, o->precision, gs, gm, 2, nullptr));
+    GBHF_TRY(gradient_dev(c, Dg, Wm, gs, gm, o->precision, dgrad.p));
     GBHF_CUDA(c, cudaMemcpyAsync(grads, dgrad.p, 3 * (size_t)b.natoms * sizeof(double), cudaMemcpyDeviceToHost,
                                  c->stream));
     GBHF_CUDA(c, cudaStreamSynchronize(c->stream));

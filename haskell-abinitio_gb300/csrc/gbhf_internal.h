@@ -258,6 +258,7 @@ struct Profile {
   // host wall-clock per SCF phase (ms): setup, Fock, DIIS, diagonalisation, other; Jacobi sweeps
   double ph_setup = 0, ph_fock = 0, ph_diis = 0, ph_diag = 0, ph_other = 0, jacobi_sweeps = 0, jacobi_calls = 0;
   double ph_grad = 0, batch_steps = 0, purify_steps = 0, purify_calls = 0, ph_pairs = 0;
+  double gcls_ms[NCOMBO_MAX][2] = {};   // per gradient combo and precision: kernel ms (events mode)
 };
 
 }  // namespace gbhf
@@ -310,6 +311,12 @@ struct gbhf_ctx {
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   cudaEvent_t evc[2 * gbhf::NCOMBO + 1] = {};   // per-class J/K launch boundaries (profiling)
   cudaEvent_t evu[8] = {};       // user slots (gbhf_event_record)
+  cudaEvent_t evg[2 * gbhf::NCOMBO_MAX + 1] = {};   // per-combo gradient launch boundaries (profiling)
+  // task budgets of the direct builds per quartet class (J/K) and class pair
+  // (gradient): primitive quartets per lane and task, kets per task
+  int jk_lp[gbhf::NCOMBO_MAX] = {}, jk_tk[gbhf::NCOMBO_MAX] = {};
+  int gr_lp[gbhf::NCOMBO_MAX] = {}, gr_tk[gbhf::NCOMBO_MAX] = {};
+  bool tuned[2] = {false, false};   // budgets chosen by the autotuner or the caller
   // side streams of the J/K build: the class kernels of one build run
   // concurrently so that the tail of one persistent launch overlaps the next
   static constexpr int NSIDE = 4;
@@ -462,6 +469,14 @@ gbhf_status bscf_run(gbhf_ctx* c, const gbhf_scf_opts* o, double* energies, int*
                      double* grads);
 // sad.cu: superposition-of-atomic-densities guess (n x n square, device)
 gbhf_status sad_density(gbhf_ctx* c, double* d_D);
+// Task budgets (tune.cu, jk.cu): defaults, the lane-per-ket test, the
+// autotuner, and the two-electron gradient alone (for the autotuner).
+void default_budgets(gbhf_ctx* c, int which);
+bool lane_per_ket(int which, int k);
+gbhf_status autotune_dev(gbhf_ctx* c, int which, const double* d_D, int precision, double schwarz,
+                         double mixed_cutoff, int reps, double* class_ms);
+gbhf_status grad_2e(gbhf_ctx* c, const double* d_D, double schwarz, double mixed_cutoff, int precision,
+                    double* d_grad);
 // grad.cu: D, W square on the device; gradient (3*natoms) on the device
 gbhf_status gradient_dev(gbhf_ctx* c, const double* d_D, const double* d_W, double schwarz, double mixed_cutoff,
                          int precision, double* d_grad);

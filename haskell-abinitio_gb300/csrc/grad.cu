@@ -298,8 +298,10 @@ bool grad_gen_combo(int k) {
   return k < NGCOMBO_SP || k == 9 || k == 10 || k == 12 || k == 18 || k == 19;
 }
 
-// Two-electron gradient of D (n x n, device) into d_grad (accumulated).
-static gbhf_status grad_2e(gbhf_ctx* c, const double* d_D, double schwarz, double mixed_cutoff, int precision,
+// Two-electron gradient of D (n x n, device) into d_grad (accumulated).  With
+// profiling events the launches run in order on the context stream, each timed
+// into prof.gcls_ms; otherwise round-robin on the side streams.
+gbhf_status grad_2e(gbhf_ctx* c, const double* d_D, double schwarz, double mixed_cutoff, int precision,
                            double* d_grad) {
   GBHF_TRY(build_grad_tasks(c, d_D, schwarz, mixed_cutoff, precision));
   TaskLists& gt = c->gtasks;
@@ -311,8 +313,14 @@ static gbhf_status grad_2e(gbhf_ctx* c, const double* d_D, double schwarz, doubl
     GBHF_TRY(to_float(c, nst, d_D, c->dfloat.p));
   }
   GBHF_CUDA(c, cudaMemsetAsync(gt.counters.p, 0, 2 * NCOMBO_MAX * sizeof(int), c->stream));
-  GBHF_CUDA(c, cudaEventRecord(c->fork_ev, c->stream));
-  for (int i = 0; i < gbhf_ctx::NSIDE; ++i) GBHF_CUDA(c, cudaStreamWaitEvent(c->side[i], c->fork_ev, 0));
+  const bool ev = c->prof.events;
+  int ne = 0, ev_combo[2 * NCOMBO_MAX], ev_prec[2 * NCOMBO_MAX];
+  if (ev) {
+    GBHF_CUDA(c, cudaEventRecord(c->evg[0], c->stream));
+  } else {
+    GBHF_CUDA(c, cudaEventRecord(c->fork_ev, c->stream));
+    for (int i = 0; i < gbhf_ctx::NSIDE; ++i) GBHF_CUDA(c, cudaStreamWaitEvent(c->side[i], c->fork_ev, 0));
+  }
   PairData& P = c->pairs;
   int nl = 0;
   // heaviest first: the d combinations, then the s/p ones
@@ -324,7 +332,7 @@ static gbhf_status grad_2e(gbhf_ctx* c, const double* d_D, double schwarz, doubl
       const int k = order[oi];
       const int nt = gt.hranges[4 * k + 2 * prec + 1] - gt.hranges[4 * k + 2 * prec];
       if (nt <= 0) continue;
-      cudaStream_t strm = c->side[nl++ % gbhf_ctx::NSIDE];
+      cudaStream_t strm = ev ? c->stream : c->side[nl++ % gbhf_ctx::NSIDE];
       if (!grad_gen_combo(k))
         GBHF_TRY(launch_grad_dclass(c, strm, k, prec, d_D, c->dfloat.p, d_grad, nt));
       else if (prec == 0)
@@ -332,11 +340,26 @@ static gbhf_status grad_2e(gbhf_ctx* c, const double* d_D, double schwarz, doubl
       else
         GBHF_TRY(launch_grad_combo<float>(c, strm, k, 1, c->dfloat.p, P.bra32.p, P.ket32.p, c->boysh32.p, d_grad,
                                           nt));
+      if (ev) {
+        ev_combo[ne] = k;
+        ev_prec[ne] = prec;
+        ++ne;
+        GBHF_CUDA(c, cudaEventRecord(c->evg[ne], c->stream));
+      }
     }
   }
-  for (int i = 0; i < gbhf_ctx::NSIDE; ++i) {
-    GBHF_CUDA(c, cudaEventRecord(c->join_ev[i], c->side[i]));
-    GBHF_CUDA(c, cudaStreamWaitEvent(c->stream, c->join_ev[i], 0));
+  if (!ev) {
+    for (int i = 0; i < gbhf_ctx::NSIDE; ++i) {
+      GBHF_CUDA(c, cudaEventRecord(c->join_ev[i], c->side[i]));
+      GBHF_CUDA(c, cudaStreamWaitEvent(c->stream, c->join_ev[i], 0));
+    }
+    return GBHF_OK;
+  }
+  GBHF_CUDA(c, cudaEventSynchronize(c->evg[ne]));
+  for (int e = 0; e < ne; ++e) {
+    float ms = 0;
+    GBHF_CUDA(c, cudaEventElapsedTime(&ms, c->evg[e], c->evg[e + 1]));
+    c->prof.gcls_ms[ev_combo[e]][ev_prec[e]] += ms;
   }
   return GBHF_OK;
 }

@@ -710,21 +710,45 @@ static gbhf_status build_task_lists(gbhf_ctx* c, TaskLists& TL, int ncombo, cons
   return GBHF_OK;
 }
 
-// J/K lists: the classes with bra class >= ket class, unique quartets.
-// lane_prims bounds the primitive quartets one lane evaluates in one task, per
-// class (ss|ss) (ps|ss) (ps|ps) (pp|ss) (pp|ps) (pp|pp): about the same
-// arithmetic per task, so that the longest task - the tail of a persistent
-// launch - stays short.  A task never splits the ket primitives, so a lane
-// always evaluates at least K_ket of them.  For the d classes (a warp per
-// quartet) it bounds the primitive quartets of one quartet in one task.
+// d combos evaluated by the generated lane-per-ket code (few components per
+// quartet); the others go to the warp-per-quartet kernels of jkd.cu.
+static bool gen_dclass(int k) { return (k >= 6 && k <= 11) || k == 15; }
+
+// Default task budgets.  J/K (which 0): lane_prims bounds the primitive
+// quartets one lane evaluates in one task, per class (ss|ss) (ps|ss) (ps|ps)
+// (pp|ss) (pp|ps) (pp|pp) ...: about the same arithmetic per task, so that the
+// longest task - the tail of a persistent launch - stays short.  A task never
+// splits the ket primitives, so a lane always evaluates at least K_ket of them.
+// For the warp-per-quartet d classes it bounds the primitive quartets of one
+// quartet in one task, and such a task holds one quartet (a launch then spreads
+// its quartets over every resident warp).  Gradient (which 1): the derivative
+// code does about twice the ERI work per primitive quartet.
+void default_budgets(gbhf_ctx* c, int which) {
+  static const int jk_lp[NCOMBO] = {256, 128, 48, 48, 16, 8, 48, 16, 8, 8, 16, 8, 36, 36, 36, 16, 36, 36,
+                                    36, 36, 36};
+  static const int jk_tk[NCOMBO] = {32, 32, 32, 32, 32, 32, 32, 32, 32, 32, 32, 32, 1, 1, 1, 32, 1, 1, 1, 1, 1};
+  static const int gr_lp_sp[NGCOMBO_SP] = {128, 64, 24, 64, 24, 8, 24, 8, 4};
+  for (int k = 0; k < NCOMBO_MAX; ++k) {
+    if (which == 0) {
+      c->jk_lp[k] = k < NCOMBO ? jk_lp[k] : 1;
+      c->jk_tk[k] = k < NCOMBO ? jk_tk[k] : 32;
+    } else {
+      c->gr_lp[k] = k < NGCOMBO_SP ? gr_lp_sp[k] : (grad_gen_combo(k) ? 8 : 36);
+      c->gr_tk[k] = grad_gen_combo(k) ? 32 : 1;
+    }
+  }
+}
+
+// Kets per task: 32 (a lane per ket) for the lane-per-ket classes, else free.
+bool lane_per_ket(int which, int k) {
+  return which == 0 ? (k < NCOMBO_SP || gen_dclass(k)) : grad_gen_combo(k);
+}
+
+// J/K lists: the classes with bra class >= ket class, unique quartets, with
+// the context's task budgets.
 static gbhf_status build_tasks(gbhf_ctx* c, double thr_all, double thr64, const double* pw = nullptr,
                                const double* sw = nullptr) {
-  static const int lane_prims[NCOMBO] = {256, 128, 48, 48, 16, 8, 48, 16, 8, 8, 16, 8, 36, 36, 36, 16, 36, 36,
-                                         36, 36, 36};
-  // one quartet per task for the warp-per-quartet classes: a launch then spreads
-  // its quartets over every resident warp
-  static const int task_kets[NCOMBO] = {32, 32, 32, 32, 32, 32, 32, 32, 32, 32, 32, 32, 1, 1, 1, 32, 1, 1, 1, 1, 1};
-  return build_task_lists(c, c->tasks, NCOMBO, COMBO_BRA, COMBO_KET, lane_prims, task_kets, false, false, thr_all,
+  return build_task_lists(c, c->tasks, NCOMBO, COMBO_BRA, COMBO_KET, c->jk_lp, c->jk_tk, false, false, thr_all,
                           thr64, pw, sw);
 }
 
@@ -788,16 +812,8 @@ gbhf_status build_grad_tasks(gbhf_ctx* c, const double* d_D, double cutoff, doub
   TaskLists& gt = c->gtasks;
   GBHF_TRY(density_weights(c, gt, d_D));
   const double t64 = precision == GBHF_PREC_FP64 ? 0.0 : mixed_cutoff;
-  // (bra class, ket class) of the derivative code: about twice the ERI work per primitive quartet;
-  // the d combinations (warp per quartet) bound the primitive quartets of one quartet per task
-  int lp[NCOMBO_MAX], tk[NCOMBO_MAX];
-  static const int lp_sp[NGCOMBO_SP] = {128, 64, 24, 64, 24, 8, 24, 8, 4};
-  for (int k = 0; k < NCOMBO_MAX; ++k) {
-    lp[k] = k < NGCOMBO_SP ? lp_sp[k] : (grad_gen_combo(k) ? 8 : 36);
-    tk[k] = grad_gen_combo(k) ? 32 : 1;
-  }
-  GBHF_TRY(build_task_lists(c, gt, NCOMBO_MAX, GRAD_COMBO_BRA, GRAD_COMBO_KET, lp, tk, true, true, cutoff, t64,
-                            gt.pw.p, gt.sw.p));
+  GBHF_TRY(build_task_lists(c, gt, NCOMBO_MAX, GRAD_COMBO_BRA, GRAD_COMBO_KET, c->gr_lp, c->gr_tk, true, true,
+                            cutoff, t64, gt.pw.p, gt.sw.p));
   return GBHF_OK;
 }
 
@@ -849,9 +865,6 @@ static gbhf_status launch_class(gbhf_ctx* c, cudaStream_t strm, int combo, int p
   return GBHF_OK;
 }
 
-// d combos evaluated by the generated lane-per-ket code (few components per
-// quartet); the others go to the warp-per-quartet kernels of jkd.cu.
-static bool gen_dclass(int k) { return (k >= 6 && k <= 11) || k == 15; }
 
 gbhf_status jk_build(gbhf_ctx* c, const double* d_Dsq, double* d_G, int precision, double schwarz,
                      double mixed_cutoff, double weight, bool local_weights, bool with_j) {

@@ -195,6 +195,10 @@ gbhf_status scf_run(gbhf_ctx* c, const gbhf_scf_opts* o, gbhf_result* r) {
     GBHF_TRY(new_density(H, D));
   }
   if (!ref) eri.release();
+  if (o->autotune && !ref && !c->tuned[0]) {
+    GBHF_TRY(autotune_dev(c, 0, D, o->precision, o->schwarz_cutoff,
+                          o->precision == GBHF_PREC_FP64 ? 0.0 : o->mixed_cutoff, 2, nullptr));
+  }
   // DIIS history buffers: slots in c->w beyond the driver's
   const int maxstore = std::max(o->diis_size - 1, 0);
   std::vector<DBuf<double>> hbuf(2 * (maxstore + 1));

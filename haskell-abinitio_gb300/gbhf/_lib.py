@@ -43,7 +43,7 @@ class SCFOpts(C.Structure):
                 ("final_fp64", C.c_int), ("ref_stop_rule", C.c_int), ("conv_error", C.c_double),
                 ("conv_energy", C.c_double), ("conv_density", C.c_double), ("diis_start", C.c_double),
                 ("schwarz_cutoff", C.c_double), ("mixed_cutoff", C.c_double), ("charge", C.c_double),
-                ("grad_mixed_cutoff", C.c_double)]
+                ("grad_mixed_cutoff", C.c_double), ("autotune", C.c_int)]
 
 
 class UHFResultC(C.Structure):
@@ -111,6 +111,9 @@ def load():
         "gbhf_event_elapsed": (st, [_vp, C.c_int, C.c_int, _dp]),
         "gbhf_flush_l2": (st, [_vp]),
         "gbhf_peak_flops": (st, [_vp, C.c_int, _dp]),
+        "gbhf_get_task_budgets": (st, [_vp, C.c_int, _ip, C.c_int]),
+        "gbhf_set_task_budgets": (st, [_vp, C.c_int, _ip, C.c_int]),
+        "gbhf_autotune": (st, [_vp, C.c_int, C.c_int, C.c_double, C.c_double, _dp, C.c_int, _dp]),
     }
     for name, (res, args) in sigs.items():
         f = getattr(L, name)
@@ -435,6 +438,42 @@ class Context:
 
     def flush_l2(self):
         self._check(self.L.gbhf_flush_l2(self.h))
+
+    # -- task budgets and the autotuner --------------------------------------
+    GRAD_PAIRS = ("ss", "ps", "pp", "ds", "dp", "dd")
+
+    def budget_classes(self, which):
+        """Class names of the budget table: J/K quartet classes (which 0) or
+        gradient (bra pair class, ket pair class) combinations (which 1)."""
+        if which == 0:
+            return self.CLASSES
+        return tuple(f"{a}|{b}" for a in self.GRAD_PAIRS for b in self.GRAD_PAIRS)
+
+    def task_budgets(self, which=0):
+        """int array (classes, 2): primitive quartets per lane, kets per task."""
+        n = len(self.budget_classes(which))
+        v = np.zeros(2 * n, dtype=np.int32)
+        self._check(self.L.gbhf_get_task_budgets(self.h, which, _i(v), 2 * n))
+        return v.reshape(n, 2)
+
+    def set_task_budgets(self, which, budgets=None):
+        """Set the budget table (classes, 2), or restore the defaults (None)."""
+        n = len(self.budget_classes(which))
+        if budgets is None:
+            self._check(self.L.gbhf_set_task_budgets(self.h, which, None, 2 * n))
+            return
+        v = np.ascontiguousarray(budgets, dtype=np.int32).reshape(-1)
+        self._check(self.L.gbhf_set_task_budgets(self.h, which, _i(v), v.size))
+
+    def autotune(self, which=0, precision=PREC_MIXED, schwarz=1e-12, mixed=1e-4, d_flat=None, repeats=2):
+        """Tune the budgets on the current basis; returns (ms before, ms after) per class."""
+        n = len(self.budget_classes(which))
+        ms = np.zeros(2 * n)
+        dd = None if d_flat is None else _f64(d_flat)
+        d = None if dd is None else _d(dd)
+        self._check(self.L.gbhf_autotune(self.h, which, precision, schwarz, mixed, d, repeats, _d(ms)))
+        ms = ms.reshape(n, 2)
+        return ms[:, 0].copy(), ms[:, 1].copy()
 
     def peak_flops(self, precision):
         t = C.c_double(0)

@@ -86,6 +86,9 @@ typedef struct {
   double charge;         /* total charge; n_occ = floor((sum Z - charge)/2) (HartreeFock.hs:75-76) */
   double grad_mixed_cutoff; /* gbhf_scf_batch gradients, mixed precision: FP32 derivative integrals for
                                quartets with bound Q_ab Q_cd max(w)^2 below this (0: mixed_cutoff) */
+  int autotune;          /* 1: unless this context already holds tuned task budgets, run gbhf_autotune
+                            on the call's basis before the first step (J/K, with the starting density)
+                            and, in gbhf_scf_batch, before the gradients (with their density) */
 } gbhf_scf_opts;
 
 /* Result buffers are caller-owned; any pointer may be NULL.  Sizes:
@@ -266,6 +269,29 @@ gbhf_status gbhf_scf_batch(gbhf_ctx* ctx, int n_mol, const int* atom_off, const 
                            const int* cgf_lxyz, const int* cgf_nprim, const double* prim_coef,
                            const double* prim_exp, const gbhf_scf_opts* opts, double* energies,
                            int* iterations, int* converged, double* grads);
+
+/* Task budgets of the direct builds (no counterpart in the reference).  A
+ * class's task list splits its work into tasks of (bra pair, up to
+ * kets_per_task kets, a range of bra primitives) with at most
+ * prim_quartets_per_lane primitive quartets per lane and task.  which = 0:
+ * J/K, 21 quartet classes in the order of gbhf_profile_classes; which = 1:
+ * gradient, 36 (bra class, ket class) pairs, pair classes ss, ps, pp, ds, dp,
+ * dd, bra-major.  budgets[2k] = prim_quartets_per_lane (1..65535),
+ * budgets[2k+1] = kets_per_task (1..32; the lane-per-ket classes take 32);
+ * n >= 2 x classes.  gbhf_set_task_budgets with budgets == NULL restores the
+ * defaults. */
+gbhf_status gbhf_get_task_budgets(gbhf_ctx* ctx, int which, int* budgets, int n);
+gbhf_status gbhf_set_task_budgets(gbhf_ctx* ctx, int which, const int* budgets, int n);
+/* Autotuner: times every class's launch of the J/K (which 0) or two-electron
+ * gradient (which 1) build on the current basis under candidate budgets
+ * (primitive quartets per lane x 1/4 .. 4, then kets per task 1, 2, 4, 8 for
+ * the warp-per-quartet d classes), each candidate the minimum of `repeats`
+ * builds with the density density_flat (N(N+1)/2; NULL: the SAD guess), and
+ * keeps per class the fastest when it beats the current budget by more than
+ * 3%.  class_ms (may be NULL; 2 x classes) receives per class the
+ * milliseconds before and after. */
+gbhf_status gbhf_autotune(gbhf_ctx* ctx, int which, int precision, double schwarz_cutoff, double mixed_cutoff,
+                          const double* density_flat, int repeats, double* class_ms);
 
 /* Measurement hooks: device-time of the J/K kernels since the last reset
  * (CUDA events on the context stream), launches issued by the library, and
