@@ -138,16 +138,243 @@ __global__ void k_onee(bool ref, int nbf, const int* __restrict__ fmol, const in
   }
 }
 
+// Exact mode with complete shells: one warp per shell pair (A, B) of a
+// molecule, l_A >= l_B, every component pair at once.  The primitive pairs'
+// Obara-Saika tables (overlap, kinetic) and Hermite E coefficients serve all
+// NA x NB components, and the nuclear-attraction R^n_tuv of one (primitive
+// pair, atom) all of them too; lanes take primitive pairs, and when a pair has
+// fewer primitive pairs than lanes, slices of the molecule's atoms as well.
+// Component integrals use the first component's contraction coefficients
+// times the shells' component ratios (d shells).  Same formulas as k_onee.
+__host__ __device__ constexpr int cart_l(int L, int k, int axis) {
+  // components in createCGF order: x, y, z; xx, xy, xz, yy, yz, zz
+  return L == 0 ? 0
+         : L == 1 ? (k == axis ? 1 : 0)
+                  : (axis == 0 ? (k == 0 ? 2 : (k == 1 || k == 2) ? 1 : 0)
+                     : axis == 1 ? (k == 3 ? 2 : (k == 1 || k == 4) ? 1 : 0)
+                                 : (k == 5 ? 2 : (k == 2 || k == 4) ? 1 : 0));
+}
+
+struct OneeArgs {
+  const int2* pairs;
+  int npairs;
+  int nbf;
+  const int *f0, *smol, *mfo, *mao, *mn, *fn;
+  const long long* moff;   // stacked output (nullptr: flat upper triangle of one molecule)
+  const double *xyz, *Z, *coef, *expo, *tab, *sscale;
+  double *S, *H;
+};
+
+constexpr int ONEE_WARPS = 4;
+
+template <int N>
+__device__ __forceinline__ void warp_sum_all(double (&v)[N]) {
+#pragma unroll
+  for (int i = 0; i < N; ++i)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v[i] += __shfl_xor_sync(0xffffffffu, v[i], o);
+}
+
+template <int LA, int LB>
+__global__ void __launch_bounds__(ONEE_WARPS * 32) k_onee_sh(OneeArgs a) {
+  constexpr int NA = ncart_c(LA), NB = ncart_c(LB), NAB = NA * NB, L = LA + LB;
+  const int w = blockIdx.x * ONEE_WARPS + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (w >= a.npairs) return;   // whole warps
+  const int2 pr = a.pairs[w];
+  const int A = pr.x, B = pr.y;
+  const int mol = a.smol[A];
+  const int fa = a.mfo[mol] + a.f0[A], fb = a.mfo[mol] + a.f0[B];
+  const DevFn f = load_fn(a.fn, fa), g = load_fn(a.fn, fb);
+  const double* RA = a.xyz + 3 * f.atom;
+  const double* RB = a.xyz + 3 * g.atom;
+  const int kb = f.np * g.np;
+  double sv[NAB], tv[NAB], vv[NAB];
+#pragma unroll
+  for (int i = 0; i < NAB; ++i) sv[i] = tv[i] = vv[i] = 0.0;
+  // overlap and kinetic (sijContracted / tijContracted, IntegralsEvaluation.hs:181-206, 252-280)
+  for (int kp = lane; kp < kb; kp += 32) {
+    const int p1 = kp / g.np, p2 = kp - p1 * g.np;
+    const double c1 = a.coef[f.off + p1], e1 = a.expo[f.off + p1];
+    const double c2 = a.coef[g.off + p2], e2 = a.expo[g.off + p2];
+    const double p = e1 + e2, mu = e1 * e2 / p, cte = sqrt(GBHF_PI / p);
+    double sx[3][LA + 1][LB + 1], tx[3][LA + 1][LB + 1];
+#pragma unroll
+    for (int x = 0; x < 3; ++x) {
+      const double P = (e1 * RA[x] + e2 * RB[x]) / p, ab = RA[x] - RB[x];
+      double st[3][5];
+      os_table(p, exp(-mu * ab * ab) * cte, P - RA[x], P - RB[x], LA, LB + 2, st);
+#pragma unroll
+      for (int i = 0; i <= LA; ++i)
+#pragma unroll
+        for (int j = 0; j <= LB; ++j) {
+          sx[x][i][j] = st[i][j];
+          tx[x][i][j] = -2.0 * e2 * e2 * st[i][j + 2] + e2 * (2 * j + 1) * st[i][j] -
+                        (j >= 2 ? 0.5 * j * (j - 1) * st[i][j - 2] : 0.0);
+        }
+    }
+    const double cc = c1 * c2;
+#pragma unroll
+    for (int ia = 0; ia < NA; ++ia)
+#pragma unroll
+      for (int ib = 0; ib < NB; ++ib) {
+        const int ax = cart_l(LA, ia, 0), ay = cart_l(LA, ia, 1), az = cart_l(LA, ia, 2);
+        const int bx = cart_l(LB, ib, 0), by = cart_l(LB, ib, 1), bz = cart_l(LB, ib, 2);
+        const double X = sx[0][ax][bx], Y = sx[1][ay][by], Zs = sx[2][az][bz];
+        sv[ia * NB + ib] += cc * (X * Y * Zs);
+        tv[ia * NB + ib] += cc * (tx[0][ax][bx] * Y * Zs + X * tx[1][ay][by] * Zs + X * Y * tx[2][az][bz]);
+      }
+  }
+  // nuclear attraction (vijHermite/mcMurchie, IntegralsEvaluation.hs:395-414)
+  const int at0 = a.mao[mol], nat = a.mao[mol + 1] - at0;
+  if (a.H && kb > 0) {
+    const int nch = max(1, min(nat, 32 / kb));
+    const int cs = (nat + nch - 1) / nch;
+    for (int it = lane; it < kb * nch; it += 32) {
+      const int kp = it / nch, ch = it - kp * nch;
+      const int p1 = kp / g.np, p2 = kp - p1 * g.np;
+      const double c1 = a.coef[f.off + p1], e1 = a.expo[f.off + p1];
+      const double c2 = a.coef[g.off + p2], e2 = a.expo[g.off + p2];
+      const double p = e1 + e2, mu = e1 * e2 / p;
+      double P[3];
+      EAx E[3];
+#pragma unroll
+      for (int x = 0; x < 3; ++x) {
+        P[x] = (e1 * RA[x] + e2 * RB[x]) / p;
+        const double ab = RA[x] - RB[x];
+        e_axis(E[x], LA, LB, p, P[x] - RA[x], P[x] - RB[x], exp(-mu * ab * ab));
+      }
+      const double pref = c1 * c2 * 2.0 * (GBHF_PI / p);
+      const int c_end = min(nat, (ch + 1) * cs);
+      for (int cn = at0 + ch * cs; cn < at0 + c_end; ++cn) {
+        const double* Cc = a.xyz + 3 * cn;
+        const double PC[3] = {P[0] - Cc[0], P[1] - Cc[1], P[2] - Cc[2]};
+        double F[L + 1];
+        constexpr int D = L + 1;
+        double R[D * D * D];
+        boys_generic(false, nullptr, a.tab, L, p * (PC[0] * PC[0] + PC[1] * PC[1] + PC[2] * PC[2]), F);
+        hermite_r<L>(L, p, PC[0], PC[1], PC[2], F, R);
+        const double zp = -a.Z[cn] * pref;
+#pragma unroll
+        for (int ia = 0; ia < NA; ++ia)
+#pragma unroll
+          for (int ib = 0; ib < NB; ++ib) {
+            const int ax = cart_l(LA, ia, 0), ay = cart_l(LA, ia, 1), az = cart_l(LA, ia, 2);
+            const int bx = cart_l(LB, ib, 0), by = cart_l(LB, ib, 1), bz = cart_l(LB, ib, 2);
+            double sum = 0;
+#pragma unroll
+            for (int t = 0; t <= ax + bx; ++t)
+#pragma unroll
+              for (int u = 0; u <= ay + by; ++u)
+#pragma unroll
+                for (int v = 0; v <= az + bz; ++v)
+                  sum += E[0].get(ax, bx, t) * E[1].get(ay, by, u) * E[2].get(az, bz, v) * R[(t * D + u) * D + v];
+            vv[ia * NB + ib] += zp * sum;
+          }
+      }
+    }
+  }
+  warp_sum_all(sv);
+  warp_sum_all(tv);
+  warp_sum_all(vv);
+  const int nm = a.mn[mol];
+#pragma unroll
+  for (int ia = 0; ia < NA; ++ia)
+#pragma unroll
+    for (int ib = 0; ib < NB; ++ib) {
+      const int k = ia * NB + ib;
+      if ((k & 31) != lane || (A == B && ia > ib)) continue;
+      const double sc = a.sscale[6 * A + ia] * a.sscale[6 * B + ib];
+      const double s_ = sc * sv[k], h_ = sc * (tv[k] + vv[k]);
+      const int li = a.f0[A] + ia, lj = a.f0[B] + ib;
+      if (a.moff) {
+        const long long o1 = a.moff[mol] + (long long)li * nm + lj, o2 = a.moff[mol] + (long long)lj * nm + li;
+        if (a.S) a.S[o1] = s_, a.S[o2] = s_;
+        if (a.H) a.H[o1] = h_, a.H[o2] = h_;
+      } else {
+        const long o = flat2_dev(a.nbf, fa + ia, fb + ib);
+        if (a.S) a.S[o] = s_;
+        if (a.H) a.H[o] = h_;
+      }
+    }
+}
+
+// Shell pairs (A, B), l_A >= l_B, of each molecule, grouped by pair class.
+static gbhf_status onee_pair_lists(gbhf_ctx* c) {
+  if (c->onee_gen == c->basis_gen) return GBHF_OK;
+  const Basis& b = c->basis;
+  std::vector<int2> lst[NPCLS];
+  const int ns = (int)b.shells.size();
+  std::vector<std::vector<int>> by_mol(b.nmol);
+  for (int A = 0; A < ns; ++A) by_mol[b.shells[A].mol].push_back(A);
+  for (const auto& sh : by_mol)
+    for (size_t ia = 0; ia < sh.size(); ++ia)
+      for (size_t ib = 0; ib <= ia; ++ib) {
+        int x = sh[ia], y = sh[ib];
+        if (b.shells[y].L > b.shells[x].L) std::swap(x, y);
+        lst[pair_class_of(b.shells[x].L, b.shells[y].L)].push_back(make_int2(x, y));
+      }
+  std::vector<int2> all;
+  c->onee_cls[0] = 0;
+  for (int k = 0; k < NPCLS; ++k) {
+    all.insert(all.end(), lst[k].begin(), lst[k].end());
+    c->onee_cls[k + 1] = (int)all.size();
+  }
+  GBHF_CUDA(c, c->onee_pairs.alloc(std::max<size_t>(all.size(), 1)));
+  if (!all.empty())
+    GBHF_CUDA(c, cudaMemcpyAsync(c->onee_pairs.p, all.data(), all.size() * sizeof(int2), cudaMemcpyHostToDevice,
+                                 c->stream));
+  GBHF_CUDA(c, cudaStreamSynchronize(c->stream));   // `all` goes out of scope
+  c->onee_gen = c->basis_gen;
+  return GBHF_OK;
+}
+
+template <int LA, int LB>
+static void onee_sh_class(gbhf_ctx* c, OneeArgs a, int k) {
+  a.pairs = c->onee_pairs.p + c->onee_cls[k];
+  a.npairs = c->onee_cls[k + 1] - c->onee_cls[k];
+  if (a.npairs <= 0) return;
+  k_onee_sh<LA, LB><<<(a.npairs + ONEE_WARPS - 1) / ONEE_WARPS, ONEE_WARPS * 32, 0, c->stream>>>(a);
+  count_launch(c);
+}
+
 static gbhf_status onee_launch(gbhf_ctx* c, bool ref, bool stacked, double* d_S, double* d_H) {
   const Basis& b = c->basis;
   if (b.maxL > 2) return fail(c, GBHF_ERR_UNSUPPORTED, "one-electron integrals support s, p, d functions");
   if (ref && !c->have_grid) return fail(c, GBHF_ERR_BAD_INPUT, "reference mode needs gbhf_set_boys_grid");
   if (!stacked && b.nmol != 1) return fail(c, GBHF_ERR_BAD_INPUT, "flat one-electron matrices need one molecule");
   GBHF_TRY(ensure_shell_arrays(c));
+  const TaskLists& t = c->tasks;
+  if (!ref && b.shells_ok) {
+    GBHF_TRY(onee_pair_lists(c));
+    OneeArgs a;
+    a.nbf = b.nbf;
+    a.f0 = t.f0.p;
+    a.smol = t.smol.p;
+    a.mfo = t.mfo.p;
+    a.mao = t.mao.p;
+    a.mn = t.mn.p;
+    a.fn = c->d_fn.p;
+    a.moff = stacked ? t.moff.p : nullptr;
+    a.xyz = c->d_xyz.p;
+    a.Z = c->d_Z.p;
+    a.coef = c->d_coef.p;
+    a.expo = c->d_exp.p;
+    a.tab = c->boys64.p;
+    a.sscale = t.sscale.p;
+    a.S = d_S;
+    a.H = d_H;
+    onee_sh_class<0, 0>(c, a, 0);
+    onee_sh_class<1, 0>(c, a, 1);
+    onee_sh_class<1, 1>(c, a, 2);
+    onee_sh_class<2, 0>(c, a, 3);
+    onee_sh_class<2, 1>(c, a, 4);
+    onee_sh_class<2, 2>(c, a, 5);
+    GBHF_CUDA(c, cudaGetLastError());
+    return GBHF_OK;
+  }
   int max_fn = 0;
   for (int m = 0; m < b.nmol; ++m) max_fn = std::max(max_fn, b.mol_fn_off[m + 1] - b.mol_fn_off[m]);
   dim3 grid((max_fn + 63) / 64, b.nbf);
-  const TaskLists& t = c->tasks;
   k_onee<<<grid, 64, 0, c->stream>>>(ref, b.nbf, t.fmol.p, t.mfo.p, t.mao.p, stacked ? t.moff.p : nullptr,
                                       c->d_xyz.p, c->d_Z.p, c->d_fn.p, c->d_coef.p, c->d_exp.p, c->boys_ref.p,
                                       c->boys64.p, d_S, d_H);

@@ -287,6 +287,10 @@ struct gbhf_ctx {
   gbhf::TaskLists gtasks;        // gradient task lists
   const int* mol_active = nullptr;   // batched SCF: per molecule 0/1 (device); nullptr = all
   gbhf::GraphCache g_purify, g_bpurify;   // four purification steps (one molecule, batch)
+  // shell pairs of the one-electron kernels, grouped by pair class (basis generation onee_gen)
+  gbhf::DBuf<int2> onee_pairs;
+  int onee_cls[gbhf::NPCLS + 1] = {};
+  long onee_gen = -1;
   // dense work buffers (n*n doubles)
   gbhf::DBuf<double> w[24];
   gbhf::JacobiWork jac;

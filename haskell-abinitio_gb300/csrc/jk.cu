@@ -358,37 +358,48 @@ __global__ void __launch_bounds__(JK_THREADS) k_jk(JKArgs<T> a) {
 
 // ------------------------------------------------------- Schwarz bounds ----
 // Q_AB = sqrt(max_ab (ab|ab)) for the pairs of one class (bra = ket = pair),
-// with the generated FP64 class code; one thread per pair, its primitive
-// pairs staged in its own slice of shared memory.
-constexpr int SCHWARZ_THREADS = 8;   // 8 x 3840 B of staged primitives per block
+// with the generated FP64 class code; one warp per pair, its primitive pairs
+// staged in the warp's slice of shared memory, lanes over (bra primitive,
+// slice of the ket primitives) so that pairs with few primitives still fill
+// the warp.
+constexpr int SCHWARZ_WARPS = 4;   // 4 x 4608 B of staged primitives per block
 
 template <int LA, int LB>
-__global__ void __launch_bounds__(SCHWARZ_THREADS) k_schwarz_cls(int p0, int p1, const int* __restrict__ pK,
-                                                                  const int* __restrict__ poff,
-                                                                  const double* __restrict__ bra, long long npp,
-                                                                  const double* __restrict__ boys,
-                                                                  double* __restrict__ Q) {
+__global__ void __launch_bounds__(SCHWARZ_WARPS * 32) k_schwarz_cls(int p0, int p1, const int* __restrict__ pK,
+                                                                     const int* __restrict__ poff,
+                                                                     const double* __restrict__ bra, long long npp,
+                                                                     const double* __restrict__ boys,
+                                                                     double* __restrict__ Q) {
   constexpr int NA = ncart_c(LA), NB = ncart_c(LB), NAB = NA * NB;
-  __shared__ __align__(16) double sb[SCHWARZ_THREADS][KMAX_PRIM_PAIRS * BRA_SB];
-  const int t = p0 + blockIdx.x * SCHWARZ_THREADS + threadIdx.x;
-  if (t >= p1) return;
+  __shared__ __align__(16) double sb[SCHWARZ_WARPS][KMAX_PRIM_PAIRS * BRA_SB];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int t = p0 + blockIdx.x * SCHWARZ_WARPS + warp;
+  if (t >= p1) return;   // whole warps
   const int K = pK[t];
   const long long o = poff[t];
-  double* s = sb[threadIdx.x];
-  for (int f = 0; f < BRA_NFIELD; ++f)
-    for (int k = 0; k < K; ++k) s[k * BRA_SB + f] = bra[f * npp + o + k];
+  double* s = sb[warp];
+  for (int idx = lane; idx < BRA_NFIELD * K; idx += 32) {
+    const int f = idx / K, k = idx - f * K;
+    s[k * BRA_SB + f] = bra[f * npp + o + k];
+  }
+  __syncwarp();
+  const int nch = max(1, min(K, 32 / max(K, 1)));
+  const int cs = (K + nch - 1) / nch;
   RegAcc<double, NAB * NAB> acc;
   acc.zero();
-  for (int k = 0; k < K; ++k) {
+  for (int it = lane; it < K * nch; it += 32) {
+    const int k = it / nch, ch = it - k * nch;
+    const int k0 = ch * cs, nk = min(K, k0 + cs) - k0;
+    if (nk <= 0) continue;
     auto g = [&](int f) { return s[k * BRA_SB + f]; };
     ClassFn<LA, LB, LA, LB>::template run<double, RegAcc<double, NAB * NAB>>(
-        s, K, BRA_SB, g(BRA_P), g(BRA_INVP), g(BRA_PX), g(BRA_PY), g(BRA_PZ), g(BRA_PAX), g(BRA_PAY), g(BRA_PAZ),
-        g(BRA_PBX), g(BRA_PBY), g(BRA_PBZ), g(BRA_K), boys, acc);
+        s + k0 * BRA_SB, nk, BRA_SB, g(BRA_P), g(BRA_INVP), g(BRA_PX), g(BRA_PY), g(BRA_PZ), g(BRA_PAX), g(BRA_PAY),
+        g(BRA_PAZ), g(BRA_PBX), g(BRA_PBY), g(BRA_PBZ), g(BRA_K), boys, acc);
   }
   double mx = 0;
 #pragma unroll
-  for (int ab = 0; ab < NAB; ++ab) mx = fmax(mx, fabs(acc.get(ab * NAB + ab)));
-  Q[t] = sqrt(mx);
+  for (int ab = 0; ab < NAB; ++ab) mx = fmax(mx, fabs(warp_sum(acc.get(ab * NAB + ab))));
+  if (lane == 0) Q[t] = sqrt(mx);
 }
 
 gbhf_status schwarz_classes_dev(gbhf_ctx* c, const int* cls_start, const int* d_K, const int* d_poff,
@@ -396,13 +407,13 @@ gbhf_status schwarz_classes_dev(gbhf_ctx* c, const int* cls_start, const int* d_
   for (int cl = 0; cl < 3; ++cl) {   // s/p classes; jkd.cu has the d classes
     const int p0 = cls_start[cl], p1 = cls_start[cl + 1];
     if (p1 <= p0) continue;
-    const int blocks = (p1 - p0 + SCHWARZ_THREADS - 1) / SCHWARZ_THREADS;
+    const int blocks = (p1 - p0 + SCHWARZ_WARPS - 1) / SCHWARZ_WARPS, thr = SCHWARZ_WARPS * 32;
     if (cl == 0)
-      k_schwarz_cls<0, 0><<<blocks, SCHWARZ_THREADS, 0, c->stream>>>(p0, p1, d_K, d_poff, d_bra, npp, c->boysh64.p, d_Q);
+      k_schwarz_cls<0, 0><<<blocks, thr, 0, c->stream>>>(p0, p1, d_K, d_poff, d_bra, npp, c->boysh64.p, d_Q);
     else if (cl == 1)
-      k_schwarz_cls<1, 0><<<blocks, SCHWARZ_THREADS, 0, c->stream>>>(p0, p1, d_K, d_poff, d_bra, npp, c->boysh64.p, d_Q);
+      k_schwarz_cls<1, 0><<<blocks, thr, 0, c->stream>>>(p0, p1, d_K, d_poff, d_bra, npp, c->boysh64.p, d_Q);
     else
-      k_schwarz_cls<1, 1><<<blocks, SCHWARZ_THREADS, 0, c->stream>>>(p0, p1, d_K, d_poff, d_bra, npp, c->boysh64.p, d_Q);
+      k_schwarz_cls<1, 1><<<blocks, thr, 0, c->stream>>>(p0, p1, d_K, d_poff, d_bra, npp, c->boysh64.p, d_Q);
     count_launch(c);
     GBHF_CUDA(c, cudaGetLastError());
   }

@@ -403,14 +403,32 @@ gbhf_status ensure_pairs(gbhf_ctx* c) {
     Kp[t] = b.shells[A[t]].np * b.shells[B[t]].np;
     molp[t] = b.shells[A[t]].mol;
   }
-  std::iota(order.begin(), order.end(), 0);
-  std::sort(order.begin(), order.end(), [&](int x, int y) {
-    if (cls[x] != cls[y]) return cls[x] < cls[y];
-    if (molp[x] != molp[y]) return molp[x] < molp[y];
+  // ord0 holds the pairs grouped by class, each class in generation order, i.e.
+  // by molecule when the shells come molecule by molecule: then only the runs of
+  // one (class, molecule) need sorting
+  auto within = [&](int x, int y) {
     if (Kp[x] != Kp[y]) return Kp[x] > Kp[y];
     if (Q[x] != Q[y]) return Q[x] > Q[y];
     return x < y;
-  });
+  };
+  bool mol_ordered = true;
+  for (int s2 = 1; s2 < ns; ++s2) mol_ordered &= b.shells[s2].mol >= b.shells[s2 - 1].mol;
+  if (mol_ordered) {
+    order = ord0;
+    for (int r0 = 0; r0 < np;) {
+      int r1 = r0 + 1;
+      while (r1 < np && cls[order[r1]] == cls[order[r0]] && molp[order[r1]] == molp[order[r0]]) ++r1;
+      std::sort(order.begin() + r0, order.begin() + r1, within);
+      r0 = r1;
+    }
+  } else {
+    std::iota(order.begin(), order.end(), 0);
+    std::sort(order.begin(), order.end(), [&](int x, int y) {
+      if (cls[x] != cls[y]) return cls[x] < cls[y];
+      if (molp[x] != molp[y]) return molp[x] < molp[y];
+      return within(x, y);
+    });
+  }
   PairData& P = c->pairs;
   P.npairs = np;
   P.hA.resize(np);
