@@ -149,12 +149,15 @@ struct Shell {
 // Shell-pair classes (la >= lb): 0 (s,s), 1 (p,s), 2 (p,p), 3 (d,s), 4 (d,p), 5 (d,d).
 constexpr int NPCLS = 6;
 __host__ __device__ constexpr int pair_class_of(int la, int lb) { return la * (la + 1) / 2 + lb; }
-// J/K quartet combos (bra class >= ket class): the six s/p classes first, then
+// J/K quartet combos (one per unordered pair of pair classes): the six s/p classes first, then
 // the fifteen with a d pair (warp-per-quartet kernels).
 constexpr int NCOMBO = 21;
 constexpr int NCOMBO_SP = 6;
-constexpr int COMBO_BRA[NCOMBO] = {0, 1, 1, 2, 2, 2, 3, 3, 3, 3, 4, 4, 4, 4, 4, 5, 5, 5, 5, 5, 5};
-constexpr int COMBO_KET[NCOMBO] = {0, 0, 1, 0, 1, 2, 0, 1, 2, 3, 0, 1, 2, 3, 4, 0, 1, 2, 3, 4, 5};
+// The s/p combos (pp|ss) and (pp|ps) run with the lower pair as the warp-shared
+// bra ((ss|pp), (ps|pp)): their generated code defers the transformation of the
+// per-lane, higher-momentum pair.
+constexpr int COMBO_BRA[NCOMBO] = {0, 1, 1, 0, 1, 2, 3, 3, 3, 3, 4, 4, 4, 4, 4, 5, 5, 5, 5, 5, 5};
+constexpr int COMBO_KET[NCOMBO] = {0, 0, 1, 2, 2, 2, 0, 1, 2, 3, 0, 1, 2, 3, 4, 0, 1, 2, 3, 4, 5};
 // Gradient combos: every ordered (bra class, ket class); the nine s/p ones first.
 constexpr int NCOMBO_MAX = 36;
 constexpr int NGCOMBO_SP = 9;

@@ -100,8 +100,8 @@ struct ClassFn;
 GBHF_CLASS_FN(0, 0, 0, 0, ssss)
 GBHF_CLASS_FN(1, 0, 0, 0, psss)
 GBHF_CLASS_FN(1, 0, 1, 0, psps)
-GBHF_CLASS_FN(1, 1, 0, 0, ppss)
-GBHF_CLASS_FN(1, 1, 1, 0, ppps)
+GBHF_CLASS_FN(0, 0, 1, 1, sspp)
+GBHF_CLASS_FN(1, 0, 1, 1, pspp)
 GBHF_CLASS_FN(1, 1, 1, 1, pppp)
 GBHF_CLASS_FN(2, 0, 0, 0, dsss)
 GBHF_CLASS_FN(2, 0, 1, 0, dsps)
@@ -157,9 +157,13 @@ __global__ void __launch_bounds__(JK_THREADS) k_jk(JKArgs<T> a) {
     const int jk = task.y + (lane & ((1 << lg) - 1));
     const int kb0 = task.w & 0xffff, Kb = (task.w >> 16) - kb0, pb0 = a.poff[ib] + kb0;
     const int K = a.seg[a.kseg[task.y]].z;   // ket primitive pairs, shared by the task's kets
+    // the classes whose per-lane pair has the higher momentum transform it once
+    // per call (ket primitive and bra-primitive range): about one primitive
+    // quartet of extra work per call
+    constexpr int CALLC = (LA + LB < LC + LD) ? 1 : 0;
     int lb = 0;
     for (int l = 0, best = 1 << 30; (1 << l) <= nsl; ++l) {   // fewest primitive quartets per lane
-      const int cost = ((Kb + (1 << l) - 1) >> l) * ((K + (nsl >> l) - 1) / (nsl >> l));
+      const int cost = (((Kb + (1 << l) - 1) >> l) + CALLC) * ((K + (nsl >> l) - 1) / (nsl >> l));
       if (cost <= best) {
         best = cost;
         lb = l;
@@ -735,7 +739,7 @@ static bool gen_dclass(int k) { return (k >= 6 && k <= 11) || k == 15; }
 // its quartets over every resident warp).  Gradient (which 1): the derivative
 // code does about twice the ERI work per primitive quartet.
 void default_budgets(gbhf_ctx* c, int which) {
-  static const int jk_lp[NCOMBO] = {256, 128, 48, 48, 16, 8, 48, 16, 8, 8, 16, 8, 36, 36, 36, 16, 36, 36,
+  static const int jk_lp[NCOMBO] = {256, 128, 48, 96, 32, 8, 48, 16, 8, 8, 16, 8, 36, 36, 36, 16, 36, 36,
                                     36, 36, 36};
   static const int jk_tk[NCOMBO] = {32, 32, 32, 32, 32, 32, 32, 32, 32, 32, 32, 32, 1, 1, 1, 32, 1, 1, 1, 1, 1};
   static const int gr_lp_sp[NGCOMBO_SP] = {128, 64, 24, 64, 24, 8, 24, 8, 4};
@@ -954,8 +958,8 @@ gbhf_status jk_build(gbhf_ctx* c, const double* d_Dsq, double* d_G, int precisio
           case 11: s = launch_class<2, 1, 1, 0, double, true>(c, strm, 11, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boysh64.p, f0, nt[11][0], wj); break;
           case 15: s = launch_class<2, 2, 0, 0, double, true>(c, strm, 15, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boysh64.p, f0, nt[15][0], wj); break;
           case 5: s = launch_class<1, 1, 1, 1, double, true>(c, strm, 5, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boysh64.p, f0, nt[5][0], wj); break;
-          case 4: s = launch_class<1, 1, 1, 0, double, false>(c, strm, 4, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boysh64.p, f0, nt[4][0], wj); break;
-          case 3: s = launch_class<1, 1, 0, 0, double, false>(c, strm, 3, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boysh64.p, f0, nt[3][0], wj); break;
+          case 4: s = launch_class<1, 0, 1, 1, double, false>(c, strm, 4, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boysh64.p, f0, nt[4][0], wj); break;
+          case 3: s = launch_class<0, 0, 1, 1, double, false>(c, strm, 3, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boysh64.p, f0, nt[3][0], wj); break;
           case 2: s = launch_class<1, 0, 1, 0, double, false>(c, strm, 2, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boysh64.p, f0, nt[2][0], wj); break;
           case 1: s = launch_class<1, 0, 0, 0, double, false>(c, strm, 1, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boysh64.p, f0, nt[1][0], wj); break;
           default: s = launch_class<0, 0, 0, 0, double, false>(c, strm, 0, 0, D64, d_G, P.bra64.p, P.ket64.p, c->boysh64.p, f0, nt[0][0], wj); break;
@@ -970,8 +974,8 @@ gbhf_status jk_build(gbhf_ctx* c, const double* d_Dsq, double* d_G, int precisio
           case 11: s = launch_class<2, 1, 1, 0, float, false>(c, strm, 11, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boysh32.p, f0, nt[11][1], wj); break;
           case 15: s = launch_class<2, 2, 0, 0, float, false>(c, strm, 15, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boysh32.p, f0, nt[15][1], wj); break;
           case 5: s = launch_class<1, 1, 1, 1, float, false>(c, strm, 5, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boysh32.p, f0, nt[5][1], wj); break;
-          case 4: s = launch_class<1, 1, 1, 0, float, false>(c, strm, 4, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boysh32.p, f0, nt[4][1], wj); break;
-          case 3: s = launch_class<1, 1, 0, 0, float, false>(c, strm, 3, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boysh32.p, f0, nt[3][1], wj); break;
+          case 4: s = launch_class<1, 0, 1, 1, float, false>(c, strm, 4, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boysh32.p, f0, nt[4][1], wj); break;
+          case 3: s = launch_class<0, 0, 1, 1, float, false>(c, strm, 3, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boysh32.p, f0, nt[3][1], wj); break;
           case 2: s = launch_class<1, 0, 1, 0, float, false>(c, strm, 2, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boysh32.p, f0, nt[2][1], wj); break;
           case 1: s = launch_class<1, 0, 0, 0, float, false>(c, strm, 1, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boysh32.p, f0, nt[1][1], wj); break;
           default: s = launch_class<0, 0, 0, 0, float, false>(c, strm, 0, 1, D32, d_G, P.bra32.p, P.ket32.p, c->boysh32.p, f0, nt[0][1], wj); break;
