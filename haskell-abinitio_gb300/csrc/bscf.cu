@@ -302,6 +302,44 @@ __global__ void k_b_purify_coef(BDesc d, const double* __restrict__ P, const dou
   }
 }
 
+// TC2 purification (one GEMM per step): start P = (hi I - F) / (hi - lo), then
+// P <- P^2 or 2P - P^2, whichever moves tr P toward nocc.
+__global__ void k_b_tc2_init(BDesc d, const double* __restrict__ F, const double* __restrict__ g,
+                             double* __restrict__ P) {
+  BD_ELEMENT;
+  const double lo = g[4 * m], hi = g[4 * m + 1];
+  const double sc = hi > lo ? 1.0 / (hi - lo) : 0.0;
+  P[o + idx] = sc * ((i == j ? hi : 0.0) - F[o + idx]);
+}
+
+// traces of P and P^2 -> coef[4m] = (a, b, 0, tr(P - P^2)) of P' = a P + b P^2;
+// converged molecules leave as in k_b_purify_coef
+__global__ void k_b_tc2_coef(BDesc d, const double* __restrict__ P, const double* __restrict__ P2,
+                             double* __restrict__ coef, const int* __restrict__ nocc, double tol,
+                             int* __restrict__ pact) {
+  const int m = blockIdx.x;
+  if (!d.active[m]) return;
+  const int n = d.n[m];
+  const long long o = d.off[m];
+  double t1 = 0, t2 = 0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    t1 += P[o + (long)i * n + i];
+    t2 += P2[o + (long)i * n + i];
+  }
+  t1 = block_reduce(t1, false);
+  __syncthreads();
+  t2 = block_reduce(t2, false);
+  if (threadIdx.x == 0) {
+    const double den = t1 - t2, ne = (double)nocc[m];
+    const bool sq = fabs(t2 - ne) < fabs(2 * t1 - t2 - ne);
+    coef[4 * m] = sq ? 0.0 : 2.0;
+    coef[4 * m + 1] = sq ? 1.0 : -1.0;
+    coef[4 * m + 2] = 0.0;
+    coef[4 * m + 3] = den;
+    if (fabs(den) < tol * (double)max(1, nocc[m])) pact[m] = 0;
+  }
+}
+
 struct HistPtrs {
   double* p[BMAX_DIIS];
 };
@@ -501,8 +539,12 @@ gbhf_status b_density(BatchRun& br, const double* F, const double* X, double* D,
   gbhf_ctx* c = br.c;
   GBHF_TRY(br.gemm(true, false, 1.0, X, F, 0.0, T1));
   GBHF_TRY(br.gemm(false, false, 1.0, T1, X, 0.0, Fp, true));
+  // trace-correcting purification: a third fewer GEMMs than the canonical one
+  // on water clusters (see purify in linalg.cu)
+  constexpr bool tc2 = true;
   k_b_gershgorin<<<br.M, 256, 0, c->stream>>>(br.desc, Fp, g);
-  k_b_purify_init<<<br.egrid(), 256, 0, c->stream>>>(br.desc, br.d_nocc.p, Fp, g, P);
+  if (tc2) k_b_tc2_init<<<br.egrid(), 256, 0, c->stream>>>(br.desc, Fp, g, P);
+  else k_b_purify_init<<<br.egrid(), 256, 0, c->stream>>>(br.desc, br.d_nocc.p, Fp, g, P);
   count_launch(c, 2);
   std::vector<double> hc(4 * (size_t)br.M);
   // molecules still purifying: a copy of the active flags that k_b_purify_coef clears
@@ -515,6 +557,12 @@ gbhf_status b_density(BatchRun& br, const double* F, const double* X, double* D,
   auto four_steps = [&]() -> gbhf_status {
     for (int k = 0; k < 4; ++k) {
       GBHF_TRY(br.gemm(false, false, 1.0, P, P, 0.0, P2, true, &pd));
+      if (tc2) {
+        k_b_tc2_coef<<<br.M, 256, 0, c->stream>>>(pd, P, P2, coef, br.d_nocc.p, tol, br.d_pact.p);
+        k_b_purify_update<<<br.egrid(), 256, 0, c->stream>>>(pd, coef, P, P2, P2);   // third coefficient 0
+        count_launch(c, 2);
+        continue;
+      }
       GBHF_TRY(br.gemm(false, false, 1.0, P, P2, 0.0, P3, true, &pd));
       k_b_purify_coef<<<br.M, 256, 0, c->stream>>>(pd, P, P2, P3, coef, br.d_nocc.p, tol, br.d_pact.p);
       k_b_purify_update<<<br.egrid(), 256, 0, c->stream>>>(pd, coef, P, P2, P3);

@@ -459,7 +459,7 @@ gbhf_status square_to_flat(gbhf_ctx* c, int n, const double* d_sq, double* d_fla
 gbhf_status symm_ortho_dev(gbhf_ctx* c, int n, const double* d_S, double* d_X);
 // S^-1/2 by Newton-Schulz (GEMMs only); density by canonical purification.
 gbhf_status inv_sqrt_dev(gbhf_ctx* c, int n, const double* d_S, double* d_X, int* iters);
-gbhf_status purify(gbhf_ctx* c, int n, int ne, const double* d_F, double* d_P, double* err_out);
+gbhf_status purify(gbhf_ctx* c, int n, int ne, const double* d_F, double* d_P, double* err_out, bool tc2 = true);
 gbhf_status density_purified_dev(gbhf_ctx* c, int n, const double* d_Fsq, const double* d_X, int nocc,
                                  double* d_Dsq);
 gbhf_status diagonal_hf_dev(gbhf_ctx* c, int n, const double* d_Fsq, const double* d_X, int nocc, double* d_C,

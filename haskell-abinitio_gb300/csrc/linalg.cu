@@ -825,6 +825,7 @@ __global__ void k_purify_coef(int n, const double* __restrict__ P, const double*
 // steps; P2, P3 and tr must be zero at launch.
 struct PurifyArgs {
   int n, ne, nt, ks, kslice, max_steps;
+  int tc2;                          // 1: trace-correcting steps (one GEMM per step), 0: canonical
   double tol;
   double *P, *P2, *P3, *tr, *out;   // out: [0] last tr(P - P^2), [1] steps
   unsigned* bar;
@@ -882,6 +883,28 @@ __global__ void __launch_bounds__(128) k_purify_fused(PurifyArgs a) {
       dgemm_tile(false, false, true, n, n, rt, ct, k0, k1, 1.0, a.P, n, a.P, n, a.P2, n, trp + 1, sm);
     }
     if (!grid_barrier(cnt, gen, a.status)) return;
+    if (a.tc2) {
+      // trace-correcting step: P <- P^2 or 2P - P^2, whichever brings tr toward ne
+      const double t1 = *((volatile double*)trp), t2 = *((volatile double*)(trp + 1));
+      const double den = t1 - t2;
+      if (gt == 0) {
+        a.out[0] = den;
+        a.out[1] = step + 1;
+      }
+      if (fabs(den) < a.tol * max(1, a.ne)) break;   // the same decision in every block
+      const bool sq = fabs(t2 - a.ne) < fabs(2 * t1 - t2 - a.ne);
+      const double ca = sq ? 0.0 : 2.0, cb = sq ? 1.0 : -1.0;
+      double dsum = 0;
+      for (long e = gt; e < nn; e += gs) {
+        const double v = ca * a.P[e] + cb * a.P2[e];
+        a.P[e] = v;
+        a.P2[e] = 0.0;
+        if (e / n == e % n) dsum += v;
+      }
+      block_sum_add(dsum, trq);
+      if (!grid_barrier(cnt, gen, a.status)) return;
+      continue;
+    }
     for (int it = blockIdx.x; it < items; it += gridDim.x) {
       int rt, ct;
       tile_of(it / a.ks, rt, ct);
@@ -923,11 +946,24 @@ __global__ void __launch_bounds__(128) k_purify_fused(PurifyArgs a) {
   }
 }
 
-// Canonical purification (Palser & Manolopoulos, Phys. Rev. B 58, 12704 (1998)):
-// the spectral projector onto the ne lowest eigenvectors of the symmetric F,
-// by trace-conserving cubic polynomials of P, two GEMMs per step.  Returns the
+// TC2 start: the spectrum of F mapped onto [0, 1], reversed (P0 = (hi I - F) / (hi - lo)).
+__global__ void k_tc2_init(int n, const double* __restrict__ F, const double* __restrict__ g, double* __restrict__ P) {
+  const int i = blockIdx.y, j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  const double lo = g[0], hi = g[1];
+  const double sc = hi > lo ? 1.0 / (hi - lo) : 0.0;
+  const double f = F[(long)i * n + j];
+  P[(long)i * n + j] = sc * ((i == j ? hi : 0.0) - f);
+}
+
+// The spectral projector onto the ne lowest eigenvectors of the symmetric F.
+// Trace-correcting purification (TC2; Niklasson, Phys. Rev. B 66, 155115 (2002)):
+// P <- P^2 or 2P - P^2 by the trace, one GEMM per step; on water clusters it
+// needs ~24 steps where the canonical purification (Palser & Manolopoulos,
+// Phys. Rev. B 58, 12704 (1998); trace-conserving cubic polynomials, two GEMMs
+// per step, tc2 = false) needs ~17, so a third fewer GEMMs.  Returns the
 // idempotency error tr(P - P^2) of the result.
-gbhf_status purify(gbhf_ctx* c, int n, int ne, const double* d_F, double* d_P, double* err_out) {
+gbhf_status purify(gbhf_ctx* c, int n, int ne, const double* d_F, double* d_P, double* err_out, bool tc2) {
   const size_t nn = (size_t)n * n;
   GBHF_WS(c, P2, 23, nn);
   GBHF_CUDA(c, c->jac.t1.alloc(nn));
@@ -939,7 +975,8 @@ gbhf_status purify(gbhf_ctx* c, int n, int ne, const double* d_F, double* d_P, d
   GBHF_CUDA(c, c->jac.bar.alloc(2));
   GBHF_CUDA(c, c->dev_status.alloc(1));
   k_gershgorin<<<1, 1024, 0, c->stream>>>(n, d_F, g);
-  k_purify_init<<<dim3((n + 127) / 128, n), 128, 0, c->stream>>>(n, ne, d_F, g, d_P);
+  if (tc2) k_tc2_init<<<dim3((n + 127) / 128, n), 128, 0, c->stream>>>(n, d_F, g, d_P);
+  else k_purify_init<<<dim3((n + 127) / 128, n), 128, 0, c->stream>>>(n, ne, d_F, g, d_P);
   count_launch(c, 2);
   GBHF_CUDA(c, cudaMemsetAsync(P2, 0, nn * sizeof(double), c->stream));
   GBHF_CUDA(c, cudaMemsetAsync(P3, 0, nn * sizeof(double), c->stream));
@@ -956,6 +993,7 @@ gbhf_status purify(gbhf_ctx* c, int n, int ne, const double* d_F, double* d_P, d
   a.kslice = ((n + ks - 1) / ks + SK - 1) / SK * SK;
   a.ks = (n + a.kslice - 1) / a.kslice;
   a.max_steps = 200;
+  a.tc2 = tc2 ? 1 : 0;
   a.tol = 1e-13;   // E[D] is first order in the idempotency error
   a.P = d_P;
   a.P2 = P2;
