@@ -8,7 +8,7 @@
 // 104-123) in the exact mode of scf.cu, for all molecules at once:
 //   * the J/K build is the single-molecule build (the kernels take each
 //     task's molecule from its bra pair), one launch per quartet class;
-//   * the dense steps (DIIS error, orthogonalisation, canonical purification,
+//   * the dense steps (DIIS error, orthogonalisation, trace-correcting purification,
 //     Newton-Schulz S^-1/2) are grouped DMMA GEMMs whose CTAs each own one
 //     32 x 32 tile of one molecule's block;
 //   * per-molecule scalars (DIIS dot products, energies, convergence) come back

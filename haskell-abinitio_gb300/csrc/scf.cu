@@ -133,7 +133,7 @@ gbhf_status scf_run(gbhf_ctx* c, const gbhf_scf_opts* o, gbhf_result* r) {
     GBHF_TRY(inv_sqrt_dev(c, n, S, X, &ns_iters));
   }
   // Per-iteration density: reference mode diagonalises (diagonalHF); exact
-  // mode takes the same projector by canonical purification and diagonalises
+  // mode takes the same projector by purification (trace-correcting) and diagonalises
   // once at the end for the orbitals.
   auto new_density = [&](const double* Fsq, double* Dout) -> gbhf_status {
     if (ref) return diagonal_hf_dev(c, n, Fsq, X, nocc, Cm, Dout, eps, Cp);
