@@ -533,7 +533,7 @@ gbhf_status b_inv_sqrt(BatchRun& br, const double* S, double* X, double* Y, doub
 }
 
 // D_m = X_m (2 P_m) X_m^T with P_m the projector onto the nocc_m lowest
-// eigenvectors of X_m^T F_m X_m (canonical purification, as density_purified_dev).
+// eigenvectors of X_m^T F_m X_m (trace-correcting purification, as density_purified_dev).
 gbhf_status b_density(BatchRun& br, const double* F, const double* X, double* D, double* T1, double* Fp, double* P,
                       double* P2, double* P3, double* g, double* coef) {
   gbhf_ctx* c = br.c;
