@@ -245,8 +245,8 @@ struct TaskLists {
 };
 
 struct JacobiWork {
-  DBuf<double> A, V, rot, red, t1, t2, t3;
-  DBuf<int> partner, sweeps;
+  DBuf<double> A, A2, V, rot, red, t1, t2, t3;
+  DBuf<int> sweeps;
   DBuf<unsigned> bar;
   int grid = 0;
   int last_sweeps = 0;

@@ -6,10 +6,10 @@ namespace gbhf {
 
 struct JacobiArgs {
   int n, m;            // matrix size, padded even size
-  double* A;           // m x m (padded with zeros), destroyed
+  double* A;           // m x m (padded with zeros), destroyed; holds the diagonalised matrix on return
+  double* A2;          // m x m second buffer (rounds alternate between A and A2)
   double* V;           // n x m accumulated rotations (rows n)
-  double* rot;         // per index: alpha, beta (2*m), then t per pair (m/2)
-  int* partner;        // per index
+  double* rot;         // two rounds' rotations: per index alpha, beta (2 x 2m)
   double* red;         // reduction scratch (2 doubles)
   unsigned* bar;       // barrier count, generation (must start at 0)
   int* status;         // device status word (must start at 0)

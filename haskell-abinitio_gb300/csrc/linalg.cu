@@ -440,29 +440,27 @@ gbhf_status gauss_elem_dev_call(gbhf_ctx* c, int m, const double* h_a, const dou
 // GBHF_DEV_ERR_TIMEOUT in *status and every block leaves.
 constexpr long long BARRIER_SPIN_LIMIT = 1ll << 24;
 
-__device__ bool grid_barrier(unsigned* count, unsigned* gen, int* status) {
+// Every block adds one to *count and waits until it reaches epoch + gridDim.x
+// (epoch counts the barriers passed times the grid size, the same in every
+// block), so the last block to arrive releases the others with its own add; the
+// counter starts at 0 with each launch.
+__device__ bool grid_barrier(unsigned* count, unsigned& epoch, int* status) {
   __shared__ int s_ok;
   __syncthreads();
+  epoch += gridDim.x;
   if (threadIdx.x == 0) {
     int ok = 1;
-    volatile unsigned* vgen = gen;
-    const unsigned g = *vgen;
     __threadfence();
-    const unsigned arrived = atomicAdd(count, 1u);
-    if (arrived == gridDim.x - 1) {
-      atomicExch(count, 0u);
-      __threadfence();
-      atomicAdd(gen, 1u);
-    } else {
-      long long it = 0;
-      while (*vgen == g) {
-        if (++it > BARRIER_SPIN_LIMIT || *((volatile int*)status) & GBHF_DEV_ERR_TIMEOUT) {
-          atomicOr(status, GBHF_DEV_ERR_TIMEOUT);
-          ok = 0;
-          break;
-        }
-        __nanosleep(64);
+    atomicAdd(count, 1u);
+    volatile unsigned* vc = count;
+    long long it = 0;
+    while (*vc < epoch) {
+      if (++it > BARRIER_SPIN_LIMIT || *((volatile int*)status) & GBHF_DEV_ERR_TIMEOUT) {
+        atomicOr(status, GBHF_DEV_ERR_TIMEOUT);
+        ok = 0;
+        break;
       }
+      __nanosleep(32);
     }
     __threadfence();
     s_ok = ok;
@@ -487,117 +485,139 @@ __device__ __forceinline__ void pair_of(int r, int k, int m, int& p, int& q) {
   }
 }
 
+// Rotation of the pair (p, q) that zeroes A_pq (Numerical Recipes form):
+// c, s and t = s / c.  Every thread that needs it computes it from the same
+// matrix, so all agree bit for bit.
+__device__ __forceinline__ void jacobi_rot(const double* __restrict__ A, int m, int p, int q, double& c, double& s,
+                                           double& t) {
+  const double app = A[(long)p * m + p], aqq = A[(long)q * m + q], apq = A[(long)p * m + q];
+  c = 1.0;
+  s = 0.0;
+  t = 0.0;
+  if (apq != 0.0 && fabs(apq) > 1e-300 && !(fabs(apq) < 1e-18 * fmax(fabs(app), fabs(aqq)))) {
+    const double theta = (aqq - app) / (2.0 * apq);
+    if (fabs(theta) > 1e150) {
+      t = 0.5 / theta;
+    } else {
+      t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+    }
+    c = rsqrt(t * t + 1.0);
+    s = t * c;
+  }
+}
+
+// One grid barrier per round: the round reads A from one buffer and writes
+// the rotated matrix to the other, each 2 x 2 block's thread computing the two
+// rotations it needs from the unrotated matrix; V takes each round's rotations
+// one round later from the parameters the diagonal blocks' threads stored.
 __global__ void __launch_bounds__(256) k_jacobi(JacobiArgs a) {
   const int m = a.m, n = a.n, half = m / 2;
   const long gt = blockIdx.x * (long)blockDim.x + threadIdx.x;
   const long gs = (long)gridDim.x * blockDim.x;
   unsigned* cnt = a.bar;
-  unsigned* gen = a.bar + 1;
+  unsigned epoch = 0;   // barrier target (grid_barrier)
+  double* buf[2] = {a.A, a.A2};
   // Frobenius norm^2 of A (fixed under rotations)
   if (gt == 0) {
     a.red[0] = 0;
     a.red[1] = 0;
   }
-  if (!grid_barrier(cnt, gen, a.status)) return;
+  if (!grid_barrier(cnt, epoch, a.status)) return;
   {
     double s = 0;
     for (long i = gt; i < (long)m * m; i += gs) s += a.A[i] * a.A[i];
     s = block_reduce(s, false);
     if (threadIdx.x == 0) atomicAdd(&a.red[0], s);
   }
-  if (!grid_barrier(cnt, gen, a.status)) return;
+  if (!grid_barrier(cnt, epoch, a.status)) return;
   const double fro2 = a.red[0];
+  const long nblk = (long)half * half;
+  long g = 0;   // rounds done; round g reads buf[g & 1], writes buf[(g + 1) & 1]
+  // V <- V J for the rotations of round gv (parameters in rot[(gv & 1) * 2m ..])
+  auto apply_v = [&](long gv, long idx) {
+    const int row = (int)(idx / half), P = (int)(idx % half);
+    int p, q;
+    pair_of((int)(gv % (m - 1)), P, m, p, q);
+    const double* rt = a.rot + (gv & 1) * 2 * m;
+    const double vp = a.V[(long)row * m + p], vq = a.V[(long)row * m + q];
+    a.V[(long)row * m + p] = rt[2 * p] * vp + rt[2 * p + 1] * vq;
+    a.V[(long)row * m + q] = rt[2 * q] * vq + rt[2 * q + 1] * vp;
+  };
   int sweep = 0;
   for (; sweep < a.max_sweeps; ++sweep) {
+    const double* Acur = buf[g & 1];
     // convergence test on the off-diagonal norm
     if (gt == 0) a.red[1] = 0;
-    if (!grid_barrier(cnt, gen, a.status)) return;
+    if (!grid_barrier(cnt, epoch, a.status)) return;
     {
       double s = 0;
       for (long i = gt; i < (long)m * m; i += gs) {
         const long r = i / m, cc = i % m;
-        if (r != cc) s += a.A[i] * a.A[i];
+        if (r != cc) s += Acur[i] * Acur[i];
       }
       s = block_reduce(s, false);
       if (threadIdx.x == 0) atomicAdd(&a.red[1], s);
     }
-    if (!grid_barrier(cnt, gen, a.status)) return;
+    if (!grid_barrier(cnt, epoch, a.status)) return;
     const double off2 = a.red[1];
     if (off2 <= a.tol * a.tol * fro2 || off2 == 0.0) break;
-    for (int r = 0; r < m - 1; ++r) {
-      // phase A: rotation per pair
-      for (long k = gt; k < half; k += gs) {
-        int p, q;
-        pair_of(r, (int)k, m, p, q);
-        const double app = a.A[(long)p * m + p], aqq = a.A[(long)q * m + q], apq = a.A[(long)p * m + q];
-        double c = 1.0, s = 0.0, t = 0.0;
-        if (apq != 0.0 && fabs(apq) > 1e-300 && !(fabs(apq) < 1e-18 * fmax(fabs(app), fabs(aqq)))) {
-          const double theta = (aqq - app) / (2.0 * apq);
-          if (fabs(theta) > 1e150) {
-            t = 0.5 / theta;
-          } else {
-            t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
-          }
-          c = rsqrt(t * t + 1.0);
-          s = t * c;
+    for (int r = 0; r < m - 1; ++r, ++g) {
+      const double* Ain = buf[g & 1];
+      double* Aout = buf[(g + 1) & 1];
+      double* rt = a.rot + (g & 1) * 2 * m;
+      for (long idx = gt; idx < nblk + (g > 0 ? (long)n * half : 0); idx += gs) {
+        if (idx >= nblk) {
+          apply_v(g - 1, idx - nblk);   // the previous round's rotations
+          continue;
         }
-        a.rot[2 * p] = c;
-        a.rot[2 * p + 1] = -s;
-        a.rot[2 * q] = c;
-        a.rot[2 * q + 1] = s;
-        a.partner[p] = q;
-        a.partner[q] = p;
-        // stash t for the exact diagonal update (index p slot of red area is not used)
-        a.rot[2 * m + k] = t;
-      }
-      if (!grid_barrier(cnt, gen, a.status)) return;
-      // phase B: 2x2 block updates of A (upper block triangle) and V columns
-      const long nblk = (long)half * half;
-      for (long idx = gt; idx < nblk + (long)n * half; idx += gs) {
-        if (idx < nblk) {
-          const int P = (int)(idx / half), Qb = (int)(idx % half);
-          if (Qb < P) continue;
-          int p1, q1, p2, q2;
-          pair_of(r, P, m, p1, q1);
-          pair_of(r, Qb, m, p2, q2);
-          if (P == Qb) {
-            const double t = a.rot[2 * m + P];
-            const double apq = a.A[(long)p1 * m + q1];
-            a.A[(long)p1 * m + p1] -= t * apq;
-            a.A[(long)q1 * m + q1] += t * apq;
-            if (t != 0.0) {
-              a.A[(long)p1 * m + q1] = 0.0;
-              a.A[(long)q1 * m + p1] = 0.0;
-            }
-          } else {
-            const int ii[2] = {p1, q1}, jj[2] = {p2, q2};
-            double old[2][2];
-            for (int x = 0; x < 2; ++x)
-              for (int y = 0; y < 2; ++y) old[x][y] = a.A[(long)ii[x] * m + jj[y]];
-            for (int x = 0; x < 2; ++x) {
-              const double al_i = a.rot[2 * ii[x]], be_i = a.rot[2 * ii[x] + 1];
-              for (int y = 0; y < 2; ++y) {
-                const double al_j = a.rot[2 * jj[y]], be_j = a.rot[2 * jj[y] + 1];
-                const double v = al_i * al_j * old[x][y] + al_i * be_j * old[x][1 - y] + be_i * al_j * old[1 - x][y] +
-                                 be_i * be_j * old[1 - x][1 - y];
-                a.A[(long)ii[x] * m + jj[y]] = v;
-                a.A[(long)jj[y] * m + ii[x]] = v;
-              }
-            }
-          }
+        const int P = (int)(idx / half), Qb = (int)(idx % half);
+        if (Qb < P) continue;
+        int p1, q1;
+        pair_of(r, P, m, p1, q1);
+        double c1, s1, t1;
+        jacobi_rot(Ain, m, p1, q1, c1, s1, t1);
+        if (P == Qb) {
+          const double app = Ain[(long)p1 * m + p1], aqq = Ain[(long)q1 * m + q1], apq = Ain[(long)p1 * m + q1];
+          Aout[(long)p1 * m + p1] = app - t1 * apq;
+          Aout[(long)q1 * m + q1] = aqq + t1 * apq;
+          const double off = t1 != 0.0 ? 0.0 : apq;
+          Aout[(long)p1 * m + q1] = off;
+          Aout[(long)q1 * m + p1] = off;
+          rt[2 * p1] = c1;
+          rt[2 * p1 + 1] = -s1;
+          rt[2 * q1] = c1;
+          rt[2 * q1 + 1] = s1;
         } else {
-          const long v = idx - nblk;
-          const int row = (int)(v / half), P = (int)(v % half);
-          int p, q;
-          pair_of(r, P, m, p, q);
-          const double vp = a.V[(long)row * m + p], vq = a.V[(long)row * m + q];
-          a.V[(long)row * m + p] = a.rot[2 * p] * vp + a.rot[2 * p + 1] * vq;
-          a.V[(long)row * m + q] = a.rot[2 * q] * vq + a.rot[2 * q + 1] * vp;
+          int p2, q2;
+          pair_of(r, Qb, m, p2, q2);
+          double c2, s2, t2;
+          jacobi_rot(Ain, m, p2, q2, c2, s2, t2);
+          const int ii[2] = {p1, q1}, jj[2] = {p2, q2};
+          const double ali[2] = {c1, c1}, bei[2] = {-s1, s1}, alj[2] = {c2, c2}, bej[2] = {-s2, s2};
+          double old[2][2];
+#pragma unroll
+          for (int x = 0; x < 2; ++x)
+#pragma unroll
+            for (int y = 0; y < 2; ++y) old[x][y] = Ain[(long)ii[x] * m + jj[y]];
+#pragma unroll
+          for (int x = 0; x < 2; ++x)
+#pragma unroll
+            for (int y = 0; y < 2; ++y) {
+              const double v = ali[x] * alj[y] * old[x][y] + ali[x] * bej[y] * old[x][1 - y] +
+                               bei[x] * alj[y] * old[1 - x][y] + bei[x] * bej[y] * old[1 - x][1 - y];
+              Aout[(long)ii[x] * m + jj[y]] = v;
+              Aout[(long)jj[y] * m + ii[x]] = v;
+            }
         }
       }
-      if (!grid_barrier(cnt, gen, a.status)) return;
+      if (!grid_barrier(cnt, epoch, a.status)) return;
     }
   }
+  // the last round's rotations into V, and the final matrix into A
+  if (g > 0)
+    for (long idx = gt; idx < (long)n * half; idx += gs) apply_v(g - 1, idx);
+  if (g & 1)
+    for (long i = gt; i < (long)m * m; i += gs) a.A[i] = a.A2[i];
   if (gt == 0) {
     *a.sweeps_out = sweep;
     if (sweep >= a.max_sweeps) atomicOr(a.status, GBHF_DEV_ERR_NOTCONV);
@@ -644,10 +664,10 @@ gbhf_status eigh(gbhf_ctx* c, int n, const double* d_A, double* d_evals, double*
   JacobiWork& w = c->jac;
   const int mm = std::max(2, n + (n & 1));
   GBHF_CUDA(c, w.A.alloc((size_t)mm * mm));
+  GBHF_CUDA(c, w.A2.alloc((size_t)mm * mm));
   GBHF_CUDA(c, w.V.alloc((size_t)n * mm));
-  GBHF_CUDA(c, w.rot.alloc(3 * (size_t)mm));
+  GBHF_CUDA(c, w.rot.alloc(4 * (size_t)mm));
   GBHF_CUDA(c, w.red.alloc(4));
-  GBHF_CUDA(c, w.partner.alloc(mm));
   GBHF_CUDA(c, w.sweeps.alloc(1));
   GBHF_CUDA(c, w.bar.alloc(2));
   GBHF_CUDA(c, c->dev_status.alloc(1));
@@ -670,9 +690,9 @@ gbhf_status eigh(gbhf_ctx* c, int n, const double* d_A, double* d_evals, double*
   a.n = n;
   a.m = mm;
   a.A = w.A.p;
+  a.A2 = w.A2.p;
   a.V = w.V.p;
   a.rot = w.rot.p;
-  a.partner = w.partner.p;
   a.red = w.red.p;
   a.bar = w.bar.p;
   a.status = c->dev_status.p;
@@ -840,7 +860,7 @@ __global__ void __launch_bounds__(128) k_purify_fused(PurifyArgs a) {
   const int ntile = a.nt * (a.nt + 1) / 2, items = ntile * a.ks;
   const long gt = blockIdx.x * (long)blockDim.x + threadIdx.x, gs = (long)gridDim.x * blockDim.x;
   unsigned* cnt = a.bar;
-  unsigned* gen = a.bar + 1;
+  unsigned epoch = 0;   // barrier target (grid_barrier)
   auto block_sum_add = [&](double v, double* dst) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -866,7 +886,7 @@ __global__ void __launch_bounds__(128) k_purify_fused(PurifyArgs a) {
     for (long i = gt; i < n; i += gs) v += a.P[i * n + i];
     block_sum_add(v, a.tr);
   }
-  if (!grid_barrier(cnt, gen, a.status)) return;
+  if (!grid_barrier(cnt, epoch, a.status)) return;
   int step = 0;
   for (; step < a.max_steps; ++step) {
     double* trp = a.tr + 3 * (step & 1);
@@ -882,7 +902,7 @@ __global__ void __launch_bounds__(128) k_purify_fused(PurifyArgs a) {
       const int k0 = (it % a.ks) * a.kslice, k1 = min(n, k0 + a.kslice);
       dgemm_tile(false, false, true, n, n, rt, ct, k0, k1, 1.0, a.P, n, a.P, n, a.P2, n, trp + 1, sm);
     }
-    if (!grid_barrier(cnt, gen, a.status)) return;
+    if (!grid_barrier(cnt, epoch, a.status)) return;
     if (a.tc2) {
       // trace-correcting step: P <- P^2 or 2P - P^2, whichever brings tr toward ne
       const double t1 = *((volatile double*)trp), t2 = *((volatile double*)(trp + 1));
@@ -902,7 +922,7 @@ __global__ void __launch_bounds__(128) k_purify_fused(PurifyArgs a) {
         if (e / n == e % n) dsum += v;
       }
       block_sum_add(dsum, trq);
-      if (!grid_barrier(cnt, gen, a.status)) return;
+      if (!grid_barrier(cnt, epoch, a.status)) return;
       continue;
     }
     for (int it = blockIdx.x; it < items; it += gridDim.x) {
@@ -911,7 +931,7 @@ __global__ void __launch_bounds__(128) k_purify_fused(PurifyArgs a) {
       const int k0 = (it % a.ks) * a.kslice, k1 = min(n, k0 + a.kslice);
       dgemm_tile(false, false, true, n, n, rt, ct, k0, k1, 1.0, a.P, n, a.P2, n, a.P3, n, trp + 2, sm);
     }
-    if (!grid_barrier(cnt, gen, a.status)) return;
+    if (!grid_barrier(cnt, epoch, a.status)) return;
     const double t1 = *((volatile double*)trp), t2 = *((volatile double*)(trp + 1)),
                  t3 = *((volatile double*)(trp + 2));
     const double den = t1 - t2, num = t2 - t3;
@@ -942,7 +962,7 @@ __global__ void __launch_bounds__(128) k_purify_fused(PurifyArgs a) {
       if (e / n == e % n) dsum += v;
     }
     block_sum_add(dsum, trq);
-    if (!grid_barrier(cnt, gen, a.status)) return;
+    if (!grid_barrier(cnt, epoch, a.status)) return;
   }
 }
 

@@ -19,11 +19,12 @@ namespace {
 constexpr int kMaxN = GBHF_NOALLOC_EIGEN_MAX_N;
 // Layout (doubles): A (kMaxN^2) | V (kMaxN^2) | rot (3 kMaxN) | red (4) | ints (8 doubles' worth)
 constexpr size_t kOffA = 0;
-constexpr size_t kOffV = kOffA + (size_t)kMaxN * kMaxN;
+constexpr size_t kOffA2 = kOffA + (size_t)kMaxN * kMaxN;
+constexpr size_t kOffV = kOffA2 + (size_t)kMaxN * kMaxN;
 constexpr size_t kOffRot = kOffV + (size_t)kMaxN * kMaxN;
-constexpr size_t kOffRed = kOffRot + 3 * (size_t)kMaxN;
+constexpr size_t kOffRed = kOffRot + 4 * (size_t)kMaxN;
 constexpr size_t kOffInts = kOffRed + 4;
-constexpr size_t kScratchDoubles = kOffInts + 8 + (size_t)kMaxN;   // barrier, status, sweeps, partner[kMaxN]
+constexpr size_t kScratchDoubles = kOffInts + 8;   // barrier, status, sweeps
 
 static __device__ __align__(256) double g_eigen_scratch[kScratchDoubles];
 
@@ -74,7 +75,6 @@ extern "C" gbhf_status gbhf_eigen_solve_noalloc(int n, const double* d_a, double
   unsigned* bar = reinterpret_cast<unsigned*>(base + kOffInts);   // [0] count, [1] generation
   int* status = reinterpret_cast<int*>(base + kOffInts + 1);
   int* sweeps = reinterpret_cast<int*>(base + kOffInts + 2);
-  int* partner = reinterpret_cast<int*>(base + kOffInts + 8);
   // the array keeps the previous call's contents: zero what must start at zero
   if (cudaMemsetAsync(base + kOffInts, 0, 3 * sizeof(double), strm) != cudaSuccess) return GBHF_ERR_CUDA;
   gbhf::k_jacobi_init<<<64, 256, 0, strm>>>(n, m, d_a, base + kOffA, base + kOffV);
@@ -83,9 +83,9 @@ extern "C" gbhf_status gbhf_eigen_solve_noalloc(int n, const double* d_a, double
   a.n = n;
   a.m = m;
   a.A = base + kOffA;
+  a.A2 = base + kOffA2;
   a.V = base + kOffV;
   a.rot = base + kOffRot;
-  a.partner = partner;
   a.red = base + kOffRed;
   a.bar = bar;
   a.status = status;

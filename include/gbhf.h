@@ -176,7 +176,7 @@ gbhf_status gbhf_eigen_solve(gbhf_ctx* ctx, int n, const double* a_square, doubl
  * device pointers owned by the caller; `stream` is a cudaStream_t (NULL =
  * the default stream) and the call returns after that stream has finished the
  * work.  The solver's working memory is one static device array sized for
- * n <= GBHF_NOALLOC_EIGEN_MAX_N (about 1 MiB, held by every GPU that loads
+ * n <= GBHF_NOALLOC_EIGEN_MAX_N (about 1.5 MiB, held by every GPU that loads
  * the library until the process exits); larger n returns GBHF_ERR_BAD_INPUT.
  * The first call on a device resolves that array's device address and the
  * launch geometry; make that first call before any stream capture.  All calls
