@@ -202,6 +202,7 @@ struct PairData {
   std::vector<double> hQ;
   DBuf<int> A, B, K, poff, kseg;             // kseg: segment index (global list)
   DBuf<double> Q;
+  DBuf<float> Qf;                  // Q in FP32 (the FP32 kernels' per-quartet density test)
   DBuf<int4> seg_info;                       // (start, end, K, data_off) per segment, all classes
   int nseg_total = 0;
   int seg_cls_start[NPCLS + 1] = {};
@@ -220,6 +221,7 @@ struct PairData {
 struct TaskLists {
   DBuf<int> item_count;    // per (combo, bra) item: [n64, n32]
   DBuf<int> item_off;      // exclusive scan
+  DBuf<int> scan_part;     // per scan tile: sums, then their exclusive scan
   DBuf<int4> tasks64, tasks32;
   DBuf<int> ranges;        // per combo: start64, end64, start32, end32
   DBuf<int> counters;      // per combo & precision: work-queue heads

@@ -80,7 +80,9 @@ struct JKArgs {
   const double* sscale;        // per shell 6 component scales (d shells)
   int with_j;                  // 0: exchange only (the open-shell spin-density build)
   const double* Q;             // Schwarz bound of each pair
+  const float* Qf;             // the same in FP32
   double thr;                  // drop a quartet when Q_ab Q_cd max|D| over its six density blocks is below
+  float thrf;
 };
 
 template <int LA, int LB, int LC, int LD>
@@ -218,7 +220,8 @@ __global__ void __launch_bounds__(JK_THREADS) k_jk(JKArgs<T> a) {
 #pragma unroll
         for (int ibb = 0; ibb < NB; ++ibb) dmx = fmax_t(dmx, fabs_t(Dm[(long long)(b0 + ibb) * n + d0 + id]));
       }
-      keep = a.Q[ib] * a.Q[jk] * (double)dmx >= a.thr;
+      if constexpr (sizeof(T) == 4) keep = a.Qf[ib] * a.Qf[jk] * dmx >= a.thrf;   // no FP64-pipe work
+      else keep = a.Q[ib] * a.Q[jk] * dmx >= a.thr;
     }
     if (keep) {
       const int4 sg = a.seg[a.kseg[jk]];
@@ -518,37 +521,120 @@ __global__ void k_tasks(TaskGenArgs g) {
   }
 }
 
-// Exclusive scan of count[2*i+which] into off (nitems+1 entries), one block.
-__global__ void k_scan2(int n, const int* __restrict__ count, int* __restrict__ off64, int* __restrict__ off32) {
-  __shared__ int s64[1024], s32[1024];
-  const int t = threadIdx.x;
-  const int chunk = (n + 1023) / 1024;
-  const int lo = min(n, t * chunk), hi = min(n, lo + chunk);
-  int a = 0, b = 0;
-  for (int i = lo; i < hi; ++i) {
-    a += count[2 * i];
-    b += count[2 * i + 1];
+// Exclusive scans of count[2 i] and count[2 i + 1] into off64 and off32
+// (n + 1 entries each) in three launches: tile sums, a one-block scan of the
+// tile sums, and the tiles' own scans with their offsets.  A tile is 2048
+// items staged in shared memory with coalesced loads; each thread scans 8
+// consecutive items.
+constexpr int SCAN_THREADS = 256, SCAN_ITEMS = 8, SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
+
+// Exclusive block scan of (a, b) over the block's 256 threads; totals in ta, tb.
+__device__ __forceinline__ void block_exscan2(int& a, int& b, int& ta, int& tb) {
+  __shared__ int wa[SCAN_THREADS / 32], wb[SCAN_THREADS / 32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  int ia = a, ib = b;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int xa = __shfl_up_sync(0xffffffffu, ia, o), xb = __shfl_up_sync(0xffffffffu, ib, o);
+    if (lane >= o) {
+      ia += xa;
+      ib += xb;
+    }
   }
-  s64[t] = a;
-  s32[t] = b;
+  if (lane == 31) {
+    wa[w] = ia;
+    wb[w] = ib;
+  }
   __syncthreads();
-  for (int o = 1; o < 1024; o <<= 1) {
-    int va = t >= o ? s64[t - o] : 0, vb = t >= o ? s32[t - o] : 0;
-    __syncthreads();
-    s64[t] += va;
-    s32[t] += vb;
-    __syncthreads();
+  int pa = 0, pb = 0;
+  ta = 0;
+  tb = 0;
+  for (int k = 0; k < SCAN_THREADS / 32; ++k) {
+    if (k < w) {
+      pa += wa[k];
+      pb += wb[k];
+    }
+    ta += wa[k];
+    tb += wb[k];
   }
-  int ra = s64[t] - a, rb = s32[t] - b;
-  for (int i = lo; i < hi; ++i) {
-    off64[i] = ra;
-    off32[i] = rb;
-    ra += count[2 * i];
-    rb += count[2 * i + 1];
+  a = pa + ia - a;
+  b = pb + ib - b;
+  __syncthreads();
+}
+
+__device__ __forceinline__ void scan_load_tile(int n, const int* __restrict__ count, int tile, int* sm) {
+  const int base = tile * SCAN_TILE;
+  for (int e = threadIdx.x; e < 2 * SCAN_TILE; e += SCAN_THREADS) {
+    const int i = base + e / 2;
+    sm[e] = i < n ? count[2 * (long)base + e] : 0;
   }
-  if (t == 1023) {
-    off64[n] = s64[1023];
-    off32[n] = s32[1023];
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_tiles(int n, const int* __restrict__ count,
+                                                             int* __restrict__ part) {
+  __shared__ int sm[2 * SCAN_TILE];
+  scan_load_tile(n, count, blockIdx.x, sm);
+  int a = 0, b = 0;
+#pragma unroll
+  for (int k = 0; k < SCAN_ITEMS; ++k) {
+    a += sm[2 * (threadIdx.x * SCAN_ITEMS + k)];
+    b += sm[2 * (threadIdx.x * SCAN_ITEMS + k) + 1];
+  }
+  int ta, tb;
+  block_exscan2(a, b, ta, tb);
+  if (threadIdx.x == 0) {
+    part[2 * blockIdx.x] = ta;
+    part[2 * blockIdx.x + 1] = tb;
+  }
+}
+
+// One block: exclusive scan of the tile sums in place, totals into off64[n], off32[n].
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_parts(int ntile, int n, int* __restrict__ part,
+                                                             int* __restrict__ off64, int* __restrict__ off32) {
+  int ca = 0, cb = 0;   // carry over chunks of 256 tiles
+  for (int t0 = 0; t0 < ntile; t0 += SCAN_THREADS) {
+    const int t = t0 + threadIdx.x;
+    int a = t < ntile ? part[2 * t] : 0, b = t < ntile ? part[2 * t + 1] : 0;
+    int ta, tb;
+    block_exscan2(a, b, ta, tb);
+    if (t < ntile) {
+      part[2 * t] = ca + a;
+      part[2 * t + 1] = cb + b;
+    }
+    ca += ta;
+    cb += tb;
+  }
+  if (threadIdx.x == 0) {
+    off64[n] = ca;
+    off32[n] = cb;
+  }
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply(int n, const int* __restrict__ count,
+                                                             const int* __restrict__ part, int* __restrict__ off64,
+                                                             int* __restrict__ off32) {
+  __shared__ int sm[2 * SCAN_TILE];
+  scan_load_tile(n, count, blockIdx.x, sm);
+  int a = 0, b = 0;
+#pragma unroll
+  for (int k = 0; k < SCAN_ITEMS; ++k) {
+    a += sm[2 * (threadIdx.x * SCAN_ITEMS + k)];
+    b += sm[2 * (threadIdx.x * SCAN_ITEMS + k) + 1];
+  }
+  int ta, tb;
+  block_exscan2(a, b, ta, tb);
+  a += part[2 * blockIdx.x];
+  b += part[2 * blockIdx.x + 1];
+  const int i0 = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_ITEMS;
+#pragma unroll
+  for (int k = 0; k < SCAN_ITEMS; ++k) {
+    if (i0 + k < n) {
+      off64[i0 + k] = a;
+      off32[i0 + k] = b;
+    }
+    a += sm[2 * (threadIdx.x * SCAN_ITEMS + k)];
+    b += sm[2 * (threadIdx.x * SCAN_ITEMS + k) + 1];
   }
 }
 
@@ -703,8 +789,14 @@ static gbhf_status build_task_lists(gbhf_ctx* c, TaskLists& TL, int ncombo, cons
     k_tasks<false><<<(ni + 127) / 128, 128, 0, c->stream>>>(g);
     count_launch(c);
   }
-  k_scan2<<<1, 1024, 0, c->stream>>>(ni, TL.item_count.p, off64, off32);
-  count_launch(c);
+  {
+    const int ntile = std::max(1, (ni + SCAN_TILE - 1) / SCAN_TILE);
+    GBHF_CUDA(c, TL.scan_part.alloc(2 * (size_t)ntile));
+    k_scan_tiles<<<ntile, SCAN_THREADS, 0, c->stream>>>(ni, TL.item_count.p, TL.scan_part.p);
+    k_scan_parts<<<1, SCAN_THREADS, 0, c->stream>>>(ntile, ni, TL.scan_part.p, off64, off32);
+    k_scan_apply<<<ntile, SCAN_THREADS, 0, c->stream>>>(ni, TL.item_count.p, TL.scan_part.p, off64, off32);
+    count_launch(c, 3);
+  }
   int tot[2];
   GBHF_CUDA(c, cudaMemcpyAsync(&tot[0], off64 + ni, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   GBHF_CUDA(c, cudaMemcpyAsync(&tot[1], off32 + ni, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
@@ -873,7 +965,9 @@ static gbhf_status launch_class(gbhf_ctx* c, cudaStream_t strm, int combo, int p
   a.sscale = c->tasks.sscale.p;
   a.with_j = with_j;
   a.Q = P.Q.p;
+  a.Qf = P.Qf.p;
   a.thr = c->tasks.thr_exact;
+  a.thrf = (float)c->tasks.thr_exact;
   kern<<<grid, JK_THREADS, smem, strm>>>(a);
   count_launch(c);
   GBHF_CUDA(c, cudaGetLastError());

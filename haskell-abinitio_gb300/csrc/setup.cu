@@ -511,6 +511,9 @@ gbhf_status ensure_pairs(gbhf_ctx* c) {
   GBHF_CUDA(c, up(P.poff.p, P.hPoff.data(), np * sizeof(int)));
   GBHF_CUDA(c, up(P.kseg.p, P.hSeg.data(), np * sizeof(int)));
   GBHF_CUDA(c, up(P.Q.p, P.hQ.data(), np * sizeof(double)));
+  std::vector<float> qf(P.hQ.begin(), P.hQ.end());
+  GBHF_CUDA(c, P.Qf.alloc(std::max(np, 1)));
+  GBHF_CUDA(c, up(P.Qf.p, qf.data(), np * sizeof(float)));
   GBHF_CUDA(c, up(P.seg_info.p, seginfo.data(), seginfo.size() * sizeof(int4)));
   GBHF_CUDA(c, up(P.mol.p, pmol.data(), np * sizeof(int)));
   GBHF_CUDA(c, up(P.mseg.p, P.hmseg.data(), P.hmseg.size() * sizeof(int)));
