@@ -10,7 +10,7 @@
 //     task's molecule from its bra pair), one launch per quartet class;
 //   * the dense steps (DIIS error, orthogonalisation, trace-correcting purification,
 //     Newton-Schulz S^-1/2) are grouped DMMA GEMMs whose CTAs each own one
-//     32 x 32 tile of one molecule's block;
+//     16 x 16 tile of one molecule's block;
 //   * per-molecule scalars (DIIS dot products, energies, convergence) come back
 //     to the host in one read per step; the DIIS linear systems are solved on
 //     the device, one thread per molecule.
@@ -35,7 +35,7 @@ struct BDesc {
   int M;
   const int* n;            // functions per molecule
   const long long* off;    // block offsets
-  const int* tstart;       // first 32 x 32 tile of each molecule (M + 1)
+  const int* tstart;       // first 16 x 16 tile of each molecule (M + 1)
   const int* active;       // per molecule 0/1
 };
 
@@ -49,7 +49,10 @@ __device__ __forceinline__ int bd_mol(const int* tstart, int M, int x) {
   return lo;
 }
 
-constexpr int BT = 32, BKK = 16;
+// 16 x 16 output tiles: with the batch's small blocks, 32 x 32 tiles carried 1.83x the
+// symmetric product's flops in padding, 16 x 16 tiles 1.41x
+constexpr int BT = 16, BKK = 16;
+constexpr int WT = BT / 2, NI = WT / 8;   // per-warp tile (2 x 2 warps), 8 x 8 DMMA tiles per warp side
 
 // C_m = alpha op(A_m) op(B_m) + beta C_m for every active molecule; one 32 x 32
 // tile of one molecule's C per CTA (4 warps of 16 x 16, 2 x 2 DMMA tiles each).
@@ -72,8 +75,8 @@ __global__ void __launch_bounds__(128) k_bgemm(BDesc d, int ta, int tb, int sym,
   __shared__ double As[BT][BKK + 1];
   __shared__ double Bs[BKK][BT + 2];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int wr = (warp >> 1) * 16, wc = (warp & 1) * 16;
-  double acc[2][2][2] = {};
+  const int wr = (warp >> 1) * WT, wc = (warp & 1) * WT;
+  double acc[NI][NI][2] = {};
   for (int kk = 0; kk < n; kk += BKK) {
     for (int idx = tid; idx < BT * BKK; idx += 128) {
       int r, cc;
@@ -106,22 +109,22 @@ __global__ void __launch_bounds__(128) k_bgemm(BDesc d, int ta, int tb, int sym,
     __syncthreads();
 #pragma unroll
     for (int k4 = 0; k4 < BKK; k4 += 4) {
-      double af[2], bf[2];
+      double af[NI], bf[NI];
 #pragma unroll
-      for (int i = 0; i < 2; ++i) af[i] = As[wr + i * 8 + (lane >> 2)][k4 + (lane & 3)];
+      for (int i = 0; i < NI; ++i) af[i] = As[wr + i * 8 + (lane >> 2)][k4 + (lane & 3)];
 #pragma unroll
-      for (int j = 0; j < 2; ++j) bf[j] = Bs[k4 + (lane & 3)][wc + j * 8 + (lane >> 2)];
+      for (int j = 0; j < NI; ++j) bf[j] = Bs[k4 + (lane & 3)][wc + j * 8 + (lane >> 2)];
 #pragma unroll
-      for (int i = 0; i < 2; ++i)
+      for (int i = 0; i < NI; ++i)
 #pragma unroll
-        for (int j = 0; j < 2; ++j) dmma(acc[i][j][0], acc[i][j][1], af[i], bf[j]);
+        for (int j = 0; j < NI; ++j) dmma(acc[i][j][0], acc[i][j][1], af[i], bf[j]);
     }
     __syncthreads();
   }
 #pragma unroll
-  for (int i = 0; i < 2; ++i)
+  for (int i = 0; i < NI; ++i)
 #pragma unroll
-    for (int j = 0; j < 2; ++j)
+    for (int j = 0; j < NI; ++j)
 #pragma unroll
       for (int h = 0; h < 2; ++h) {
         const int r = row0 + wr + i * 8 + (lane >> 2);
