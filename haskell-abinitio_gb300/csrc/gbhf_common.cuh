@@ -8,13 +8,16 @@
 
 // Boys tables: F_m(T_j) on a uniform grid, row j holds m = 0 .. BOYS_NCOL-1.
 #define BOYS_NCOL 16
-// FP64: spacing 0.05 up to 60, 7-term Taylor about the nearest node.  Beyond
-// TMAX the asymptotic form drops a term of relative size
-// exp(-T) T^(m-1/2) / Gamma(m+1/2): below 1e-16 for m <= 9 at T = 60.
-#define BOYS64_H 0.05
+// FP64: spacing 0.025 up to 60, 6-term Taylor about the nearest node (the
+// remainder |dx|^6 / 6! F_(m+6) <= 5e-15 F_m with |dx| <= 0.0125; one FMA per
+// Horner evaluation fewer than 7 terms at spacing 0.05, on the FP64 pipe that
+// bounds the FP64 ERI kernels).  Beyond TMAX the asymptotic form drops a term
+// of relative size exp(-T) T^(m-1/2) / Gamma(m+1/2): below 1e-16 for m <= 9 at
+// T = 60.
+#define BOYS64_H 0.025
 #define BOYS64_TMAX 60.0
-#define BOYS64_NROW 1202
-#define BOYS64_NTERM 7
+#define BOYS64_NROW 2402
+#define BOYS64_NTERM 6
 // FP32: spacing 0.1 up to 36, 5-term Taylor about the nearest node (the
 // asymptotic term above is below 4e-8 for m <= 9 at T = 36).
 #define BOYS32_H 0.1f
@@ -130,7 +133,7 @@ template <int L> struct BoysCfg<float, L> {
 // F_m = (2t F_(m+1) + exp(-t)) / (2m + 1), whose terms are all positive.  Rows are
 // 16-byte aligned and read with vector loads.
 #define BOYSH_LMAX 9   // (dd|dd) gradient: L = 9
-#define BOYSH64_STRIDE 16   // 7 + 7 doubles, the node T_j, padding
+#define BOYSH64_STRIDE 16   // 6 + 6 doubles, the node T_j, padding
 #define BOYSH32_STRIDE 12   // 5 + 5 floats, padded to 16 bytes
 template <typename T> struct BoysHStride;
 template <> struct BoysHStride<double> { static constexpr int S = BOYSH64_STRIDE, NROW = BOYS64_NROW; };
@@ -168,7 +171,7 @@ __device__ __forceinline__ void boys_eval(T t, const T* __restrict__ tab, T* F) 
   using C = BoysCfg<T, L>;
   static_assert(L <= BOYSH_LMAX, "the Boys tables hold orders up to BOYSH_LMAX");
   // Node index and range test in FP32 for FP64 arguments (t truncated to float by
-  // moving its exponent and mantissa bits; |t - T_j| stays within 0.0251), so the
+  // moving its exponent and mantissa bits; |t - T_j| stays within 0.0126), so the
   // FP64 pipe only does dx = T_j - t.
   bool in_table;
   int j;
