@@ -18,12 +18,13 @@
 #define BOYS64_TMAX 60.0
 #define BOYS64_NROW 2402
 #define BOYS64_NTERM 6
-// FP32: spacing 0.1 up to 36, 5-term Taylor about the nearest node (the
-// asymptotic term above is below 4e-8 for m <= 9 at T = 36).
-#define BOYS32_H 0.1f
+// FP32: spacing 0.05 up to 36, 4-term Taylor about the nearest node (remainder
+// |dx|^4 / 4! F_(m+4) <= 1.7e-8 F_m with |dx| <= 0.025, below the FP32 rounding
+// of the sum; the asymptotic term above is below 4e-8 for m <= 9 at T = 36).
+#define BOYS32_H 0.05f
 #define BOYS32_TMAX 36.0f
-#define BOYS32_NROW 362
-#define BOYS32_NTERM 5
+#define BOYS32_NROW 722
+#define BOYS32_NTERM 4
 
 // Bra primitive-pair fields (shared-memory staging and global SoA layout).
 enum {
@@ -134,7 +135,7 @@ template <int L> struct BoysCfg<float, L> {
 // 16-byte aligned and read with vector loads.
 #define BOYSH_LMAX 9   // (dd|dd) gradient: L = 9
 #define BOYSH64_STRIDE 16   // 6 + 6 doubles, the node T_j, padding
-#define BOYSH32_STRIDE 12   // 5 + 5 floats, padded to 16 bytes
+#define BOYSH32_STRIDE 8    // 4 + 4 floats (two 16-byte loads)
 template <typename T> struct BoysHStride;
 template <> struct BoysHStride<double> { static constexpr int S = BOYSH64_STRIDE, NROW = BOYS64_NROW; };
 template <> struct BoysHStride<float> { static constexpr int S = BOYSH32_STRIDE, NROW = BOYS32_NROW; };
