@@ -95,6 +95,10 @@ struct GradArgs {
   const T* boys;
   double* grad;              // 3 * natoms
   const double* sscale;      // per shell 6 component scales (d shells)
+  const double* Q;           // Schwarz bound of each pair, and in FP32
+  const float* Qf;
+  double thr;                // drop a quartet when Q_ab Q_cd max|Gamma_abcd| is below
+  float thrf;
 };
 
 __device__ __forceinline__ double warp_sum_d(double v) {
@@ -161,6 +165,7 @@ __global__ void __launch_bounds__(GR_THREADS) k_grad_jk(GradArgs<T> a) {
     if (active) {
       const int C = a.pA[jk], Dd = a.pB[jk];
       const int c0 = a.shell_f0[C], d0 = a.shell_f0[Dd];
+      T gmax = T(0);
       // Gamma_abcd = D_ab D_cd - (D_ac D_bd + D_ad D_bc) / 4
 #pragma unroll
       for (int ia = 0; ia < NA; ++ia)
@@ -184,12 +189,18 @@ __global__ void __launch_bounds__(GR_THREADS) k_grad_jk(GradArgs<T> a) {
                 if (LD == 2) gv *= T(a.sscale[6 * Dd + id]);
               }
               gam.set(((ia * NB + ibb) * NC + ic) * ND + id, gv);
+              gmax = fmax_t(gmax, fabs_t(gv));
             }
+      // exact screening of this quartet by its own Gamma (the task lists bound it
+      // by the pairs' density weights)
+      bool keep;
+      if constexpr (sizeof(T) == 4) keep = a.Qf[ib] * a.Qf[jk] * gmax >= a.thrf;
+      else keep = a.Q[ib] * a.Q[jk] * gmax >= a.thr;
       const int4 sg = a.seg[a.kseg[jk]];
       const int len = sg.y - sg.x;
       const long long base = (long long)sg.w + (jk - sg.x);
-      const int nbl = sb < Kb ? (Kb - sb + nsb - 1) / nsb : 0;
-      for (int kc = sk; kc < K; kc += nsk) {
+      const int nbl = sb < Kb && keep ? (Kb - sb + nsb - 1) / nsb : 0;
+      for (int kc = sk; keep && kc < K; kc += nsk) {
         const long long idx = base + (long long)kc * len;
         const T q = a.ket[BRA_P * npp + idx];
         const T invq = a.ket[BRA_INVP * npp + idx];
@@ -263,6 +274,10 @@ static gbhf_status launch_grad_class(gbhf_ctx* c, cudaStream_t strm, int combo, 
   a.boys = boys;
   a.grad = grad;
   a.sscale = c->tasks.sscale.p;
+  a.Q = P.Q.p;
+  a.Qf = P.Qf.p;
+  a.thr = gt.thr_exact;
+  a.thrf = (float)gt.thr_exact;
   kern<<<grid, GR_THREADS, smem, strm>>>(a);
   count_launch(c);
   GBHF_CUDA(c, cudaGetLastError());
@@ -305,6 +320,7 @@ gbhf_status grad_2e(gbhf_ctx* c, const double* d_D, double schwarz, double mixed
                            double* d_grad) {
   GBHF_TRY(build_grad_tasks(c, d_D, schwarz, mixed_cutoff, precision));
   TaskLists& gt = c->gtasks;
+  gt.thr_exact = schwarz;   // per-quartet Gamma test in the kernels
   const size_t nst = (size_t)c->basis.stacked;
   bool any32 = false;
   for (int k = 0; k < NCOMBO_MAX; ++k) any32 |= gt.hranges[4 * k + 3] > gt.hranges[4 * k + 2];
