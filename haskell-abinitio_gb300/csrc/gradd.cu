@@ -43,6 +43,8 @@ struct GradDArgs {
   const double* sscale;
   const T* D;
   const T* boys;
+  const double* Q;       // Schwarz bound of each pair
+  double thr;            // drop a quartet when Q_ab Q_cd max|Gamma_abcd| is below
   double* grad;
 };
 
@@ -82,6 +84,7 @@ __global__ void __launch_bounds__(GRD_THREADS) k_gradd(GradDArgs<T> a) {
       const int Cs = a.pA[jk], Ds = a.pB[jk];
       const int c0 = a.shell_f0[Cs], d0 = a.shell_f0[Ds];
       const T wgt = (A == B ? T(1) : T(2)) * (Cs == Ds ? T(1) : T(2));
+      double gmax = 0.0;
       for (int e = lane; e < C::NOUT; e += 32) {
         const int ab = e / C::NCD, cd = e - ab * C::NCD;
         const int ia = ab / C::NB, ibb = ab - ia * C::NB, ic = cd / C::ND, id = cd - ic * C::ND;
@@ -89,9 +92,15 @@ __global__ void __launch_bounds__(GRD_THREADS) k_gradd(GradDArgs<T> a) {
         const T dac = Dm[(long long)(a0 + ia) * n + c0 + ic], dbd = Dm[(long long)(b0 + ibb) * n + d0 + id];
         const T dad = Dm[(long long)(a0 + ia) * n + d0 + id], dbc = Dm[(long long)(b0 + ibb) * n + c0 + ic];
         const double sc = a.sscale[6 * A + ia] * a.sscale[6 * B + ibb] * a.sscale[6 * Cs + ic] * a.sscale[6 * Ds + id];
-        Gam[e] = (dab * dcd - T(0.25) * (dac * dbd + dad * dbc)) * (wgt * T(sc));
+        const T gv = (dab * dcd - T(0.25) * (dac * dbd + dad * dbc)) * T(sc);
+        Gam[e] = gv * wgt;
+        gmax = fmax(gmax, fabs((double)gv));
       }
       __syncwarp();
+      // exact screening of this quartet by its own Gamma (warp-uniform decision)
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) gmax = fmax(gmax, __shfl_xor_sync(0xffffffffu, gmax, o));
+      if (a.Q[ib] * a.Q[jk] * gmax < a.thr) continue;
       const int4 sg = a.seg[a.kseg[jk]];
       const int K = sg.z, len = sg.y - sg.x;
       const long long base = (long long)sg.w + (jk - sg.x);
@@ -156,6 +165,8 @@ static gbhf_status launch_gradd_t(gbhf_ctx* c, cudaStream_t strm, int combo, int
   a.mn = c->tasks.mn.p;
   a.moff = c->tasks.moff.p;
   a.sscale = c->tasks.sscale.p;
+  a.Q = P.Q.p;
+  a.thr = gt.thr_exact;
   a.D = D;
   a.boys = boys;
   a.grad = grad;
