@@ -181,26 +181,39 @@ gbhf_status build_basis_mols(gbhf_ctx* c, int n_atoms, const double* xyz, const 
 // Exact Boys function by the power series
 //   F_m(x) = exp(-x) sum_k (2x)^k / ((2m+1)(2m+3)...(2m+2k+1))
 // in long double (all terms positive, so no cancellation).
-static double boys_series(int m, double xd) {
-  long double x = xd;
-  long double term = 1.0L / (2 * m + 1), sum = term;
+// F_0 .. F_(BOYS_NCOL-1)(x) in extended precision: the power series for the
+// highest order (terms until below 1e-22 of the sum), then the downward
+// recursion F_m = (2x F_(m+1) + exp(-x)) / (2m + 1), which is stable.  One
+// series per node (long double is software-emulated quad precision on some
+// hosts, so the tables cost one series per node rather than one per order).
+static void boys_row_host(double xd, double* out) {
+  const long double x = xd;
+  const int mt = BOYS_NCOL - 1;
+  long double term = 1.0L / (2 * mt + 1), sum = term;
   for (int k = 1; k < 4000; ++k) {
-    term *= 2 * x / (2 * m + 2 * k + 1);
+    term *= 2 * x / (2 * mt + 2 * k + 1);
     sum += term;
     if (term < sum * 1e-22L) break;
   }
-  return (double)(expl(-x) * sum);
+  const long double ex = expl(-x);
+  long double f = ex * sum;
+  out[mt] = (double)f;
+  for (int m = mt - 1; m >= 0; --m) {
+    f = (2 * x * f + ex) / (2 * m + 1);
+    out[m] = (double)f;
+  }
 }
 
 gbhf_status ensure_boys_tables(gbhf_ctx* c) {
   if (c->boys64.p && c->boys32.p && c->boysh64.p && c->boysh32.p) return GBHF_OK;
   std::vector<double> t64((size_t)BOYS64_NROW * BOYS_NCOL);
   std::vector<float> t32((size_t)BOYS32_NROW * BOYS_NCOL);
-  for (int j = 0; j < BOYS64_NROW; ++j)
-    for (int m = 0; m < BOYS_NCOL; ++m) t64[(size_t)j * BOYS_NCOL + m] = boys_series(m, j * BOYS64_H);
+  std::vector<double> t32d((size_t)BOYS32_NROW * BOYS_NCOL);   // the FP32 nodes' values before rounding
+  for (int j = 0; j < BOYS64_NROW; ++j) boys_row_host(j * BOYS64_H, t64.data() + (size_t)j * BOYS_NCOL);
   for (int j = 0; j < BOYS32_NROW; ++j) {
     const float tj = (float)j * BOYS32_H;   // the node the device forms in float
-    for (int m = 0; m < BOYS_NCOL; ++m) t32[(size_t)j * BOYS_NCOL + m] = (float)boys_series(m, (double)tj);
+    boys_row_host((double)tj, t32d.data() + (size_t)j * BOYS_NCOL);
+    for (int m = 0; m < BOYS_NCOL; ++m) t32[(size_t)j * BOYS_NCOL + m] = (float)t32d[(size_t)j * BOYS_NCOL + m];
   }
   // Horner tables per order L: row j = [F_(L+k)(T_j)/k!, k < NT][exp(-T_j)/k!, k < NT]
   std::vector<double> h64((size_t)(BOYSH_LMAX + 1) * BOYS64_NROW * BOYSH64_STRIDE, 0.0);
@@ -222,7 +235,7 @@ gbhf_status ensure_boys_tables(gbhf_ctx* c) {
       double inv_fact = 1.0;
       for (int k = 0; k < BOYS32_NTERM; ++k) {
         if (k > 0) inv_fact /= k;
-        row[k] = (float)(boys_series(L + k, tj) * inv_fact);
+        row[k] = (float)(t32d[(size_t)j * BOYS_NCOL + L + k] * inv_fact);
         row[BOYS32_NTERM + k] = (float)(std::exp(-tj) * inv_fact);
       }
     }
