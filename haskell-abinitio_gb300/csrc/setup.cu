@@ -178,11 +178,10 @@ gbhf_status build_basis_mols(gbhf_ctx* c, int n_atoms, const double* xyz, const 
   return GBHF_OK;
 }
 
-// Exact Boys function by the power series
+// Exact Boys function F_0 .. F_(BOYS_NCOL-1)(x) in extended precision: the power series
 //   F_m(x) = exp(-x) sum_k (2x)^k / ((2m+1)(2m+3)...(2m+2k+1))
-// in long double (all terms positive, so no cancellation).
-// F_0 .. F_(BOYS_NCOL-1)(x) in extended precision: the power series for the
-// highest order (terms until below 1e-22 of the sum), then the downward
+// (all terms positive, so no cancellation) for the highest order, terms until
+// below 1e-22 of the sum, then the downward
 // recursion F_m = (2x F_(m+1) + exp(-x)) / (2m + 1), which is stable.  One
 // series per node (long double is software-emulated quad precision on some
 // hosts, so the tables cost one series per node rather than one per order).
