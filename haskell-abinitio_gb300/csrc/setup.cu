@@ -426,11 +426,25 @@ gbhf_status ensure_pairs(gbhf_ctx* c) {
   bool mol_ordered = true;
   for (int s2 = 1; s2 < ns; ++s2) mol_ordered &= b.shells[s2].mol >= b.shells[s2 - 1].mol;
   if (mol_ordered) {
+    // each run sorted as compact (K, Q, index) records: the comparisons stay in cache
+    struct PairKey {
+      int K;
+      double Q;
+      int idx;
+    };
+    std::vector<PairKey> keys;
     order = ord0;
     for (int r0 = 0; r0 < np;) {
       int r1 = r0 + 1;
       while (r1 < np && cls[order[r1]] == cls[order[r0]] && molp[order[r1]] == molp[order[r0]]) ++r1;
-      std::sort(order.begin() + r0, order.begin() + r1, within);
+      keys.resize(r1 - r0);
+      for (int t = r0; t < r1; ++t) keys[t - r0] = {Kp[order[t]], Q[order[t]], order[t]};
+      std::sort(keys.begin(), keys.end(), [](const PairKey& x, const PairKey& y) {
+        if (x.K != y.K) return x.K > y.K;
+        if (x.Q != y.Q) return x.Q > y.Q;
+        return x.idx < y.idx;
+      });
+      for (int t = r0; t < r1; ++t) order[t] = keys[t - r0].idx;
       r0 = r1;
     }
   } else {
