@@ -2,13 +2,14 @@
 //
 // Some callers cannot allocate device memory while they call us: code that
 // runs inside another framework's custom-call or plugin hook, where the host
-// framework owns every device buffer and forbids cudaMalloc (it would break
-// its memory planning, or synchronise a stream it is recording).  They hand
-// in device buffers for the input matrix and the results and nothing else.
-// This entry point serves them: the Jacobi solver's working memory lives in
-// the file-scope array g_eigen_scratch below, sized for matrices up to
-// GBHF_NOALLOC_EIGEN_MAX_N, which every GPU that loads the library keeps for
-// the life of the process.
+// framework owns every device buffer and its memory planner forbids
+// cudaMalloc.  They hand in device buffers for the input matrix and the
+// results and nothing else.  This entry point serves them: the Jacobi
+// solver's working memory lives in the file-scope array g_eigen_scratch
+// below, sized for matrices up to GBHF_NOALLOC_EIGEN_MAX_N, which every GPU
+// that loads the library keeps for the life of the process.  Every call waits
+// for the caller's stream to finish before it returns (it reads back the
+// solver's status word).
 #include <mutex>
 
 #include "gbhf_internal.h"
@@ -17,7 +18,8 @@
 namespace {
 
 constexpr int kMaxN = GBHF_NOALLOC_EIGEN_MAX_N;
-// Layout (doubles): A (kMaxN^2) | V (kMaxN^2) | rot (3 kMaxN) | red (4) | ints (8 doubles' worth)
+// Layout (doubles): A (kMaxN^2) | A2 (kMaxN^2, the second Jacobi buffer) | V (kMaxN^2) |
+// rot (4 kMaxN) | red (4) | ints (8 doubles' worth: barrier count and generation, status, sweeps)
 constexpr size_t kOffA = 0;
 constexpr size_t kOffA2 = kOffA + (size_t)kMaxN * kMaxN;
 constexpr size_t kOffV = kOffA2 + (size_t)kMaxN * kMaxN;
@@ -38,7 +40,11 @@ DeviceSetup g_setup[kMaxDevices];
 std::mutex g_setup_mutex;
 
 // Once per device, with that device current: resolve the array's device
-// address (the host-side symbol is only a stand-in) and size the cooperative grid.
+// address (the host-side symbol is only a stand-in) and size the cooperative
+// grid.  The address belongs to the CUDA context current at that first call;
+// a cudaDeviceReset of the device ends that context and leaves the cached
+// address stale, so a process that resets a device must not call this entry
+// point on it again.  A failed set-up caches nothing and the next call retries.
 gbhf_status setup_device(int dev, DeviceSetup** out) {
   if (dev < 0 || dev >= kMaxDevices) return GBHF_ERR_NO_DEVICE;
   std::lock_guard<std::mutex> lock(g_setup_mutex);
@@ -50,8 +56,10 @@ gbhf_status setup_device(int dev, DeviceSetup** out) {
     if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return GBHF_ERR_CUDA;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gbhf::k_jacobi, 256, 0) != cudaSuccess)
       return GBHF_ERR_CUDA;
+    // no resident block per SM: a cooperative launch could never start
+    if (nsm < 1 || per_sm < 1) return GBHF_ERR_CUDA;
     s.scratch = static_cast<double*>(ptr);
-    s.grid = nsm * (per_sm < 2 ? (per_sm < 1 ? 1 : per_sm) : 2);
+    s.grid = nsm * (per_sm < 2 ? per_sm : 2);
     s.done = true;
   }
   *out = &s;
@@ -64,6 +72,10 @@ extern "C" gbhf_status gbhf_eigen_solve_noalloc(int n, const double* d_a, double
                                                 void* stream) {
   if (n < 1 || n > kMaxN) return GBHF_ERR_BAD_INPUT;
   if (!d_a || !d_evals || !d_evecs) return GBHF_ERR_BAD_INPUT;
+  // An error left pending by earlier runtime calls of this host thread (the
+  // caller's own) is not this call's: clear it, so that the checks after the
+  // launches below report only this call's failures.
+  (void)cudaGetLastError();
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return GBHF_ERR_NO_DEVICE;
   DeviceSetup* s = nullptr;

@@ -129,4 +129,6 @@ def main(root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/data")
+    if len(sys.argv) < 2:
+        sys.exit("usage: python make_basis_data.py <reference checkout>/data > basis_sets.json")
+    main(sys.argv[1])

@@ -178,10 +178,12 @@ gbhf_status gbhf_eigen_solve(gbhf_ctx* ctx, int n, const double* a_square, doubl
  * work.  The solver's working memory is one static device array sized for
  * n <= GBHF_NOALLOC_EIGEN_MAX_N (about 1.5 MiB, held by every GPU that loads
  * the library until the process exits); larger n returns GBHF_ERR_BAD_INPUT.
- * The first call on a device resolves that array's device address and the
- * launch geometry; make that first call before any stream capture.  All calls
- * share the array, so calls that overlap on the GPU (other host threads or
- * streams) race: serialise them. */
+ * The first call on a device resolves that array's device address (in the
+ * CUDA context current then) and the launch geometry; make that first call
+ * before any stream capture.  After a cudaDeviceReset of that device the
+ * resolved address is stale: do not call this entry point on it again.  All
+ * calls share the array, so calls that overlap on the GPU (other host threads
+ * or streams) race: serialise them. */
 #define GBHF_NOALLOC_EIGEN_MAX_N 256
 gbhf_status gbhf_eigen_solve_noalloc(int n, const double* d_a, double* d_evals, double* d_evecs, void* stream);
 

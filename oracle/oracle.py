@@ -510,7 +510,7 @@ def sad_density(fb):
 @dataclass
 class SCFOptions:
     ref_compat: bool = True        # reference numerics + reference driver rules
-    guess: str = "harris"          # "harris" | "core" | "sad"
+    guess: str = "harris"          # "harris" | "core" | "sad" | "density"
     diis_size: int = 5             # vectors in the extrapolation (current + stored)
     max_iter: int = 30
     conv_error: float = 1e-7       # max|e| (reference rule, used when ref_compat)
@@ -521,6 +521,7 @@ class SCFOptions:
     charge: float = 0.0
     direct: bool = False           # shell-based direct Fock instead of stored ERIs
     stop_rule: str = ""            # "reference" | "energy"; default follows ref_compat
+    guess_density: Optional[np.ndarray] = None   # flat start density for guess="density" (restart)
 
     @staticmethod
     def reference():
@@ -577,6 +578,10 @@ def scf(fb, opts: Optional[SCFOptions] = None, grid=None):
         _, density, _ = diagonal_hf(core + g, x, occupied)
     elif opts.guess == "sad":
         density = sad_density(fb)
+    elif opts.guess == "density":
+        density = np.array(opts.guess_density, dtype=np.float64, copy=True)
+        if density.shape != core.shape:
+            raise ValueError("guess density does not match the basis")
     else:
         _, density, _ = diagonal_hf(core, x, occupied)
     dat = DataDIIS(size=opts.diis_size)

@@ -1,4 +1,5 @@
 import json
+import os
 import sys
 from pathlib import Path
 
@@ -10,7 +11,9 @@ for p in (ROOT / "haskell-abinitio_gb300", ROOT / "oracle"):
         sys.path.insert(0, str(p))
 
 GOLDEN = Path(__file__).resolve().parent / "golden"
-REFERENCE = Path("/root/reference")
+# The reference checkout, only where REFERENCE_ROOT names it (tests that read
+# it skip otherwise and fall back to the committed fixtures).
+REFERENCE = Path(os.environ["REFERENCE_ROOT"]) if os.environ.get("REFERENCE_ROOT") else None
 
 
 def pytest_configure(config):

@@ -6,7 +6,12 @@ Run from the repository root:  python tests/golden/make_golden.py
   table (points256/weights256 in
   Science/QuantumChemistry/NumericalTools/PointsWeights.hs, parsed as
   float64, big-endian) and how far the oracle's own nodes/weights lie from it.
-  Needs the reference checkout (REFERENCE_ROOT, default /root/reference).
+  Needs the reference checkout, given as the first argument or by the
+  REFERENCE_ROOT environment variable.
+* ``sample_projects.json``: the literal primitives and geometries of the
+  reference's four sample projects (HsFock/SampleProjects.hs:18-98: HHe+,
+  CO and water in STO-3G, water in 6-31G*), parsed from that file, with the
+  oracle's energies on exactly those inputs.  Needs the reference checkout.
 * ``water_sto3g.json``: single water (O (0,0,0); H (0,+-1.4305,1.1093) bohr),
   STO-3G, for both basis variants (as shipped = SP exponents 1.0, and the
   EMSL text): overlap, core Hamiltonian and the canonical ERI array in both
@@ -33,7 +38,8 @@ import oracle as O  # noqa: E402
 from gbhf import basis as B, molecules as M  # noqa: E402
 
 OUT = Path(__file__).resolve().parent
-REF = Path(os.environ.get("REFERENCE_ROOT", "/root/reference"))
+_ref_arg = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("REFERENCE_ROOT", "")
+REF = Path(_ref_arg) if _ref_arg else None
 
 
 def table_hash(x, w):
@@ -106,9 +112,74 @@ def clusters():
     return out
 
 
+# Atom of each entry of ``atomList`` (HsFock/SampleProjects.hs).  The
+# reference's own test pairs "water" as O, H, H with [baseH, baseO] = pBasis
+# (test/AbinitioTests.hs:16-22); HHe+ and CO have no caller and pair pBasis
+# with atomList in order.  Charges: HHe+ is a cation.
+SAMPLE_ATOMS = {("HHe+", "STO-3G"): (["He", "H"], 1.0), ("CO", "STO-3G"): (["O", "C"], 0.0),
+                ("water", "STO-3G"): (["O", "H", "H"], 0.0), ("water", "6-31G*"): (["O", "H", "H"], 0.0)}
+SAMPLE_BASE = {"H": "baseH", "He": "baseHe", "C": "baseC", "O": "baseO"}
+ZNUM = {"H": 1.0, "He": 2.0, "C": 6.0, "O": 8.0}
+
+
+def _hs_float(tok):
+    return float(tok.strip())
+
+
+def sample_projects():
+    """Parse project "<label>" "<basis>" = PD {...} where ... blocks."""
+    src = (REF / "Science/QuantumChemistry/HsFock/SampleProjects.hs").read_text()
+    heads = list(re.finditer(r'^project "([^"]+)" "([^"]+)" *=', src, flags=re.M))
+    out = {}
+    for k, m in enumerate(heads):
+        body = src[m.end():heads[k + 1].start() if k + 1 < len(heads) else len(src)]
+        atoms_txt = re.search(r"atomList\s*=\s*\[(.*?)\]\s*\}", body, flags=re.S).group(1)
+        coords = [[_hs_float(v) for v in t.split(",")] for t in re.findall(r"\[([^\[\]]+)\]", atoms_txt)]
+        prims = {}
+        for name, lst in re.findall(r"^\s*(\w+)\s*=\s*\[\s*(\([^=]*?\))\s*\]\s*$", body, flags=re.M):
+            prims[name] = [[_hs_float(c), _hs_float(e)] for c, e in re.findall(r"\(([^,()]+),([^,()]+)\)", lst)]
+        bases = {}
+        for name, lst in re.findall(r"^\s*(base\w+)\s*=\s*normGlobal`fmap`\s*\[(.*?)\]\s*$", body, flags=re.M):
+            bases[name] = [{"primitives": prims[pn], "funtype": ft}
+                           for pn, ft in re.findall(r"CGF\s+(\w+)\s+(\w+)", lst)]
+        labels, charge = SAMPLE_ATOMS[(m.group(1), m.group(2))]
+        assert len(labels) == len(coords)
+        rec = {"label": m.group(1), "basis": m.group(2), "charge": charge,
+               "atoms": [{"element": l, "znumber": ZNUM[l], "coord_bohr": c, "cgfs": bases[SAMPLE_BASE[l]]}
+                         for l, c in zip(labels, coords)]}
+        fb = B.flatten(sample_atoms(rec))
+        occ_opts = dict(charge=charge)
+        rec["oracle_energy_exact"] = O.scf(fb, O.SCFOptions.baseline(guess="sad", **occ_opts)).energy
+        try:
+            rec["oracle_energy_reference"] = O.scf(fb, O.SCFOptions(charge=charge)).energy
+        except IndexError as e:   # the Harris guess leaves the ERI array (as the reference would)
+            rec["oracle_energy_reference"] = None
+            rec["reference_driver_error"] = str(e)
+        out[f"{m.group(1)} {m.group(2)}"] = rec
+    return out
+
+
+def sample_atoms(rec):
+    """``[AtomData]`` of a sample project: the literal primitives through
+    ``normGlobal`` (``basis.norm_coeff``), in the project's own CGF order."""
+    atoms = []
+    for a in rec["atoms"]:
+        cgfs = []
+        for c in a["cgfs"]:
+            cs = [p[0] for p in c["primitives"]]
+            es = [p[1] for p in c["primitives"]]
+            cgfs.append(B.CGF(tuple(zip(B.norm_coeff(c["funtype"], cs, es), es)), c["funtype"]))
+        atoms.append(B.AtomData(tuple(a["coord_bohr"]), cgfs, a["znumber"], a["element"]))
+    return atoms
+
+
 def main():
-    if REF.exists():
+    if REF is not None and REF.exists():
         (OUT / "quadrature256.json").write_text(json.dumps(quadrature(), indent=1) + "\n")
+        (OUT / "sample_projects.json").write_text(json.dumps(sample_projects(), indent=1) + "\n")
+    else:
+        print("no reference checkout given (argument or REFERENCE_ROOT): "
+              "quadrature256.json and sample_projects.json are kept as they are")
     (OUT / "water_sto3g.json").write_text(json.dumps(water()) + "\n")
     (OUT / "clusters.json").write_text(json.dumps(clusters(), indent=1) + "\n")
 
