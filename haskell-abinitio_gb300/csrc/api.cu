@@ -1,4 +1,5 @@
 // C ABI of libgbhf (declarations and reference citations in include/gbhf.h).
+#include <cstdlib>
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -72,6 +73,11 @@ gbhf_status gbhf_create(gbhf_ctx** out, int device) {
     return GBHF_ERR_NO_DEVICE;
   }
   c->nsm = prop.multiProcessorCount;
+  c->smem_optin = prop.sharedMemPerBlockOptin;
+  {
+    const char* ev = std::getenv("GBHF_EIGEN");
+    c->force_jacobi = ev && std::string(ev) == "jacobi";
+  }
   if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
     delete c;
     return GBHF_ERR_CUDA;

@@ -254,6 +254,16 @@ struct JacobiWork {
   int last_sweeps = 0;
 };
 
+// Work buffers of the tridiagonal eigen-solver (tridiag.cu).
+struct TridiagWork {
+  DBuf<double> d, e, tau, lam, scal, Vt, Zt, Z2, S, M;
+  DBuf<int> blk, rank;
+  size_t smem_set = 0;   // dynamic shared memory k_sytrd was opened up to
+};
+// Largest n of the tridiagonal path: the packed lower triangle of A plus two
+// vectors in one CTA's shared memory (232: 215 KiB).  Larger n use Jacobi.
+constexpr int TRIDIAG_MAX_N = 232;
+
 struct Profile {
   bool events = false;
   double jk_ms64 = 0, jk_ms32 = 0, dense_ms = 0;
@@ -299,6 +309,9 @@ struct gbhf_ctx {
   // dense work buffers (n*n doubles)
   gbhf::DBuf<double> w[24];
   gbhf::JacobiWork jac;
+  gbhf::TridiagWork tri;
+  size_t smem_optin = 0;          // largest dynamic shared memory per block (opt-in)
+  bool force_jacobi = false;      // GBHF_EIGEN=jacobi at gbhf_create: every eigen-solve by Jacobi
   // state of the last SCF (for the gradient): density, Fock matrix, occupation
   gbhf::DBuf<double> last_D, last_F;
   gbhf::DBuf<double> guess_D;        // gbhf_set_guess_density (flat), valid for basis generation guess_gen
@@ -456,6 +469,9 @@ gbhf_status launch_grad_dclass(gbhf_ctx* c, cudaStream_t strm, int combo, int pr
 gbhf_status gemm(gbhf_ctx* c, bool ta, bool tb, int m, int n, int k, double alpha, const double* A, int lda,
                  const double* B, int ldb, double beta, double* C, int ldc, bool sym = false);
 gbhf_status eigh(gbhf_ctx* c, int n, const double* d_A, double* d_evals, double* d_evecs, const double* d_V0);
+// tridiag.cu: Householder + bisection + inverse iteration, n <= TRIDIAG_MAX_N
+gbhf_status eigh_tridiag(gbhf_ctx* c, int n, const double* d_A, double* d_evals, double* d_evecs);
+size_t tridiag_smem_bytes(int n);
 gbhf_status flat_to_square(gbhf_ctx* c, int n, const double* d_flat, double* d_sq);
 gbhf_status square_to_flat(gbhf_ctx* c, int n, const double* d_sq, double* d_flat);
 gbhf_status symm_ortho_dev(gbhf_ctx* c, int n, const double* d_S, double* d_X);

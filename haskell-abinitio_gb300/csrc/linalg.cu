@@ -659,8 +659,13 @@ __global__ void k_jacobi_init(int n, int m, const double* __restrict__ Ain, doub
 }
 
 // d_evecs (n x n): eigenvectors of A in columns, ascending eigenvalues.
+// Up to TRIDIAG_MAX_N: Householder tridiagonalisation, bisection and inverse
+// iteration (tridiag.cu; the warm start d_V0 is not needed there).  Above it,
+// or with GBHF_EIGEN=jacobi: the Jacobi solver below.
 gbhf_status eigh(gbhf_ctx* c, int n, const double* d_A, double* d_evals, double* d_evecs, const double* d_V0) {
   if (n <= 0 || n > 1024) return fail(c, GBHF_ERR_UNSUPPORTED, "eigen-solve supports 1 <= n <= 1024");
+  if (n <= TRIDIAG_MAX_N && !c->force_jacobi && tridiag_smem_bytes(n) <= c->smem_optin)
+    return eigh_tridiag(c, n, d_A, d_evals, d_evecs);
   JacobiWork& w = c->jac;
   const int mm = std::max(2, n + (n & 1));
   GBHF_CUDA(c, w.A.alloc((size_t)mm * mm));

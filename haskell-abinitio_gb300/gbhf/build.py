@@ -19,7 +19,7 @@ LIB = BUILD / "libgbhf.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["api.cu", "setup.cu", "eri_canon.cu", "jk.cu", "linalg.cu", "scf.cu", "measure.cu", "noalloc.cu", "grad.cu", "batch.cu",
            "sad.cu", "bscf.cu", "jkd.cu", "gradd.cu", "uhf.cu",
-           "tune.cu"]
+           "tune.cu", "tridiag.cu"]
 HEADERS = ["gbhf_common.cuh", "gbhf_internal.h", "gbhf_md.cuh", "eri_gen.cuh", "grad_gen.cuh", "jacobi.cuh",
            "dense.cuh", "mdwarp.cuh"]
 

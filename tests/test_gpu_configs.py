@@ -117,7 +117,8 @@ def test_batch_mixed_against_oracle(ctx, batch_inputs, cut, gcut):
         ctx.scf(_lib.baseline_opts(**TIGHT), want_matrices=False)
         g64 = ctx.gradient()
         assert np.max(np.abs(grads[k] - g64)) <= 1e-5, i
-        assert np.max(np.abs(grads[k].sum(axis=0))) < 1e-8
+        # translational invariance, to the FP32 rounding of the derivative integrals
+        assert np.max(np.abs(grads[k].sum(axis=0))) < 1e-6
 
 
 def test_batch_gradient_against_oracle_fd(ctx, batch_inputs):

@@ -83,3 +83,62 @@ def test_diis_extrapolation_matches_oracle(ctx):
     ref2, dat2 = O.diis(es2[0], fs[0], O.DataDIIS(es2[1:], fs[1:3], 5))
     assert used2 == len(dat2.errors)
     np.testing.assert_allclose(got2, ref2, rtol=0, atol=1e-10)
+
+
+@pytest.mark.parametrize("n", [231, 232, 233])
+def test_eigen_solve_tridiagonal_limit(ctx, n):
+    """Up to 232 the eigen-solve runs Householder + bisection + inverse
+    iteration; from 233 the Jacobi solver.  Both against LAPACK."""
+    a = np.random.default_rng(1000 + n).standard_normal((n, n))
+    a = a + a.T
+    w, v = ctx.eigen_solve(a)
+    wr = np.linalg.eigvalsh(a)
+    sc = np.abs(wr).max()
+    np.testing.assert_allclose(w, wr, rtol=0, atol=1e-12 * sc)
+    assert np.max(np.abs(a @ v - v * w)) < 1e-11 * sc
+    assert np.max(np.abs(v.T @ v - np.eye(n))) < 1e-12
+
+
+def _clustered(n_cl, rng):
+    lam = np.concatenate([np.full(10, -3.0) + 1e-12 * np.arange(10), np.linspace(0.0, 1.0, n_cl),
+                          5.0 + 1e-9 * np.arange(10), np.repeat([7.0, 8.0], 5)])
+    q, _ = np.linalg.qr(rng.standard_normal((lam.size, lam.size)))
+    return q @ np.diag(lam) @ q.T, lam
+
+
+def test_eigen_solve_clustered_and_repeated(ctx):
+    """Eigenvalues 1e-12 and 1e-9 apart and exactly repeated ones in a dense
+    matrix: orthonormal eigenvectors with small residuals."""
+    a, lam = _clustered(100, np.random.default_rng(5))
+    w, v = ctx.eigen_solve(a)
+    np.testing.assert_allclose(w, np.sort(lam), rtol=0, atol=1e-13 * 8)
+    assert np.max(np.abs(a @ v - v * w)) < 1e-13 * 8
+    assert np.max(np.abs(v.T @ v - np.eye(lam.size))) < 1e-13
+
+
+def test_eigen_solve_scf_fock_both_solvers():
+    """The orthogonal-basis Fock matrix of (H2O)4/STO-3G at convergence (near-
+    degenerate O 1s levels 1e-3 apart): tridiagonal solver and Jacobi agree."""
+    import os
+    fb = B.flatten(M.cluster_atoms("batch256", "sto-3g", index=20))
+    ob = O.OracleBasis(fb)
+    r = O.scf(fb, O.SCFOptions.baseline(guess="sad"))
+    x = O.symm_ortho(O.tri_to_square(ob.overlap(False)))
+    fp = x.T @ O.tri_to_square(r.fock) @ x
+    with _lib.Context(0) as c:
+        w, v = c.eigen_solve(fp)
+    old = os.environ.get("GBHF_EIGEN")
+    os.environ["GBHF_EIGEN"] = "jacobi"
+    try:
+        with _lib.Context(0) as c:
+            wj, vj = c.eigen_solve(fp)
+    finally:
+        if old is None:
+            del os.environ["GBHF_EIGEN"]
+        else:
+            os.environ["GBHF_EIGEN"] = old
+    wr = np.linalg.eigvalsh(fp)
+    np.testing.assert_allclose(w, wr, rtol=0, atol=1e-12 * 21)
+    np.testing.assert_allclose(wj, wr, rtol=0, atol=1e-12 * 21)
+    assert np.max(np.abs(np.abs(np.sum(v * vj, axis=0)) - 1.0)) < 1e-9
+    assert np.max(np.abs(v.T @ v - np.eye(fp.shape[0]))) < 1e-13
