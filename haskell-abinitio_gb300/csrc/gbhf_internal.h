@@ -258,7 +258,6 @@ struct JacobiWork {
 struct TridiagWork {
   DBuf<double> d, e, tau, lam, scal, Vt, Zt, Z2, S, M;
   DBuf<int> blk, rank;
-  size_t smem_set = 0;   // dynamic shared memory k_sytrd was opened up to
 };
 // Largest n of the tridiagonal path: the packed lower triangle of A plus two
 // vectors in one CTA's shared memory (232: 215 KiB).  Larger n use Jacobi.
@@ -365,6 +364,12 @@ gbhf_status cuda_fail(gbhf_ctx* c, cudaError_t e, const char* where);
   do {                                                              \
     cudaError_t e__ = (call);                                       \
     if (e__ != cudaSuccess) return gbhf::cuda_fail(ctx, e__, #call); \
+  } while (0)
+// The launch just issued (named by `what`) was accepted.
+#define GBHF_LAUNCHED(ctx, what)                                      \
+  do {                                                                \
+    cudaError_t e__ = cudaGetLastError();                             \
+    if (e__ != cudaSuccess) return gbhf::cuda_fail(ctx, e__, what);   \
   } while (0)
 #define GBHF_TRY(call)                   \
   do {                                   \

@@ -691,6 +691,7 @@ gbhf_status eigh(gbhf_ctx* c, int n, const double* d_A, double* d_evals, double*
   k_jacobi_init<<<std::max(1, std::min(c->nsm * 4, (mm * mm + 255) / 256)), 256, 0, c->stream>>>(n, mm, src, w.A.p,
                                                                                                    w.V.p);
   count_launch(c);
+  GBHF_LAUNCHED(c, "k_jacobi_init launch");
   JacobiArgs a;
   a.n = n;
   a.m = mm;
@@ -717,6 +718,7 @@ gbhf_status eigh(gbhf_ctx* c, int n, const double* d_A, double* d_evals, double*
   double* vec_out = d_V0 ? w.t3.p : d_evecs;
   k_sort_eig<<<1, 1024, 0, c->stream>>>(n, mm, w.A.p, w.V.p, d_evals, vec_out);
   count_launch(c);
+  GBHF_LAUNCHED(c, "k_sort_eig launch");
   if (d_V0) GBHF_TRY(gemm(c, false, false, n, n, n, 1.0, d_V0, n, w.t3.p, n, 0.0, d_evecs, n));
   int st = 0, sweeps = 0;
   GBHF_CUDA(c, cudaMemcpyAsync(&st, c->dev_status.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));

@@ -353,7 +353,7 @@ __global__ void k_tri_vec(int n, const double* __restrict__ d, const double* __r
 // of the previous one in the same block, orthogonalised against the earlier
 // members of that run; then every thread ranks the eigenvalues (ascending,
 // ties by index) and writes evals in sorted order.
-__global__ void k_tri_fix(int n, const double* __restrict__ d, const double* __restrict__ e,
+__global__ void __launch_bounds__(256) k_tri_fix(int n, const double* __restrict__ d, const double* __restrict__ e,
                           const int* __restrict__ blk, const double* __restrict__ scal,
                           const double* __restrict__ lam, double* __restrict__ Zt, int* __restrict__ rank,
                           double* __restrict__ evals) {
@@ -437,25 +437,29 @@ gbhf_status eigh_tridiag(gbhf_ctx* c, int n, const double* d_A, double* d_evals,
   GBHF_CUDA(c, w.blk.alloc(2 * (size_t)n));
   GBHF_CUDA(c, w.rank.alloc(n));
   const size_t smem = tridiag_smem_bytes(n);
-  if (w.smem_set < smem) {
-    GBHF_CUDA(c, cudaFuncSetAttribute(k_sytrd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    w.smem_set = smem;
-  }
+  // The attribute belongs to the kernel (per device, for the whole process):
+  // always the largest size, so that no context lowers it under another's launch.
+  GBHF_CUDA(c, cudaFuncSetAttribute(k_sytrd, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)tridiag_smem_bytes(TRIDIAG_MAX_N)));
   if (n > 1) {
     GBHF_CUDA(c, cudaMemsetAsync(w.e.p, 0, n * sizeof(double), c->stream));
   }
   k_sytrd<<<1, 1024, smem, c->stream>>>(n, d_A, w.d.p, w.e.p, w.tau.p, w.Vt.p);
   count_launch(c);
+  GBHF_LAUNCHED(c, "k_sytrd launch");
   k_tri_prep<<<1, 32, 0, c->stream>>>(n, w.d.p, w.e.p, w.blk.p, w.scal.p);
   count_launch(c);
+  GBHF_LAUNCHED(c, "k_tri_prep launch");
   const int wpb = 2;   // warps per block: vectors spread over many SMs
   const size_t vsm = (size_t)wpb * 6 * n * sizeof(double);
   k_tri_vec<<<(n + wpb - 1) / wpb, 32 * wpb, vsm, c->stream>>>(n, w.d.p, w.e.p, w.blk.p, w.scal.p, w.lam.p,
                                                                w.Zt.p);
   count_launch(c);
-  k_tri_fix<<<1, 1024, 6 * n * sizeof(double), c->stream>>>(n, w.d.p, w.e.p, w.blk.p, w.scal.p, w.lam.p, w.Zt.p,
+  GBHF_LAUNCHED(c, "k_tri_vec launch");
+  k_tri_fix<<<1, 256, 6 * n * sizeof(double), c->stream>>>(n, w.d.p, w.e.p, w.blk.p, w.scal.p, w.lam.p, w.Zt.p,
                                                             w.rank.p, d_evals);
   count_launch(c);
+  GBHF_LAUNCHED(c, "k_tri_fix launch");
   // Newton-Schulz: Zt <- (3 I - Zt Zt^T) Zt / 2, twice
   double* zin = w.Zt.p;
   double* zout = w.Z2.p;
@@ -463,6 +467,7 @@ gbhf_status eigh_tridiag(gbhf_ctx* c, int n, const double* d_A, double* d_evals,
     GBHF_TRY(gemm(c, false, true, n, n, n, 1.0, zin, n, zin, n, 0.0, w.S.p, n, true));
     k_ns_mat<<<std::max(1, std::min(c->nsm * 4, (int)((nn + 255) / 256))), 256, 0, c->stream>>>(n, w.S.p, w.M.p);
     count_launch(c);
+    GBHF_LAUNCHED(c, "k_ns_mat launch");
     GBHF_TRY(gemm(c, false, false, n, n, n, 1.0, w.M.p, n, zin, n, 0.0, zout, n));
     std::swap(zin, zout);
   }
@@ -470,7 +475,7 @@ gbhf_status eigh_tridiag(gbhf_ctx* c, int n, const double* d_A, double* d_evals,
   k_tri_back<<<(n + bpb - 1) / bpb, 32 * bpb, (size_t)bpb * n * sizeof(double), c->stream>>>(n, w.Vt.p, w.tau.p,
                                                                                              zin, w.rank.p, d_evecs);
   count_launch(c);
-  GBHF_CUDA(c, cudaGetLastError());
+  GBHF_LAUNCHED(c, "k_tri_back launch");
   return GBHF_OK;
 }
 
