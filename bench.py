@@ -149,7 +149,47 @@ def oracle_sample(fb, n_iter):
             "estimate": setup + n_iter * per_iter, "max_err": float(np.max(np.abs(err)))}
 
 
+class OracleSCFSteps:
+    """Complete FP64 oracle SCFs of one molecule, one SCF iteration per step.
+
+    A step is one SCF iteration (direct Fock build, DIIS error and
+    extrapolation, diagonalisation); the setup of an SCF (integrals,
+    orthogonaliser, SAD start) is timed inside the first step of that SCF.
+    When an SCF converges the next step starts a new one, so ``complete``
+    collects the wall time of every SCF that ran from setup to convergence."""
+
+    def __init__(self, fb):
+        import oracle as O
+        self.O, self.fb = O, fb
+        self.gen, self.t_scf, self.iters = None, 0.0, 0
+        self.complete = []          # (seconds, iterations, energy) of finished SCFs
+        self.iteration_s = []       # step times without a setup
+
+    def step(self):
+        t0 = time.perf_counter()
+        setup = self.gen is None
+        if setup:
+            self.gen = self.O.scf_steps(self.fb, self.O.SCFOptions.baseline(guess="sad"))
+            next(self.gen)          # setup
+        _, res = next(self.gen)
+        dt = time.perf_counter() - t0
+        self.t_scf += dt
+        self.iters += 1
+        if not setup:
+            self.iteration_s.append(dt)
+        if res is not None:
+            self.complete.append((self.t_scf, self.iters, res.energy))
+            self.gen, self.t_scf, self.iters = None, 0.0, 0
+        return dt
+
+
 def run_reference(args, world, rank):
+    """The reference arm: the FP64 oracle (a restatement of the reference's
+    numerics; the Haskell original cannot be built here) running complete SCFs
+    of the workload on all host threads.  value = the mean wall time of the
+    SCFs that ran from setup to convergence inside the timed steps; with fewer
+    timed steps than one SCF needs, the setup plus the measured mean iteration
+    times the oracle's own iteration count (and the line says so)."""
     if rank != 0:
         return
     import oracle as O
@@ -157,24 +197,34 @@ def run_reference(args, world, rank):
     fb = B.flatten(M.cluster_atoms("w16", "6-31g"))
     rec = json.loads((ROOT / "tests" / "golden" / "clusters.json").read_text()).get("w16_631g", {})
     n_iter = int(rec.get("iterations_sad", rec.get("iterations", 17)))
+    warm = OracleSCFSteps(fb)
     for _ in range(args.warmup):
-        oracle_sample(fb, n_iter)
-    times = []
+        warm.step()
+    run = OracleSCFSteps(fb)
     t0 = time.perf_counter()
-    for _ in range(args.steps):
-        times.append(oracle_sample(fb, n_iter)["estimate"])
+    times = [run.step() for _ in range(args.steps)]
     wall = time.perf_counter() - t0
-    v = statistics.mean(times)
+    if run.complete:
+        v = statistics.mean(c[0] for c in run.complete)
+        how = (f"{len(run.complete)} complete SCF(s) ({run.complete[0][1]} iterations, E = {run.complete[0][2]:.10f}) "
+               f"timed from setup to convergence within the {args.steps} timed steps")
+    else:
+        setup_s = times[0] - (statistics.mean(run.iteration_s) if run.iteration_s else 0.0)
+        v = setup_s + n_iter * statistics.mean(run.iteration_s or times)
+        how = (f"no SCF completed within {args.steps} steps: setup + {n_iter} x the mean measured iteration "
+               f"({n_iter} = the oracle's own iteration count for this molecule)")
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "s/molecule", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * wall / args.steps,
             "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "config": {"workload": WORKLOAD, "precision": "FP64 (CPU)",
                                             "parallelism": "OpenMP, all host threads"},
+            "complete_scfs": [{"seconds": c[0], "iterations": c[1], "energy": c[2]} for c in run.complete],
+            "iteration_s_mean": statistics.mean(run.iteration_s) if run.iteration_s else None,
             "cpu_baseline": {"value": v, "unit": "s/molecule", "cores": O.lib().orc_num_threads(),
                              "kind": "port",
-                             "sample": f"per step: setup + 1 direct Fock build (Schwarz screening only) + DIIS error + diagonalisation "
-                                       f"of the FP64 oracle, SCF time = setup + {n_iter} x iteration "
-                                       f"({n_iter} = the oracle's own iteration count for this molecule)"},
+                             "sample": "per step one iteration of a complete FP64 oracle SCF (direct Fock build "
+                                       "with Schwarz and density screening, DIIS, diagonalisation; SAD start, "
+                                       "dE < 1e-10, RMS dD < 1e-8), setup inside each SCF's first step; " + how},
             "e2e": {"value": v, "unit": "s/molecule", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -198,7 +248,7 @@ def autotune_jk(ctx, fb, args):
 def run_gbhf(args, world, rank, local):
     import numpy as np
     from gbhf import _lib, basis as B, molecules as M
-    from gbhf.flops_model import F_ALG
+    from gbhf.flops_model import F_KERNEL
     ctx = _lib.Context(local)
     fb = B.flatten(M.cluster_atoms("w16", "6-31g"))
     # incremental builds without periodic full rebuilds (|dE| vs FP64 stays ~5e-10 Eh)
@@ -249,15 +299,36 @@ def run_gbhf(args, world, rank, local):
         ctx.scf(mixed, want_matrices=True)
         e2e_t.append(time.perf_counter() - t0)
     e2e_v = max_over_ranks(world, sum(e2e_t)) / (args.steps * world)
+    # the same call on a new context each time (gbhf_create, basis, SCF with every
+    # matrix back, gbhf_destroy): what a caller that keeps no context pays
+    cold_t = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        with _lib.Context(local) as c2:
+            c2.set_basis(fb)
+            c2.scf(mixed, want_matrices=True)
+        cold_t.append(time.perf_counter() - t0)
+    cold_v = max_over_ranks(world, statistics.median(cold_t))
+    batch = None
+    if not args.no_batch:
+        batch = [batch_measure(args, world, rank, local, cut, gcut) for cut, gcut in ((1e-2, 1.0), (1e-4, 1e-4))]
+    peaks_clk = measure_fma_peaks(ctx, local)
     if rank != 0:
         return
     # roofline of the dominant J/K kernel class (profiling SCF)
     dom = max(cls.items(), key=lambda kv: kv[1]["ms"])
     (cname, prec), st = dom
-    flops = st["prim_quartets"] * F_ALG[cname]
+    flops = st["prim_quartets"] * F_KERNEL[cname]
     achieved = flops / (st["ms"] * 1e-3) / 1e12 if st["ms"] > 0 else 0.0
-    peak64, peak32 = ctx.peak_flops(_lib.PREC_FP64), ctx.peak_flops(_lib.PREC_MIXED)
+    peak64, peak32 = peaks_clk["fp64_tflops"], peaks_clk["fp32_tflops"]
     peak = peak64 if prec == "fp64" else peak32
+    cls_tab = {}
+    for (cn, pr), v in cls.items():
+        if v["ms"] <= 0:
+            continue
+        a = v["prim_quartets"] * F_KERNEL[cn] / (v["ms"] * 1e-3) / 1e12
+        cls_tab[f"{cn}_{pr}"] = {**v, "flops_per_prim_quartet": F_KERNEL[cn], "achieved_tflops": a,
+                                 "frac": a / (peak64 if pr == "fp64" else peak32)}
     prof_tr = traffic_profile().get(f"{cname}_{prec}", {}).get("dram_bytes_per_launch")
     jk_ms = prof_cls["jk_ms_fp64"] + prof_cls["jk_ms_fp32"]
     fnq_step = prof["fn_quartets"] / args.steps
@@ -289,16 +360,26 @@ def run_gbhf(args, world, rank, local):
                      "timing": "CUDA events around each launch of this class in one profiling SCF run after "
                                "the timed steps (class launches serialised on one stream)",
                      "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
-                     "peak_source": f"FMA microbenchmark on this GPU (FP64 {peak64:.2f}, FP32 {peak32:.1f} TFLOP/s); "
+                     "peak_source": f"FMA microbenchmark on this GPU (FP64 {peak64:.2f}, FP32 {peak32:.1f} TFLOP/s, "
+                                    f"SM clock median {peaks_clk['sm_mhz']} MHz while it ran); "
                                     "MEASURED_PEAKS.json holds only HBM and bf16 tensor peaks",
+                     "flop_model": "primitive quartets x F_KERNEL (gbhf/flops_model.py): F_alg, or for the "
+                                   "deferred-ket classes the work per primitive quartet of that form",
                      "flops_per_launch": flops / max(r_prof["iterations"], 1), "traffic": prof_tr,
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of this class's launch "
                                        "in a full mixed Fock build (profiles/traffic.json); the ERI kernels "
                                        "are compute-bound, traffic far below their roofline"},
-        "classes": {f"{k[0]}_{k[1]}": v for k, v in cls.items() if v["ms"] > 0},
+        "classes": cls_tab,
+        "fma_peaks": peaks_clk,
         "clocks": clk.summary(),
-        "e2e": {"value": e2e_v, "unit": "s/molecule", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "e2e": {"value": e2e_v, "unit": "s/molecule", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                "context": "one context kept across calls (Boys tables, SAD atoms, tuned budgets resident)"},
+        "e2e_cold_context": {"value": cold_v, "unit": "s/molecule", "calls": len(cold_t),
+                             "what": "median of gbhf_create + gbhf_set_basis + gbhf_scf (all matrices back) + "
+                                     "gbhf_destroy, a new context per call (default task budgets)"},
     }
+    if batch:
+        line["batch256"] = batch
     peaks = load_measured_peaks()
     if peaks:
         line["measured_peaks"] = {"hbm_gbs": peaks.get("hbm_gbs"), "bf16_tflops": peaks.get("bf16_tflops")}
@@ -311,19 +392,35 @@ def run_gbhf(args, world, rank, local):
     print(json.dumps(line), flush=True)
 
 
-def run_batch(args, world, rank, local):
+def measure_fma_peaks(ctx, local, seconds=1.0):
+    """FP64 and FP32 FMA microbenchmark peaks (best of repeated runs over about
+    a second each) with the SM clock sampled while they ran."""
+    from gbhf import _lib
+    out = {}
+    with ClockSampler(local) as clk:
+        for key, prec in (("fp64_tflops", _lib.PREC_FP64), ("fp32_tflops", _lib.PREC_MIXED)):
+            best, t0 = 0.0, time.perf_counter()
+            while time.perf_counter() - t0 < seconds:
+                best = max(best, ctx.peak_flops(prec))
+            out[key] = best
+    out.update({"sm_mhz": clk.summary()["sm_mhz"], "clock_reasons": clk.summary()["reasons"]})
+    return out
+
+
+def batch_measure(args, world, rank, local, mixed_cutoff, grad_cutoff, quick=False):
     """256 seeded conformers (H2O)_n, n in [1, 12], STO-3G (even) / 6-31G (odd):
-    mixed-precision SCF + analytic gradient for every molecule in batched calls,
-    versus one-at-a-time plain FP64 SCFs (timed on a sample and scaled)."""
+    mixed-precision SCF + analytic gradient for every molecule in one batched
+    call, versus one-at-a-time plain FP64 SCF + gradient (timed on every 8th
+    molecule and scaled).  Returns the record (rank 0) or None."""
     import numpy as np
     from gbhf import _lib, basis as B, molecules as M, replicas
-    ctx = _lib.Context(local)
     mols = M.batch_workload()
     flats = [B.flatten(a) for a in mols]
     mine = replicas.shard([f.n_cgf ** 4 for f in flats], world, rank)
     sub = [flats[i] for i in mine]
     mixed = _lib.baseline_opts(precision=_lib.PREC_MIXED, incremental=1, final_fp64=0, full_rebuild_every=0,
-                               mixed_cutoff=args.mixed_cutoff, grad_mixed_cutoff=args.grad_mixed_cutoff)
+                               mixed_cutoff=mixed_cutoff, grad_mixed_cutoff=grad_cutoff)
+    ctx = _lib.Context(local)                                 # its own context: budgets tuned for the batch
     ctx.scf_batch(sub[:16], mixed, gradients=True)          # warm-up (tables, SAD atoms)
     tune = {"enabled": not args.no_autotune}
     if not args.no_autotune:
@@ -332,8 +429,7 @@ def run_batch(args, world, rank, local):
         t0 = time.perf_counter()
         ctx.scf_batch(sub, mixed, gradients=True)
         tune["tuning_run_s"] = time.perf_counter() - t0
-        tune["jk_budgets"] = ctx.task_budgets(0).tolist()
-        tune["grad_budgets"] = ctx.task_budgets(1).tolist()
+        mixed.autotune = 0
     barrier(world)
     ctx.profile_reset(events=False)
     t0 = time.perf_counter()
@@ -341,9 +437,8 @@ def run_batch(args, world, rank, local):
     wall = time.perf_counter() - t0
     prof = ctx.profile_read()
     wall = max_over_ranks(world, wall)
-    # one-at-a-time FP64 SCF + gradient on every 8th molecule of this rank, scaled to the shard
     fp64 = _lib.baseline_opts()
-    sample = list(range(0, len(sub), 8)) if not args.quick else []
+    sample = list(range(0, len(sub), 8)) if not quick else []
     t_single, de, dg = 0.0, [], []
     for k in sample:
         t1 = time.perf_counter()
@@ -354,24 +449,32 @@ def run_batch(args, world, rank, local):
         de.append(abs(r["energy"] - e[k]))
         dg.append(float(np.max(np.abs(g64 - g[k]))))
     single_est = t_single * len(sub) / max(len(sample), 1)
+    ctx.close()
     if rank != 0:
-        return
+        return None
     n_total = len(flats)
-    line = {"workload": "batch256", "metric": "molecules/s (mixed SCF + analytic gradient, batched)",
+    return {"workload": "batch256", "metric": "molecules/s (mixed SCF + analytic gradient, batched)",
             "value": n_total / wall, "unit": "molecules/s", "n_gpus": world, "wall_s": wall,
             "converged": int(cv.sum()) * world, "molecules": n_total,
             "fp64_one_at_a_time_molecules_per_s": len(sub) / single_est if single_est > 0 else None,
             "speedup_vs_fp64_one_at_a_time": single_est / wall * world if wall > 0 else None,
             "max_abs_delta_e_mixed_vs_fp64_sample": float(max(de)) if de else None,
             "max_abs_grad_mixed_vs_fp64_sample": float(max(dg)) if dg else None,
-            "mixed_cutoff": args.mixed_cutoff, "grad_mixed_cutoff": args.grad_mixed_cutoff or args.mixed_cutoff,
-            "sample": f"FP64 one-at-a-time SCF + gradient timed on {len(sample)} of {len(sub)} molecules and scaled",
+            "meets_1e-6_eh_and_1e-5_eh_per_bohr": bool(de and max(de) <= 1e-6 and max(dg) <= 1e-5),
+            "mixed_cutoff": mixed_cutoff, "grad_mixed_cutoff": grad_cutoff,
+            "sample": f"FP64 one-at-a-time SCF + gradient timed on {len(sample)} of {len(sub)} molecules "
+                      "(every 8th) and scaled; dE and gradient errors on the same sample",
             "batch_steps": int(prof["batch_steps"]), "gpu_launches": int(prof["launches"]), "autotune": tune,
             "phases_ms": {k: prof[k] for k in ("ms_pairs", "ms_setup", "ms_fock", "ms_diis", "ms_diag", "ms_other",
                                                "ms_grad")},
             "jk_prim_quartets": prof["prim_quartets_fp64"] + prof["prim_quartets_fp32"],
             "data": "synthetic (256 seeded water conformers)", "dtype": "f32+f64", "higher_is_better": True}
-    print(json.dumps(line), flush=True)
+
+
+def run_batch(args, world, rank, local):
+    rec = batch_measure(args, world, rank, local, args.mixed_cutoff, args.grad_mixed_cutoff, quick=args.quick)
+    if rec is not None:
+        print(json.dumps(rec), flush=True)
 
 
 def run_gradient(args, world, rank, local):
@@ -430,7 +533,6 @@ def run_large(args, world, rank, local, cluster="w64", basis="6-31g"):
     (H2O)64 RHF/6-31G (832 functions); w16d: (H2O)16 RHF/6-31G* (304 functions,
     the d-shell classes)."""
     from gbhf import _lib, basis as B, molecules as M
-    from gbhf.flops_model import F_ALG
     ctx = _lib.Context(local)
     fb = B.flatten(M.cluster_atoms(cluster, basis))
     ctx.set_basis(fb)
@@ -499,6 +601,7 @@ def main():
     ap.add_argument("--quick", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default task budgets")
+    ap.add_argument("--no-batch", action="store_true", help="w16: leave out the 256-conformer batch record")
     ap.add_argument("--mixed-cutoff", type=float, default=1e-2,
                     help="batch256: Schwarz-bound cutoff below which ERIs run in FP32 (the workload leaves "
                          "it free; 1e-2 keeps |dE| vs FP64 near 1e-8 Eh)")

@@ -553,6 +553,18 @@ class SCFNotConverged(RuntimeError):
 
 def scf(fb, opts: Optional[SCFOptions] = None, grid=None):
     """Closed-shell RHF of a ``FlatBasis`` following ``scfHF``/``scfDIIS``."""
+    for item in scf_steps(fb, opts, grid):
+        if item is not None and item[1] is not None:
+            return item[1]
+    raise SCFNotConverged("SCF maxium steps exceeded")   # scf_steps raises first
+
+
+def scf_steps(fb, opts: Optional[SCFOptions] = None, grid=None):
+    """The driver of ``scf``, one SCF iteration at a time: yields ``None``
+    after the setup (integrals, orthogonaliser, start density), then
+    ``(step, result)`` after every iteration, ``result`` being the
+    ``SCFResult`` at convergence and ``None`` before; raises
+    ``SCFNotConverged`` after ``max_iter`` steps (HartreeFock.hs:123)."""
     opts = opts or SCFOptions.reference()
     ob = OracleBasis(fb, grid)
     ref = opts.ref_compat
@@ -584,6 +596,7 @@ def scf(fb, opts: Optional[SCFOptions] = None, grid=None):
             raise ValueError("guess density does not match the basis")
     else:
         _, density, _ = diagonal_hf(core, x, occupied)
+    yield None
     dat = DataDIIS(size=opts.diis_size)
     switch = False
     energies = []
@@ -597,15 +610,18 @@ def scf(fb, opts: Optional[SCFOptions] = None, grid=None):
             etot = variational_e(core, f_diis, new_density) + e_nn
             energies.append(etot)
             if step != 0 and np.max(np.abs(err)) < opts.conv_error:
-                return SCFResult(etot, f_diis, c, new_density, eps, step + 1, energies, True)
+                yield step, SCFResult(etot, f_diis, c, new_density, eps, step + 1, energies, True)
+                return
         else:
             etot = variational_e(core, f, density) + e_nn
             energies.append(etot)
             rms = float(np.sqrt(np.mean((tri_to_square(new_density) - tri_to_square(density)) ** 2)))
             if e_prev is not None and abs(etot - e_prev) < opts.conv_energy and rms < opts.conv_density:
-                return SCFResult(etot, f, c, new_density, eps, step + 1, energies, True)
+                yield step, SCFResult(etot, f, c, new_density, eps, step + 1, energies, True)
+                return
             e_prev = etot
         density = new_density
+        yield step, None
     raise SCFNotConverged("SCF maxium steps exceeded")
 
 

@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 
 from gbhf import basis as B, molecules as M, replicas
-from gbhf.flops_model import F_ALG
+from gbhf.flops_model import DEFERRED, F_ALG, F_KERNEL
 
 
 def test_sp_shell_split_and_normalisation():
@@ -128,3 +128,13 @@ def test_gloo_two_ranks_replica_split():
         assert sorted(got[0] + got[1]) == list(range(len(costs)))
         assert not set(got[0]) & set(got[1])
         assert t == 2.0
+
+
+def test_kernel_flop_model_of_the_deferred_classes():
+    """The deferred-ket classes count the R recursion, Boys values, bra E
+    products and the V contraction per primitive quartet: below F_alg, and
+    F_KERNEL = F_alg for every other class."""
+    assert set(DEFERRED) == {"psps", "ppss", "ppps"}
+    assert (F_KERNEL["psps"], F_KERNEL["ppss"], F_KERNEL["ppps"]) == (165, 127, 302)
+    for k, v in F_ALG.items():
+        assert F_KERNEL[k] < v if k in DEFERRED else F_KERNEL[k] == v
