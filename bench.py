@@ -123,32 +123,6 @@ def traffic_profile():
     return json.loads(p.read_text()) if p.exists() else {}
 
 
-def oracle_sample(fb, n_iter):
-    """CPU oracle: setup + one full direct Fock build + one diagonalisation, all host threads.
-
-    The Fock build screens by the Schwarz bound only, as the reference's own build
-    does: the SAD start density is block-diagonal by atom, and the per-quartet
-    density test would drop most quartets of this one build but not of the later
-    SCF steps the estimate stands for."""
-    import numpy as np
-    import oracle as O
-    nth = O.lib().orc_num_threads()
-    t0 = time.perf_counter()
-    ob = O.OracleBasis(fb)
-    core = ob.hcore(False)
-    s = ob.overlap(False)
-    x = O.symm_ortho(O.tri_to_square(s))
-    d = O.sad_density(fb)
-    t1 = time.perf_counter()
-    f, st = ob.fock_direct(core, d, 1e-12, density_screen=False)
-    err = O.calc_error_mtx(f, s, d, x)
-    O.diagonal_hf(f, x, fb.n_occupied)
-    t2 = time.perf_counter()
-    setup, per_iter = t1 - t0, t2 - t1
-    return {"setup_s": setup, "iteration_s": per_iter, "threads": nth, "fn_quartet_stats": st.tolist(),
-            "estimate": setup + n_iter * per_iter, "max_err": float(np.max(np.abs(err)))}
-
-
 class OracleSCFSteps:
     """Complete FP64 oracle SCFs of one molecule, one SCF iteration per step.
 
@@ -384,11 +358,16 @@ def run_gbhf(args, world, rank, local):
     if peaks:
         line["measured_peaks"] = {"hbm_gbs": peaks.get("hbm_gbs"), "bf16_tflops": peaks.get("bf16_tflops")}
     if world == 1 and not args.no_cpu_baseline:
-        cb = oracle_sample(fb, r64["iterations"])
-        line["cpu_baseline"] = {"value": cb["estimate"], "unit": "s/molecule", "cores": cb["threads"], "kind": "port",
-                                "sample": f"FP64 oracle on the host: setup + 1 direct Fock build (Schwarz screening only) + DIIS error + "
-                                          f"diagonalisation, SCF time = setup + {r64['iterations']} x iteration "
-                                          f"(the FP64 GPU SCF's iteration count)"}
+        # one complete FP64 oracle SCF of the same molecule on all host threads
+        import oracle as O
+        steps = OracleSCFSteps(fb)
+        while not steps.complete:
+            steps.step()
+        secs, iters, e_cpu = steps.complete[0]
+        line["cpu_baseline"] = {"value": secs, "unit": "s/molecule", "cores": O.lib().orc_num_threads(), "kind": "port",
+                                "sample": f"one complete FP64 oracle SCF of the workload ({iters} iterations, "
+                                          f"E = {e_cpu:.10f}): setup, SAD start, direct Fock builds with Schwarz "
+                                          "and density screening, DIIS, diagonalisations"}
     print(json.dumps(line), flush=True)
 
 

@@ -77,3 +77,47 @@ def test_calls_without_gpu_fail_cleanly(lib):
     assert n.value == 0
     with pytest.raises(_lib.GBHFError):
         _lib.Context(0)
+
+
+HS = _lib.HEADER.parents[1] / "haskell-abinitio_gb300" / "haskell" / "Science" / "QuantumChemistry" / "GPU.hs"
+
+
+def _c_prototypes():
+    text = re.sub(r"/\*.*?\*/", " ", _lib.HEADER.read_text(), flags=re.S)
+    out = {}
+    for m in re.finditer(r"\b(gbhf_[a-z0-9_]+)\s*\(([^)]*)\)\s*;", text):
+        args = [a for a in m.group(2).split(",") if a.strip() and a.strip() != "void"]
+        out[m.group(1)] = len(args)
+    return out
+
+
+def test_haskell_binding_matches_the_header():
+    """The Haskell module's foreign imports name declared entry points with the
+    C argument counts, and its struct offsets are the C layout's."""
+    src = HS.read_text()
+    protos = _c_prototypes()
+    imports = re.findall(r'foreign import ccall (?:safe|unsafe) "(gbhf_[a-z0-9_]+)"\s*\n\s*(\w+)\s*::([^\n]*(?:\n\s+->[^\n]*)*)',
+                         src)
+    assert len(imports) >= 14
+    for cname, hname, ty in imports:
+        assert cname in protos, cname
+        arrows = ty.count("->")
+        assert arrows == max(protos[cname], 1) if protos[cname] else arrows in (0, 1), (cname, arrows, protos[cname])
+
+    def const(name):
+        return int(re.search(rf"^{name} = (\d+)$", src, flags=re.M).group(1))
+
+    def lst(name):
+        return [int(v) for v in re.search(rf"^{name} = \[([^\]]*)\]", src, flags=re.M).group(1).split(",")]
+
+    o, r = _lib.SCFOpts, _lib.SCFResultC
+    names = [f for f, _ in o._fields_]
+    assert lst("scfOptsIntOffsets") == [getattr(o, f).offset for f in names[:9]]
+    assert lst("scfOptsDoubleOffsets") == [getattr(o, f).offset for f in names[9:17]]
+    assert const("scfOptsAutotuneOffset") == o.autotune.offset
+    assert const("scfOptsSize") == C.sizeof(o)
+    assert const("scfResultSize") == C.sizeof(r)
+    for hs_name, field in (("resEnergy", "energy"), ("resIterations", "iterations"), ("resConverged", "converged"),
+                           ("resNOccupied", "n_occupied"), ("resFock", "fock_flat"), ("resCoeff", "coeff"),
+                           ("resDensity", "density_flat"), ("resOrbE", "orb_energies")):
+        assert const(hs_name) == getattr(r, field).offset, hs_name
