@@ -502,6 +502,47 @@ gbhf_status gbhf_gradient(gbhf_ctx* c, int precision, double schwarz_cutoff, con
   return download(c, grad, g.p, 3 * (size_t)na * sizeof(double));
 }
 
+gbhf_status gbhf_gradient_uhf(gbhf_ctx* c, int precision, double schwarz_cutoff, const double* da_flat,
+                              const double* db_flat, const double* w_flat, double* grad) {
+  CTX_CHECK(c);
+  if (precision != GBHF_PREC_FP64 && precision != GBHF_PREC_MIXED)
+    return fail(c, GBHF_ERR_BAD_INPUT, "precision must be GBHF_PREC_FP64 or GBHF_PREC_MIXED");
+  if (!need_basis(c)) return GBHF_ERR_BAD_INPUT;
+  if (!grad || !(schwarz_cutoff >= 0)) return fail(c, GBHF_ERR_BAD_INPUT, "bad arguments");
+  const bool given = da_flat || db_flat || w_flat;
+  if (given && !(da_flat && db_flat && w_flat))
+    return fail(c, GBHF_ERR_BAD_INPUT, "give D_alpha, D_beta and W, or none (use the last UHF SCF)");
+  const int n = c->basis.nbf, na = c->basis.natoms;
+  const size_t nn = (size_t)n * n, ntri = (size_t)n * (n + 1) / 2;
+  const double *Da = nullptr, *Db = nullptr, *W = nullptr;
+  GBHF_WS(c, Sa, 15, nn);
+  GBHF_WS(c, Sb, 16, nn);
+  GBHF_WS(c, Sw, 18, nn);
+  GBHF_WS(c, t, 17, std::max(ntri, (size_t)n));
+  if (given) {
+    const double* src[3] = {da_flat, db_flat, w_flat};
+    double* dst[3] = {Sa, Sb, Sw};
+    for (int k = 0; k < 3; ++k) {
+      GBHF_CUDA(c, cudaMemcpyAsync(t, src[k], ntri * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+      GBHF_TRY(flat_to_square(c, n, t, dst[k]));
+      GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
+    }
+    Da = Sa;
+    Db = Sb;
+    W = Sw;
+  } else {
+    if (c->last_ugen != c->basis_gen || !c->last_uDa.p)
+      return fail(c, GBHF_ERR_BAD_INPUT, "no converged UHF SCF for this basis: run gbhf_scf_uhf first or pass the densities");
+    Da = c->last_uDa.p;
+    Db = c->last_uDb.p;
+    W = c->last_uW.p;
+  }
+  DBuf<double> g;
+  GBHF_CUDA(c, g.alloc(3 * (size_t)na));
+  GBHF_TRY(gradient_uhf_dev(c, Da, Db, W, schwarz_cutoff, 1e-4, precision, g.p));
+  return download(c, grad, g.p, 3 * (size_t)na * sizeof(double));
+}
+
 static int budget_classes(int which) { return which == 0 ? NCOMBO : which == 1 ? NCOMBO_MAX : 0; }
 
 gbhf_status gbhf_get_task_budgets(gbhf_ctx* c, int which, int* budgets, int n) {

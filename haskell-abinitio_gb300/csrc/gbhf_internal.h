@@ -313,6 +313,10 @@ struct gbhf_ctx {
   bool force_jacobi = false;      // GBHF_EIGEN=jacobi at gbhf_create: every eigen-solve by Jacobi
   // state of the last SCF (for the gradient): density, Fock matrix, occupation
   gbhf::DBuf<double> last_D, last_F;
+  // state of the last converged UHF SCF: alpha and beta densities, energy-weighted density
+  gbhf::DBuf<double> last_uDa, last_uDb, last_uW;
+  long last_ugen = -1;
+  double grad_jcoef = 1.0;        // Coulomb weight in the gradient kernels' Gamma (0: exchange only)
   gbhf::DBuf<double> guess_D;        // gbhf_set_guess_density (flat), valid for basis generation guess_gen
   long guess_gen = -1;
   std::vector<double> scf_trace;     // per-step records of the last SCF (GBHF_SCF_TRACE_FIELDS each)
@@ -505,6 +509,8 @@ void default_budgets(gbhf_ctx* c, int which);
 bool lane_per_ket(int which, int k);
 gbhf_status autotune_dev(gbhf_ctx* c, int which, const double* d_D, int precision, double schwarz,
                          double mixed_cutoff, int reps, double* class_ms);
+gbhf_status gradient_uhf_dev(gbhf_ctx* c, const double* d_Da, const double* d_Db, const double* d_W, double schwarz,
+                             double mixed_cutoff, int precision, double* d_grad);
 gbhf_status grad_2e(gbhf_ctx* c, const double* d_D, double schwarz, double mixed_cutoff, int precision,
                     double* d_grad);
 // grad.cu: D, W square on the device; gradient (3*natoms) on the device

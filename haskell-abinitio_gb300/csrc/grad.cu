@@ -12,6 +12,13 @@
 // coefficients: dE^(ij)_t/dA_x = 2a E^(i+1,j)_t - i E^(i-1,j)_t.
 // Translational invariance gives the fourth centre of an ERI and the
 // operator centre of a nuclear-attraction integral.
+//
+// Open shell (UHF): with D = D_a + D_b, D_s = D_a - D_b and
+// W = sum_s C_s,occ eps_s C_s,occ^T, the two-electron density is
+// Gamma = D_ab D_cd - (D_a,ac D_a,bd + D_b,ac D_b,bd + D_a,ad D_a,bc + D_b,ad D_b,bc)/2
+//       = Gamma_RHF(D) - (D_s,ac D_s,bd + D_s,ad D_s,bc)/4,
+// so the kernels run twice: on D as above, and on D_s with the Coulomb
+// weight jcoef = 0 (gradient_uhf_dev).
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -99,6 +106,7 @@ struct GradArgs {
   const float* Qf;
   double thr;                // drop a quartet when Q_ab Q_cd max|Gamma_abcd| is below
   float thrf;
+  T jcoef;                   // weight of the Coulomb term D_ab D_cd in Gamma (0: exchange only)
 };
 
 __device__ __forceinline__ double warp_sum_d(double v) {
@@ -166,7 +174,7 @@ __global__ void __launch_bounds__(GR_THREADS) k_grad_jk(GradArgs<T> a) {
       const int C = a.pA[jk], Dd = a.pB[jk];
       const int c0 = a.shell_f0[C], d0 = a.shell_f0[Dd];
       T gmax = T(0);
-      // Gamma_abcd = D_ab D_cd - (D_ac D_bd + D_ad D_bc) / 4
+      // Gamma_abcd = jcoef D_ab D_cd - (D_ac D_bd + D_ad D_bc) / 4
 #pragma unroll
       for (int ia = 0; ia < NA; ++ia)
 #pragma unroll
@@ -181,7 +189,7 @@ __global__ void __launch_bounds__(GR_THREADS) k_grad_jk(GradArgs<T> a) {
               const T dbd = Dm[(long long)(b0 + ibb) * n + d0 + id];
               const T dad = Dm[(long long)(a0 + ia) * n + d0 + id];
               const T dbc = Dm[(long long)(b0 + ibb) * n + c0 + ic];
-              T gv = dab * dcd - T(0.25) * (dac * dbd + dad * dbc);
+              T gv = a.jcoef * dab * dcd - T(0.25) * (dac * dbd + dad * dbc);
               if constexpr (LA == 2 || LB == 2 || LC == 2 || LD == 2) {   // d components: scaled functions
                 if (LA == 2) gv *= T(a.sscale[6 * A + ia]);
                 if (LB == 2) gv *= T(a.sscale[6 * B + ibb]);
@@ -278,6 +286,7 @@ static gbhf_status launch_grad_class(gbhf_ctx* c, cudaStream_t strm, int combo, 
   a.Qf = P.Qf.p;
   a.thr = gt.thr_exact;
   a.thrf = (float)gt.thr_exact;
+  a.jcoef = T(c->grad_jcoef);
   kern<<<grid, GR_THREADS, smem, strm>>>(a);
   count_launch(c);
   GBHF_CUDA(c, cudaGetLastError());
@@ -725,6 +734,24 @@ __global__ void k_scale_occ(int n, int nocc, const double* __restrict__ C, const
   const int i = blockIdx.y, j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= nocc) return;
   out[(long)i * nocc + j] = C[(long)i * n + j] * eps[j];
+}
+
+// UHF gradient: D_a, D_b and W square (device), gradient into d_grad.
+gbhf_status gradient_uhf_dev(gbhf_ctx* c, const double* d_Da, const double* d_Db, const double* d_W, double schwarz,
+                             double mixed_cutoff, int precision, double* d_grad) {
+  const size_t nn = (size_t)c->basis.nbf * c->basis.nbf;
+  DBuf<double> DT, DS;
+  GBHF_CUDA(c, DT.alloc(nn));
+  GBHF_CUDA(c, DS.alloc(nn));
+  GBHF_TRY(axpby(c, nn, 1.0, d_Da, 1.0, d_Db, DT.p));
+  GBHF_TRY(axpby(c, nn, 1.0, d_Da, -1.0, d_Db, DS.p));
+  GBHF_TRY(gradient_dev(c, DT.p, d_W, schwarz, mixed_cutoff, precision, d_grad));
+  c->grad_jcoef = 0.0;
+  const gbhf_status st = grad_2e(c, DS.p, schwarz, mixed_cutoff, precision, d_grad);
+  c->grad_jcoef = 1.0;
+  GBHF_TRY(st);
+  GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
+  return GBHF_OK;
 }
 
 gbhf_status energy_weighted_density(gbhf_ctx* c, int n, int nocc, const double* d_C, const double* d_eps,

@@ -4,7 +4,7 @@
 // pair of shell pairs with weights (2 - delta_AB)(2 - delta_CD), the
 // bra-centre terms give the whole two-electron gradient.
 //
-// Per quartet the warp forms Gamma_abcd = D_ab D_cd - (D_ac D_bd + D_ad D_bc)/4
+// Per quartet the warp forms Gamma_abcd = jcoef D_ab D_cd - (D_ac D_bd + D_ad D_bc)/4
 // (with the pair weights and the d-component scales) in shared memory; per
 // primitive quartet it builds X[h][cd] for the bra Hermite range one order up
 // and contracts Z[ab][h] = sum_cd Gamma_abcd X[h][cd] with the derivative
@@ -46,6 +46,7 @@ struct GradDArgs {
   const double* Q;       // Schwarz bound of each pair
   double thr;            // drop a quartet when Q_ab Q_cd max|Gamma_abcd| is below
   double* grad;
+  T jcoef;               // weight of the Coulomb term D_ab D_cd in Gamma (0: exchange only)
 };
 
 template <int LA, int LB, int LC, int LD, typename T>
@@ -92,7 +93,7 @@ __global__ void __launch_bounds__(GRD_THREADS) k_gradd(GradDArgs<T> a) {
         const T dac = Dm[(long long)(a0 + ia) * n + c0 + ic], dbd = Dm[(long long)(b0 + ibb) * n + d0 + id];
         const T dad = Dm[(long long)(a0 + ia) * n + d0 + id], dbc = Dm[(long long)(b0 + ibb) * n + c0 + ic];
         const double sc = a.sscale[6 * A + ia] * a.sscale[6 * B + ibb] * a.sscale[6 * Cs + ic] * a.sscale[6 * Ds + id];
-        const T gv = (dab * dcd - T(0.25) * (dac * dbd + dad * dbc)) * T(sc);
+        const T gv = (a.jcoef * dab * dcd - T(0.25) * (dac * dbd + dad * dbc)) * T(sc);
         Gam[e] = gv * wgt;
         gmax = fmax(gmax, fabs((double)gv));
       }
@@ -167,6 +168,7 @@ static gbhf_status launch_gradd_t(gbhf_ctx* c, cudaStream_t strm, int combo, int
   a.sscale = c->tasks.sscale.p;
   a.Q = P.Q.p;
   a.thr = gt.thr_exact;
+  a.jcoef = T(c->grad_jcoef);
   a.D = D;
   a.boys = boys;
   a.grad = grad;

@@ -233,6 +233,20 @@ gbhf_status uhf_run(gbhf_ctx* c, const gbhf_scf_opts* o, int multiplicity, gbhf_
     GBHF_CUDA(c, cudaMemcpyAsync(Db.p, Nb.p, nn * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
     if (converged) break;
   }
+  if (converged) {
+    // keep the converged state for gbhf_gradient_uhf: D_a, D_b and
+    // W = D_a F_a D_a + D_b F_b D_b (= sum_s C_s,occ eps_s C_s,occ^T)
+    GBHF_CUDA(c, c->last_uDa.alloc(nn));
+    GBHF_CUDA(c, c->last_uDb.alloc(nn));
+    GBHF_CUDA(c, c->last_uW.alloc(nn));
+    GBHF_CUDA(c, cudaMemcpyAsync(c->last_uDa.p, Da.p, nn * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+    GBHF_CUDA(c, cudaMemcpyAsync(c->last_uDb.p, Db.p, nn * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+    GBHF_TRY(gemm(c, false, false, n, n, n, 1.0, Fa.p, n, Da.p, n, 0.0, T1.p, n));
+    GBHF_TRY(gemm(c, false, false, n, n, n, 1.0, Da.p, n, T1.p, n, 0.0, c->last_uW.p, n, true));
+    GBHF_TRY(gemm(c, false, false, n, n, n, 1.0, Fb.p, n, Db.p, n, 0.0, T1.p, n));
+    GBHF_TRY(gemm(c, false, false, n, n, n, 1.0, Db.p, n, T1.p, n, 1.0, c->last_uW.p, n, true));
+    c->last_ugen = c->basis_gen;
+  }
   if (r) {
     r->energy = energy;
     r->iterations = std::min(step + 1, o->max_iter);

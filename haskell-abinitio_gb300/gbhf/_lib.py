@@ -102,6 +102,7 @@ def load():
         "gbhf_scf_opts_baseline": (None, [C.POINTER(SCFOpts)]),
         "gbhf_scf": (st, [_vp, C.POINTER(SCFOpts), C.POINTER(SCFResultC)]),
         "gbhf_gradient": (st, [_vp, C.c_int, C.c_double, _dp, _dp, _dp]),
+        "gbhf_gradient_uhf": (st, [_vp, C.c_int, C.c_double, _dp, _dp, _dp, _dp]),
         "gbhf_scf_batch": (st, [_vp, C.c_int, _ip, _ip, _dp, _dp, _ip, _ip, _ip, _dp, _dp, C.POINTER(SCFOpts),
                                 _dp, _ip, _ip, _dp]),
         "gbhf_profile_reset": (st, [_vp, C.c_int]),
@@ -399,6 +400,19 @@ class Context:
         else:
             d, w = _f64(d_flat), _f64(w_flat)
             s = self.L.gbhf_gradient(self.h, precision, schwarz, _d(d), _d(w), _d(g))
+        self._check(s)
+        return g.reshape(na, 3)
+
+    def gradient_uhf(self, da_flat=None, db_flat=None, w_flat=None, schwarz=1e-12, precision=PREC_FP64):
+        """Open-shell dE/dR (n_atoms, 3) in hartree/bohr.  Without densities:
+        the last converged UHF SCF of this basis."""
+        na = self._keep[1].size
+        g = np.zeros(3 * na)
+        if da_flat is None:
+            s = self.L.gbhf_gradient_uhf(self.h, precision, schwarz, None, None, None, _d(g))
+        else:
+            da, db, w = _f64(da_flat), _f64(db_flat), _f64(w_flat)
+            s = self.L.gbhf_gradient_uhf(self.h, precision, schwarz, _d(da), _d(db), _d(w), _d(g))
         self._check(s)
         return g.reshape(na, 3)
 

@@ -261,6 +261,16 @@ gbhf_status gbhf_scf(gbhf_ctx* ctx, const gbhf_scf_opts* opts, gbhf_result* resu
 gbhf_status gbhf_gradient(gbhf_ctx* ctx, int precision, double schwarz_cutoff, const double* d_flat,
                           const double* w_flat, double* grad);
 
+/* Analytic unrestricted (open-shell) gradient, the backward call of
+ * gbhf_scf_uhf; no counterpart in the reference, which has neither an
+ * open-shell driver (--multi is parsed and ignored, Main.hs:55) nor a working
+ * gradient (Derivatives.hs:40-48).  da_flat, db_flat: alpha and beta densities
+ * D_s = C_s,occ C_s,occ^T; w_flat: W = sum_s C_s,occ eps_s C_s,occ^T (all flat,
+ * N(N+1)/2); all three NULL: the last converged gbhf_scf_uhf of this basis.
+ * grad[3*atom + axis] in hartree/bohr; screening and precision as gbhf_gradient. */
+gbhf_status gbhf_gradient_uhf(gbhf_ctx* ctx, int precision, double schwarz_cutoff, const double* da_flat,
+                              const double* db_flat, const double* w_flat, double* grad);
+
 /* Many molecules in one call (batched SCF, no counterpart in the reference,
  * whose scfHF takes one molecule): molecule k owns atoms
  * [atom_off[k], atom_off[k+1]) and CGFs [cgf_off[k], cgf_off[k+1]) of the
