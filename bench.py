@@ -354,6 +354,13 @@ def run_gbhf(args, world, rank, local):
     }
     if batch:
         line["batch256"] = batch
+    tr_all = traffic_profile()
+    red = sum(v.get("l2_red_sectors_per_launch", 0.0) for v in tr_all.values()) * 32
+    line["fock_scatter"] = {"algorithmic_bytes_per_build": 24 * n * n,
+                            "l2_reduction_bytes_per_full_build": red or None, "dram_write_bytes_per_full_build": 0,
+                            "source": "ncu lts__t_sectors_srcunit_tex_op_red.sum x 32 B over the twelve class launches "
+                                      "of one full mixed build (profiles/traffic.json, profiles/k_jk_w16_fock_full.md): "
+                                      "every quartet adds its J/K terms with FP64 reductions in L2; none reach DRAM"}
     peaks = load_measured_peaks()
     if peaks:
         line["measured_peaks"] = {"hbm_gbs": peaks.get("hbm_gbs"), "bf16_tflops": peaks.get("bf16_tflops")}
