@@ -330,6 +330,7 @@ struct gbhf_ctx {
   gbhf::DBuf<float> dfloat;
   gbhf::DBuf<int> dev_status;
   int purify_grid = 0;              // co-resident blocks of the fused purification kernel
+  int tc2_grid = 0;                 // co-resident blocks of the one-barrier TC2 kernel
   gbhf::DBuf<unsigned> barrier;
   gbhf::DBuf<double> small;
   gbhf::Profile prof;

@@ -842,7 +842,8 @@ __global__ void k_purify_coef(int n, const double* __restrict__ P, const double*
   }
 }
 
-// The whole purification in one cooperative launch: per step the symmetric
+// The canonical purification (two GEMMs per step) in one cooperative launch;
+// the trace-correcting one runs in k_tc2_fused below.  Per step the symmetric
 // products P2 = P P and P3 = P P2 are shared out as (upper tile, k slice) items
 // with atomic accumulation, their traces summed in the tile epilogues; then
 // every block derives the step's coefficients from the same three traces (so
@@ -973,6 +974,164 @@ __global__ void __launch_bounds__(128) k_purify_fused(PurifyArgs a) {
   }
 }
 
+// Trace-correcting purification with one grid barrier per step.  Step s
+// computes P2_s = P_s P_s while P_s itself is only formed on the fly:
+// P_s = ca P_(s-1) + cb P2_(s-1) (tc2_next) when the GEMM tiles are loaded, and
+// written out (for step s + 1) by a strided pass that runs beside the GEMM.
+// P alternates between two buffers, P2 rotates over three (the one zeroed in
+// step s was last read in step s - 1), and the traces of P_s and P2_s sit in
+// three rotating slots, so that the single barrier at the end of a step is the
+// only ordering needed.  After the barrier every block takes the same step
+// decision from the same two traces.
+struct Tc2Args {
+  int n, ne, max_steps;
+  double tol;
+  double *P0, *P1;        // P0 holds P_0 at launch; the result is copied back there
+  double *Q0, *Q1, *Q2;   // the three P2 buffers, zero at launch
+  double* tr;        // 6 slots: tr P_s at 2 (s % 3), tr P2_s at 2 (s % 3) + 1; zero at launch
+  double* out;       // [0] last tr(P - P^2), [1] steps
+  unsigned* bar;
+  int* status;
+};
+
+// The one formula for an element of P_s, used by the GEMM loads and by the
+// pass that writes P_s out, so that both give the same bits.
+__device__ __forceinline__ double tc2_next(double ca, double cb, double p, double p2) {
+  return __fma_rn(ca, p, __dmul_rn(cb, p2));
+}
+
+// GEMM units of a step: (16 x 16 tile on or above the diagonal, 16-long k
+// chunk), one warp each, fragments loaded straight from global memory (P_s is
+// exactly symmetric, so the column fragment of B is a row fragment of P_s) and
+// multiplied by DMMA; the tile (and its mirror) is added into P2_s with FP64
+// atomics.  256 threads per block.
+constexpr int TC2_THREADS = 256, TC2_T = 16, TC2_K = 16;
+
+__global__ void __launch_bounds__(TC2_THREADS) k_tc2_fused(Tc2Args a) {
+  __shared__ double s_red[TC2_THREADS / 32];
+  const int n = a.n, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const long nn = (long)n * n;
+  const int nt = (n + TC2_T - 1) / TC2_T, nkc = (n + TC2_K - 1) / TC2_K;
+  const int units = nt * (nt + 1) / 2 * nkc;
+  const int gwarp = blockIdx.x * (TC2_THREADS / 32) + warp, nwarps = gridDim.x * (TC2_THREADS / 32);
+  const long gt = blockIdx.x * (long)blockDim.x + tid, gs = (long)gridDim.x * blockDim.x;
+  unsigned epoch = 0;
+  auto block_sum_add = [&](double v, double* dst) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) s_red[warp] = v;
+    __syncthreads();
+    if (tid == 0) {
+      double t = 0.0;
+#pragma unroll
+      for (int w = 0; w < TC2_THREADS / 32; ++w) t += s_red[w];
+      if (t != 0.0) atomicAdd(dst, t);
+    }
+    __syncthreads();
+  };
+  auto pbuf = [&](int i) -> double* { return i == 0 ? a.P0 : a.P1; };
+  auto qbuf = [&](int i) -> double* { return i == 0 ? a.Q0 : (i == 1 ? a.Q1 : a.Q2); };
+  {
+    double v = 0;
+    for (long i = gt; i < n; i += gs) v += a.P0[i * n + i];
+    block_sum_add(v, a.tr);   // tr P_0 in slot 0
+  }
+  if (!grid_barrier(a.bar, epoch, a.status)) return;
+  double ca = 1.0, cb = 0.0;   // P_s = ca P_(s-1) + cb P2_(s-1); step 0 reads P_0 as it is
+  int step = 0, final_buf = 0;
+  for (; step < a.max_steps; ++step) {
+    const double* Pin = pbuf(step == 0 ? 0 : (step - 1) & 1);   // P_(s-1) (P_0 at step 0)
+    const double* P2in = qbuf(step == 0 ? 2 : (step - 1) % 3);  // P2_(s-1) (zero at step 0)
+    double* Pout = pbuf(step & 1);
+    double* P2out = qbuf(step % 3);
+    double* trp = a.tr + 2 * (step % 3);
+    // the slots of step s + 1, last read after the barrier of step s - 2
+    if (gt == 0) {
+      a.tr[2 * ((step + 1) % 3)] = 0.0;
+      a.tr[2 * ((step + 1) % 3) + 1] = 0.0;
+    }
+    if (step > 0) {
+      // P_s written out with its trace (step 0: P_0 is already in P0), and the
+      // P2 buffer of step s + 1 cleared (it held P2_(s-2), read during step s - 1)
+      double* z = qbuf((step + 1) % 3);
+      double dsum = 0;
+      for (long e = gt; e < nn; e += gs) {
+        const double v = tc2_next(ca, cb, Pin[e], P2in[e]);
+        Pout[e] = v;
+        z[e] = 0.0;
+        if (e / n == e % n) dsum += v;
+      }
+      block_sum_add(dsum, trp);
+    }
+    // P2_s = P_s P_s
+    double dtr = 0.0;
+    for (int u = gwarp; u < units; u += nwarps) {
+      int t = u / nkc;
+      const int kc = u - t * nkc;
+      int rt = 0;
+      while (t >= nt - rt) {
+        t -= nt - rt;
+        ++rt;
+      }
+      const int ct = rt + t;
+      const int k0 = kc * TC2_K;
+      const int r = lane >> 2, q = lane & 3;
+      double af[TC2_K / 4][2], bf[TC2_K / 4][2];
+#pragma unroll
+      for (int k4 = 0; k4 < TC2_K / 4; ++k4) {
+        const int k = k0 + 4 * k4 + q;
+#pragma unroll
+        for (int i = 0; i < 2; ++i) {
+          const int row = rt * TC2_T + 8 * i + r, col = ct * TC2_T + 8 * i + r;
+          double va = 0.0, vb = 0.0;
+          if (row < n && k < n) va = tc2_next(ca, cb, Pin[(long)row * n + k], P2in[(long)row * n + k]);
+          if (col < n && k < n) vb = tc2_next(ca, cb, Pin[(long)col * n + k], P2in[(long)col * n + k]);
+          af[k4][i] = va;
+          bf[k4][i] = vb;
+        }
+      }
+      double acc[2][2][2] = {};
+#pragma unroll
+      for (int k4 = 0; k4 < TC2_K / 4; ++k4)
+#pragma unroll
+        for (int i = 0; i < 2; ++i)
+#pragma unroll
+          for (int j = 0; j < 2; ++j) dmma(acc[i][j][0], acc[i][j][1], af[k4][i], bf[k4][j]);
+#pragma unroll
+      for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 2; ++j)
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            const int row = rt * TC2_T + 8 * i + r, col = ct * TC2_T + 8 * j + 2 * q + h;
+            if (row < n && col < n) {
+              const double v = acc[i][j][h];
+              atomicAdd(P2out + (long)row * n + col, v);
+              if (rt < ct) atomicAdd(P2out + (long)col * n + row, v);
+              if (row == col) dtr += v;
+            }
+          }
+    }
+    block_sum_add(dtr, trp + 1);
+    if (!grid_barrier(a.bar, epoch, a.status)) return;
+    // the same decision in every block
+    const double t1 = *((volatile double*)trp), t2 = *((volatile double*)(trp + 1));
+    const double den = t1 - t2;
+    if (gt == 0) {
+      a.out[0] = den;
+      a.out[1] = step + 1;
+    }
+    final_buf = step == 0 ? 0 : (step & 1);
+    if (fabs(den) < a.tol * max(1, a.ne)) break;
+    const bool sq = fabs(t2 - a.ne) < fabs(2 * t1 - t2 - a.ne);
+    ca = sq ? 0.0 : 2.0;
+    cb = sq ? 1.0 : -1.0;
+  }
+  // the converged P_s back into P0
+  if (final_buf != 0)
+    for (long e = gt; e < nn; e += gs) a.P0[e] = a.P1[e];
+}
+
 // TC2 start: the spectrum of F mapped onto [0, 1], reversed (P0 = (hi I - F) / (hi - lo)).
 __global__ void k_tc2_init(int n, const double* __restrict__ F, const double* __restrict__ g, double* __restrict__ P) {
   const int i = blockIdx.y, j = blockIdx.x * blockDim.x + threadIdx.x;
@@ -988,8 +1147,9 @@ __global__ void k_tc2_init(int n, const double* __restrict__ F, const double* __
 // P <- P^2 or 2P - P^2 by the trace, one GEMM per step; on water clusters it
 // needs ~24 steps where the canonical purification (Palser & Manolopoulos,
 // Phys. Rev. B 58, 12704 (1998); trace-conserving cubic polynomials, two GEMMs
-// per step, tc2 = false) needs ~17, so a third fewer GEMMs.  Returns the
-// idempotency error tr(P - P^2) of the result.
+// per step, tc2 = false) needs ~17, so a third fewer GEMMs.  TC2 runs the
+// one-barrier kernel k_tc2_fused.  Returns the idempotency error tr(P - P^2)
+// of the result.
 gbhf_status purify(gbhf_ctx* c, int n, int ne, const double* d_F, double* d_P, double* err_out, bool tc2) {
   const size_t nn = (size_t)n * n;
   GBHF_WS(c, P2, 23, nn);
@@ -1010,35 +1170,70 @@ gbhf_status purify(gbhf_ctx* c, int n, int ne, const double* d_F, double* d_P, d
   GBHF_CUDA(c, cudaMemsetAsync(tr, 0, 16 * sizeof(double), c->stream));
   GBHF_CUDA(c, cudaMemsetAsync(c->jac.bar.p, 0, 2 * sizeof(unsigned), c->stream));
   GBHF_CUDA(c, cudaMemsetAsync(c->dev_status.p, 0, sizeof(int), c->stream));
-  PurifyArgs a;
-  a.n = n;
-  a.ne = ne;
-  a.nt = (n + ST - 1) / ST;
-  const int ntile = a.nt * (a.nt + 1) / 2;
+  const int nt = (n + ST - 1) / ST;
+  const int ntile = nt * (nt + 1) / 2;
   // k slices: about one item per SM, at least two k-steps per slice
-  int ks = std::max(1, std::min((c->nsm + ntile - 1) / ntile, (n + 2 * SK - 1) / (2 * SK)));
-  a.kslice = ((n + ks - 1) / ks + SK - 1) / SK * SK;
-  a.ks = (n + a.kslice - 1) / a.kslice;
-  a.max_steps = 200;
-  a.tc2 = tc2 ? 1 : 0;
-  a.tol = 1e-13;   // E[D] is first order in the idempotency error
-  a.P = d_P;
-  a.P2 = P2;
-  a.P3 = P3;
-  a.tr = tr;
-  a.out = out;
-  a.bar = c->jac.bar.p;
-  a.status = c->dev_status.p;
-  if (c->purify_grid == 0) {
-    int per_sm = 0;
-    GBHF_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_purify_fused, 128, 0));
-    c->purify_grid = std::max(1, c->nsm * std::max(per_sm, 1));
-  }
-  const int grid = std::max(1, std::min(c->purify_grid, ntile * a.ks));
-  void* args[] = {&a};
-  GBHF_CUDA(c, cudaLaunchCooperativeKernel((void*)k_purify_fused, dim3(grid), dim3(128), args, 0, c->stream));
-  count_launch(c);
+  const int ks0 = std::max(1, std::min((c->nsm + ntile - 1) / ntile, (n + 2 * SK - 1) / (2 * SK)));
+  const int kslice = ((n + ks0 - 1) / ks0 + SK - 1) / SK * SK;
+  const int ks = (n + kslice - 1) / kslice;
   double hout[2] = {1.0, 0.0};
+  if (tc2) {
+    // one barrier per step: a second P buffer and three P2 buffers
+    GBHF_CUDA(c, c->jac.t2.alloc(nn));
+    GBHF_CUDA(c, c->jac.t3.alloc(nn));
+    GBHF_CUDA(c, cudaMemsetAsync(c->jac.t2.p, 0, nn * sizeof(double), c->stream));
+    Tc2Args t;
+    t.n = n;
+    t.ne = ne;
+    t.max_steps = 200;
+    t.tol = 1e-13;   // E[D] is first order in the idempotency error
+    t.P0 = d_P;
+    t.P1 = c->jac.t3.p;
+    t.Q0 = P2;
+    t.Q1 = P3;
+    t.Q2 = c->jac.t2.p;
+    t.tr = tr;
+    t.out = out;
+    t.bar = c->jac.bar.p;
+    t.status = c->dev_status.p;
+    if (c->tc2_grid == 0) {
+      int per_sm = 0;
+      GBHF_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tc2_fused, TC2_THREADS, 0));
+      c->tc2_grid = std::max(1, c->nsm * std::min(std::max(per_sm, 1), 2));
+    }
+    const int nt16 = (n + TC2_T - 1) / TC2_T;
+    const long units = (long)nt16 * (nt16 + 1) / 2 * ((n + TC2_K - 1) / TC2_K);
+    const int grid = (int)std::max(1L, std::min<long>(c->tc2_grid, (units + 7) / 8));
+    void* args[] = {&t};
+    GBHF_CUDA(c, cudaLaunchCooperativeKernel((void*)k_tc2_fused, dim3(grid), dim3(TC2_THREADS), args, 0, c->stream));
+    count_launch(c);
+  } else {
+    PurifyArgs a;
+    a.n = n;
+    a.ne = ne;
+    a.nt = nt;
+    a.kslice = kslice;
+    a.ks = ks;
+    a.max_steps = 200;
+    a.tc2 = tc2 ? 1 : 0;
+    a.tol = 1e-13;   // E[D] is first order in the idempotency error
+    a.P = d_P;
+    a.P2 = P2;
+    a.P3 = P3;
+    a.tr = tr;
+    a.out = out;
+    a.bar = c->jac.bar.p;
+    a.status = c->dev_status.p;
+    if (c->purify_grid == 0) {
+      int per_sm = 0;
+      GBHF_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_purify_fused, 128, 0));
+      c->purify_grid = std::max(1, c->nsm * std::max(per_sm, 1));
+    }
+    const int grid = std::max(1, std::min(c->purify_grid, ntile * a.ks));
+    void* args[] = {&a};
+    GBHF_CUDA(c, cudaLaunchCooperativeKernel((void*)k_purify_fused, dim3(grid), dim3(128), args, 0, c->stream));
+    count_launch(c);
+  }
   int st = 0;
   GBHF_CUDA(c, cudaMemcpyAsync(hout, out, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   GBHF_CUDA(c, cudaMemcpyAsync(&st, c->dev_status.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
