@@ -187,6 +187,77 @@ __global__ void __launch_bounds__(128) k_dgemm_split(bool ta, bool tb, bool sym,
   dgemm_tile(ta, tb, sym, m, n, blockIdx.y, blockIdx.x, k0, k1, alpha, A, lda, B, ldb, C, ldc, nullptr, sm);
 }
 
+// Small-matrix variant on warp units: one warp per (16 x 16 tile of C, 16-long
+// k chunk), fragments of op(A) and op(B) loaded straight from global memory
+// (L2-resident for these sizes), DMMA, then alpha * partial added to C with
+// FP64 atomics (C pre-scaled by beta).  sym: only tiles on and above the
+// diagonal, each added at its mirror as well.  With 16 DMMA per unit the work
+// spreads evenly over every SM where 32 x 32 tiles leave SMs idle or doubled.
+constexpr int WG_T = 16, WG_K = 16, WG_THREADS = 256;
+
+__global__ void __launch_bounds__(WG_THREADS) k_dgemm_warp(bool ta, bool tb, bool sym, int m, int n, int k,
+                                                           double alpha, const double* __restrict__ A, int lda,
+                                                           const double* __restrict__ B, int ldb,
+                                                           double* __restrict__ C, int ldc) {
+  const int lane = threadIdx.x & 31;
+  const int gwarp = blockIdx.x * (WG_THREADS / 32) + (threadIdx.x >> 5), nwarps = gridDim.x * (WG_THREADS / 32);
+  const int mt = (m + WG_T - 1) / WG_T, ntl = (n + WG_T - 1) / WG_T, nkc = (k + WG_K - 1) / WG_K;
+  const long ntiles = sym ? (long)ntl * (ntl + 1) / 2 : (long)mt * ntl;
+  const long units = ntiles * nkc;
+  const int r = lane >> 2, q = lane & 3;
+  for (long u = gwarp; u < units; u += nwarps) {
+    long t = u / nkc;
+    const int kc = (int)(u - t * nkc);
+    int rt, ct;
+    if (sym) {
+      rt = 0;
+      while (t >= ntl - rt) {
+        t -= ntl - rt;
+        ++rt;
+      }
+      ct = rt + (int)t;
+    } else {
+      rt = (int)(t / ntl);
+      ct = (int)(t - (long)rt * ntl);
+    }
+    const int k0 = kc * WG_K;
+    double af[WG_K / 4][2], bf[WG_K / 4][2];
+#pragma unroll
+    for (int k4 = 0; k4 < WG_K / 4; ++k4) {
+      const int kk = k0 + 4 * k4 + q;
+#pragma unroll
+      for (int i = 0; i < 2; ++i) {
+        const int row = rt * WG_T + 8 * i + r, col = ct * WG_T + 8 * i + r;
+        double va = 0.0, vb = 0.0;
+        if (row < m && kk < k) va = ta ? A[(long)kk * lda + row] : A[(long)row * lda + kk];
+        if (col < n && kk < k) vb = tb ? B[(long)col * ldb + kk] : B[(long)kk * ldb + col];
+        af[k4][i] = va;
+        bf[k4][i] = vb;
+      }
+    }
+    double acc[2][2][2] = {};
+#pragma unroll
+    for (int k4 = 0; k4 < WG_K / 4; ++k4)
+#pragma unroll
+      for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 2; ++j) dmma(acc[i][j][0], acc[i][j][1], af[k4][i], bf[k4][j]);
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+      for (int j = 0; j < 2; ++j)
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const int row = rt * WG_T + 8 * i + r, col = ct * WG_T + 8 * j + 2 * q + h;
+          if (row < m && col < n) {
+            const double v = alpha * acc[i][j][h];
+            atomicAdd(C + (long)row * ldc + col, v);
+            if (sym && rt < ct) atomicAdd(C + (long)col * ldc + row, v);
+          }
+        }
+  }
+}
+
 __global__ void k_scale_matrix(int m, int n, double beta, double* __restrict__ C, int ldc) {
   const int r = blockIdx.y, cc = blockIdx.x * blockDim.x + threadIdx.x;
   if (cc >= n) return;
@@ -203,6 +274,19 @@ gbhf_status gemm(gbhf_ctx* c, bool ta, bool tb, int m, int n, int k, double alph
     dim3 grid((n + GT - 1) / GT, (m + GT - 1) / GT);
     k_dgemm<<<grid, 128, 0, c->stream>>>(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
     count_launch(c);
+    GBHF_CUDA(c, cudaGetLastError());
+    return GBHF_OK;
+  }
+  if (m <= 1024 && n <= 1024) {
+    // warp units: (16 x 16 tile, 16-long k chunk), about eight per SM or fewer
+    const long t16 = sym ? (long)((n + WG_T - 1) / WG_T) * ((n + WG_T - 1) / WG_T + 1) / 2
+                         : (long)((m + WG_T - 1) / WG_T) * ((n + WG_T - 1) / WG_T);
+    const long units = t16 * ((k + WG_K - 1) / WG_K);
+    const int grid = (int)std::max(1L, std::min<long>((units + WG_THREADS / 32 - 1) / (WG_THREADS / 32),
+                                                      4L * c->nsm));
+    k_scale_matrix<<<dim3((n + 127) / 128, m), 128, 0, c->stream>>>(m, n, beta, C, ldc);
+    k_dgemm_warp<<<grid, WG_THREADS, 0, c->stream>>>(ta, tb, sym, m, n, k, alpha, A, lda, B, ldb, C, ldc);
+    count_launch(c, 2);
     GBHF_CUDA(c, cudaGetLastError());
     return GBHF_OK;
   }
