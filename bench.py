@@ -204,11 +204,16 @@ def run_reference(args, world, rank):
 
 
 def autotune_jk(ctx, fb, args):
-    """Tune the J/K task budgets on the workload's basis (SAD density, mixed
-    precision) before the warm-up; returns a summary for the JSON line."""
+    """With --autotune: tune the J/K task budgets on the workload's basis (SAD
+    density, mixed precision) before the warm-up; returns a summary for the
+    JSON line.  Off by default for this workload: the tuner times one full build
+    on the start density, and budgets that win there (once (pp|pp) at 2
+    primitive quartets per lane) slowed the incremental builds that follow
+    (Fock phase 31.4 -> 36.3 ms per SCF on one box)."""
     from gbhf import _lib
-    if args.no_autotune:
-        return {"enabled": False}
+    if not args.autotune:
+        return {"enabled": False, "why": "default budgets: tuning on the first build's density can slow the "
+                                         "incremental builds of the SCF"}
     ctx.set_basis(fb)
     t0 = time.perf_counter()
     ms0, ms1 = ctx.autotune(0, _lib.PREC_MIXED, 1e-12, 1e-4)
@@ -586,7 +591,8 @@ def main():
     ap.add_argument("--workload", default="w16", choices=["w16", "batch256", "grad8", "w64", "w16d", "fock"])
     ap.add_argument("--quick", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-autotune", action="store_true", help="keep the default task budgets")
+    ap.add_argument("--no-autotune", action="store_true", help="batch256: keep the default task budgets")
+    ap.add_argument("--autotune", action="store_true", help="w16: tune the J/K task budgets first")
     ap.add_argument("--no-batch", action="store_true", help="w16: leave out the 256-conformer batch record")
     ap.add_argument("--mixed-cutoff", type=float, default=1e-2,
                     help="batch256: Schwarz-bound cutoff below which ERIs run in FP32 (the workload leaves "
