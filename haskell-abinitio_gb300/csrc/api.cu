@@ -77,6 +77,7 @@ gbhf_status gbhf_create(gbhf_ctx** out, int device) {
   {
     const char* ev = std::getenv("GBHF_EIGEN");
     c->force_jacobi = ev && std::string(ev) == "jacobi";
+    c->force_sytrd_single = ev && std::string(ev) == "single-cta";
   }
   if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
     delete c;

@@ -256,7 +256,8 @@ struct JacobiWork {
 
 // Work buffers of the tridiagonal eigen-solver (tridiag.cu).
 struct TridiagWork {
-  DBuf<double> d, e, tau, lam, scal, Vt, Zt, Z2, S, M;
+  DBuf<double> d, e, e2, tau, lam, scal, Vt, Zt, Z2, S, M;
+  DBuf<float> df, e2f;
   DBuf<int> blk, rank;
 };
 // Largest n of the tridiagonal path: the packed lower triangle of A plus two
@@ -311,6 +312,8 @@ struct gbhf_ctx {
   gbhf::TridiagWork tri;
   size_t smem_optin = 0;          // largest dynamic shared memory per block (opt-in)
   bool force_jacobi = false;      // GBHF_EIGEN=jacobi at gbhf_create: every eigen-solve by Jacobi
+  bool force_sytrd_single = false; // GBHF_EIGEN=single-cta: tridiagonalisation in one CTA
+  int sytrd_cluster = 0;          // 1: the cluster tridiagonalisation runs here, -1: it does not, 0: not checked
   // state of the last SCF (for the gradient): density, Fock matrix, occupation
   gbhf::DBuf<double> last_D, last_F;
   // state of the last converged UHF SCF: alpha and beta densities, energy-weighted density

@@ -142,3 +142,29 @@ def test_eigen_solve_scf_fock_both_solvers():
     np.testing.assert_allclose(wj, wr, rtol=0, atol=1e-12 * 21)
     assert np.max(np.abs(np.abs(np.sum(v * vj, axis=0)) - 1.0)) < 1e-9
     assert np.max(np.abs(v.T @ v - np.eye(fp.shape[0]))) < 1e-13
+
+
+@pytest.mark.parametrize("n", [16, 17, 100, 232])
+def test_tridiagonalisation_cluster_and_single_cta(ctx, n):
+    """The 8-CTA cluster tridiagonalisation (the default) and the one-CTA form
+    (GBHF_EIGEN=single-cta) both give LAPACK's spectrum and orthonormal vectors."""
+    import os
+    a = np.random.default_rng(2000 + n).standard_normal((n, n))
+    a = a + a.T
+    wr = np.linalg.eigvalsh(a)
+    sc = np.abs(wr).max()
+    w, v = ctx.eigen_solve(a)
+    old = os.environ.get("GBHF_EIGEN")
+    os.environ["GBHF_EIGEN"] = "single-cta"
+    try:
+        with _lib.Context(0) as c:
+            w1, v1 = c.eigen_solve(a)
+    finally:
+        if old is None:
+            del os.environ["GBHF_EIGEN"]
+        else:
+            os.environ["GBHF_EIGEN"] = old
+    for ww, vv in ((w, v), (w1, v1)):
+        np.testing.assert_allclose(ww, wr, rtol=0, atol=1e-12 * sc)
+        assert np.max(np.abs(a @ vv - vv * ww)) < 1e-11 * sc
+        assert np.max(np.abs(vv.T @ vv - np.eye(n))) < 1e-12
