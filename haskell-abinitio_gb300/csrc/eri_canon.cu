@@ -427,6 +427,27 @@ __global__ void k_eri_canonical(bool ref, int nbf, const int* __restrict__ pair_
       eri_fn_generic<LM>(ref, xyz, fn, coef, expo, grid, tab, (int)i, (int)j, (int)k, (int)l);
 }
 
+// The same array with a warp per (P <= Q): the lanes take the quartet's
+// primitive quartets in turn and a shuffle sum closes it (the atoms of the SAD
+// guess have up to 6^4 primitive quartets per function quartet).
+template <int LM>
+__global__ void k_eri_canonical_warp(bool ref, int nbf, const int* __restrict__ pair_i,
+                                     const int* __restrict__ pair_j, long npair, const long* __restrict__ off,
+                                     const double* __restrict__ xyz, const int* __restrict__ fn,
+                                     const double* __restrict__ coef, const double* __restrict__ expo,
+                                     const double* __restrict__ grid, const double* __restrict__ tab,
+                                     double* __restrict__ eri) {
+  const long P = blockIdx.y;
+  const long Q = (long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (Q >= npair || Q < P) return;   // whole warps leave together
+  const long i = pair_i[P], j = pair_j[P], k = pair_i[Q], l = pair_j[Q];
+  double v = eri_fn_generic<LM>(ref, xyz, fn, coef, expo, grid, tab, (int)i, (int)j, (int)k, (int)l, lane, 32);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if (lane == 0) eri[canon_pos(off, nbf, i, j, k, l)] = v;
+}
+
 static void canonical_offsets(long n, std::vector<long>& off) {
   off.assign(n * n, 0);
   long acc = 0;
@@ -473,7 +494,17 @@ gbhf_status eri_canonical_dev(gbhf_ctx* c, bool ref, double* d_eri) {
   if (np > 65535) return fail(c, GBHF_ERR_UNSUPPORTED, "canonical ERI array too large");
   dim3 grid((unsigned)((np + 127) / 128), (unsigned)np);
   // per-thread Hermite cubes sized for the largest total angular momentum: s/p quartets L <= 4, d L <= 8
-  if (b.maxL <= 1)
+  if (!ref) {   // exact numerics: a warp per quartet (the reference mode keeps its serial primitive order)
+    dim3 wgrid((unsigned)((np + 3) / 4), (unsigned)np);
+    if (b.maxL <= 1)
+      k_eri_canonical_warp<MD_LMAX><<<wgrid, 128, 0, c->stream>>>(ref, b.nbf, aux.pi.p, aux.pj.p, np, aux.off.p,
+                                                                  c->d_xyz.p, c->d_fn.p, c->d_coef.p, c->d_exp.p,
+                                                                  c->boys_ref.p, c->boys64.p, d_eri);
+    else
+      k_eri_canonical_warp<8><<<wgrid, 128, 0, c->stream>>>(ref, b.nbf, aux.pi.p, aux.pj.p, np, aux.off.p,
+                                                            c->d_xyz.p, c->d_fn.p, c->d_coef.p, c->d_exp.p,
+                                                            c->boys_ref.p, c->boys64.p, d_eri);
+  } else if (b.maxL <= 1)
     k_eri_canonical<MD_LMAX><<<grid, 128, 0, c->stream>>>(ref, b.nbf, aux.pi.p, aux.pj.p, np, aux.off.p, c->d_xyz.p,
                                                           c->d_fn.p, c->d_coef.p, c->d_exp.p, c->boys_ref.p,
                                                           c->boys64.p, d_eri);

@@ -33,6 +33,8 @@ enum {
 };
 // Cartesian components of a shell of angular momentum L.
 constexpr int ncart_c(int L) { return (L + 1) * (L + 2) / 2; }
+// Hermite indices (t, u, v) with t + u + v <= L.
+constexpr int nherm_c(int L) { return (L + 1) * (L + 2) * (L + 3) / 6; }
 
 // The J/K kernels stage the first BRA_NJK fields; BRA_AEXP (the exponent of
 // the pair's first primitive) is read by the gradient kernels only.

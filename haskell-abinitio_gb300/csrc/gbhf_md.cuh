@@ -184,7 +184,9 @@ template <int LM = MD_LMAX>
 __device__ inline double eri_fn_generic(bool ref, const double* __restrict__ xyz, const int* __restrict__ fn,
                                         const double* __restrict__ coef, const double* __restrict__ expo,
                                         const double* __restrict__ grid, const double* __restrict__ tab, int i,
-                                        int j, int k, int l) {
+                                        int j, int k, int l, int r0 = 0, int rstep = 1) {
+  // the primitive quartets (p1 p2 | p3 p4) in nested-loop order r, this call
+  // summing r = r0, r0 + rstep, ... (r0 = 0, rstep = 1: all of them, in order)
   DevFn f[4] = {load_fn(fn, i), load_fn(fn, j), load_fn(fn, k), load_fn(fn, l)};
   const double* R4[4];
   for (int a = 0; a < 4; ++a) R4[a] = xyz + 3 * f[a].atom;
@@ -199,59 +201,61 @@ __device__ inline double eri_fn_generic(bool ref, const double* __restrict__ xyz
   double F[LM + 1];
   double R[D * D * D];
   EAx E1[3], E2[3];
-  for (int p1 = 0; p1 < f[0].np; ++p1) {
-    const double c1 = coef[f[0].off + p1], e1 = expo[f[0].off + p1];
-    for (int p2 = 0; p2 < f[1].np; ++p2) {
+  const int n2 = f[1].np, n3 = f[2].np, n4 = f[3].np, nr = f[0].np * n2 * n3 * n4;
+  int last12 = -1;
+  double c12 = 0, qab = 0, p = 0, P[3] = {0, 0, 0};
+  for (int r = r0; r < nr; r += rstep) {
+    const int p4 = r % n4, r3 = r / n4, p3 = r3 % n3, r12 = r3 / n3, p2 = r12 % n2, p1 = r12 / n2;
+    if (r12 != last12) {
+      last12 = r12;
+      const double c1 = coef[f[0].off + p1], e1 = expo[f[0].off + p1];
       const double c2 = coef[f[1].off + p2], e2 = expo[f[1].off + p2];
-      const double qab = ref ? sqrt(two_terms_eri(R4[0], f[0].l, c1, e1, R4[1], f[1].l, c2, e2)) : 0.0;
-      const double p = e1 + e2, mu = e1 * e2 / p;
-      double P[3];
+      c12 = c1 * c2;
+      qab = ref ? sqrt(two_terms_eri(R4[0], f[0].l, c1, e1, R4[1], f[1].l, c2, e2)) : 0.0;
+      p = e1 + e2;
+      const double mu = e1 * e2 / p;
       for (int x = 0; x < 3; ++x) {
         P[x] = (e1 * R4[0][x] + e2 * R4[1][x]) / p;
         double ab = R4[0][x] - R4[1][x];
         e_axis(E1[x], f[0].l[x], f[1].l[x], p, P[x] - R4[0][x], P[x] - R4[1][x], exp(-mu * ab * ab));
       }
-      for (int p3 = 0; p3 < f[2].np; ++p3) {
-        const double c3 = coef[f[2].off + p3], e3 = expo[f[2].off + p3];
-        for (int p4 = 0; p4 < f[3].np; ++p4) {
-          const double c4 = coef[f[3].off + p4], e4 = expo[f[3].off + p4];
-          if (ref) {
-            double qcd = sqrt(two_terms_eri(R4[2], f[2].l, c3, e3, R4[3], f[3].l, c4, e4));
-            if (qab * qcd < 1e-8) continue;   // !(val < 1e-8) keeps NaN, as guard (schwarz gs)
-          }
-          const double q = e3 + e4, nu = e3 * e4 / q;
-          double Q[3], PQ[3];
-          for (int x = 0; x < 3; ++x) {
-            Q[x] = (e3 * R4[2][x] + e4 * R4[3][x]) / q;
-            double cd = R4[2][x] - R4[3][x];
-            e_axis(E2[x], f[2].l[x], f[3].l[x], q, Q[x] - R4[2][x], Q[x] - R4[3][x], exp(-nu * cd * cd));
-            PQ[x] = P[x] - Q[x];
-          }
-          const double alpha = p * q / (p + q);
-          boys_generic(ref, grid, tab, L, alpha * (PQ[0] * PQ[0] + PQ[1] * PQ[1] + PQ[2] * PQ[2]), F);
-          hermite_r<LM>(L, alpha, PQ[0], PQ[1], PQ[2], F, R);
-          double total = 0;
-          for (int t = 0; t <= lab[0]; ++t)
-            for (int u = 0; u <= lab[1]; ++u)
-              for (int v = 0; v <= lab[2]; ++v) {
-                double eb = E1[0].get(f[0].l[0], f[1].l[0], t) * E1[1].get(f[0].l[1], f[1].l[1], u) *
-                            E1[2].get(f[0].l[2], f[1].l[2], v);
-                double inner = 0;
-                for (int tau = 0; tau <= lcd[0]; ++tau)
-                  for (int nu2 = 0; nu2 <= lcd[1]; ++nu2)
-                    for (int phi = 0; phi <= lcd[2]; ++phi) {
-                      double ek = E2[0].get(f[2].l[0], f[3].l[0], tau) * E2[1].get(f[2].l[1], f[3].l[1], nu2) *
-                                  E2[2].get(f[2].l[2], f[3].l[2], phi);
-                      double r = R[((t + tau) * D + (u + nu2)) * D + (v + phi)];
-                      inner += ((tau + nu2 + phi) & 1) ? -ek * r : ek * r;
-                    }
-                total += eb * inner;
-              }
-          const double cte = (c1 * c2 * c3 * c4) * ((2.0 * 17.493418327624862) * (1.0 / ((p * q) * sqrt(p + q))));
-          sum += cte * total;
-        }
-      }
     }
+    const double c3 = coef[f[2].off + p3], e3 = expo[f[2].off + p3];
+    const double c4 = coef[f[3].off + p4], e4 = expo[f[3].off + p4];
+    if (ref) {
+      double qcd = sqrt(two_terms_eri(R4[2], f[2].l, c3, e3, R4[3], f[3].l, c4, e4));
+      if (qab * qcd < 1e-8) continue;   // !(val < 1e-8) keeps NaN, as guard (schwarz gs)
+    }
+    const double q = e3 + e4, nu = e3 * e4 / q;
+    double Q[3], PQ[3];
+    for (int x = 0; x < 3; ++x) {
+      Q[x] = (e3 * R4[2][x] + e4 * R4[3][x]) / q;
+      double cd = R4[2][x] - R4[3][x];
+      e_axis(E2[x], f[2].l[x], f[3].l[x], q, Q[x] - R4[2][x], Q[x] - R4[3][x], exp(-nu * cd * cd));
+      PQ[x] = P[x] - Q[x];
+    }
+    const double alpha = p * q / (p + q);
+    boys_generic(ref, grid, tab, L, alpha * (PQ[0] * PQ[0] + PQ[1] * PQ[1] + PQ[2] * PQ[2]), F);
+    hermite_r<LM>(L, alpha, PQ[0], PQ[1], PQ[2], F, R);
+    double total = 0;
+    for (int t = 0; t <= lab[0]; ++t)
+      for (int u = 0; u <= lab[1]; ++u)
+        for (int v = 0; v <= lab[2]; ++v) {
+          double eb = E1[0].get(f[0].l[0], f[1].l[0], t) * E1[1].get(f[0].l[1], f[1].l[1], u) *
+                      E1[2].get(f[0].l[2], f[1].l[2], v);
+          double inner = 0;
+          for (int tau = 0; tau <= lcd[0]; ++tau)
+            for (int nu2 = 0; nu2 <= lcd[1]; ++nu2)
+              for (int phi = 0; phi <= lcd[2]; ++phi) {
+                double ek = E2[0].get(f[2].l[0], f[3].l[0], tau) * E2[1].get(f[2].l[1], f[3].l[1], nu2) *
+                            E2[2].get(f[2].l[2], f[3].l[2], phi);
+                double rr = R[((t + tau) * D + (u + nu2)) * D + (v + phi)];
+                inner += ((tau + nu2 + phi) & 1) ? -ek * rr : ek * rr;
+              }
+          total += eb * inner;
+        }
+    const double cte = (c12 * c3 * c4) * ((2.0 * 17.493418327624862) * (1.0 / ((p * q) * sqrt(p + q))));
+    sum += cte * total;
   }
   return sum;
 }

@@ -453,7 +453,8 @@ def gen_class_deferred(la, lb, lc, ld):
     return "\n".join(out), cls, nab, ncd, L
 
 
-def main():
+def render():
+    """The text of eri_gen.cuh."""
     # s/p classes: (ss|ss), (ps|ss) and (pp|pp) as they are; (ps|ps), and (pp|ss)
     # and (pp|ps) with the lower pair as the warp-shared bra, with the ket
     # transformation deferred.  For (ps|ss) the swapped form saved FP64 time but
@@ -474,7 +475,11 @@ def main():
         code, *_ = gen_class_deferred(*c)
         parts.append(code)
         parts.append("")
-    Path(__file__).with_name("eri_gen.cuh").write_text("\n".join(parts))
+    return "\n".join(parts)
+
+
+def main():
+    Path(__file__).with_name("eri_gen.cuh").write_text(render())
 
 
 if __name__ == "__main__":

@@ -20,12 +20,93 @@ The ket side is contracted with Gamma first, per bra component pair ab:
     g_A,x           += sum_tuv [2a E^(i+1,j)_t - i E^(i-1,j)_t] E_u E_v U_ab(tuv)
 
 with R up to order L + 1 and the prefactor folded into R^(n)_000 as in
-gen_eri.py.  The generated file is ``grad_gen.cuh``; run
+gen_eri.py.  T depends on the ket primitive only, so it is formed once per
+ket primitive (``grad_ket_<class>``, into the caller's storage) and the bra
+loop (``grad_ketprim_<class>``) reads it block by block; the last line is
+summed axis by axis with partial sums shared by the six components
+(``contract_factored``).  The generated file is ``grad_gen.cuh``; run
 ``python gen_grad.py`` after editing.
 """
 from pathlib import Path
 
 from gen_eri import CART, LNAME, e_axis_code, r_code
+
+
+def lincomb(terms):
+    """Expression for sum_k c_k v_k over (c_k, v_k) pairs; c_k 'ONE' is a plain add."""
+    expr = None
+    for c, v in terms:
+        if c == "ONE":
+            expr = v if expr is None else f"{expr} + {v}"
+        else:
+            expr = f"{c} * {v}" if expr is None else f"fma_t({c}, {v}, {expr})"
+    return expr
+
+
+def contract_factored(w, a, b, bmaps, dfac, unames, ind):
+    """The six bra-centre components of one bra component pair ab,
+
+        g_S,d += sum_tuv F^S,d_x(t) F^S,d_y(u) F^S,d_z(v) U(tuv),
+
+    with F the Hermite coefficient E^(a_x b_x)_t of each axis except the
+    derivative axis d, where it is the derivative factor of side S, summed
+    axis by axis (z, then y, then x) so that the partial sums over the
+    undifferentiated axes are shared by the components:
+
+        Z0(t,u)  = sum_v E_z(v) U(tuv)           (d = x and d = y)
+        Y0(t)    = sum_u E_y(u) Z0(t,u)          g_S,x = sum_t D^S_x(t) Y0(t)
+        g_S,y    = sum_t E_x(t) sum_u D^S_y(u) Z0(t,u)
+        g_S,z    = sum_t E_x(t) sum_u E_y(u) sum_v D^S_z(v) U(tuv)
+    """
+    nx, ny, nz = (a[x] + b[x] for x in range(3))
+
+    def E(x, t):
+        return bmaps[x].get((a[x], b[x], t))
+
+    def D(side, x, t):
+        return dfac(side, x, a[x], b[x], t)
+
+    cnt = [0]
+
+    def emit(expr, terms):
+        """A name for the combination: the value itself for one unit term."""
+        if expr is None:
+            return None
+        if len(terms) == 1 and terms[0][0] == "ONE":
+            return terms[0][1]
+        nm = f"s{cnt[0]}"
+        cnt[0] += 1
+        w(f"{ind}const T {nm} = {expr};")
+        return nm
+
+    def comb(pairs):
+        terms = [(c, v) for c, v in pairs if c is not None and v is not None]
+        return emit(lincomb(terms), terms)
+
+    z0 = {}
+    for t in range(nx + 2):
+        for u in range(ny + 2):
+            if t == nx + 1 and u == ny + 1:
+                continue
+            z0[(t, u)] = comb((E(2, v), unames.get((t, u, v))) for v in range(nz + 1))
+    y0 = {t: comb((E(1, u), z0.get((t, u))) for u in range(ny + 1)) for t in range(nx + 2)}
+    for si, side in enumerate("AB"):
+        outs = []
+        # d = x
+        outs.append(lincomb([(D(side, 0, t), y0[t]) for t in range(nx + 2)
+                             if D(side, 0, t) is not None and y0[t] is not None]))
+        # d = y
+        yy = {t: comb((D(side, 1, u), z0.get((t, u))) for u in range(ny + 2)) for t in range(nx + 1)}
+        outs.append(lincomb([(E(0, t), yy[t]) for t in range(nx + 1) if E(0, t) is not None and yy[t] is not None]))
+        # d = z
+        yz = {}
+        for t in range(nx + 1):
+            zz = {u: comb((D(side, 2, v), unames.get((t, u, v))) for v in range(nz + 2)) for u in range(ny + 1)}
+            yz[t] = comb((E(1, u), zz[u]) for u in range(ny + 1))
+        outs.append(lincomb([(E(0, t), yz[t]) for t in range(nx + 1) if E(0, t) is not None and yz[t] is not None]))
+        for d, expr in enumerate(outs):
+            if expr is not None:
+                w(f"{ind}g[{3 * si + d}] += {expr};")
 
 
 def gen_class(la, lb, lc, ld):
@@ -90,15 +171,16 @@ def gen_class(la, lb, lc, ld):
 
     out = []
     w = out.append
+    nku = len(ket_union)
     w(f"// ---- gradient class ({cls[0]}{cls[1]}|{cls[2]}{cls[3]}): bra-centre derivatives, L + 1 = {L}")
-    w("template <typename T, typename G>")
-    w(f"__device__ __forceinline__ void grad_ketprim_{cls}(const T* __restrict__ sb, int nbra, int bstep,")
-    w("    const T q, const T invq, const T Qx, const T Qy, const T Qz,")
-    w("    const T QCx, const T QCy, const T QCz, const T QDx, const T QDy, const T QDz,")
-    w("    const T Kcd, const T* __restrict__ boys, const G& gam, T* g) {")
+    w(f"// ket side of one ket primitive pair: T_ab(tau) for ab x {nku} Hermite indices tau")
+    w("template <typename T, typename G, typename TK>")
+    w(f"__device__ __forceinline__ void grad_ket_{cls}(const T invq,")
+    w("    const T QCx, const T QCy, const T QCz, const T QDx, const T QDy, const T QDz, const G& gam, TK& tk) {")
     w("  const T ONE = T(1);")
-    w("  (void)QCx; (void)QCy; (void)QCz; (void)QDx; (void)QDy; (void)QDz;")
+    w("  (void)ONE; (void)QCx; (void)QCy; (void)QCz; (void)QDx; (void)QDy; (void)QDz;")
     w("  const T hq = T(0.5) * invq;")
+    w("  (void)hq;")
     kmaps = []
     for x, ax in enumerate("xyz"):
         lines, memo = e_axis_code(f"ek{ax}", f"QC{ax}", f"QD{ax}", "hq", lc, ld, kneed[x])
@@ -127,6 +209,37 @@ def gen_class(la, lb, lc, ld):
             w(f"  const T {nm} = {expr};")
             lst[(t, u, v)] = nm
         ket_terms[(ic, idd)] = lst
+    # T_ab(tau) = sum_cd Gamma_abcd ekp_cd(tau)
+    for (ia, ib) in bra:
+        iab = ia * len(cb) + ib
+        for k, tau in enumerate(ket_union):
+            expr = None
+            for (ic, idd), lst in ket_terms.items():
+                if tau not in lst:
+                    continue
+                icd = ic * len(cd) + idd
+                gm = f"gam.get({iab * ncd + icd})"
+                e = lst[tau]
+                if e == "ONE":
+                    term_add, term_fma = gm, None
+                elif e == "-ONE":
+                    term_add, term_fma = f"-{gm}", None
+                else:
+                    term_add, term_fma = None, (gm, e)
+                if expr is None:
+                    expr = term_add if term_add is not None else f"{term_fma[0]} * {term_fma[1]}"
+                else:
+                    expr = (f"{expr} + {term_add}" if term_add is not None
+                            else f"fma_t({term_fma[0]}, {term_fma[1]}, {expr})")
+            assert expr is not None
+            w(f"  tk.set({iab * nku + k}, {expr});")
+    w("}")
+    w(f"// bra loop of one ket primitive pair, with its T_ab(tau) from grad_ket_{cls}")
+    w("template <typename T, typename TK>")
+    w(f"__device__ __forceinline__ void grad_ketprim_{cls}(const T* __restrict__ sb, int nbra, int bstep,")
+    w("    const T q, const T Qx, const T Qy, const T Qz, const T Kcd, const T* __restrict__ boys,")
+    w("    const TK& tk, T* g) {")
+    w("  const T ONE = T(1);")
     w("  #pragma unroll 1")
     w("  for (int kb = 0; kb < nbra; ++kb) {")
     w("    BraPrim<T> bp;")
@@ -189,7 +302,7 @@ def gen_class(la, lb, lc, ld):
         dnames[key] = nm
         return nm
 
-    # declare every derivative factor at loop scope (shared by the ab blocks)
+    # every derivative factor at loop scope (shared by the ab blocks)
     for (a, b, ds, _) in bra.values():
         for side in "AB":
             for d in range(3):
@@ -199,31 +312,11 @@ def gen_class(la, lb, lc, ld):
     for (ia, ib), (a, b, ds, uset) in bra.items():
         iab = ia * len(cb) + ib
         w("    {")
-        # T_ab(tau) = sum_cd Gamma_abcd ekp_cd(tau)
         tnames = {}
-        for tau in ket_union:
-            expr = None
-            for (ic, idd), lst in ket_terms.items():
-                if tau not in lst:
-                    continue
-                icd = ic * len(cd) + idd
-                gm = f"gam.get({iab * ncd + icd})"
-                e = lst[tau]
-                if e == "ONE":
-                    term_add, term_fma = gm, None
-                elif e == "-ONE":
-                    term_add, term_fma = f"-{gm}", None
-                else:
-                    term_add, term_fma = None, (gm, e)
-                if expr is None:
-                    expr = term_add if term_add is not None else f"{term_fma[0]} * {term_fma[1]}"
-                else:
-                    expr = (f"{expr} + {term_add}" if term_add is not None
-                            else f"fma_t({term_fma[0]}, {term_fma[1]}, {expr})")
-            if expr is not None:
-                nm = f"T_{tau[0]}{tau[1]}{tau[2]}"
-                w(f"      const T {nm} = {expr};")
-                tnames[tau] = nm
+        for k, tau in enumerate(ket_union):
+            nm = f"T_{tau[0]}{tau[1]}{tau[2]}"
+            w(f"      const T {nm} = tk.get({iab * nku + k});")
+            tnames[tau] = nm
         # U_ab(tuv)
         unames = {}
         for (tb_, ub, vb) in uset:
@@ -235,36 +328,7 @@ def gen_class(la, lb, lc, ld):
                 nm = f"U_{tb_}{ub}{vb}"
                 w(f"      const T {nm} = {expr};")
                 unames[(tb_, ub, vb)] = nm
-        # contractions
-        for si, side in enumerate("AB"):
-            for d in range(3):
-                expr = None
-                for (t, u, v) in ds[(side, d)]:
-                    if (t, u, v) not in unames:
-                        continue
-                    tt = (t, u, v)
-                    facs = []
-                    ok = True
-                    for x in range(3):
-                        if x == d:
-                            f = dfac(side, x, a[x], b[x], tt[x])
-                        else:
-                            f = bmaps[x].get((a[x], b[x], tt[x]))
-                        if f is None:
-                            ok = False
-                            break
-                        if f != "ONE":
-                            facs.append(f)
-                    if not ok:
-                        continue
-                    un = unames[tt]
-                    coef = " * ".join(facs) if facs else None
-                    if expr is None:
-                        expr = un if coef is None else f"{coef} * {un}"
-                    else:
-                        expr = f"{expr} + {un}" if coef is None else f"fma_t({coef}, {un}, {expr})"
-                if expr is not None:
-                    w(f"      g[{3 * si + d}] += {expr};")
+        contract_factored(w, a, b, bmaps, dfac, unames, "      ")
         w("    }")
     w("  }")
     w("}")
@@ -401,7 +465,8 @@ def gen_vne(la, lb):
 GEN_D_CLASSES = [(0, 0, 2, 0), (0, 0, 2, 1), (1, 0, 2, 0), (2, 0, 0, 0), (2, 0, 1, 0)]
 
 
-def main():
+def render():
+    """The text of grad_gen.cuh."""
     pcls = [(0, 0), (1, 0), (1, 1)]
     parts = ["// GENERATED by gen_grad.py -- do not edit by hand.", "#pragma once", ""]
     for (la, lb) in pcls:
@@ -418,7 +483,11 @@ def main():
     for (la, lb) in pcls + [(2, 0), (2, 1), (2, 2)]:
         parts.append(gen_vne(la, lb))
         parts.append("")
-    Path(__file__).with_name("grad_gen.cuh").write_text("\n".join(parts))
+    return "\n".join(parts)
+
+
+def main():
+    Path(__file__).with_name("grad_gen.cuh").write_text(render())
 
 
 if __name__ == "__main__":

@@ -51,7 +51,9 @@ struct GamReg {
 template <typename T, int N>
 struct GamSmem {   // per-thread column of a [N][GR_THREADS] shared array
   T* p;
-  __device__ __forceinline__ T get(int i) const { return p[i * GR_THREADS]; }
+  // volatile: a read stays where the code places it (the bra loop reads T_ab
+  // block by block; hoisted out of the loop, all of T would be live at once)
+  __device__ __forceinline__ T get(int i) const { return *(volatile const T*)(p + i * GR_THREADS); }
   __device__ __forceinline__ void set(int i, T x) { p[i * GR_THREADS] = x; }
 };
 
@@ -60,12 +62,15 @@ struct GradFn;
 #define GBHF_GRAD_FN(la, lb, lc, ld, name)                                                                      \
   template <>                                                                                                  \
   struct GradFn<la, lb, lc, ld> {                                                                              \
-    template <typename T, typename G>                                                                          \
-    static __device__ __forceinline__ void run(const T* sb, int nbra, int bstep, T q, T invq, T Qx, T Qy, T Qz, \
-                                               T QCx, T QCy, T QCz, T QDx, T QDy, T QDz, T Kcd, const T* boys,  \
-                                               const G& gam, T* g) {                                           \
-      grad_ketprim_##name<T, G>(sb, nbra, bstep, q, invq, Qx, Qy, Qz, QCx, QCy, QCz, QDx, QDy, QDz, Kcd, boys, \
-                                gam, g);                                                                       \
+    template <typename T, typename G, typename TK>                                                             \
+    static __device__ __forceinline__ void ket(T invq, T QCx, T QCy, T QCz, T QDx, T QDy, T QDz, const G& gam, \
+                                               TK& tk) {                                                       \
+      grad_ket_##name<T, G, TK>(invq, QCx, QCy, QCz, QDx, QDy, QDz, gam, tk);                                  \
+    }                                                                                                          \
+    template <typename T, typename TK>                                                                         \
+    static __device__ __forceinline__ void run(const T* sb, int nbra, int bstep, T q, T Qx, T Qy, T Qz, T Kcd, \
+                                               const T* boys, const TK& tk, T* g) {                            \
+      grad_ketprim_##name<T, TK>(sb, nbra, bstep, q, Qx, Qy, Qz, Kcd, boys, tk, g);                            \
     }                                                                                                          \
   };
 GBHF_GRAD_FN(0, 0, 2, 0, ssds)
@@ -122,9 +127,15 @@ __global__ void __launch_bounds__(GR_THREADS) k_grad_jk(GradArgs<T> a) {
   __shared__ __align__(16) T sbra[GR_WARPS][KMAX_PRIM_PAIRS * BRA_SB];
   __shared__ T sDab[GR_WARPS][NAB];
   extern __shared__ double gsm_dyn[];
+  constexpr int NT = NAB * nherm_c(LC + LD);
   using GamT = typename std::conditional<SG, GamSmem<T, NOUT>, GamReg<T, NOUT>>::type;
+  using TkT = typename std::conditional<SG, GamSmem<T, NT>, GamReg<T, NT>>::type;
   GamT gam;
-  if constexpr (SG) gam.p = reinterpret_cast<T*>(gsm_dyn) + threadIdx.x;
+  TkT tk;
+  if constexpr (SG) {
+    gam.p = reinterpret_cast<T*>(gsm_dyn) + threadIdx.x;
+    tk.p = reinterpret_cast<T*>(gsm_dyn) + NOUT * GR_THREADS + threadIdx.x;
+  }
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int start = a.range[0];
   const int ntask = a.range[1] - start;
@@ -225,8 +236,8 @@ __global__ void __launch_bounds__(GR_THREADS) k_grad_jk(GradArgs<T> a) {
           QDz = a.ket[BRA_PBZ * npp + idx];
         }
         const T Kcd = a.ket[BRA_K * npp + idx];
-        GradFn<LA, LB, LC, LD>::run(sbra[warp] + sb * BRA_SB, nbl, nsb * BRA_SB, q, invq, Qx, Qy, Qz, QCx, QCy,
-                                    QCz, QDx, QDy, QDz, Kcd, a.boys, gam, g);
+        GradFn<LA, LB, LC, LD>::ket(invq, QCx, QCy, QCz, QDx, QDy, QDz, gam, tk);
+        GradFn<LA, LB, LC, LD>::run(sbra[warp] + sb * BRA_SB, nbl, nsb * BRA_SB, q, Qx, Qy, Qz, Kcd, a.boys, tk, g);
       }
       wgt = (A == B ? T(1) : T(2)) * (C == Dd ? T(1) : T(2));
     }
@@ -246,8 +257,9 @@ static gbhf_status launch_grad_class(gbhf_ctx* c, cudaStream_t strm, int combo, 
                                      const T* ket, const T* boys, double* grad, int ntask) {
   if (ntask <= 0) return GBHF_OK;
   constexpr int NOUT = ncart_c(LA) * ncart_c(LB) * ncart_c(LC) * ncart_c(LD);
-  constexpr bool SG = sizeof(T) == 8 ? NOUT > 9 : NOUT > 27;   // Gamma in shared memory
-  const size_t smem = SG ? (size_t)NOUT * GR_THREADS * sizeof(T) : 0;
+  constexpr int NT = ncart_c(LA) * ncart_c(LB) * nherm_c(LC + LD);
+  constexpr bool SG = sizeof(T) == 8 ? NOUT > 9 : NOUT > 27;   // Gamma and T in shared memory
+  const size_t smem = SG ? (size_t)(NOUT + NT) * GR_THREADS * sizeof(T) : 0;
   auto kern = k_grad_jk<LA, LB, LC, LD, T, SG>;
   static bool attr_set = false;
   if (SG && !attr_set) {

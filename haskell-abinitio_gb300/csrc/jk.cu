@@ -824,14 +824,17 @@ static bool gen_dclass(int k) { return (k >= 6 && k <= 11) || k == 15; }
 // Default task budgets.  J/K (which 0): lane_prims bounds the primitive
 // quartets one lane evaluates in one task, per class (ss|ss) (ps|ss) (ps|ps)
 // (pp|ss) (pp|ps) (pp|pp) ...: about the same arithmetic per task, so that the
-// longest task - the tail of a persistent launch - stays short.  A task never
+// longest task - the tail of a persistent launch - stays short ((ss|ss) and
+// (ps|ss) take less than that: their launches are short, so the tail is a
+// larger share of them, while more tasks cost the overlapped SCF next to
+// nothing - 0.1 ms of 48 on (H2O)16/6-31G).  A task never
 // splits the ket primitives, so a lane always evaluates at least K_ket of them.
 // For the warp-per-quartet d classes it bounds the primitive quartets of one
 // quartet in one task, and such a task holds one quartet (a launch then spreads
 // its quartets over every resident warp).  Gradient (which 1): the derivative
 // code does about twice the ERI work per primitive quartet.
 void default_budgets(gbhf_ctx* c, int which) {
-  static const int jk_lp[NCOMBO] = {256, 128, 48, 96, 32, 8, 48, 16, 8, 8, 16, 8, 36, 36, 36, 16, 36, 36,
+  static const int jk_lp[NCOMBO] = {96, 64, 48, 96, 32, 8, 48, 16, 8, 8, 16, 8, 36, 36, 36, 16, 36, 36,
                                     36, 36, 36};
   static const int jk_tk[NCOMBO] = {32, 32, 32, 32, 32, 32, 32, 32, 32, 32, 32, 32, 1, 1, 1, 32, 1, 1, 1, 1, 1};
   static const int gr_lp_sp[NGCOMBO_SP] = {128, 64, 24, 64, 24, 8, 24, 8, 4};

@@ -138,3 +138,18 @@ def test_kernel_flop_model_of_the_deferred_classes():
     assert (F_KERNEL["psps"], F_KERNEL["ppss"], F_KERNEL["ppps"]) == (165, 127, 302)
     for k, v in F_ALG.items():
         assert F_KERNEL[k] < v if k in DEFERRED else F_KERNEL[k] == v
+
+
+def test_generated_headers_match_their_generators():
+    """eri_gen.cuh and grad_gen.cuh are what gen_eri.py and gen_grad.py emit."""
+    import importlib
+    import sys
+    from pathlib import Path
+    csrc = Path(B.__file__).resolve().parents[1] / "csrc"
+    sys.path.insert(0, str(csrc))
+    try:
+        for gen, out in (("gen_eri", "eri_gen.cuh"), ("gen_grad", "grad_gen.cuh")):
+            mod = importlib.import_module(gen)
+            assert mod.render() == (csrc / out).read_text(), out
+    finally:
+        sys.path.remove(str(csrc))
