@@ -198,7 +198,9 @@ def gen_class(la, lb, lc, ld):
             w(f"  const T {nm} = {expr};")
             lst.append((nm, (t, u, v)))
         ket_terms[(ic, idd)] = lst
-    w("  #pragma unroll 1")
+    # (ss|ss) and (ps|ss): two bra primitives in flight (two independent load
+    # and Boys chains; the larger classes keep their registers for one)
+    w("  #pragma unroll 2" if L <= 1 else "  #pragma unroll 1")
     w("  for (int kb = 0; kb < nbra; ++kb) {")
     w("    BraPrim<T> bp;")
     w("    load_bra_prim(sb + kb * bstep, bp);")

@@ -161,18 +161,20 @@ __global__ void __launch_bounds__(GR_THREADS) k_grad_jk(GradArgs<T> a) {
     const bool active = (lane & ((1 << lg) - 1)) < nk;
     const int kb0 = task.w & 0xffff, Kb = (task.w >> 16) - kb0, pb0 = a.poff[ib] + kb0;
     const int K = a.seg[a.kseg[task.y]].z;
+    constexpr int KETC = sizeof(T) == 4 ? 1 : 0;   // per-ket-primitive work, as in k_jk
     int lb = 0;
     for (int l = 0, best = 1 << 30; (1 << l) <= nsl; ++l) {
-      const int cost = ((Kb + (1 << l) - 1) >> l) * ((K + (nsl >> l) - 1) / (nsl >> l));
-      if (cost <= best) {
+      const int cost = (((Kb + (1 << l) - 1) >> l) + KETC) * ((K + (nsl >> l) - 1) / (nsl >> l));
+      if (KETC ? cost < best : cost <= best) {
         best = cost;
         lb = l;
       }
     }
     const int nsb = 1 << lb, nsk = nsl >> lb;
     const int sb = slice & (nsb - 1), sk = slice >> lb;
+    const unsigned rkb = (65536u + Kb - 1) / Kb;   // idx / Kb = (idx * rkb) >> 16 for idx < 16 * 36
     for (int idx = lane; idx < BRA_NFIELD * Kb; idx += 32) {
-      const int f = idx / Kb, k = idx - f * Kb;
+      const int f = (int)(((unsigned)idx * rkb) >> 16), k = idx - f * Kb;
       sbra[warp][k * BRA_SB + f] = a.bra[(long long)f * npp + pb0 + k];
     }
     const int A = a.pA[ib], B = a.pB[ib];

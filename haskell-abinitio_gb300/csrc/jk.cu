@@ -163,10 +163,14 @@ __global__ void __launch_bounds__(JK_THREADS) k_jk(JKArgs<T> a) {
     // per call (ket primitive and bra-primitive range): about one primitive
     // quartet of extra work per call
     constexpr int CALLC = (LA + LB < LC + LD) ? 1 : 0;
+    // per ket primitive a lane also loads the ket pair's fields and enters the
+    // bra loop: about one FP32 primitive quartet of issue slots, next to nothing
+    // beside the FP64 arithmetic of an FP64 primitive quartet
+    constexpr int KETC = sizeof(T) == 4 ? 1 : 0;
     int lb = 0;
-    for (int l = 0, best = 1 << 30; (1 << l) <= nsl; ++l) {   // fewest primitive quartets per lane
-      const int cost = (((Kb + (1 << l) - 1) >> l) + CALLC) * ((K + (nsl >> l) - 1) / (nsl >> l));
-      if (cost <= best) {
+    for (int l = 0, best = 1 << 30; (1 << l) <= nsl; ++l) {   // least work for the busiest lane
+      const int cost = (((Kb + (1 << l) - 1) >> l) + CALLC + KETC) * ((K + (nsl >> l) - 1) / (nsl >> l));
+      if (KETC ? cost < best : cost <= best) {
         best = cost;
         lb = l;
       }
@@ -181,8 +185,9 @@ __global__ void __launch_bounds__(JK_THREADS) k_jk(JKArgs<T> a) {
     const bool active = (lane & ((1 << lg) - 1)) < nk;   // computes
     const bool lead = active && slice == 0;               // scatters
     // bra primitives [kb0, kb1) of pair ib
+    const unsigned rkb = (65536u + Kb - 1) / Kb;   // idx / Kb = (idx * rkb) >> 16 for idx < 16 * 36
     for (int idx = lane; idx < BRA_NJK * Kb; idx += 32) {
-      const int f = idx / Kb, k = idx - f * Kb;
+      const int f = (int)(((unsigned)idx * rkb) >> 16), k = idx - f * Kb;
       sbra[warp][k * BRA_SB + f] = a.bra[(long long)f * npp + pb0 + k];
     }
     const int A = a.pA[ib], B = a.pB[ib];
@@ -433,7 +438,8 @@ struct TaskGenArgs {
   int nitems;
   int ncombo;                    // quartet classes (bra pair class, ket pair class)
   int cbra[NCOMBO_MAX], cket[NCOMBO_MAX];
-  int all_pairs;                 // every ordered (bra, ket) pair, else ket <= bra in one class
+  int all_pairs;                 // every ordered (bra, ket) pair, else each unordered pair once in one class
+  int ket_ge[NCOMBO_MAX];        // one class: 1 = (i | j >= i), the bra with more primitives; 0 = (i | j <= i)
   int lane_prims[NCOMBO_MAX];    // per combo: primitive quartets per lane and task (bra split)
   int task_kets[NCOMBO_MAX];     // per combo: kets per task (32: a lane per ket; fewer: a warp per quartet)
   int square_w;                  // bound uses the squared density weight (gradient)
@@ -491,11 +497,19 @@ __global__ void k_tasks(TaskGenArgs g) {
       if (g.square_w) w *= w;
       if (!(w > 0)) continue;
       const double ta = g.thr_all / (qi * w), t64 = g.thr64 / (qi * w);
-      int hi = s.y;
-      if (!g.all_pairs && X == Y && hi > i + 1) hi = i + 1;
-      if (hi <= s.x) continue;
-      const int keep = count_ge(g.Q, s.x, hi, ta);
-      int k64 = count_ge(g.Q, s.x, s.x + keep, t64);
+      // one class: each unordered pair of pairs once.  Pairs are sorted by
+      // primitive count (descending) within a (class, molecule), so with
+      // (i | j >= i) the bra - staged once for the warp - is the pair with
+      // more primitives and a lane's ket loop (a load of the ket pair's fields
+      // per primitive) is the shorter one; (i | j <= i) the other way round
+      int lo = s.x, hi = s.y;
+      if (!g.all_pairs && X == Y) {
+        if (g.ket_ge[k]) lo = max(lo, i);
+        else hi = min(hi, i + 1);
+      }
+      if (lo >= hi) continue;
+      const int keep = count_ge(g.Q, lo, hi, ta);
+      int k64 = count_ge(g.Q, lo, lo + keep, t64);
       const int k32 = keep - k64;
       // split the bra primitives so that one lane handles at most about
       // lane_prims primitive quartets per task (bounds the launch tail)
@@ -506,8 +520,8 @@ __global__ void k_tasks(TaskGenArgs g) {
       if (FILL) {
         for (int ch = 0; ch < nch; ++ch) {
           const int w = (ch * cs) | (min(kb, (ch + 1) * cs) << 16);
-          for (int o = 0; o < k64; o += tk) g.tasks64[w64++] = make_int4(i, s.x + o, min(tk, k64 - o), w);
-          for (int o = 0; o < k32; o += tk) g.tasks32[w32++] = make_int4(i, s.x + k64 + o, min(tk, k32 - o), w);
+          for (int o = 0; o < k64; o += tk) g.tasks64[w64++] = make_int4(i, lo + o, min(tk, k64 - o), w);
+          for (int o = 0; o < k32; o += tk) g.tasks32[w32++] = make_int4(i, lo + k64 + o, min(tk, k32 - o), w);
         }
       } else {
         n64 += nch * ((k64 + tk - 1) / tk);
@@ -763,6 +777,10 @@ static gbhf_status build_task_lists(gbhf_ctx* c, TaskLists& TL, int ncombo, cons
     g.cket[k] = k < ncombo ? cket[k] : 0;
     g.lane_prims[k] = k < ncombo ? std::max(1, lane_prims[k]) : 1;
     g.task_kets[k] = k < ncombo ? std::min(32, std::max(1, task_kets[k])) : 32;
+    // the (ss|ss) and (ps|ps) quartets with the bra of more primitives: the
+    // FP32 launches gain 13-14% (fewer ket-field loads per primitive
+    // quartet); (pp|pp) FP64 lost 18% that way (its launch is tail-bound)
+    g.ket_ge[k] = k < ncombo && cbra[k] == cket[k] && cbra[k] <= 1 ? 1 : 0;
   }
   g.all_pairs = all_pairs ? 1 : 0;
   g.square_w = square_w ? 1 : 0;

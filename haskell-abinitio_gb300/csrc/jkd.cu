@@ -70,8 +70,9 @@ __global__ void __launch_bounds__(JKD_THREADS) k_jkd(JKDArgs<T> a) {
     const T* __restrict__ Dm = a.D + a.moff[mol];
     double* __restrict__ Gm = a.G + a.moff[mol];
     const int kb0 = task.w & 0xffff, Kb = (task.w >> 16) - kb0, pb0 = a.poff[ib] + kb0;
+    const unsigned rkb = (65536u + Kb - 1) / Kb;   // idx / Kb = (idx * rkb) >> 16 for idx < 16 * 36
     for (int idx = lane; idx < BRA_NJK * Kb; idx += 32) {
-      const int f = idx / Kb, k = idx - f * Kb;
+      const int f = (int)(((unsigned)idx * rkb) >> 16), k = idx - f * Kb;
       sbra[k * BRA_SB + f] = a.bra[(long long)f * npp + pb0 + k];
     }
     __syncwarp();
