@@ -87,6 +87,7 @@ gbhf_status gbhf_create(gbhf_ctx** out, int device) {
   for (auto& e : c->evc) cudaEventCreate(&e);
   for (auto& e : c->evu) cudaEventCreate(&e);
   for (auto& e : c->evg) cudaEventCreate(&e);
+  for (auto& e : c->evp) cudaEventCreate(&e);
   default_budgets(c, 0);
   default_budgets(c, 1);
   for (int i = 0; i < gbhf_ctx::NSIDE; ++i) {
@@ -115,6 +116,8 @@ gbhf_status gbhf_destroy(gbhf_ctx* c) {
   for (auto& e : c->evu)
     if (e) cudaEventDestroy(e);
   for (auto& e : c->evg)
+    if (e) cudaEventDestroy(e);
+  for (auto& e : c->evp)
     if (e) cudaEventDestroy(e);
   for (int i = 0; i < gbhf_ctx::NSIDE; ++i) {
     if (c->side[i]) {
@@ -612,6 +615,7 @@ gbhf_status gbhf_autotune(gbhf_ctx* c, int which, int precision, double schwarz_
 
 gbhf_status gbhf_profile_reset(gbhf_ctx* c, int enable_events) {
   CTX_CHECK(c);
+  GBHF_TRY(flush_jk_stats(c));   // counts of earlier builds go with the old profile
   c->prof = Profile();
   c->prof.events = enable_events != 0;
   return GBHF_OK;
@@ -641,6 +645,7 @@ gbhf_status gbhf_scf_trace(gbhf_ctx* c, double* out, int max_records, int* n_rec
 gbhf_status gbhf_profile_read(gbhf_ctx* c, double* stats, int n_stats) {
   CTX_CHECK(c);
   if (!stats) return fail(c, GBHF_ERR_BAD_INPUT, "null pointer");
+  GBHF_TRY(flush_jk_stats(c));
   const double v[20] = {c->prof.jk_ms64,   c->prof.jk_ms32,  c->prof.prim64,        c->prof.prim32,
                         c->prof.shellq,    c->prof.fnq,      (double)c->prof.launches, c->prof.dense_ms,
                         c->prof.ph_setup,  c->prof.ph_fock,  c->prof.ph_diis,       c->prof.ph_diag,

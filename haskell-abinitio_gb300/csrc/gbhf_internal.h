@@ -226,6 +226,8 @@ struct TaskLists {
   DBuf<int> ranges;        // per combo: start64, end64, start32, end32
   DBuf<int> counters;      // per combo & precision: work-queue heads
   DBuf<unsigned long long> stats;  // per combo: shell quartets, fn quartets, prim quartets (64, 32)
+  bool stats_pending = false;      // stats holds counts of builds not yet added to the profile
+  DBuf<int> ics_d, cls_d, scs_d;   // task generation inputs (live until its kernels have run)
   int nitems = 0;
   std::vector<int> combo_item_start;   // host: first item of each combo
   double thr_all = -1, thr64 = -1;     // thresholds the current lists were built for
@@ -341,6 +343,7 @@ struct gbhf_ctx {
   cudaEvent_t evc[2 * gbhf::NCOMBO + 1] = {};   // per-class J/K launch boundaries (profiling)
   cudaEvent_t evu[8] = {};       // user slots (gbhf_event_record)
   cudaEvent_t evg[2 * gbhf::NCOMBO_MAX + 1] = {};   // per-combo gradient launch boundaries (profiling)
+  cudaEvent_t evp[5] = {};       // SCF step phase boundaries (Fock, DIIS, density, convergence)
   // task budgets of the direct builds per quartet class (J/K) and class pair
   // (gradient): primitive quartets per lane and task, kets per task
   int jk_lp[gbhf::NCOMBO_MAX] = {}, jk_tk[gbhf::NCOMBO_MAX] = {};
@@ -458,6 +461,9 @@ gbhf_status boys_ref_grid_dev(gbhf_ctx* c, double* d_grid);
 gbhf_status ensure_shell_arrays(gbhf_ctx* c);
 gbhf_status build_grad_tasks(gbhf_ctx* c, const double* d_D, double cutoff, double mixed_cutoff, int precision);
 // with_j = false: exchange only, G = -K(D)/2 (the open-shell spin-density term).
+// Add the J/K kernels' counters of the builds since the last call to the
+// profile (one copy and one host synchronisation).
+gbhf_status flush_jk_stats(gbhf_ctx* c);
 gbhf_status jk_build(gbhf_ctx* c, const double* d_Dsq, double* d_G, int precision, double schwarz,
                      double mixed_cutoff, double weight, bool local_weights = false, bool with_j = true);
 // Q of every pair in [cls_start[cl], cls_start[cl+1]) (pairs grouped by class,

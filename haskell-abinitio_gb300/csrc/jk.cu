@@ -755,7 +755,9 @@ static gbhf_status build_task_lists(gbhf_ctx* c, TaskLists& TL, int ncombo, cons
   TL.combo_item_start = ics;
   TL.ncombo = ncombo;
   const int ni = TL.nitems;
-  DBuf<int> d_ics, d_cls, d_scs;
+  DBuf<int>& d_ics = TL.ics_d;
+  DBuf<int>& d_cls = TL.cls_d;
+  DBuf<int>& d_scs = TL.scs_d;
   GBHF_CUDA(c, d_ics.alloc(ncombo + 1));
   GBHF_CUDA(c, d_cls.alloc(NPCLS + 1));
   GBHF_CUDA(c, d_scs.alloc(NPCLS + 1));
@@ -815,10 +817,14 @@ static gbhf_status build_task_lists(gbhf_ctx* c, TaskLists& TL, int ncombo, cons
     k_scan_apply<<<ntile, SCAN_THREADS, 0, c->stream>>>(ni, TL.item_count.p, TL.scan_part.p, off64, off32);
     count_launch(c, 3);
   }
-  int tot[2];
-  GBHF_CUDA(c, cudaMemcpyAsync(&tot[0], off64 + ni, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
-  GBHF_CUDA(c, cudaMemcpyAsync(&tot[1], off32 + ni, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  // the per-class ranges follow from the offsets alone: one copy and one
+  // synchronisation give the host both the ranges and the list sizes
+  k_ranges<<<1, 64, 0, c->stream>>>(ncombo, d_ics.p, off64, off32, TL.ranges.p);
+  count_launch(c);
+  GBHF_CUDA(c, cudaGetLastError());
+  GBHF_CUDA(c, cudaMemcpyAsync(h_ranges, TL.ranges.p, 4 * ncombo * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
+  const int tot[2] = {ncombo > 0 ? h_ranges[4 * (ncombo - 1) + 1] : 0, ncombo > 0 ? h_ranges[4 * (ncombo - 1) + 3] : 0};
   GBHF_CUDA(c, TL.tasks64.alloc(std::max(tot[0], 1)));
   GBHF_CUDA(c, TL.tasks32.alloc(std::max(tot[1], 1)));
   g.tasks64 = TL.tasks64.p;
@@ -827,11 +833,7 @@ static gbhf_status build_task_lists(gbhf_ctx* c, TaskLists& TL, int ncombo, cons
     k_tasks<true><<<(ni + 127) / 128, 128, 0, c->stream>>>(g);
     count_launch(c);
   }
-  k_ranges<<<1, 64, 0, c->stream>>>(ncombo, d_ics.p, off64, off32, TL.ranges.p);
-  count_launch(c);
   GBHF_CUDA(c, cudaGetLastError());
-  GBHF_CUDA(c, cudaMemcpyAsync(h_ranges, TL.ranges.p, 4 * ncombo * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
-  GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
   return GBHF_OK;
 }
 
@@ -1022,7 +1024,10 @@ gbhf_status jk_build(gbhf_ctx* c, const double* d_Dsq, double* d_G, int precisio
     }
   }
   GBHF_CUDA(c, cudaMemsetAsync(c->tasks.counters.p, 0, 2 * NCOMBO * sizeof(int), c->stream));
-  GBHF_CUDA(c, cudaMemsetAsync(c->tasks.stats.p, 0, 6 * NCOMBO * sizeof(unsigned long long), c->stream));
+  if (!st.stats_pending) {   // the counters add up over builds until flush_jk_stats reads them
+    GBHF_CUDA(c, cudaMemsetAsync(c->tasks.stats.p, 0, 6 * NCOMBO * sizeof(unsigned long long), c->stream));
+    st.stats_pending = true;
+  }
   bool any32 = false;
   for (int k = 0; k < NCOMBO; ++k) any32 |= st.hranges[4 * k + 3] > st.hranges[4 * k + 2];
   if (any32) {
@@ -1111,10 +1116,26 @@ gbhf_status jk_build(gbhf_ctx* c, const double* d_Dsq, double* d_G, int precisio
       GBHF_CUDA(c, cudaStreamWaitEvent(c->stream, c->join_ev[i], 0));
     }
   }
-  // statistics
+  // statistics: read with the per-class event times when those are taken,
+  // else when the profile is read (no host synchronisation per build)
+  if (!ev) return GBHF_OK;
+  GBHF_TRY(flush_jk_stats(c));
+  for (int e = 0; e < ne; ++e) {
+    float ms = 0;
+    GBHF_CUDA(c, cudaEventElapsedTime(&ms, c->evc[e], c->evc[e + 1]));
+    c->prof.cls[ev_combo[e]][ev_prec[e]][3] += ms;
+    (ev_prec[e] == 0 ? c->prof.jk_ms64 : c->prof.jk_ms32) += ms;
+  }
+  return GBHF_OK;
+}
+
+gbhf_status flush_jk_stats(gbhf_ctx* c) {
+  TaskLists& st = c->tasks;
+  if (!st.stats_pending) return GBHF_OK;
   unsigned long long hs[6 * NCOMBO];
-  GBHF_CUDA(c, cudaMemcpyAsync(hs, c->tasks.stats.p, sizeof(hs), cudaMemcpyDeviceToHost, c->stream));
+  GBHF_CUDA(c, cudaMemcpyAsync(hs, st.stats.p, sizeof(hs), cudaMemcpyDeviceToHost, c->stream));
   GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
+  st.stats_pending = false;
   for (int k = 0; k < NCOMBO; ++k)
     for (int p = 0; p < 2; ++p) {
       const unsigned long long* s = hs + 3 * (2 * k + p);
@@ -1125,12 +1146,6 @@ gbhf_status jk_build(gbhf_ctx* c, const double* d_Dsq, double* d_G, int precisio
       c->prof.cls[k][p][1] += (double)s[1];
       c->prof.cls[k][p][2] += (double)s[2];
     }
-  for (int e = 0; e < ne; ++e) {
-    float ms = 0;
-    GBHF_CUDA(c, cudaEventElapsedTime(&ms, c->evc[e], c->evc[e + 1]));
-    c->prof.cls[ev_combo[e]][ev_prec[e]][3] += ms;
-    (ev_prec[e] == 0 ? c->prof.jk_ms64 : c->prof.jk_ms32) += ms;
-  }
   return GBHF_OK;
 }
 

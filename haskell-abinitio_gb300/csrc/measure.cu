@@ -32,6 +32,7 @@ extern "C" {
 
 gbhf_status gbhf_profile_classes(gbhf_ctx* c, double* out) {
   if (!c || !out) return GBHF_ERR_BAD_INPUT;
+  GBHF_TRY(gbhf::flush_jk_stats(c));
   for (int k = 0; k < gbhf::NCOMBO; ++k)
     for (int p = 0; p < 2; ++p)
       for (int q = 0; q < 4; ++q) out[(k * 2 + p) * 4 + q] = c->prof.cls[k][p][q];

@@ -223,13 +223,15 @@ gbhf_status scf_run(gbhf_ctx* c, const gbhf_scf_opts* o, gbhf_result* r) {
   double fock_builds = 0;
   const double* last_fuse = F;
   double hstats[4];
+  GBHF_TRY(flush_jk_stats(c));
   const double prim64_0 = c->prof.prim64, prim32_0 = c->prof.prim32, shq0 = c->prof.shellq, fnq0 = c->prof.fnq;
   GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
   c->prof.ph_setup += ms_since(t_phase);
   c->scf_trace.clear();
   for (step = 0; step < o->max_iter; ++step) {
-    t_phase = clk::now();
-    const auto t_step = t_phase;
+    // phase boundaries as events on the stream (read after the step's last
+    // host synchronisation, so that no phase waits for the GPU to drain)
+    GBHF_CUDA(c, cudaEventRecord(c->evp[0], c->stream));
     // ---- Fock matrix of the current density
     if (ref) {
       GBHF_TRY(square_to_flat(c, n, D, fD));
@@ -259,9 +261,7 @@ gbhf_status scf_run(gbhf_ctx* c, const gbhf_scf_opts* o, gbhf_result* r) {
       GBHF_TRY(axpby(c, nn, 1.0, H, 1.0, Gacc, F));
       fock_builds += 1;
     }
-    GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
-    c->prof.ph_fock += ms_since(t_phase);
-    t_phase = clk::now();
+    GBHF_CUDA(c, cudaEventRecord(c->evp[1], c->stream));
     // ---- DIIS error and extrapolation (DIIS.hs:55-132)
     GBHF_TRY(diis_error_dev(c, n, F, S, D, X, E));
     double maxe = 0;
@@ -343,15 +343,11 @@ gbhf_status scf_run(gbhf_ctx* c, const gbhf_scf_opts* o, gbhf_result* r) {
       }
       GBHF_TRY(prepend());
     }
-    GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
-    c->prof.ph_diis += ms_since(t_phase);
-    t_phase = clk::now();
+    GBHF_CUDA(c, cudaEventRecord(c->evp[2], c->stream));
     // ---- diagonalise the (extrapolated) Fock matrix
     GBHF_TRY(new_density(Fuse, Dnew));
     last_fuse = o->ref_stop_rule ? Fuse : F;
-    GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
-    c->prof.ph_diag += ms_since(t_phase);
-    t_phase = clk::now();
+    GBHF_CUDA(c, cudaEventRecord(c->evp[3], c->stream));
     // ---- energies and convergence
     double rms = 0;
     if (o->ref_stop_rule) {
@@ -374,11 +370,18 @@ gbhf_status scf_run(gbhf_ctx* c, const gbhf_scf_opts* o, gbhf_result* r) {
                      energy, have_prev ? energy - e_prev : 0.0, rms, maxe, diis_on ? (int)stored.size() : 0,
                      precision == GBHF_PREC_FP64 ? "fp64" : "mixed", fp64_final_phase ? " final" : "");
     }
-    c->prof.ph_other += ms_since(t_phase);
+    GBHF_CUDA(c, cudaEventRecord(c->evp[4], c->stream));
+    GBHF_CUDA(c, cudaEventSynchronize(c->evp[4]));
+    float ph[4] = {0, 0, 0, 0};
+    for (int i = 0; i < 4; ++i) GBHF_CUDA(c, cudaEventElapsedTime(&ph[i], c->evp[i], c->evp[i + 1]));
+    c->prof.ph_fock += ph[0];
+    c->prof.ph_diis += ph[1];
+    c->prof.ph_diag += ph[2];
+    c->prof.ph_other += ph[3];
     {
       const double rec[GBHF_SCF_TRACE_FIELDS] = {
           (double)step, energy, have_prev ? energy - e_prev : 0.0, rms, maxe, diis_on ? (double)stored.size() : 0.0,
-          fp64_final_phase ? 2.0 : (precision == GBHF_PREC_MIXED ? 1.0 : 0.0), ms_since(t_step)};
+          fp64_final_phase ? 2.0 : (precision == GBHF_PREC_MIXED ? 1.0 : 0.0), (double)(ph[0] + ph[1] + ph[2] + ph[3])};
       c->scf_trace.insert(c->scf_trace.end(), rec, rec + GBHF_SCF_TRACE_FIELDS);
     }
     e_prev = energy;
@@ -407,6 +410,7 @@ gbhf_status scf_run(gbhf_ctx* c, const gbhf_scf_opts* o, gbhf_result* r) {
     GBHF_TRY(diagonal_hf_dev(c, n, last_fuse, X, nocc, Cm, Dnew, eps, Cp));
   }
   if (r) {
+    GBHF_TRY(flush_jk_stats(c));
     r->energy = energy;
     r->iterations = std::min(step + 1, o->max_iter);
     r->converged = converged ? 1 : 0;

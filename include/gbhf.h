@@ -201,7 +201,8 @@ gbhf_status gbhf_sad_density(gbhf_ctx* ctx, double* density_flat);
  * gbhf_scf_trace copies the per-step records of the last gbhf_scf,
  * GBHF_SCF_TRACE_FIELDS doubles each: step, energy, energy change, RMS density
  * change, max |DIIS error|, stored DIIS vectors, phase (0 FP64, 1 mixed, 2 the
- * FP64 phase after a mixed one), milliseconds of the step; *n_records = steps. */
+ * FP64 phase after a mixed one), milliseconds of the step (device time between
+ * stream events at its start and end); *n_records = steps. */
 #define GBHF_SCF_TRACE_FIELDS 8
 
 /* Open-shell (unrestricted) SCF for multiplicity 2S+1: the reference parses a
