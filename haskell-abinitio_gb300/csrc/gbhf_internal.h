@@ -536,6 +536,7 @@ gbhf_status reduce_stats(gbhf_ctx* c, int n, const double* d_e, const double* d_
 gbhf_status axpby(gbhf_ctx* c, size_t n, double a, const double* x, double b, const double* y, double* out);
 gbhf_status add_sym(gbhf_ctx* c, int n, const double* d_H, const double* d_Gpp, double* d_out);
 gbhf_status max_abs(gbhf_ctx* c, size_t n, const double* d_x, double* host_out);
+gbhf_status max_abs_dev(gbhf_ctx* c, size_t n, const double* d_x, double* d_out);   // into device memory
 gbhf_status to_float(gbhf_ctx* c, size_t n, const double* d_x, float* d_y);
 
 }  // namespace gbhf

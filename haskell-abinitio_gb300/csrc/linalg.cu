@@ -434,10 +434,16 @@ __global__ void k_max_abs(size_t n, const double* __restrict__ x, double* out) {
 
 gbhf_status max_abs(gbhf_ctx* c, size_t n, const double* d_x, double* host_out) {
   GBHF_CUDA(c, c->small.alloc(64));
-  k_max_abs<<<1, 1024, 0, c->stream>>>(n, d_x, c->small.p + 8);
-  count_launch(c);
+  GBHF_TRY(max_abs_dev(c, n, d_x, c->small.p + 8));
   GBHF_CUDA(c, cudaMemcpyAsync(host_out, c->small.p + 8, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
+  return GBHF_OK;
+}
+
+gbhf_status max_abs_dev(gbhf_ctx* c, size_t n, const double* d_x, double* d_out) {
+  k_max_abs<<<1, 1024, 0, c->stream>>>(n, d_x, d_out);
+  count_launch(c);
+  GBHF_CUDA(c, cudaGetLastError());
   return GBHF_OK;
 }
 

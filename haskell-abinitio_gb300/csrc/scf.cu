@@ -248,13 +248,10 @@ gbhf_status scf_run(gbhf_ctx* c, const gbhf_scf_opts* o, gbhf_result* r) {
         since_full = 1;
       } else {
         GBHF_TRY(axpby(c, nn, 1.0, D, -1.0, Dref, Dnew));   // dD (Dnew as scratch)
-        double w = 0;
-        GBHF_TRY(max_abs(c, nn, Dnew, &w));
-        if (w > 0) {
-          // per-pair weights from the local size of dD (tighter than the global max)
-          GBHF_TRY(jk_build(c, Dnew, Gpp, precision, o->schwarz_cutoff, o->mixed_cutoff, w, true));
-          GBHF_TRY(add_sym(c, n, Gacc, Gpp, Gacc));
-        }
+        // per-pair weights from the local size of dD (tighter than its global
+        // max; a zero dD leaves the task lists empty)
+        GBHF_TRY(jk_build(c, Dnew, Gpp, precision, o->schwarz_cutoff, o->mixed_cutoff, 1.0, true));
+        GBHF_TRY(add_sym(c, n, Gacc, Gpp, Gacc));
         ++since_full;
       }
       GBHF_CUDA(c, cudaMemcpyAsync(Dref, D, nn * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
@@ -265,19 +262,23 @@ gbhf_status scf_run(gbhf_ctx* c, const gbhf_scf_opts* o, gbhf_result* r) {
     // ---- DIIS error and extrapolation (DIIS.hs:55-132)
     GBHF_TRY(diis_error_dev(c, n, F, S, D, X, E));
     double maxe = 0;
-    GBHF_TRY(max_abs(c, nn, E, &maxe));
     const double* Fuse = F;
-    // newdots[j] = tr(e e_j) for stored j (newest first), newdots.back() = tr(e e)
+    // newdots[j] = tr(e e_j) for stored j (newest first), newdots.back() = tr(e e);
+    // max |e| and the dots come back in one copy
     std::vector<double> newdots;
     {
       std::vector<const double*> mats;
       for (int s : stored) mats.push_back(hbuf[2 * s].p);
       mats.push_back(E);
-      GBHF_TRY(dot_matrices(c, (int)nn, (int)mats.size(), mats.data(), E, coefs));
-      newdots.resize(mats.size());
-      GBHF_CUDA(c, cudaMemcpyAsync(newdots.data(), coefs, mats.size() * sizeof(double), cudaMemcpyDeviceToHost,
+      const int nd = (int)mats.size();
+      GBHF_TRY(dot_matrices(c, (int)nn, nd, mats.data(), E, coefs));
+      GBHF_TRY(max_abs_dev(c, nn, E, coefs + nd));
+      newdots.resize(nd + 1);
+      GBHF_CUDA(c, cudaMemcpyAsync(newdots.data(), coefs, (nd + 1) * sizeof(double), cudaMemcpyDeviceToHost,
                                    c->stream));
       GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
+      maxe = newdots[nd];
+      newdots.pop_back();
     }
     auto drop_oldest = [&]() {
       free_slots.push_back(stored.back());
