@@ -336,6 +336,9 @@ struct gbhf_ctx {
   gbhf::DBuf<int> dev_status;
   int purify_grid = 0;              // co-resident blocks of the fused purification kernel
   int tc2_grid = 0;                 // co-resident blocks of the one-barrier TC2 kernel
+  bool purify_defer = false;        // purify leaves its check to the next reduce_stats (SCF loop)
+  bool purify_pending = false;      // a purification record waits in small[PURIFY_REC..+2]
+  int purify_ne = 0;                // electrons of the pending purification
   gbhf::DBuf<unsigned> barrier;
   gbhf::DBuf<double> small;
   gbhf::Profile prof;
@@ -536,6 +539,11 @@ gbhf_status reduce_stats(gbhf_ctx* c, int n, const double* d_e, const double* d_
 gbhf_status axpby(gbhf_ctx* c, size_t n, double a, const double* x, double b, const double* y, double* out);
 gbhf_status add_sym(gbhf_ctx* c, int n, const double* d_H, const double* d_Gpp, double* d_out);
 gbhf_status max_abs(gbhf_ctx* c, size_t n, const double* d_x, double* host_out);
+// Purification record slots in c->small and its checks (the deferred one runs
+// in reduce_stats; purify_flush reads a pending one on its own).
+constexpr int PURIFY_REC = 16;
+gbhf_status purify_finish(gbhf_ctx* c, const double* rec);
+gbhf_status purify_flush(gbhf_ctx* c);
 gbhf_status max_abs_dev(gbhf_ctx* c, size_t n, const double* d_x, double* d_out);   // into device memory
 gbhf_status to_float(gbhf_ctx* c, size_t n, const double* d_x, float* d_y);
 

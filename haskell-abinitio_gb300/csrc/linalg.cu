@@ -420,8 +420,13 @@ gbhf_status reduce_stats(gbhf_ctx* c, int n, const double* d_e, const double* d_
   k_stats<<<1, 1024, 0, c->stream>>>(n, d_e, d_H, d_F, d_Dnew, d_Dold, c->small.p);
   count_launch(c);
   GBHF_CUDA(c, cudaGetLastError());
-  GBHF_CUDA(c, cudaMemcpyAsync(host_out4, c->small.p, 4 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  // with a purification check pending, its record (small[16..18]) comes back in the same copy
+  double h[PURIFY_REC + 3];
+  const int nget = c->purify_pending ? PURIFY_REC + 3 : 4;
+  GBHF_CUDA(c, cudaMemcpyAsync(h, c->small.p, nget * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
+  std::copy(h, h + 4, host_out4);
+  if (c->purify_pending) GBHF_TRY(purify_finish(c, h + PURIFY_REC));
   return GBHF_OK;
 }
 
@@ -1240,6 +1245,13 @@ __global__ void k_tc2_init(int n, const double* __restrict__ F, const double* __
 // per step, tc2 = false) needs ~17, so a third fewer GEMMs.  TC2 runs the
 // one-barrier kernel k_tc2_fused.  Returns the idempotency error tr(P - P^2)
 // of the result.
+// The purification record (final error, steps, device status) for a deferred check.
+__global__ void k_purify_record(const double* __restrict__ out, const int* __restrict__ st, double* __restrict__ rec) {
+  rec[0] = out[0];
+  rec[1] = out[1];
+  rec[2] = (double)*st;
+}
+
 gbhf_status purify(gbhf_ctx* c, int n, int ne, const double* d_F, double* d_P, double* err_out, bool tc2) {
   const size_t nn = (size_t)n * n;
   GBHF_WS(c, P2, 23, nn);
@@ -1324,16 +1336,42 @@ gbhf_status purify(gbhf_ctx* c, int n, int ne, const double* d_F, double* d_P, d
     GBHF_CUDA(c, cudaLaunchCooperativeKernel((void*)k_purify_fused, dim3(grid), dim3(128), args, 0, c->stream));
     count_launch(c);
   }
+  c->purify_ne = ne;
+  if (c->purify_defer && !err_out) {
+    // the record (error, steps, device status) waits in small[16..18] for the
+    // caller's next read (reduce_stats), which runs purify_finish
+    GBHF_CUDA(c, c->small.alloc(64));
+    k_purify_record<<<1, 1, 0, c->stream>>>(out, c->dev_status.p, c->small.p + PURIFY_REC);
+    count_launch(c);
+    GBHF_CUDA(c, cudaGetLastError());
+    c->purify_pending = true;
+    return GBHF_OK;
+  }
   int st = 0;
   GBHF_CUDA(c, cudaMemcpyAsync(hout, out, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   GBHF_CUDA(c, cudaMemcpyAsync(&st, c->dev_status.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
+  const double rec[3] = {hout[0], hout[1], (double)st};
+  if (err_out) *err_out = hout[0];
+  c->purify_pending = true;
+  return purify_finish(c, rec);
+}
+
+gbhf_status purify_flush(gbhf_ctx* c) {
+  if (!c->purify_pending) return GBHF_OK;
+  double rec[3];
+  GBHF_CUDA(c, cudaMemcpyAsync(rec, c->small.p + PURIFY_REC, 3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
+  return purify_finish(c, rec);
+}
+
+gbhf_status purify_finish(gbhf_ctx* c, const double* rec) {
+  c->purify_pending = false;
+  const int st = (int)rec[2];
   if (st & GBHF_DEV_ERR_TIMEOUT) return fail(c, GBHF_ERR_DEVICE_TIMEOUT, "purification grid barrier timed out");
-  const double err = hout[0];
-  c->prof.purify_steps += hout[1];
+  c->prof.purify_steps += rec[1];
   c->prof.purify_calls += 1;
-  if (err_out) *err_out = err;
-  if (!(std::fabs(err) < 1e-6 * std::max(1, ne)))
+  if (!(std::fabs(rec[0]) < 1e-6 * std::max(1, c->purify_ne)))
     return fail(c, GBHF_ERR_NOT_CONVERGED, "density purification did not converge");
   return GBHF_OK;
 }
@@ -1352,8 +1390,7 @@ gbhf_status density_purified_dev(gbhf_ctx* c, int n, const double* d_Fsq, const 
     GBHF_CUDA(c, cudaMemsetAsync(d_Dsq, 0, nn * sizeof(double), c->stream));
     return GBHF_OK;
   }
-  double err = 0;
-  GBHF_TRY(purify(c, n, nocc, Fp, P, &err));
+  GBHF_TRY(purify(c, n, nocc, Fp, P, nullptr));
   GBHF_TRY(gemm(c, false, false, n, n, n, 2.0, d_X, n, P, n, 0.0, T1, n));
   GBHF_TRY(gemm(c, false, true, n, n, n, 1.0, T1, n, d_X, n, 0.0, d_Dsq, n, true));
   return GBHF_OK;

@@ -228,6 +228,12 @@ gbhf_status scf_run(gbhf_ctx* c, const gbhf_scf_opts* o, gbhf_result* r) {
   GBHF_CUDA(c, cudaStreamSynchronize(c->stream));
   c->prof.ph_setup += ms_since(t_phase);
   c->scf_trace.clear();
+  // the purification checks of the loop ride on its statistics reads
+  struct DeferGuard {
+    gbhf_ctx* c;
+    ~DeferGuard() { c->purify_defer = false; }
+  } defer_guard{c};
+  c->purify_defer = true;
   for (step = 0; step < o->max_iter; ++step) {
     // phase boundaries as events on the stream (read after the step's last
     // host synchronisation, so that no phase waits for the GPU to drain)
@@ -399,6 +405,8 @@ gbhf_status scf_run(gbhf_ctx* c, const gbhf_scf_opts* o, gbhf_result* r) {
       break;
     }
   }
+  c->purify_defer = false;
+  GBHF_TRY(purify_flush(c));
   // keep the converged state for gbhf_gradient
   GBHF_CUDA(c, c->last_D.alloc(nn));
   GBHF_CUDA(c, c->last_F.alloc(nn));
