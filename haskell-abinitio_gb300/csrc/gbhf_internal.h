@@ -354,7 +354,11 @@ struct gbhf_ctx {
   bool tuned[2] = {false, false};   // budgets chosen by the autotuner or the caller
   // side streams of the J/K build: the class kernels of one build run
   // concurrently so that the tail of one persistent launch overlaps the next
-  static constexpr int NSIDE = 4;
+  // side streams for the J/K class launches (eight measured 1% faster than four on the
+  // (H2O)16 mixed SCF); the gradient's class launches use the first NSIDE_GRAD (four: eight
+  // were 3% slower there)
+  static constexpr int NSIDE = 8;
+  static constexpr int NSIDE_GRAD = 4;
   cudaStream_t side[NSIDE] = {};
   cudaEvent_t fork_ev = nullptr, join_ev[NSIDE] = {};
   gbhf::DBuf<unsigned char> flush;

@@ -358,7 +358,7 @@ gbhf_status grad_2e(gbhf_ctx* c, const double* d_D, double schwarz, double mixed
     GBHF_CUDA(c, cudaEventRecord(c->evg[0], c->stream));
   } else {
     GBHF_CUDA(c, cudaEventRecord(c->fork_ev, c->stream));
-    for (int i = 0; i < gbhf_ctx::NSIDE; ++i) GBHF_CUDA(c, cudaStreamWaitEvent(c->side[i], c->fork_ev, 0));
+    for (int i = 0; i < gbhf_ctx::NSIDE_GRAD; ++i) GBHF_CUDA(c, cudaStreamWaitEvent(c->side[i], c->fork_ev, 0));
   }
   PairData& P = c->pairs;
   int nl = 0;
@@ -371,7 +371,7 @@ gbhf_status grad_2e(gbhf_ctx* c, const double* d_D, double schwarz, double mixed
       const int k = order[oi];
       const int nt = gt.hranges[4 * k + 2 * prec + 1] - gt.hranges[4 * k + 2 * prec];
       if (nt <= 0) continue;
-      cudaStream_t strm = ev ? c->stream : c->side[nl++ % gbhf_ctx::NSIDE];
+      cudaStream_t strm = ev ? c->stream : c->side[nl++ % gbhf_ctx::NSIDE_GRAD];
       if (!grad_gen_combo(k))
         GBHF_TRY(launch_grad_dclass(c, strm, k, prec, d_D, c->dfloat.p, d_grad, nt));
       else if (prec == 0)
@@ -388,7 +388,7 @@ gbhf_status grad_2e(gbhf_ctx* c, const double* d_D, double schwarz, double mixed
     }
   }
   if (!ev) {
-    for (int i = 0; i < gbhf_ctx::NSIDE; ++i) {
+    for (int i = 0; i < gbhf_ctx::NSIDE_GRAD; ++i) {
       GBHF_CUDA(c, cudaEventRecord(c->join_ev[i], c->side[i]));
       GBHF_CUDA(c, cudaStreamWaitEvent(c->stream, c->join_ev[i], 0));
     }
