@@ -831,15 +831,22 @@ gbhf_status eigh(gbhf_ctx* c, int n, const double* d_A, double* d_evals, double*
 // --------------------------------------------- GEMM-only matrix functions ----
 // Gershgorin interval and trace of a symmetric matrix: out = {lo, hi, trace}.
 __global__ void k_gershgorin(int n, const double* __restrict__ A, double* __restrict__ out) {
+  // a warp per row (coalesced loads), the warps of the block taking rows in turn
   double lo = 1e300, hi = -1e300, tr = 0;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) {
-    double r = 0;
-    const double* row = A + (long)i * n;
-    for (int j = 0; j < n; ++j)
-      if (j != i) r += fabs(row[j]);
-    lo = fmin(lo, row[i] - r);
-    hi = fmax(hi, row[i] + r);
-    tr += row[i];
+  {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int i = wid; i < n; i += nw) {
+      const double* row = A + (long)i * n;
+      double r = 0;
+      for (int j = lane; j < n; j += 32)
+        if (j != i) r += fabs(row[j]);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
+      const double d = row[i];
+      lo = fmin(lo, d - r);
+      hi = fmax(hi, d + r);
+      if (lane == 0) tr += d;
+    }
   }
   __shared__ double s_lo[32], s_hi[32], s_tr[32];
 #pragma unroll
@@ -1228,13 +1235,25 @@ __global__ void __launch_bounds__(TC2_THREADS) k_tc2_fused(Tc2Args a) {
 }
 
 // TC2 start: the spectrum of F mapped onto [0, 1], reversed (P0 = (hi I - F) / (hi - lo)).
-__global__ void k_tc2_init(int n, const double* __restrict__ F, const double* __restrict__ g, double* __restrict__ P) {
+__global__ void k_tc2_init(int n, const double* __restrict__ F, const double* __restrict__ g, double* __restrict__ P,
+                           double* __restrict__ Q0, double* __restrict__ Q1, double* __restrict__ Q2,
+                           double* __restrict__ tr, unsigned* __restrict__ bar, int* __restrict__ status) {
+  // P0 = (hi I - F) / (hi - lo), and the zeros the fused kernel starts from
+  // (its three P^2 buffers, trace slots, barrier counter and status word)
   const int i = blockIdx.y, j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i == 0 && blockIdx.x == 0) {
+    if (threadIdx.x < 16) tr[threadIdx.x] = 0.0;
+    if (threadIdx.x < 2) bar[threadIdx.x] = 0u;
+    if (threadIdx.x == 0) *status = 0;
+  }
   if (j >= n) return;
   const double lo = g[0], hi = g[1];
   const double sc = hi > lo ? 1.0 / (hi - lo) : 0.0;
-  const double f = F[(long)i * n + j];
-  P[(long)i * n + j] = sc * ((i == j ? hi : 0.0) - f);
+  const long e = (long)i * n + j;
+  P[e] = sc * ((i == j ? hi : 0.0) - F[e]);
+  Q0[e] = 0.0;
+  Q1[e] = 0.0;
+  Q2[e] = 0.0;
 }
 
 // The spectral projector onto the ne lowest eigenvectors of the symmetric F.
@@ -1264,14 +1283,22 @@ gbhf_status purify(gbhf_ctx* c, int n, int ne, const double* d_F, double* d_P, d
   GBHF_CUDA(c, c->jac.bar.alloc(2));
   GBHF_CUDA(c, c->dev_status.alloc(1));
   k_gershgorin<<<1, 1024, 0, c->stream>>>(n, d_F, g);
-  if (tc2) k_tc2_init<<<dim3((n + 127) / 128, n), 128, 0, c->stream>>>(n, d_F, g, d_P);
-  else k_purify_init<<<dim3((n + 127) / 128, n), 128, 0, c->stream>>>(n, ne, d_F, g, d_P);
-  count_launch(c, 2);
-  GBHF_CUDA(c, cudaMemsetAsync(P2, 0, nn * sizeof(double), c->stream));
-  GBHF_CUDA(c, cudaMemsetAsync(P3, 0, nn * sizeof(double), c->stream));
-  GBHF_CUDA(c, cudaMemsetAsync(tr, 0, 16 * sizeof(double), c->stream));
-  GBHF_CUDA(c, cudaMemsetAsync(c->jac.bar.p, 0, 2 * sizeof(unsigned), c->stream));
-  GBHF_CUDA(c, cudaMemsetAsync(c->dev_status.p, 0, sizeof(int), c->stream));
+  count_launch(c);
+  if (tc2) {
+    GBHF_CUDA(c, c->jac.t2.alloc(nn));
+    GBHF_CUDA(c, c->jac.t3.alloc(nn));
+    k_tc2_init<<<dim3((n + 127) / 128, n), 128, 0, c->stream>>>(n, d_F, g, d_P, P2, P3, c->jac.t2.p, tr,
+                                                                c->jac.bar.p, c->dev_status.p);
+    count_launch(c);
+  } else {
+    k_purify_init<<<dim3((n + 127) / 128, n), 128, 0, c->stream>>>(n, ne, d_F, g, d_P);
+    count_launch(c);
+    GBHF_CUDA(c, cudaMemsetAsync(P2, 0, nn * sizeof(double), c->stream));
+    GBHF_CUDA(c, cudaMemsetAsync(P3, 0, nn * sizeof(double), c->stream));
+    GBHF_CUDA(c, cudaMemsetAsync(tr, 0, 16 * sizeof(double), c->stream));
+    GBHF_CUDA(c, cudaMemsetAsync(c->jac.bar.p, 0, 2 * sizeof(unsigned), c->stream));
+    GBHF_CUDA(c, cudaMemsetAsync(c->dev_status.p, 0, sizeof(int), c->stream));
+  }
   const int nt = (n + ST - 1) / ST;
   const int ntile = nt * (nt + 1) / 2;
   // k slices: about one item per SM, at least two k-steps per slice
@@ -1280,10 +1307,7 @@ gbhf_status purify(gbhf_ctx* c, int n, int ne, const double* d_F, double* d_P, d
   const int ks = (n + kslice - 1) / kslice;
   double hout[2] = {1.0, 0.0};
   if (tc2) {
-    // one barrier per step: a second P buffer and three P2 buffers
-    GBHF_CUDA(c, c->jac.t2.alloc(nn));
-    GBHF_CUDA(c, c->jac.t3.alloc(nn));
-    GBHF_CUDA(c, cudaMemsetAsync(c->jac.t2.p, 0, nn * sizeof(double), c->stream));
+    // one barrier per step: a second P buffer and three P2 buffers (zeroed by k_tc2_init)
     Tc2Args t;
     t.n = n;
     t.ne = ne;
