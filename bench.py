@@ -357,7 +357,9 @@ def run_gbhf(args, world, rank, local):
                 "context": "one context kept across calls (Boys tables, SAD atoms, tuned budgets resident)"},
         "e2e_cold_context": {"value": cold_v, "unit": "s/molecule", "calls": len(cold_t),
                              "what": "median of gbhf_create + gbhf_set_basis + gbhf_scf (all matrices back) + "
-                                     "gbhf_destroy, a new context per call (default task budgets)"},
+                                     "gbhf_destroy, a new context per call (default task budgets); the host Boys "
+                                     "tables and the SAD atom densities are computed once per process and shared "
+                                     "by its contexts (the first context of a process pays for them)"},
     }
     if batch:
         line["batch256"] = batch

@@ -12,6 +12,7 @@
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -163,6 +164,12 @@ static gbhf_status atomic_density(gbhf_ctx* c, gbhf_ctx* sub, const Basis& b, in
   return GBHF_OK;
 }
 
+// Atomic density blocks by atom key (element and its contracted functions):
+// shared by the contexts of the process, so that a new context (e.g. one per
+// call of a host that creates and destroys one) does not rerun the atomic SCFs.
+static std::mutex g_sad_mu;
+static std::map<std::string, std::vector<double>> g_sad_cache;
+
 // Stacked blocks of every molecule of the context's basis (one block for one molecule).
 gbhf_status sad_density(gbhf_ctx* c, double* d_D) {
   const Basis& b = c->basis;
@@ -173,6 +180,11 @@ gbhf_status sad_density(gbhf_ctx* c, double* d_D) {
   for (int a = 0; a < b.natoms; ++a) {
     const std::string key = atom_key(b, a, fns);
     auto it = c->sad_cache.find(key);
+    if (it == c->sad_cache.end()) {
+      std::lock_guard<std::mutex> lock(g_sad_mu);
+      auto g = g_sad_cache.find(key);
+      if (g != g_sad_cache.end()) it = c->sad_cache.emplace(key, g->second).first;
+    }
     if (it == c->sad_cache.end()) {
       if (!c->sad_ctx) {
         gbhf_ctx* sub = nullptr;
@@ -185,6 +197,10 @@ gbhf_status sad_density(gbhf_ctx* c, double* d_D) {
       if (s != GBHF_OK) {
         if (!c->sad_ctx->err.empty()) c->err = "SAD guess: " + c->sad_ctx->err;
         return s;
+      }
+      {
+        std::lock_guard<std::mutex> lock(g_sad_mu);
+        g_sad_cache.emplace(key, blk);
       }
       it = c->sad_cache.emplace(key, std::move(blk)).first;
     }

@@ -203,10 +203,19 @@ static void boys_row_host(double xd, double* out) {
   }
 }
 
-gbhf_status ensure_boys_tables(gbhf_ctx* c) {
-  if (c->boys64.p && c->boys32.p && c->boysh64.p && c->boysh32.p) return GBHF_OK;
-  std::vector<double> t64((size_t)BOYS64_NROW * BOYS_NCOL);
-  std::vector<float> t32((size_t)BOYS32_NROW * BOYS_NCOL);
+// The host tables, computed once per process (the series run in long double,
+// software quad precision on some hosts) and uploaded to every context.
+struct BoysHostTables {
+  std::vector<double> t64, h64;
+  std::vector<float> t32, h32;
+};
+
+static BoysHostTables build_boys_host_tables() {
+  BoysHostTables bt;
+  std::vector<double>& t64 = bt.t64;
+  t64.resize((size_t)BOYS64_NROW * BOYS_NCOL);
+  std::vector<float>& t32 = bt.t32;
+  t32.resize((size_t)BOYS32_NROW * BOYS_NCOL);
   std::vector<double> t32d((size_t)BOYS32_NROW * BOYS_NCOL);   // the FP32 nodes' values before rounding
   for (int j = 0; j < BOYS64_NROW; ++j) boys_row_host(j * BOYS64_H, t64.data() + (size_t)j * BOYS_NCOL);
   for (int j = 0; j < BOYS32_NROW; ++j) {
@@ -215,8 +224,10 @@ gbhf_status ensure_boys_tables(gbhf_ctx* c) {
     for (int m = 0; m < BOYS_NCOL; ++m) t32[(size_t)j * BOYS_NCOL + m] = (float)t32d[(size_t)j * BOYS_NCOL + m];
   }
   // Horner tables per order L: row j = [F_(L+k)(T_j)/k!, k < NT][exp(-T_j)/k!, k < NT]
-  std::vector<double> h64((size_t)(BOYSH_LMAX + 1) * BOYS64_NROW * BOYSH64_STRIDE, 0.0);
-  std::vector<float> h32((size_t)(BOYSH_LMAX + 1) * BOYS32_NROW * BOYSH32_STRIDE, 0.0f);
+  std::vector<double>& h64 = bt.h64;
+  h64.assign((size_t)(BOYSH_LMAX + 1) * BOYS64_NROW * BOYSH64_STRIDE, 0.0);
+  std::vector<float>& h32 = bt.h32;
+  h32.assign((size_t)(BOYSH_LMAX + 1) * BOYS32_NROW * BOYSH32_STRIDE, 0.0f);
   for (int L = 0; L <= BOYSH_LMAX; ++L) {
     for (int j = 0; j < BOYS64_NROW; ++j) {
       double* row = h64.data() + ((size_t)L * BOYS64_NROW + j) * BOYSH64_STRIDE;
@@ -239,6 +250,21 @@ gbhf_status ensure_boys_tables(gbhf_ctx* c) {
       }
     }
   }
+  return bt;
+}
+
+static const BoysHostTables& boys_host_tables() {
+  static const BoysHostTables bt = build_boys_host_tables();   // thread-safe one-time initialisation
+  return bt;
+}
+
+gbhf_status ensure_boys_tables(gbhf_ctx* c) {
+  if (c->boys64.p && c->boys32.p && c->boysh64.p && c->boysh32.p) return GBHF_OK;
+  const BoysHostTables& bt = boys_host_tables();
+  const std::vector<double>& t64 = bt.t64;
+  const std::vector<float>& t32 = bt.t32;
+  const std::vector<double>& h64 = bt.h64;
+  const std::vector<float>& h32 = bt.h32;
   GBHF_CUDA(c, c->boys64.alloc(t64.size()));
   GBHF_CUDA(c, c->boys32.alloc(t32.size()));
   GBHF_CUDA(c, c->boysh64.alloc(h64.size()));
