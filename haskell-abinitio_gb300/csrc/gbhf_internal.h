@@ -544,8 +544,10 @@ gbhf_status axpby(gbhf_ctx* c, size_t n, double a, const double* x, double b, co
 gbhf_status add_sym(gbhf_ctx* c, int n, const double* d_H, const double* d_Gpp, double* d_out);
 gbhf_status max_abs(gbhf_ctx* c, size_t n, const double* d_x, double* host_out);
 // Purification record slots in c->small and its checks (the deferred one runs
-// in reduce_stats; purify_flush reads a pending one on its own).
-constexpr int PURIFY_REC = 16;
+// in reduce_stats; purify_flush reads a pending one on its own).  c->small holds
+// the statistics in 0-3, max|x| in 8, this record in 12-14, the Gauss
+// elimination's operands from 16 on.
+constexpr int PURIFY_REC = 12;
 gbhf_status purify_finish(gbhf_ctx* c, const double* rec);
 gbhf_status purify_flush(gbhf_ctx* c);
 gbhf_status max_abs_dev(gbhf_ctx* c, size_t n, const double* d_x, double* d_out);   // into device memory

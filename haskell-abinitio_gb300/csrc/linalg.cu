@@ -420,7 +420,7 @@ gbhf_status reduce_stats(gbhf_ctx* c, int n, const double* d_e, const double* d_
   k_stats<<<1, 1024, 0, c->stream>>>(n, d_e, d_H, d_F, d_Dnew, d_Dold, c->small.p);
   count_launch(c);
   GBHF_CUDA(c, cudaGetLastError());
-  // with a purification check pending, its record (small[16..18]) comes back in the same copy
+  // with a purification check pending, its record (small[12..14]) comes back in the same copy
   double h[PURIFY_REC + 3];
   const int nget = c->purify_pending ? PURIFY_REC + 3 : 4;
   GBHF_CUDA(c, cudaMemcpyAsync(h, c->small.p, nget * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
