@@ -339,6 +339,8 @@ struct gbhf_ctx {
   bool purify_defer = false;        // purify leaves its check to the next reduce_stats (SCF loop)
   bool purify_pending = false;      // a purification record waits in small[PURIFY_REC..+2]
   int purify_ne = 0;                // electrons of the pending purification
+  gbhf::DBuf<double> red_part;     // per-block partials of the grid reductions (k_stats_grid, k_dots, k_max_abs)
+  gbhf::DBuf<unsigned> red_ticket; // their last-block ticket (zero between launches)
   gbhf::DBuf<unsigned> barrier;
   gbhf::DBuf<double> small;
   gbhf::Profile prof;

@@ -385,12 +385,30 @@ gbhf_status to_float(gbhf_ctx* c, size_t n, const double* d_x, float* d_y) {
 // Block reduction helper (sum or max) into a double.
 
 // out[0] = max|e|, out[1] = 1/2 sum Dnew(H+F) (when H,F given), out[2] = sum (Dnew-Dold)^2,
-// out[3] = sum(D (H + F)) with Dold.  Single block.
-__global__ void k_stats(int n, const double* __restrict__ e, const double* __restrict__ H, const double* __restrict__ F,
-                        const double* __restrict__ Dn, const double* __restrict__ Do, double* __restrict__ out) {
+// out[3] = sum(D (H + F)) with Dold (k_stats_grid below).
+// Grid-wide reductions finish deterministically: each block reduces its slice
+// and writes its partials, and the block that takes the last ticket combines
+// the partials in block order (the same sums in the same order on every run)
+// and returns the ticket to zero.
+constexpr int RED_THREADS = 256, RED_MAXPART = 4096;
+
+__device__ bool red_last_block(unsigned* ticket) {
+  __shared__ bool s_last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) s_last = atomicAdd(ticket, 1u) == gridDim.x * gridDim.y - 1;
+  __syncthreads();
+  if (s_last) __threadfence();
+  return s_last;
+}
+
+// k_stats over a grid: part[4 * block + q].
+__global__ void __launch_bounds__(RED_THREADS) k_stats_grid(int n, const double* __restrict__ e,
+    const double* __restrict__ H, const double* __restrict__ F, const double* __restrict__ Dn,
+    const double* __restrict__ Do, double* __restrict__ part, unsigned* ticket, double* __restrict__ out) {
   double mx = 0, en = 0, dd = 0, eo = 0;
   const long nn = (long)n * n;
-  for (long i = threadIdx.x; i < nn; i += blockDim.x) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < nn; i += (long)gridDim.x * blockDim.x) {
     if (e) mx = fmax(mx, fabs(e[i]));
     if (H && F && Dn) en += Dn[i] * (H[i] + F[i]);
     if (H && F && Do) eo += Do[i] * (H[i] + F[i]);
@@ -407,17 +425,47 @@ __global__ void k_stats(int n, const double* __restrict__ e, const double* __res
   __syncthreads();
   eo = block_reduce(eo, false);
   if (threadIdx.x == 0) {
-    out[0] = mx;
-    out[1] = 0.5 * en;
-    out[2] = dd;
-    out[3] = 0.5 * eo;
+    part[4 * blockIdx.x + 0] = mx;
+    part[4 * blockIdx.x + 1] = en;
+    part[4 * blockIdx.x + 2] = dd;
+    part[4 * blockIdx.x + 3] = eo;
   }
+  if (red_last_block(ticket) && threadIdx.x == 0) {
+    double m = 0, a = 0, b = 0, d = 0;
+    for (unsigned g = 0; g < gridDim.x; ++g) {
+      m = fmax(m, part[4 * g]);
+      a += part[4 * g + 1];
+      b += part[4 * g + 2];
+      d += part[4 * g + 3];
+    }
+    out[0] = m;
+    out[1] = 0.5 * a;
+    out[2] = b;
+    out[3] = 0.5 * d;
+    *ticket = 0;
+  }
+}
+
+static int red_blocks(gbhf_ctx* c, size_t n) {
+  return (int)std::max<size_t>(1, std::min<size_t>((size_t)c->nsm, (n + 4 * RED_THREADS - 1) / (4 * RED_THREADS)));
+}
+
+static gbhf_status red_buffers(gbhf_ctx* c) {
+  if (!c->red_ticket.p) {
+    GBHF_CUDA(c, c->red_ticket.alloc(1));
+    GBHF_CUDA(c, cudaMemsetAsync(c->red_ticket.p, 0, sizeof(unsigned), c->stream));
+  }
+  GBHF_CUDA(c, c->red_part.alloc(RED_MAXPART));
+  return GBHF_OK;
 }
 
 gbhf_status reduce_stats(gbhf_ctx* c, int n, const double* d_e, const double* d_H, const double* d_F,
                          const double* d_Dnew, const double* d_Dold, double* host_out4) {
   GBHF_CUDA(c, c->small.alloc(64));
-  k_stats<<<1, 1024, 0, c->stream>>>(n, d_e, d_H, d_F, d_Dnew, d_Dold, c->small.p);
+  GBHF_TRY(red_buffers(c));
+  const int g = red_blocks(c, (size_t)n * n);
+  k_stats_grid<<<g, RED_THREADS, 0, c->stream>>>(n, d_e, d_H, d_F, d_Dnew, d_Dold, c->red_part.p,
+                                                c->red_ticket.p, c->small.p);
   count_launch(c);
   GBHF_CUDA(c, cudaGetLastError());
   // with a purification check pending, its record (small[12..14]) comes back in the same copy
@@ -430,11 +478,19 @@ gbhf_status reduce_stats(gbhf_ctx* c, int n, const double* d_e, const double* d_
   return GBHF_OK;
 }
 
-__global__ void k_max_abs(size_t n, const double* __restrict__ x, double* out) {
+__global__ void __launch_bounds__(RED_THREADS) k_max_abs(size_t n, const double* __restrict__ x,
+                                                         double* __restrict__ part, unsigned* ticket, double* out) {
   double m = 0;
-  for (size_t i = threadIdx.x; i < n; i += blockDim.x) m = fmax(m, fabs(x[i]));
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    m = fmax(m, fabs(x[i]));
   m = block_reduce(m, true);
-  if (threadIdx.x == 0) *out = m;
+  if (threadIdx.x == 0) part[blockIdx.x] = m;
+  if (red_last_block(ticket) && threadIdx.x == 0) {
+    double r = 0;
+    for (unsigned g = 0; g < gridDim.x; ++g) r = fmax(r, part[g]);
+    *out = r;
+    *ticket = 0;
+  }
 }
 
 gbhf_status max_abs(gbhf_ctx* c, size_t n, const double* d_x, double* host_out) {
@@ -446,7 +502,8 @@ gbhf_status max_abs(gbhf_ctx* c, size_t n, const double* d_x, double* host_out) 
 }
 
 gbhf_status max_abs_dev(gbhf_ctx* c, size_t n, const double* d_x, double* d_out) {
-  k_max_abs<<<1, 1024, 0, c->stream>>>(n, d_x, d_out);
+  GBHF_TRY(red_buffers(c));
+  k_max_abs<<<red_blocks(c, n), RED_THREADS, 0, c->stream>>>(n, d_x, c->red_part.p, c->red_ticket.p, d_out);
   count_launch(c);
   GBHF_CUDA(c, cudaGetLastError());
   return GBHF_OK;
@@ -456,21 +513,33 @@ gbhf_status max_abs_dev(gbhf_ctx* c, size_t n, const double* d_x, double* d_out)
 struct MatPtrs {
   const double* p[16];
 };
-__global__ void k_dots(size_t n2, int k, MatPtrs mats, const double* __restrict__ e, double* __restrict__ out) {
-  const int j = blockIdx.x;
-  if (j >= k) return;
+// grid (G, k): block (g, j) sums slice g of mats[j] . e into part[j * G + g]
+__global__ void __launch_bounds__(RED_THREADS) k_dots(size_t n2, int k, MatPtrs mats, const double* __restrict__ e,
+                                                     double* __restrict__ part, unsigned* ticket,
+                                                     double* __restrict__ out) {
+  const int j = blockIdx.y, G = gridDim.x;
   const double* m = mats.p[j];
   double s = 0;
-  for (size_t i = threadIdx.x; i < n2; i += blockDim.x) s += m[i] * e[i];
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n2; i += (size_t)G * blockDim.x) s += m[i] * e[i];
   s = block_reduce(s, false);
-  if (threadIdx.x == 0) out[j] = s;
+  if (threadIdx.x == 0) part[j * G + blockIdx.x] = s;
+  if (red_last_block(ticket) && threadIdx.x == 0) {
+    for (int jj = 0; jj < k; ++jj) {
+      double t = 0;
+      for (int g = 0; g < G; ++g) t += part[jj * G + g];
+      out[jj] = t;
+    }
+    *ticket = 0;
+  }
 }
 
 gbhf_status dot_matrices(gbhf_ctx* c, int n2, int k, const double* const* mats, const double* d_e, double* d_out) {
   if (k > 16) return fail(c, GBHF_ERR_BAD_INPUT, "too many DIIS vectors");
   MatPtrs mp;
   for (int j = 0; j < k; ++j) mp.p[j] = mats[j];
-  k_dots<<<k, 512, 0, c->stream>>>((size_t)n2, k, mp, d_e, d_out);
+  GBHF_TRY(red_buffers(c));
+  const int G = std::max(1, std::min(red_blocks(c, (size_t)n2), RED_MAXPART / 16));
+  k_dots<<<dim3(G, k), RED_THREADS, 0, c->stream>>>((size_t)n2, k, mp, d_e, c->red_part.p, c->red_ticket.p, d_out);
   count_launch(c);
   GBHF_CUDA(c, cudaGetLastError());
   return GBHF_OK;
