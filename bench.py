@@ -18,6 +18,7 @@ own replica of the molecule (independent molecules, no data exchange) and
 rank 0 prints the whole-job number.
 """
 import argparse
+import datetime
 import json
 import os
 import statistics
@@ -62,24 +63,37 @@ def max_over_ranks(world, v):
 
 
 class ClockSampler:
-    """nvidia-smi clocks/throttle reasons sampled every 200 ms during the timed region."""
+    """nvidia-smi clocks/throttle reasons every 200 ms.  The sampler starts
+    before the work it watches (its start-up queries the driver for about a
+    tenth of a second, which stalled a timed SCF step when it fell inside the
+    timed region); begin()/end() mark the timed region, and the summary keeps
+    the samples stamped inside it (widened by one sampling period, so that a
+    short region keeps its neighbouring samples)."""
 
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    PERIOD_S = 0.2
 
     def __init__(self, device):
         self.device = device
         self.proc = None
+        self.t0 = self.t1 = None
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", str(int(1000 * self.PERIOD_S))],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except OSError:
             self.proc = None
         return self
+
+    def begin(self):
+        self.t0 = datetime.datetime.now()
+
+    def end(self):
+        self.t1 = datetime.datetime.now()
 
     def __exit__(self, *a):
         self.lines = []
@@ -92,19 +106,30 @@ class ClockSampler:
                 out, _ = self.proc.communicate()
             self.lines = [l for l in out.splitlines() if l.strip()]
 
+    def _in_region(self, stamp):
+        if self.t0 is None:
+            return True
+        try:
+            ts = datetime.datetime.strptime(stamp, "%Y/%m/%d %H:%M:%S.%f")
+        except ValueError:
+            return True
+        pad = datetime.timedelta(seconds=self.PERIOD_S)
+        t1 = self.t1 if self.t1 is not None else datetime.datetime.now()
+        return self.t0 - pad <= ts <= t1 + pad
+
     def summary(self):
         sm, mx, reasons = [], [], set()
         names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
         for l in getattr(self, "lines", []):
             p = [x.strip() for x in l.split(",")]
-            if len(p) < 9:
+            if len(p) < 10 or not self._in_region(p[0]):
                 continue
             try:
-                sm.append(float(p[1]))
-                mx.append(float(p[2]))
+                sm.append(float(p[2]))
+                mx.append(float(p[3]))
             except ValueError:
                 continue
-            for nm, v in zip(names, p[5:9]):
+            for nm, v in zip(names, p[6:10]):
                 if v.lower() == "active":
                     reasons.add(nm)
         if not sm:
@@ -242,20 +267,22 @@ def run_gbhf(args, world, rank, local):
         return r, ctx.event_elapsed(0, 1)
 
     tune = autotune_jk(ctx, fb, args)
-    for _ in range(max(args.warmup, 3)):
-        step(mixed)
-    # plain FP64 GPU SCF, once (reported beside the headline)
-    r64, t64 = step(fp64)
-    barrier(world)
-    ctx.profile_reset(events=False)
     times = []
-    with ClockSampler(local) as clk:
+    with ClockSampler(local) as clk:   # started before the warm-up (see ClockSampler)
+        for _ in range(max(args.warmup, 3)):
+            step(mixed)
+        # plain FP64 GPU SCF, once (reported beside the headline)
+        r64, t64 = step(fp64)
         barrier(world)
+        ctx.profile_reset(events=False)
+        barrier(world)
+        clk.begin()
         for _ in range(args.steps):
             ctx.flush_l2()
             r, ms = step(mixed)
             times.append(ms)
         barrier(world)
+        clk.end()
     prof = ctx.profile_read()
     # per-class kernel times: one more SCF with an event around every J/K
     # launch (the class launches then run one after another on one stream)
@@ -315,7 +342,8 @@ def run_gbhf(args, world, rank, local):
     fnq_step = prof["fn_quartets"] / args.steps
     line = {
         "metric": METRIC, "value": value, "unit": "s/molecule", "n_gpus": world, "steps": args.steps,
-        "warmup": max(args.warmup, 3), "ms_per_step": total_ms / args.steps, "higher_is_better": False,
+        "warmup": max(args.warmup, 3), "ms_per_step": total_ms / args.steps, "step_ms": [round(t, 3) for t in times],
+        "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
         "data": "synthetic (seeded water cluster, EMSL 6-31G)",
         "config": {"workload": WORKLOAD, "n_basis": n, "precision": "mixed: FP32 ERIs below Schwarz bound 1e-4, "
