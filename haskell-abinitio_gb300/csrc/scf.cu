@@ -229,10 +229,15 @@ gbhf_status scf_run(gbhf_ctx* c, const gbhf_scf_opts* o, gbhf_result* r) {
   c->prof.ph_setup += ms_since(t_phase);
   c->scf_trace.clear();
   // the purification checks of the loop ride on its statistics reads
+  // (a record left pending by an SCF that stopped on an error is dropped with it)
   struct DeferGuard {
     gbhf_ctx* c;
-    ~DeferGuard() { c->purify_defer = false; }
+    ~DeferGuard() {
+      c->purify_defer = false;
+      c->purify_pending = false;
+    }
   } defer_guard{c};
+  c->purify_pending = false;
   c->purify_defer = true;
   for (step = 0; step < o->max_iter; ++step) {
     // phase boundaries as events on the stream (read after the step's last
