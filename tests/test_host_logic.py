@@ -153,3 +153,26 @@ def test_generated_headers_match_their_generators():
             assert mod.render() == (csrc / out).read_text(), out
     finally:
         sys.path.remove(str(csrc))
+
+
+def test_bench_clock_sampler_keeps_samples_of_the_timed_region():
+    """bench.py's ClockSampler: samples stamped inside the marked region (widened
+    by one sampling period) count, earlier ones do not."""
+    import datetime
+    import importlib.util
+    from pathlib import Path
+    spec = importlib.util.spec_from_file_location("bench_mod", Path(__file__).resolve().parents[1] / "bench.py")
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+    c = bench.ClockSampler(0)
+    now = datetime.datetime.now()
+    c.t0, c.t1 = now, now + datetime.timedelta(seconds=0.3)
+
+    def line(dt, mhz, power_cap):
+        ts = (now + datetime.timedelta(seconds=dt)).strftime("%Y/%m/%d %H:%M:%S.%f")[:-3]
+        return f"{ts}, 0, {mhz}, 2070, 900, 0x0, Not Active, Not Active, Not Active, {power_cap}"
+
+    c.lines = [line(-1.0, 1000, "Not Active"), line(0.1, 2070, "Not Active"), line(0.45, 2060, "Active")]
+    s = c.summary()
+    assert s["samples"] == 2 and s["sm_mhz"] == 2065.0 and s["sm_max_mhz"] == 2070.0
+    assert s["reasons"] == ["sw_power_cap"]
