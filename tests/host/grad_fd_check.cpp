@@ -2,9 +2,10 @@
 // compiled for the CPU with stand-ins for the device helpers (a long-double
 // series for the Boys function), it compares the bra-centre derivatives of
 // grad_ket_<class> + grad_ketprim_<class> with central differences (h = 1e-4
-// bohr) of sum_abcd Gamma_abcd (ab|cd) from eri_ketprim_<class>, for random
-// centres, exponents and Gamma; prints the largest error relative to the
-// largest derivative for each class.  Run by tests/test_generated_code_host.py.
+// bohr) of sum_abcd Gamma_abcd (ab|cd) from eri_ketprim_<class> (or, where
+// that class is generated only as (cd|ab), from it with bra and ket
+// exchanged), for random centres, exponents and Gamma; prints the largest error
+// relative to the largest derivative for each of the 14 generated classes.  Run by tests/test_generated_code_host.py.
 #include <cmath>
 #include <cstdio>
 #include <random>
@@ -52,20 +53,28 @@ static void pair(const double* A, const double* B, double a, double b, double* r
 std::mt19937_64 rng(11);
 static double U(double lo, double hi) { return std::uniform_real_distribution<double>(lo, hi)(rng); }
 
-#define ENERGY(cls, NOUT, A, B, C, D)                                                                            \
+// E(A, B) = sum Gamma_abcd (ab|cd) from the ERI class ecls: in the gradient's
+// orientation (SW = 0) or, for a gradient class whose ERI code exists only as
+// (cd|ab), from that class with bra and ket exchanged (SW = 1)
+#define ENERGY(ecls, NOUT, NAB, SW)                                                                              \
   [&](const double* A_, const double* B_) {                                                                      \
-    double sb[BRA_SB], kt[BRA_SB];                                                                               \
-    pair(A_, B_, ea, eb, sb);                                                                                    \
-    pair(C, D, ec, ed, kt);                                                                                      \
+    double s1[BRA_SB], s2[BRA_SB];                                                                               \
+    pair(A_, B_, ea, eb, s1);                                                                                    \
+    pair(C, D, ec, ed, s2);                                                                                      \
+    const double* sb = SW ? s2 : s1;                                                                             \
+    const double* kt = SW ? s1 : s2;                                                                             \
     Acc acc;                                                                                                     \
-    eri_ketprim_##cls<double, Acc>(sb, 1, BRA_SB, kt[0], kt[1], kt[2], kt[3], kt[4], kt[5], kt[6], kt[7], kt[8], \
-                                   kt[9], kt[10], kt[11], nullptr, acc);                                         \
+    eri_ketprim_##ecls<double, Acc>(sb, 1, BRA_SB, kt[0], kt[1], kt[2], kt[3], kt[4], kt[5], kt[6], kt[7], kt[8], \
+                                    kt[9], kt[10], kt[11], nullptr, acc);                                        \
+    const int NCD = NOUT / NAB;                                                                                  \
     double e = 0;                                                                                                \
-    for (int i = 0; i < NOUT; ++i) e += gam[i] * acc.v[i];                                                       \
+    for (int iab = 0; iab < NAB; ++iab)                                                                          \
+      for (int icd = 0; icd < NCD; ++icd)                                                                        \
+        e += gam[iab * NCD + icd] * acc.v[SW ? icd * NAB + iab : iab * NCD + icd];                               \
     return e;                                                                                                    \
   }
 
-#define CHECK(cls, NOUT)                                                                                         \
+#define CHECK(cls, ecls, NOUT, NAB, SW)                                                                          \
   {                                                                                                              \
     double worst = 0;                                                                                            \
     for (int rep = 0; rep < 6; ++rep) {                                                                          \
@@ -74,7 +83,7 @@ static double U(double lo, double hi) { return std::uniform_real_distribution<do
       const double ea = U(0.3, 2), eb = U(0.3, 2), ec = U(0.3, 2), ed = U(0.3, 2);                               \
       std::vector<double> gam(NOUT);                                                                             \
       for (auto& g : gam) g = U(-1, 1);                                                                          \
-      auto E = ENERGY(cls, NOUT, A, B, C, D);                                                                    \
+      auto E = ENERGY(ecls, NOUT, NAB, SW);                                                                      \
       double sb[BRA_SB], kt[BRA_SB];                                                                             \
       pair(A, B, ea, eb, sb);                                                                                    \
       pair(C, D, ec, ed, kt);                                                                                    \
@@ -100,7 +109,10 @@ static double U(double lo, double hi) { return std::uniform_real_distribution<do
   }
 
 int main() {
-  CHECK(ssss, 1) CHECK(psss, 3) CHECK(psps, 9) CHECK(sspp, 9) CHECK(pspp, 27) CHECK(pppp, 81)
-  CHECK(dsss, 6) CHECK(dsps, 18)
+  CHECK(ssss, ssss, 1, 1, 0) CHECK(psss, psss, 3, 3, 0) CHECK(psps, psps, 9, 3, 0) CHECK(sspp, sspp, 9, 1, 0)
+  CHECK(pspp, pspp, 27, 3, 0) CHECK(pppp, pppp, 81, 9, 0) CHECK(dsss, dsss, 6, 6, 0) CHECK(dsps, dsps, 18, 6, 0)
+  // classes whose ERI code is generated in the other orientation only
+  CHECK(ssps, psss, 3, 1, 1) CHECK(ppss, sspp, 9, 9, 1) CHECK(ppps, pspp, 27, 9, 1) CHECK(ssds, dsss, 6, 1, 1)
+  CHECK(ssdp, dpss, 18, 1, 1) CHECK(psds, dsps, 18, 3, 1)
   return 0;
 }

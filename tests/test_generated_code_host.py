@@ -2,8 +2,8 @@
 the gradient code as the derivative of the ERI code.
 
 ``tests/host/grad_fd_check.cpp`` compiles ``csrc/eri_gen.cuh`` and
-``csrc/grad_gen.cuh`` for the host and compares, for eight classes ((ss|ss)
-through (pp|pp), and (ds|ss), (ds|ps)), the generated bra-centre derivatives
+``csrc/grad_gen.cuh`` for the host and compares, for all 14 generated classes
+(the s/p ones and the light d ones), the generated bra-centre derivatives
 of one primitive quartet contracted with a random Gamma against central
 differences of the generated ERIs (h = 1e-4 bohr: truncation error ~1e-8 of
 the largest derivative).  No GPU: this checks the generators' algebra (the
@@ -31,7 +31,8 @@ def test_generated_gradient_matches_finite_differences_of_generated_eris(tmp_pat
                    capture_output=True, text=True)
     out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()
     res = dict(zip(out[0::2], map(float, out[1::2])))
-    assert set(res) == {"ssss", "psss", "psps", "sspp", "pspp", "pppp", "dsss", "dsps"}
+    assert set(res) == {"ssss", "psss", "psps", "sspp", "pspp", "pppp", "dsss", "dsps",
+                        "ssps", "ppss", "ppps", "ssds", "ssdp", "psds"}
     for cls, err in res.items():
         assert err < 1e-6, (cls, err)
 
