@@ -3,7 +3,8 @@
 // exponents and contraction coefficients of one primitive per shell - and
 // prints the components of (ab|cd) from eri_ketprim_<class> (one bra and one
 // ket primitive pair), which tests/test_generated_code_host.py compares with
-// the oracle's contracted ERIs of the same one-primitive functions.
+// the oracle's contracted ERIs of the same one-primitive functions (d
+// components in the order xx, xy, xz, yy, yz, zz, one coefficient per shell).
 #include <cmath>
 #include <cstdio>
 #include <random>
@@ -74,6 +75,7 @@ int main() {
     pair(X[0], X[1], e[0], e[1], c[0], c[1], sb);
     pair(X[2], X[3], e[2], e[3], c[2], c[3], kt);
     RUN(ssss, 1) RUN(psss, 3) RUN(psps, 9) RUN(sspp, 9) RUN(pspp, 27) RUN(pppp, 81)
+    RUN(dsss, 6) RUN(dsps, 18) RUN(dspp, 54) RUN(dsds, 36) RUN(dpss, 18) RUN(dpps, 54) RUN(ddss, 36)
     return 2;
   }
   return 0;

@@ -9,8 +9,9 @@ differences of the generated ERIs (h = 1e-4 bohr: truncation error ~1e-8 of
 the largest derivative).  No GPU: this checks the generators' algebra (the
 derivative rule of the basis functions, HartreeFock/Derivatives.hs:246-257, in
 Hermite form) before any device runs it.  ``tests/host/eri_oracle_check.cpp``
-does the same for the ERIs themselves: one primitive per shell, the six s/p
-classes, against the oracle's contracted ERIs in exact numerics."""
+does the same for the ERIs themselves: one primitive per shell, the thirteen
+generated classes (six s/p, seven d), against the oracle's contracted ERIs in
+exact numerics."""
 import shutil
 import subprocess
 from pathlib import Path
@@ -38,13 +39,17 @@ def test_generated_gradient_matches_finite_differences_of_generated_eris(tmp_pat
 
 
 CLASSES = {"ssss": (0, 0, 0, 0), "psss": (1, 0, 0, 0), "psps": (1, 0, 1, 0), "sspp": (0, 0, 1, 1),
-           "pspp": (1, 0, 1, 1), "pppp": (1, 1, 1, 1)}
+           "pspp": (1, 0, 1, 1), "pppp": (1, 1, 1, 1), "dsss": (2, 0, 0, 0), "dsps": (2, 0, 1, 0),
+           "dspp": (2, 0, 1, 1), "dsds": (2, 0, 2, 0), "dpss": (2, 1, 0, 0), "dpps": (2, 1, 1, 0),
+           "ddss": (2, 2, 0, 0)}
+LABELS = {0: ("S",), 1: ("Px", "Py", "Pz"), 2: ("Dxx", "Dxy", "Dxz", "Dyy", "Dyz", "Dzz")}
 
 
 def test_generated_eris_match_the_oracle(tmp_path):
     """eri_ketprim_<class> for one primitive per shell against the oracle's
     contracted ERIs (exact numerics) of the same one-primitive functions, for
-    the six s/p classes, 1e-12 relative to the largest integral."""
+    the six s/p classes and the seven lane-per-ket d classes, 1e-12 relative to
+    the largest integral."""
     import numpy as np
     import oracle as O
     from gbhf import basis as B
@@ -55,7 +60,6 @@ def test_generated_eris_match_the_oracle(tmp_path):
     subprocess.run([cxx, "-O1", "-std=c++17", "-I", str(CSRC), str(SRC.parent / "eri_oracle_check.cpp"), "-o", str(exe)],
                    check=True, capture_output=True, text=True)
     rng = np.random.default_rng(5)
-    ptypes = ("Px", "Py", "Pz")
     worst = 0.0
     for cls, ls in CLASSES.items():
         for rep in range(3):
@@ -64,19 +68,19 @@ def test_generated_eris_match_the_oracle(tmp_path):
             co = rng.uniform(0.5, 1.5, 4)
             atoms = []
             for k in range(4):
-                fns = [B.CGF(((co[k], ex[k]),), "S")] if ls[k] == 0 else [B.CGF(((co[k], ex[k]),), t) for t in ptypes]
+                fns = [B.CGF(((co[k], ex[k]),), t) for t in LABELS[ls[k]]]
                 atoms.append(B.AtomData(tuple(xyz[k]), fns, 1.0))
             ob = O.OracleBasis(B.flatten(atoms))
-            first = np.cumsum([0] + [1 if l == 0 else 3 for l in ls])
+            first = np.cumsum([0] + [len(LABELS[l]) for l in ls])
             line = " ".join([cls] + [f"{v:.17e}" for v in xyz.ravel()] + [f"{v:.17e}" for v in ex] +
                             [f"{v:.17e}" for v in co])
             got = np.array(subprocess.run([str(exe)], input=line + "\n", check=True, capture_output=True,
                                           text=True).stdout.split(), dtype=float)
             ref = []
-            for ia in range(1 if ls[0] == 0 else 3):
-                for ib in range(1 if ls[1] == 0 else 3):
-                    for ic in range(1 if ls[2] == 0 else 3):
-                        for id_ in range(1 if ls[3] == 0 else 3):
+            for ia in range(len(LABELS[ls[0]])):
+                for ib in range(len(LABELS[ls[1]])):
+                    for ic in range(len(LABELS[ls[2]])):
+                        for id_ in range(len(LABELS[ls[3]])):
                             ref.append(ob.eri(first[0] + ia, first[1] + ib, first[2] + ic, first[3] + id_,
                                               ref_compat=False))
             ref = np.array(ref)
