@@ -614,13 +614,29 @@ def run_fock_case(args, world, rank, local):
         print(json.dumps({"workload": "fock", "n_basis": n, "checksum": float(np.abs(f).sum())}), flush=True)
 
 
+def run_scf_case(args, world, rank, local):
+    """Profiling case: one mixed-precision SCF of (H2O)16/6-31G with the J/K
+    class launches timed one by one; prints each class's counted quartets
+    (to divide ncu counters of the class launches by)."""
+    from gbhf import _lib, basis as B, molecules as M
+    ctx = _lib.Context(local)
+    fb = B.flatten(M.cluster_atoms("w16", "6-31g"))
+    mixed = _lib.baseline_opts(precision=_lib.PREC_MIXED, incremental=1, final_fp64=0, full_rebuild_every=0)
+    ctx.set_basis(fb)
+    ctx.profile_reset(events=True)
+    r = ctx.scf(mixed, want_matrices=False)
+    cls = {f"{k[0]}_{k[1]}": v for k, v in ctx.profile_classes().items() if v["ms"] > 0}
+    if rank == 0:
+        print(json.dumps({"workload": "scf1", "energy": r["energy"], "classes": cls}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gbhf", choices=["gbhf", "reference"])
-    ap.add_argument("--workload", default="w16", choices=["w16", "batch256", "grad8", "w64", "w16d", "fock"])
+    ap.add_argument("--workload", default="w16", choices=["w16", "batch256", "grad8", "w64", "w16d", "fock", "scf1"])
     ap.add_argument("--quick", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="batch256: keep the default task budgets")
@@ -646,6 +662,8 @@ def main():
         run_large(args, world, rank, local, "w16", "6-31g*")
     elif args.workload == "fock":
         run_fock_case(args, world, rank, local)
+    elif args.workload == "scf1":
+        run_scf_case(args, world, rank, local)
     else:
         run_gbhf(args, world, rank, local)
     if world > 1:
